@@ -1,0 +1,686 @@
+// Kernels of one Levenberg–Marquardt iteration (ba.rs:219-383), templated on
+// the storage type R of Jacobians, Schur blocks and PCG vectors (double for
+// the plain form, float for the mixed form).  Costs, PCG inner products and
+// the 3x3 / 6x6 block inversions are always FP64.
+#pragma once
+
+#include "solver.cuh"
+#include "structure.cuh"
+
+namespace ba {
+
+constexpr int kLinW = 28;  // per-observation record: jc 12, jp 6, jg 6, e 2, w, valid
+
+enum { LOSS_CAUCHY = 0, LOSS_HUBER = 1 };
+
+template <typename R>
+struct IterBufs {
+  R* lin;      // [no][kLinW]
+  R* gsub;     // [no][9]: Y_k V^-1 v (6) | w Jg^T Jp V^-1 v (3)
+  R* Z;        // [no][18]: Y_k L (L L^T = V^-1)
+  R* Zl;       // [nl][9]: lens entry, top 3x3
+  R* ptL;      // [np][6]: l00 l10 l11 l20 l21 l22
+  R* ptzv;     // [np][3]: L^T v
+  uint8_t* kept;  // [np]
+  double* camU;   // [nc][21] upper triangle of sum w Jc^T Jc
+  double* camgj;  // [nc][6] sum w Jc^T e
+  double* camgs;  // [nc][6] sum Y V^-1 v
+  double* camX;   // [nc][18] sum w Jc^T Jg (6x3)
+  double* caml;   // [nc][12]: lens U upper (6) | sum w Jg^T e (3) | lens Schur g (3)
+  double* grpU;   // [ng][6]
+  double* grpg;   // [ng][3]
+  R* part;        // [nsub][36]
+  R* S;           // [nz][36] full symmetric BSR
+  double* pre;    // [nb][36]
+  R* g;           // [nb][6]
+  R* x;           // [nb][6] (dx)
+  R *r, *z, *p, *q;  // PCG work vectors [nb][6]
+  double* cost_part;  // [ncost][3]
+};
+
+__device__ __forceinline__ double robust_weight(double e2, double sigma, int loss) {
+  if (loss == LOSS_HUBER) {
+    const double a = sqrt(e2);
+    return a <= sigma ? 1.0 : sigma / a;
+  }
+  return 1.0 / (1.0 + e2 / (sigma * sigma));  // ba.rs:99
+}
+
+__device__ __forceinline__ double robust_rho(double e2, double sigma, int loss) {
+  if (loss == LOSS_HUBER) {
+    const double a = sqrt(e2);
+    return a <= sigma ? e2 : 2.0 * sigma * a - sigma * sigma;
+  }
+  const double s2 = sigma * sigma;
+  return s2 * log(1.0 + e2 / s2);  // ba.rs:114
+}
+
+// linearise (ba.rs:56-101) of observation k into out[kLinW]; false if the
+// point is not in front of the camera (z <= 1e-6).
+template <typename R>
+__device__ __forceinline__ bool linearise(const Prob& P, const StateView& st, int64_t k,
+                                          double sigma, bool refine, R* out) {
+  const uint32_t cam = P.obs_cam[k];
+  const double* Rm = st.rot + 9 * (size_t)cam;
+  const double* C = st.center + 3 * (size_t)cam;
+  const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
+  const double* X = st.points + 3 * (size_t)P.obs_pt[k];
+  double xc[3];
+  bacam::to_cam(Rm, C, X, xc);
+  if (xc[2] <= 1e-6) return false;
+  const double f = K[0], k1 = K[3], k2 = K[4];
+  const double iz = 1.0 / xc[2];
+  const double px = xc[0] * iz, py = xc[1] * iz;
+  const double r2 = px * px + py * py;
+  const double d = 1.0 + k1 * r2 + k2 * r2 * r2;
+  const double qx = px * d, qy = py * d;
+  const double ex = P.obs_uv[2 * k] - (f * qx + K[1]);
+  const double ey = P.obs_uv[2 * k + 1] - (f * qy + K[2]);
+  const double c = 2.0 * (k1 + 2.0 * k2 * r2);
+  const double a00 = (d + c * px * px) * f, a01 = (c * px * py) * f;
+  const double a11 = (d + c * py * py) * f;
+  const double b02 = -xc[0] * iz * iz, b12 = -xc[1] * iz * iz;
+  double du[6];
+  du[0] = a00 * iz;
+  du[1] = a01 * iz;
+  du[2] = a00 * b02 + a01 * b12;
+  du[3] = a01 * iz;
+  du[4] = a11 * iz;
+  du[5] = a01 * b02 + a11 * b12;
+  // Jc = [dudx · (−[xc]x) | dudx · (−R)], Jp = dudx · R.
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const double u0 = du[3 * r], u1 = du[3 * r + 1], u2 = du[3 * r + 2];
+    out[6 * r + 0] = (R)(u2 * xc[1] - u1 * xc[2]);
+    out[6 * r + 1] = (R)(u0 * xc[2] - u2 * xc[0]);
+    out[6 * r + 2] = (R)(u1 * xc[0] - u0 * xc[1]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double pp = u0 * Rm[j] + u1 * Rm[3 + j] + u2 * Rm[6 + j];
+      out[6 * r + 3 + j] = (R)(-pp);
+      out[12 + 3 * r + j] = (R)pp;
+    }
+  }
+  if (refine) {  // ba.rs:87-95
+    out[18] = (R)qx;
+    out[19] = (R)(f * px * r2);
+    out[20] = (R)(f * px * r2 * r2);
+    out[21] = (R)qy;
+    out[22] = (R)(f * py * r2);
+    out[23] = (R)(f * py * r2 * r2);
+  } else {
+#pragma unroll
+    for (int i = 18; i < 24; ++i) out[i] = (R)0;
+  }
+  out[24] = (R)ex;
+  out[25] = (R)ey;
+  out[26] = (R)robust_weight(ex * ex + ey * ey, sigma, P.loss);
+  out[27] = (R)1;
+  return true;
+}
+
+// Lower Cholesky factor of a symmetric positive definite 3x3 (row-major);
+// a non-positive pivot (rounding on a near-singular block) is clamped to 0.
+__device__ __forceinline__ void chol3(const double* A, double* L) {
+  const double a00 = A[0], a10 = A[3], a11 = A[4], a20 = A[6], a21 = A[7], a22 = A[8];
+  const double l00 = a00 > 0.0 ? sqrt(a00) : 0.0;
+  const double l10 = l00 > 0.0 ? a10 / l00 : 0.0;
+  const double l20 = l00 > 0.0 ? a20 / l00 : 0.0;
+  const double t11 = a11 - l10 * l10;
+  const double l11 = t11 > 0.0 ? sqrt(t11) : 0.0;
+  const double l21 = l11 > 0.0 ? (a21 - l20 * l10) / l11 : 0.0;
+  const double t22 = a22 - l20 * l20 - l21 * l21;
+  const double l22 = t22 > 0.0 ? sqrt(t22) : 0.0;
+  L[0] = l00, L[1] = l10, L[2] = l11, L[3] = l20, L[4] = l21, L[5] = l22;
+}
+
+// ---- per point: linearise its observations, V, v, V^-1, Z (ba.rs:222-268) ----
+
+template <typename R>
+__global__ void __launch_bounds__(128)
+    point_kernel(Prob P, StateView st, StructView S, IterBufs<R> B, const int32_t* active,
+                 const double* lambda, const double* sigma) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.np) return;
+  const uint32_t m = P.pt_model[p];
+  if (!active[m]) return;
+  const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
+  const bool refine = P.model_refine[m] != 0;
+  const double sg = sigma[m], lam = lambda[m];
+  if (e - s < 2) {  // ba.rs:238
+    B.kept[p] = 0;
+    for (uint32_t k = s; k < e; ++k) {
+      R* o = B.lin + (size_t)k * kLinW;
+      if (!linearise<R>(P, st, k, sg, refine, o))
+        for (int i = 0; i < kLinW; ++i) o[i] = (R)0;
+    }
+    return;
+  }
+  double V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
+  for (uint32_t k = s; k < e; ++k) {
+    R* o = B.lin + (size_t)k * kLinW;
+    if (!linearise<R>(P, st, k, sg, refine, o)) {
+      for (int i = 0; i < kLinW; ++i) o[i] = (R)0;
+      continue;
+    }
+    const double w = (double)o[26];
+    const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+    const double e0 = o[24], e1 = o[25];
+    V[0] += (j0 * j0 + j3 * j3) * w;
+    V[1] += (j0 * j1 + j3 * j4) * w;
+    V[2] += (j0 * j2 + j3 * j5) * w;
+    V[3] += (j1 * j1 + j4 * j4) * w;
+    V[4] += (j1 * j2 + j4 * j5) * w;
+    V[5] += (j2 * j2 + j5 * j5) * w;
+    v[0] += (j0 * e0 + j3 * e1) * w;
+    v[1] += (j1 * e0 + j4 * e1) * w;
+    v[2] += (j2 * e0 + j5 * e1) * w;
+  }
+  double A[9], Ai[9];
+  sym3_full(V, A);
+  A[0] = A[0] * (1.0 + lam) + 1e-9;  // ba.rs:262-264
+  A[4] = A[4] * (1.0 + lam) + 1e-9;
+  A[8] = A[8] * (1.0 + lam) + 1e-9;
+  const bool ok = inv3(A, Ai);  // ba.rs:265
+  B.kept[p] = ok ? 1 : 0;
+  double L[6] = {0, 0, 0, 0, 0, 0};
+  if (ok) chol3(Ai, L);
+  const double l00 = L[0], l10 = L[1], l11 = L[2], l20 = L[3], l21 = L[4], l22 = L[5];
+  const double zv0 = l00 * v[0] + l10 * v[1] + l20 * v[2];
+  const double zv1 = l11 * v[1] + l21 * v[2];
+  const double zv2 = l22 * v[2];
+  // t = V^-1 v = L zv
+  const double t0 = l00 * zv0, t1 = l10 * zv0 + l11 * zv1, t2 = l20 * zv0 + l21 * zv1 + l22 * zv2;
+  R* pl = B.ptL + 6 * (size_t)p;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) pl[i] = (R)L[i];
+  B.ptzv[3 * p] = (R)zv0, B.ptzv[3 * p + 1] = (R)zv1, B.ptzv[3 * p + 2] = (R)zv2;
+  for (uint32_t k = s; k < e; ++k) {
+    const R* o = B.lin + (size_t)k * kLinW;
+    R* Z = B.Z + (size_t)k * 18;
+    R* gs = B.gsub + (size_t)k * 9;
+    if (!ok || o[27] == (R)0) {
+#pragma unroll
+      for (int i = 0; i < 18; ++i) Z[i] = (R)0;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) gs[i] = (R)0;
+      continue;
+    }
+    const double w = (double)o[26];
+    const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      const double ca = o[r], cb = o[6 + r];
+      // Y = (Jc^T Jp) w   (ba.rs:249)
+      const double y0 = (ca * j0 + cb * j3) * w;
+      const double y1 = (ca * j1 + cb * j4) * w;
+      const double y2 = (ca * j2 + cb * j5) * w;
+      Z[3 * r + 0] = (R)(y0 * l00 + y1 * l10 + y2 * l20);
+      Z[3 * r + 1] = (R)(y1 * l11 + y2 * l21);
+      Z[3 * r + 2] = (R)(y2 * l22);
+      gs[r] = (R)(y0 * t0 + y1 * t1 + y2 * t2);
+    }
+    // w Jg^T (Jp t)
+    const double pt0 = j0 * t0 + j1 * t1 + j2 * t2, pt1 = j3 * t0 + j4 * t1 + j5 * t2;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      gs[6 + a] = (R)(((double)o[18 + a] * pt0 + (double)o[21 + a] * pt1) * w);
+  }
+  // Lens entries: Y_g = sum over the point's observations in group g (ba.rs:251-259).
+  const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
+  for (uint32_t j = l0; j < l1; ++j) {
+    double Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t k = s; k < e; ++k) {
+      if (S.obs_lens[k] != j) continue;
+      const R* o = B.lin + (size_t)k * kLinW;
+      if (o[27] == (R)0) continue;
+      const double w = (double)o[26];
+      const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const double ga = o[18 + a], gb = o[21 + a];
+        Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
+        Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
+        Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
+      }
+    }
+    R* Zl = B.Zl + (size_t)j * 9;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
+      Zl[3 * a + 0] = (R)(ok ? y0 * l00 + y1 * l10 + y2 * l20 : 0.0);
+      Zl[3 * a + 1] = (R)(ok ? y1 * l11 + y2 * l21 : 0.0);
+      Zl[3 * a + 2] = (R)(ok ? y2 * l22 : 0.0);
+    }
+  }
+}
+
+// ---- per camera: U, g, lens terms (ba.rs:273-292) ----------------------------
+
+constexpr int kCamThreads = 128;
+constexpr int kCamN = 63;  // 21 U | 6 gj | 6 gs | 18 X | 6 lU | 3 lg | 3 ls
+
+template <typename R>
+__global__ void __launch_bounds__(kCamThreads)
+    camera_kernel(Prob P, StructView S, IterBufs<R> B, const int32_t* active) {
+  __shared__ double scratch[kCamN * 32];
+  const int64_t c = blockIdx.x;
+  if (c >= P.nc) return;
+  const uint32_t m = P.cam_model[c];
+  if (!active[m]) return;
+  const bool refine = P.model_refine[m] != 0;
+  double acc[kCamN];
+#pragma unroll
+  for (int i = 0; i < kCamN; ++i) acc[i] = 0.0;
+  const uint32_t b = S.cam_ptr[c], e = S.cam_ptr[c + 1];
+  for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const uint32_t k = S.cam_obs[i];
+    const R* o = B.lin + (size_t)k * kLinW;
+    if (o[27] == (R)0 || !B.kept[P.obs_pt[k]]) continue;  // ba.rs:274-277
+    const double w = (double)o[26];
+    const double e0 = o[24], e1 = o[25];
+    double jc[12];
+#pragma unroll
+    for (int t = 0; t < 12; ++t) jc[t] = o[t];
+    int u = 0;
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+      for (int bb = a; bb < 6; ++bb) acc[u++] += (jc[a] * jc[bb] + jc[6 + a] * jc[6 + bb]) * w;
+    const R* gs = B.gsub + (size_t)k * 9;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      acc[21 + a] += (jc[a] * e0 + jc[6 + a] * e1) * w;
+      acc[27 + a] += (double)gs[a];
+    }
+    if (refine) {
+      const double g0 = o[18], g1 = o[19], g2 = o[20], g3 = o[21], g4 = o[22], g5 = o[23];
+      const double jg[6] = {g0, g1, g2, g3, g4, g5};
+#pragma unroll
+      for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+          acc[33 + 3 * a + bb] += (jc[a] * jg[bb] + jc[6 + a] * jg[3 + bb]) * w;
+      int v = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = a; bb < 3; ++bb) acc[51 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        acc[57 + a] += (jg[a] * e0 + jg[3 + a] * e1) * w;
+        acc[60 + a] += (double)gs[6 + a];
+      }
+    }
+  }
+  block_sum<kCamN>(acc, scratch);
+  if (threadIdx.x == 0) {
+    double* U = B.camU + 21 * c;
+    for (int i = 0; i < 21; ++i) U[i] = acc[i];
+    for (int i = 0; i < 6; ++i) B.camgj[6 * c + i] = acc[21 + i], B.camgs[6 * c + i] = acc[27 + i];
+    for (int i = 0; i < 18; ++i) B.camX[18 * c + i] = acc[33 + i];
+    for (int i = 0; i < 12; ++i) B.caml[12 * c + i] = acc[51 + i];
+  }
+}
+
+// ---- per lens group: sum of its cameras' lens terms, in camera order ---------
+
+static __global__ void __launch_bounds__(128)
+    group_kernel(Prob P, StructView S, const double* caml, double* grpU, double* grpg,
+                 const int32_t* active) {
+  const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= P.ng) return;
+  if (!active[P.blk_model[P.grp_blk[g]]]) return;
+  double acc[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) acc[i] = 0.0;
+  for (uint32_t i = S.grp_ptr[g] + lane; i < S.grp_ptr[g + 1]; i += 32) {
+    const double* l = caml + 12 * (size_t)S.grp_cams[i];
+#pragma unroll
+    for (int t = 0; t < 12; ++t) acc[t] += l[t];
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) acc[i] = warp_sum(acc[i]);
+  if (lane == 0) {
+    for (int i = 0; i < 6; ++i) grpU[6 * g + i] = acc[i];
+    for (int i = 0; i < 3; ++i) grpg[3 * g + i] = acc[6 + i] - acc[9 + i];
+  }
+}
+
+// ---- robust cost (ba.rs:103-128), per model ---------------------------------
+
+constexpr int kCostThreads = 256;
+
+static __global__ void __launch_bounds__(kCostThreads)
+    cost_chunk_kernel(Prob P, StateView st, StructView S, double* part, const int32_t* active,
+                      const double* sigma) {
+  __shared__ double scratch[3 * 32];
+  const int64_t ch = blockIdx.x;
+  if (ch >= S.ncost) return;
+  const uint32_t m = S.cost_chunk_model[ch];
+  if (active && !active[m]) return;
+  const double sg = sigma[m];
+  const double behind = sg * sg * 10.0;  // ba.rs:116
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (uint32_t k = S.cost_chunk_begin[ch] + threadIdx.x; k < S.cost_chunk_end[ch];
+       k += blockDim.x) {
+    const uint32_t cam = P.obs_cam[k];
+    double u[2];
+    if (bacam::project(st.rot + 9 * (size_t)cam, st.center + 3 * (size_t)cam,
+                       st.intr + 5 * (size_t)P.cam_group[cam],
+                       st.points + 3 * (size_t)P.obs_pt[k], u)) {
+      const double ex = P.obs_uv[2 * (size_t)k] - u[0], ey = P.obs_uv[2 * (size_t)k + 1] - u[1];
+      const double e2 = ex * ex + ey * ey;
+      acc[0] += robust_rho(e2, sg, P.loss);
+      acc[1] += e2;
+      acc[2] += 1.0;
+    } else {
+      acc[0] += behind;
+    }
+  }
+  block_sum<3>(acc, scratch);
+  if (threadIdx.x == 0) {
+    part[3 * ch] = acc[0];
+    part[3 * ch + 1] = acc[1];
+    part[3 * ch + 2] = acc[2];
+  }
+}
+
+// Warp per model: chunk partials in order, plus the GPS prior term.
+static __global__ void cost_final_kernel(Prob P, StateView st, StructView S, const double* part,
+                                  const int32_t* active, double* cost, double* sq,
+                                  int64_t* n_front) {
+  const int64_t m = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (m >= P.nm) return;
+  if (active && !active[m]) return;
+  double a[3] = {0.0, 0.0, 0.0};
+  for (uint32_t c = S.model_chunk0[m] + lane; c < S.model_chunk0[m + 1]; c += 32)
+    for (int i = 0; i < 3; ++i) a[i] += part[3 * (size_t)c + i];
+  double pr = 0.0;
+  if (P.prior_mask) {
+    for (uint32_t c = P.model_cam0[m] + lane; c < P.model_cam0[m + 1]; c += 32) {
+      if (!P.prior_mask[c]) continue;
+      const double* q = P.prior + 6 * (size_t)c;
+      const double dx = st.center[3 * (size_t)c] - q[0];
+      const double dy = st.center[3 * (size_t)c + 1] - q[1];
+      const double dz = st.center[3 * (size_t)c + 2] - q[2];
+      pr += (dx / q[3]) * (dx / q[3]) + (dy / q[4]) * (dy / q[4]) + (dz / q[5]) * (dz / q[5]);
+    }
+  }
+  for (int i = 0; i < 3; ++i) a[i] = warp_sum(a[i]);
+  pr = warp_sum(pr);
+  if (lane == 0) {
+    cost[m] = a[0] + pr;
+    sq[m] = a[1];
+    n_front[m] = (int64_t)a[2];
+  }
+}
+
+// ---- LM accept / reject (ba.rs:367-383), thread per model --------------------
+
+static __global__ void control_kernel(int64_t nm, Control C) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nm) return;
+  if (!C.active[m]) {
+    C.accepted[m] = 0;
+    return;
+  }
+  const int32_t it = C.iters[m];
+  C.iters[m] = it + 1;
+  C.pcg_total[m] += C.pcg_iters[m];
+  const double nc = C.new_cost[m], c = C.cost[m], lam = C.lambda[m];
+  int32_t act = 1, acc = 0;
+  if (nc < c) {
+    acc = 1;
+    const double rel = (c - nc) / fmax(c, 1e-12);
+    C.cost[m] = nc;
+    C.lambda[m] = fmax(lam / 3.0, 1e-9);
+    if (rel < 1e-6) act = 0;
+  } else {
+    C.lambda[m] = lam * 5.0;
+    if (C.lambda[m] > 1e6) act = 0;
+  }
+  if (it + 1 >= C.max_iter) act = 0;
+  C.accepted[m] = acc;
+  C.active[m] = act;
+  if (act) atomicOr(C.any_active, 1);
+  if (m == 0 && it < C.log_cap) {
+    C.log_new_cost[it] = nc;
+    C.log_lambda[it] = lam;
+    C.log_pcg[it] = C.pcg_iters[m];
+    C.log_accept[it] = acc;
+  }
+}
+
+// Copy the trial state of accepted models over the current state.
+static __global__ void commit_kernel(Prob P, const uint32_t* grp_model, StateView cur, StateView trial,
+                              const int32_t* accepted) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < P.np && accepted[P.pt_model[i]])
+    for (int a = 0; a < 3; ++a) cur.points[3 * i + a] = trial.points[3 * i + a];
+  if (i < P.nc && accepted[P.cam_model[i]]) {
+    for (int a = 0; a < 9; ++a) cur.rot[9 * i + a] = trial.rot[9 * i + a];
+    for (int a = 0; a < 3; ++a) cur.center[3 * i + a] = trial.center[3 * i + a];
+  }
+  if (i < P.ng && accepted[grp_model[i]])
+    for (int a = 0; a < 5; ++a) cur.intr[5 * i + a] = trial.intr[5 * i + a];
+}
+
+// ---- Schur sums: warp per sub-segment of one destination block ---------------
+
+template <typename R>
+__device__ __forceinline__ void load_Z(const IterBufs<R>& B, int64_t no, uint32_t eid, R* z) {
+  if ((int64_t)eid < no) {
+    const R* s = B.Z + (size_t)eid * 18;
+#pragma unroll
+    for (int i = 0; i < 18; ++i) z[i] = s[i];
+  } else {
+    const R* s = B.Zl + (size_t)(eid - no) * 9;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) z[i] = s[i];
+#pragma unroll
+    for (int i = 9; i < 18; ++i) z[i] = (R)0;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256)
+    schur_kernel(Prob P, StructView S, IterBufs<R> B, const int32_t* active) {
+  const int64_t sub = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (sub >= S.nsub) return;
+  const uint32_t slot = S.sub_slot[sub];
+  if (!active[P.blk_model[S.slot_row[slot]]]) return;
+  R acc[36];
+#pragma unroll
+  for (int i = 0; i < 36; ++i) acc[i] = (R)0;
+  const uint32_t b = S.sub_begin[sub], e = S.sub_end[sub];
+  for (uint32_t i = b + lane; i < e; i += 32) {
+    const uint64_t pr = S.pairs[i];
+    if (pr == kSentinel) continue;
+    if ((int64_t)(pr & 0xffffffffu) >= P.no + S.nl || (int64_t)(pr >> 32) >= P.no + S.nl) continue;
+    R za[18], zb[18];
+    load_Z(B, P.no, (uint32_t)(pr & 0xffffffffu), za);
+    load_Z(B, P.no, (uint32_t)(pr >> 32), zb);
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+        acc[6 * r + c] += za[3 * r] * zb[3 * c] + za[3 * r + 1] * zb[3 * c + 1] +
+                          za[3 * r + 2] * zb[3 * c + 2];
+  }
+#pragma unroll
+  for (int i = 0; i < 36; ++i) acc[i] = warp_sum(acc[i]);
+  if (lane == 0) {
+    R* o = B.part + (size_t)sub * 36;
+#pragma unroll
+    for (int i = 0; i < 36; ++i) o[i] = acc[i];
+  }
+}
+
+// ---- assemble S and g (ba.rs:293-331) ----------------------------------------
+
+template <typename R>
+__global__ void assemble_kernel(Prob P, StateView st, StructView S, IterBufs<R> B,
+                                const int32_t* active, const double* lambda) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.ns * 36) return;
+  const int64_t s = t / 36;
+  const int el = (int)(t % 36), r = el / 6, c = el % 6;
+  const uint32_t a = S.slot_row[s], bcol = S.slot_col[s];
+  const uint32_t m = P.blk_model[a];
+  if (!active[m]) return;
+  R sum = (R)0;
+  for (uint32_t u = S.slot_sub_ptr[s]; u < S.slot_sub_ptr[s + 1]; ++u)
+    sum += B.part[(size_t)u * 36 + el];
+  double val;
+  const bool lens_a = P.blk_is_lens[a] != 0;
+  if (a == bcol) {
+    const double lam = lambda[m];
+    double u = 0.0;
+    const uint32_t id = P.blk_id[a];
+    const int i0 = r < c ? r : c, i1 = r < c ? c : r;
+    if (!lens_a) {
+      const int idx = i0 * 6 - (i0 * (i0 - 1)) / 2 + (i1 - i0);
+      u = B.camU[21 * (size_t)id + idx];
+      if (r == c && r >= 3 && P.prior_mask && P.prior_mask[id]) {
+        const double sd = P.prior[6 * (size_t)id + r];
+        u += 1.0 / (sd * sd);  // ba.rs:297-302
+      }
+      if (r == c) u = u * (1.0 + lam) + 1e-9;  // ba.rs:306-309
+    } else {
+      if (i1 < 3) u = B.grpU[6 * (size_t)id + (i0 * 3 - (i0 * (i0 - 1)) / 2 + (i1 - i0))];
+      if (r == c) u = u * (1.0 + lam) + 1e-9;
+      if (r == c && r >= 3) u = 1.0;  // ba.rs:310-314
+      if (!P.model_refine[m]) u = (r == c) ? 1.0 : 0.0;  // ba.rs:315-317
+    }
+    val = u - (double)sum;
+  } else {
+    double x = 0.0;
+    if (!lens_a && P.blk_is_lens[bcol] && c < 3) {
+      const uint32_t cam = P.blk_id[a];
+      if (P.grp_blk[P.cam_group[cam]] == bcol) x = B.camX[18 * (size_t)cam + 3 * r + c];
+    }
+    val = x - (double)sum;
+  }
+  const uint32_t pab = S.slot_pos_ab[s], pba = S.slot_pos_ba[s];
+  if (pab < S.nz) B.S[(size_t)pab * 36 + 6 * r + c] = (R)val;
+  if (a != bcol && pba < S.nz) B.S[(size_t)pba * 36 + 6 * c + r] = (R)val;
+}
+
+template <typename R>
+__global__ void rhs_kernel(Prob P, StateView st, IterBufs<R> B, const int32_t* active) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P.nb * 6) return;
+  const int64_t b = t / 6;
+  const int i = (int)(t % 6);
+  const uint32_t m = P.blk_model[b];
+  if (!active[m]) return;
+  const uint32_t id = P.blk_id[b];
+  double gv;
+  if (!P.blk_is_lens[b]) {
+    gv = B.camgj[6 * (size_t)id + i];
+    if (i >= 3 && P.prior_mask && P.prior_mask[id]) {
+      const double sd = P.prior[6 * (size_t)id + i];
+      gv += (1.0 / (sd * sd)) * (P.prior[6 * (size_t)id + i - 3] - st.center[3 * (size_t)id + i - 3]);
+    }
+    gv -= B.camgs[6 * (size_t)id + i];
+  } else {
+    gv = i < 3 ? B.grpg[3 * (size_t)id + i] : 0.0;
+  }
+  B.g[6 * b + i] = (R)gv;
+}
+
+template <typename R>
+__global__ void precond_kernel(Prob P, StructView S, IterBufs<R> B, const int32_t* active) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= P.nb) return;
+  if (!active[P.blk_model[b]]) return;
+  double A[36], Ai[36];
+  const R* d = B.S + (size_t)S.diag_pos[b] * 36;
+#pragma unroll
+  for (int i = 0; i < 36; ++i) A[i] = (double)d[i];
+  if (!inv6(A, Ai)) {  // ba.rs:159-160
+#pragma unroll
+    for (int i = 0; i < 36; ++i) Ai[i] = (i % 7 == 0) ? 1.0 : 0.0;
+  }
+  double* o = B.pre + 36 * (size_t)b;
+#pragma unroll
+  for (int i = 0; i < 36; ++i) o[i] = Ai[i];
+}
+
+// ---- update (ba.rs:338-366) ---------------------------------------------------
+
+template <typename R>
+__global__ void update_cameras_kernel(Prob P, StateView cur, StateView trial, IterBufs<R> B,
+                                      const int32_t* active) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < P.nc && active[P.cam_model[i]]) {
+    const R* d = B.x + 6 * (size_t)P.cam_blk[i];
+    const double w[3] = {(double)d[0], (double)d[1], (double)d[2]};
+    double E[9];
+    bacam::exp_so3(w, E);
+    bacam::matmul3(E, cur.rot + 9 * i, trial.rot + 9 * i);
+    for (int a = 0; a < 3; ++a) trial.center[3 * i + a] = cur.center[3 * i + a] + (double)d[3 + a];
+  }
+  if (i < P.ng) {
+    const uint32_t b = P.grp_blk[i];
+    const uint32_t m = P.blk_model[b];
+    if (active[m]) {
+      for (int a = 0; a < 5; ++a) trial.intr[5 * i + a] = cur.intr[5 * i + a];
+      if (P.model_refine[m]) {
+        const R* d = B.x + 6 * (size_t)b;
+        trial.intr[5 * i + 0] += (double)d[0];
+        trial.intr[5 * i + 3] += (double)d[1];
+        trial.intr[5 * i + 4] += (double)d[2];
+      }
+    }
+  }
+}
+
+template <typename R>
+__global__ void backsub_kernel(Prob P, StructView S, StateView cur, StateView trial,
+                               IterBufs<R> B, const int32_t* active) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.np) return;
+  if (!active[P.pt_model[p]]) return;
+  const double* X = cur.points + 3 * p;
+  double* Xt = trial.points + 3 * p;
+  if (!B.kept[p]) {
+    Xt[0] = X[0], Xt[1] = X[1], Xt[2] = X[2];
+    return;
+  }
+  double a0 = B.ptzv[3 * p], a1 = B.ptzv[3 * p + 1], a2 = B.ptzv[3 * p + 2];
+  const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
+  for (uint32_t k = s; k < e; ++k) {
+    const R* Z = B.Z + (size_t)k * 18;
+    const R* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      const double dr = (double)d[r];
+      a0 -= (double)Z[3 * r] * dr;
+      a1 -= (double)Z[3 * r + 1] * dr;
+      a2 -= (double)Z[3 * r + 2] * dr;
+    }
+  }
+  for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j) {
+    const R* Z = B.Zl + (size_t)j * 9;
+    const R* d = B.x + 6 * (size_t)P.grp_blk[S.lens_grp[j]];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const double dr = (double)d[r];
+      a0 -= (double)Z[3 * r] * dr;
+      a1 -= (double)Z[3 * r + 1] * dr;
+      a2 -= (double)Z[3 * r + 2] * dr;
+    }
+  }
+  const R* L = B.ptL + 6 * p;
+  const double l00 = L[0], l10 = L[1], l11 = L[2], l20 = L[3], l21 = L[4], l22 = L[5];
+  Xt[0] = X[0] + l00 * a0;
+  Xt[1] = X[1] + (l10 * a0 + l11 * a1);
+  Xt[2] = X[2] + (l20 * a0 + l21 * a1 + l22 * a2);
+}
+
+}  // namespace ba

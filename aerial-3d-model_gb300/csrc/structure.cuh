@@ -1,0 +1,30 @@
+// Per-call structure builder (see structure.cu).
+#pragma once
+
+#include <vector>
+
+#include "solver.cuh"
+
+namespace ba {
+
+struct StructBufs {
+  DevBuf<uint32_t> pt_ptr, cam_ptr, cam_obs, grp_ptr, grp_cams, lens_ptr, lens_grp, obs_lens;
+  DevBuf<uint64_t> pairs;
+  DevBuf<uint32_t> slot_ptr, slot_row, slot_col, slot_pos_ab, slot_pos_ba;
+  DevBuf<uint32_t> sub_slot, sub_begin, sub_end, slot_sub_ptr;
+  DevBuf<uint32_t> row_ptr, col_idx, diag_pos;
+  DevBuf<uint32_t> cost_chunk_model, cost_chunk_begin, cost_chunk_end, model_chunk0;
+  int64_t nl = 0, npairs = 0, ns = 0, nsub = 0, nz = 0, ncost = 0;
+  std::vector<uint32_t> h_row_ptr;
+  StructView view() const;
+};
+
+void validate_problem(const Prob& P, const uint32_t* grp_model, uint32_t* d_err,
+                      cudaStream_t s);
+// Observations by camera (cam_ptr, cam_obs) and cameras by group (grp_ptr,
+// grp_cams), both stable.
+void build_cam_index(const Prob& P, StructBufs& S, cudaStream_t s);
+void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, StructBufs& S,
+                     uint32_t* err, cudaStream_t s);
+
+}  // namespace ba

@@ -1,0 +1,281 @@
+"""``bundle_adjust`` — the drop-in for stitch-core's entry point
+``pub fn bundle_adjust(p: &mut Problem, max_iter: usize, sigma_px: f64) -> BaStats``
+(crates/stitch-core/src/recon/ba.rs:198), running on the GPU through the C
+ABI of ``libba_gb300.so``.
+
+Same argument meaning and the same in-place update of the problem's state as
+the reference.  Unlike the reference (which cannot fail), invalid input raises
+``BaError`` with status BAD_INPUT, and a missing GPU raises instead of falling
+back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native
+from .problem import BaStats, Problem
+
+
+@dataclass
+class Options:
+    """Solver options beyond the reference's (max_iter, sigma_px).
+
+    Defaults reproduce the reference: Cauchy loss (ba.rs:99,114), FP64, PCG
+    with at most 400 products (ba.rs:334) and |r|² < 1e-20 |b|² (ba.rs:182)."""
+    loss: str = "cauchy"          # "cauchy" | "huber"
+    precision: str = "fp64"       # "fp64" | "mixed"
+    pcg_max_iter: int = 400
+    pcg_tol: float = 1e-20
+    matrix_free: str = "auto"     # "auto" | "stored" | "matrix_free"
+    memory_cap_bytes: int = 0
+    stream: int | None = None     # cudaStream_t as an integer handle
+    profile: bool = False         # per-phase CUDA-event timing (SolveInfo.phases)
+
+
+@dataclass
+class SolveInfo:
+    """Everything ba_stats reports, plus the per-iteration log (model 0)."""
+    iterations: int
+    initial_rms: float
+    final_rms: float
+    initial_cost: float
+    final_cost: float
+    pcg_iterations: int
+    kernel_launches: int
+    ms_total: float
+    ms_h2d: float
+    ms_d2h: float
+    h2d_bytes: int
+    d2h_bytes: int
+    device_bytes: int
+    new_cost: np.ndarray = field(default=None, repr=False)
+    lam: np.ndarray = field(default=None, repr=False)
+    pcg_iters: np.ndarray = field(default=None, repr=False)
+    accepted: np.ndarray = field(default=None, repr=False)
+    phases: dict = field(default_factory=dict, repr=False)  # name -> (ms, launches)
+    sizes: dict = field(default_factory=dict, repr=False)   # reduced-system sizes
+
+    def stats(self) -> BaStats:
+        return BaStats(self.iterations, self.initial_rms, self.final_rms)
+
+
+_MF = {"auto": 0, "stored": 1, "matrix_free": 2}
+
+
+def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> native.BaOptions:
+    o = o or Options()
+    c = native.BaOptions()
+    native.load().ba_default_options(C.byref(c))
+    c.max_iter = int(max_iter)
+    c.sigma_px = float(sigma_px)
+    c.loss = native.LOSS[o.loss]
+    c.precision = native.PRECISION[o.precision]
+    c.pcg_max_iter = int(o.pcg_max_iter)
+    c.pcg_tol = float(o.pcg_tol)
+    c.matrix_free = _MF[o.matrix_free]
+    c.memory_cap_bytes = int(o.memory_cap_bytes)
+    c.stream = o.stream
+    c.profile = 1 if o.profile else 0
+    c.log = C.cast(C.pointer(log), C.c_void_p) if log is not None else None
+    return c
+
+
+def _arr(a, dtype):
+    if a is None:
+        return None
+    if not (isinstance(a, np.ndarray) and a.dtype == dtype and a.flags.c_contiguous):
+        raise TypeError(f"expected a C-contiguous {np.dtype(dtype)} array")
+    return a.ctypes.data
+
+
+def c_views(p: Problem):
+    """(ba_problem, ba_state) views of a Problem's arrays (no copies)."""
+    for name, dt in (("rot", np.float64), ("center", np.float64), ("intr", np.float64),
+                     ("points", np.float64)):
+        a = getattr(p, name)
+        if not (a.dtype == dt and a.flags.c_contiguous and a.flags.writeable):
+            raise TypeError(f"Problem.{name} must be a writeable C-contiguous float64 array")
+    prob = native.BaProblem(
+        p.n_cams, p.n_points, p.n_obs, p.n_groups, _arr(p.obs_cam, np.uint32),
+        _arr(p.obs_pt, np.uint32), _arr(p.obs_uv, np.float64), _arr(p.cam_group, np.uint32),
+        _arr(p.prior_mask, np.uint8), _arr(p.prior, np.float64) if p.prior_mask is not None else None,
+        1 if p.refine_intrinsics else 0)
+    st = native.BaState(p.rot.ctypes.data, p.center.ctypes.data, p.intr.ctypes.data,
+                        p.points.ctypes.data)
+    return prob, st
+
+
+def _info(s: native.BaStatsC) -> SolveInfo:
+    info = SolveInfo(s.iterations, s.initial_rms, s.final_rms, s.initial_cost, s.final_cost,
+                     s.pcg_iterations, s.kernel_launches, s.ms_total, s.ms_h2d, s.ms_d2h,
+                     s.h2d_bytes, s.d2h_bytes, s.device_bytes)
+    info.phases = {n: (s.ms_phase[i], s.n_phase[i]) for i, n in enumerate(native.PHASES)
+                   if s.n_phase[i]}
+    info.sizes = dict(blocks=s.n_blocks, nonzero_blocks=s.n_nonzero_blocks,
+                      schur_pairs=s.n_schur_pairs, lens_entries=s.n_lens_entries)
+    return info
+
+
+class _Log:
+    def __init__(self, cap: int):
+        self.new_cost = np.zeros(cap)
+        self.lam = np.zeros(cap)
+        self.pcg = np.zeros(cap, np.int32)
+        self.acc = np.zeros(cap, np.int32)
+        self.c = native.BaLog(cap, self.new_cost.ctypes.data, self.lam.ctypes.data,
+                              self.pcg.ctypes.data, self.acc.ctypes.data)
+
+    def attach(self, info: SolveInfo):
+        n = int(info.iterations)
+        info.new_cost, info.lam = self.new_cost[:n].copy(), self.lam[:n].copy()
+        info.pcg_iters, info.accepted = self.pcg[:n].copy(), self.acc[:n].astype(bool)
+
+
+def bundle_adjust(p: Problem, max_iter: int, sigma_px: float, options: Options | None = None,
+                  *, return_info: bool = False):
+    """ba.rs:198.  Mutates p.rot, p.center, p.points (and p.intr when
+    refining) in place; returns BaStats (and SolveInfo if asked)."""
+    L = native.load()
+    log = _Log(max(int(max_iter), 1))
+    opt = _c_options(max_iter, sigma_px, options, log.c)
+    prob, st = c_views(p)
+    out = native.BaStatsC()
+    native.check(L.ba_solve(C.byref(prob), C.byref(st), C.byref(opt), C.byref(out)))
+    info = _info(out)
+    log.attach(info)
+    return (info.stats(), info) if return_info else info.stats()
+
+
+def bundle_adjust_batch(problems: list[Problem], max_iter: int, sigma_px: float,
+                        options: Options | None = None) -> list[SolveInfo]:
+    """Solve independent problems in one batched launch sequence."""
+    L = native.load()
+    n = len(problems)
+    views = [c_views(p) for p in problems]
+    probs = (native.BaProblem * n)(*[v[0] for v in views])
+    states = (native.BaState * n)(*[v[1] for v in views])
+    stats = (native.BaStatsC * n)()
+    opt = _c_options(max_iter, sigma_px, options)
+    native.check(L.ba_solve_batch(probs, states, n, C.byref(opt), stats))
+    return [_info(s) for s in stats]
+
+
+class Context:
+    """Device-resident problems: upload once, solve repeatedly from the
+    uploaded initial state, download the solution."""
+
+    def __init__(self, device: int = -1, stream: int | None = None):
+        self._L = native.load()
+        h = C.c_void_p()
+        native.check(self._L.ba_context_create(device, stream, C.byref(h)))
+        self._h = h
+        self._n = 0
+        self._problems = []
+
+    def close(self):
+        if self._h:
+            self._L.ba_context_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, problems: list[Problem] | Problem):
+        if isinstance(problems, Problem):
+            problems = [problems]
+        views = [c_views(p) for p in problems]
+        n = len(problems)
+        probs = (native.BaProblem * n)(*[v[0] for v in views])
+        states = (native.BaState * n)(*[v[1] for v in views])
+        native.check(self._L.ba_context_upload(self._h, probs, states, n))
+        self._n = n
+        self._problems = list(problems)
+
+    def solve(self, max_iter: int, sigma_px: float, options: Options | None = None,
+              log: bool = False) -> list[SolveInfo]:
+        lg = _Log(max(int(max_iter), 1)) if log else None
+        opt = _c_options(max_iter, sigma_px, options, lg.c if lg else None)
+        stats = (native.BaStatsC * self._n)()
+        native.check(self._L.ba_context_solve(self._h, C.byref(opt), stats))
+        infos = [_info(s) for s in stats]
+        if lg:
+            lg.attach(infos[0])
+        return infos
+
+    def download(self, problems: list[Problem] | Problem | None = None):
+        problems = self._problems if problems is None else problems
+        if isinstance(problems, Problem):
+            problems = [problems]
+        states = (native.BaState * len(problems))(*[c_views(p)[1] for p in problems])
+        native.check(self._L.ba_context_download(self._h, states, len(problems)))
+
+    def cost(self, sigma_px: float, options: Options | None = None):
+        c = np.zeros(self._n)
+        r = np.zeros(self._n)
+        n = np.zeros(self._n, np.int64)
+        opt = _c_options(0, sigma_px, options)
+        native.check(self._L.ba_context_cost(self._h, C.byref(opt), c.ctypes.data, r.ctypes.data,
+                                             n.ctypes.data))
+        return c, r, n
+
+    def linearise(self, sigma_px: float, options: Options | None = None):
+        no = sum(p.n_obs for p in self._problems)
+        e = np.zeros((no, 2))
+        jc = np.zeros((no, 2, 6))
+        jg = np.zeros((no, 2, 3))
+        jp = np.zeros((no, 2, 3))
+        w = np.zeros(no)
+        valid = np.zeros(no, np.uint8)
+        opt = _c_options(0, sigma_px, options)
+        native.check(self._L.ba_context_linearise(
+            self._h, C.byref(opt), e.ctypes.data, jc.ctypes.data, jg.ctypes.data, jp.ctypes.data,
+            w.ctypes.data, valid.ctypes.data))
+        return dict(e=e, jc=jc, jg=jg, jp=jp, w=w, valid=valid.astype(bool))
+
+    def vjp(self, sigma_px: float, cot_obs=None, cot_prior=None, options: Options | None = None):
+        nc = sum(p.n_cams for p in self._problems)
+        npt = sum(p.n_points for p in self._problems)
+        ng = sum(p.n_groups for p in self._problems)
+        gc, gp, gi = np.zeros((nc, 6)), np.zeros((npt, 3)), np.zeros((ng, 5))
+        co = None if cot_obs is None else np.ascontiguousarray(cot_obs, np.float64)
+        cp = None if cot_prior is None else np.ascontiguousarray(cot_prior, np.float64)
+        opt = _c_options(0, sigma_px, options)
+        native.check(self._L.ba_context_vjp(
+            self._h, C.byref(opt), None if co is None else co.ctypes.data,
+            None if cp is None else cp.ctypes.data, gc.ctypes.data, gp.ctypes.data,
+            gi.ctypes.data))
+        return gc, gp, gi
+
+    def debug_step(self, lam: float, sigma_px: float, options: Options | None = None,
+                   dense: bool = True):
+        """One LM system at damping `lam` from the uploaded state (single
+        model): dense S, g, dx, PCG iterations, trial cost."""
+        p = self._problems[0]
+        nb = p.n_cams + p.n_groups
+        S = np.zeros((6 * nb, 6 * nb)) if dense else None
+        g, dx = np.zeros(6 * nb), np.zeros(6 * nb)
+        it, tc = C.c_int32(), C.c_double()
+        opt = _c_options(1, sigma_px, options)
+        native.check(self._L.ba_context_debug_step(
+            self._h, C.byref(opt), float(lam), None if S is None else S.ctypes.data,
+            g.ctypes.data, dx.ctypes.data, C.byref(it), C.byref(tc)))
+        return dict(S=S, g=g, dx=dx, pcg_iters=it.value, trial_cost=tc.value)
+
+    def intrinsics_grad(self, sigma_px: float, options: Options | None = None) -> np.ndarray:
+        ng = sum(p.n_groups for p in self._problems)
+        g = np.zeros((ng, 5))
+        opt = _c_options(0, sigma_px, options)
+        native.check(self._L.ba_context_intrinsics_grad(self._h, C.byref(opt), g.ctypes.data))
+        return g

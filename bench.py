@@ -1,0 +1,402 @@
+"""Benchmark: GPS-aided bundle adjustment solve throughput on one GB300.
+
+Workload (default ``single500``): one synthetic lawnmower survey with 500
+cameras, 400k points and ~3M observations (seeded, see
+aerial-3d-model_gb300/stitch_ba/survey.py), Cauchy loss at 1 px, GPS priors,
+refine_intrinsics, max_iter 60 (the reference's own test call, ba.rs:482).
+A step is one full ``bundle_adjust`` solve of that survey from its perturbed
+initial state.
+
+* ``value``  — solves/s with the problem already resident in HBM
+  (``ba_context_solve``: structure build, every LM iteration, PCG, updates),
+  timed with CUDA events on the solver's stream, L2 flushed between steps.
+* ``e2e``    — solves/s through the reference-facing C ABI ``ba_solve`` with
+  host (pinned) buffers: H2D of the problem, the solve and D2H of the state
+  are inside the timed region.
+* ``forms``  — FP64 plain form and FP32/FP64 mixed form side by side, with the
+  final cost of each and their relative difference.
+* ``roofline`` — the dominant kernel phase (by device time, from the
+  solver's own CUDA-event phase timing) against measured HBM bandwidth.
+* ``cpu_baseline`` — the oracle (a CPU restatement of the reference solver,
+  same data structures, OpenMP on all host cores) on a bounded sample: the
+  first LM iterations of the same solve, scaled to solves/s by the full
+  solve's iteration count.
+
+``--impl reference`` times that CPU solver alone as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "aerial-3d-model_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "BA solve time & kernel HBM GB/s, mixed vs FP64 GPU at equal final cost"
+UNIT = "solves/s"
+SIGMA_PX = 1.0
+MAX_ITER = 60
+# Per LM iteration, algorithmic bytes of each phase, written as a function of
+# the problem sizes and the storage width s (8 FP64 / 4 FP32): reads and writes
+# each kernel must make at minimum.
+#   point : obs (cam u32, pt u32, uv 2 f64) + params (cams 12 f64, points 3 f64)
+#           → lin record 28 s + Z 18 s + gsub 9 s per obs, L 6 s + zv 3 s per point
+#   camera: read lin 28 s + gsub 9 s + index 4 per obs → 63 f64 per camera
+#   schur : per pair contribution 2 entries read (18 s each) + 8 B pair → 36 s per sub-segment
+#   pcg   : per product S (36 s per block + col 4 B) + p gather 6 s per block
+#           + vectors (x, r, z, p, q: ~10 vector passes of 6 s per row) + pre 36·8 per row
+
+
+def algorithmic_bytes(phase: str, sz: dict, s: int, pcg_iters: float = 0.0) -> float:
+    no, np_, nc, nz, nb = sz["n_obs"], sz["n_points"], sz["n_cams"], sz["nz_blocks"], sz["nb"]
+    npairs, nsub = sz["pairs"], sz["subsegments"]
+    if phase == "point":
+        return no * (4 + 4 + 16 + (28 + 18 + 9) * s) + nc * 96 + np_ * (24 + 9 * s)
+    if phase == "camera":
+        return no * (4 + 4 + 37 * s) + nc * 63 * 8
+    if phase == "schur":
+        return npairs * (8 + 36 * s) + nsub * 36 * s
+    if phase == "pcg":
+        per = nz * (36 * s + 4 + 6 * s) + nb * (10 * 6 * s + 36 * 8)
+        return per * pcg_iters
+    return 0.0
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                  "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        while not self._stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            self.samples.append([x.strip() for x in line.split(",")])
+        p.terminate()
+        try:
+            p.wait(timeout=5)
+        except Exception:
+            p.kill()
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        try:
+            sm = [float(s[0]) for s in self.samples]
+            mx = float(self.samples[0][1])
+        except ValueError:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unparsed"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def make_workload(name: str, seed: int):
+    from stitch_ba import survey
+    p, truth = survey.generate(name, seed=seed)
+    return p
+
+
+def pin_problem(p):
+    """Copy a Problem's arrays into page-locked host memory (for e2e)."""
+    import torch
+    from stitch_ba import Problem
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+    return Problem(intr=pin(p.intr), rot=pin(p.rot), center=pin(p.center),
+                   cam_group=pin(p.cam_group), points=pin(p.points), obs_cam=pin(p.obs_cam),
+                   obs_pt=pin(p.obs_pt), obs_uv=pin(p.obs_uv), prior_mask=pin(p.prior_mask),
+                   prior=pin(p.prior), refine_intrinsics=p.refine_intrinsics)
+
+
+def gpu_arm(args, ws, rank):
+    import torch
+    import stitch_ba
+    from stitch_ba import Options, native
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    native.load()
+    p = make_workload(args.workload, args.seed + rank)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(int(256 * 2**20) // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    forms = {}
+    chosen = args.precision
+    precisions = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    profile_info = {}
+    with stitch_ba.Context(device=dev, stream=stream.cuda_stream) as ctx:
+        ctx.upload(p)
+        for prec in precisions:
+            opts = Options(precision=prec)
+            for _ in range(args.warmup):
+                ctx.solve(args.max_iter, SIGMA_PX, opts)
+            torch.cuda.synchronize()
+            times = []
+            info = None
+            with ClockSampler() as clk:
+                barrier()
+                for _ in range(args.steps):
+                    flush.zero_()
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    info = ctx.solve(args.max_iter, SIGMA_PX, opts)[0]
+                    b.record(stream)
+                    b.synchronize()
+                    times.append(a.elapsed_time(b))
+                barrier()
+            ms = float(np.sum(times)) / len(times)
+            if ws > 1:
+                import torch.distributed as dist
+                t = torch.tensor([ms], device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                ms = float(t.item())
+            forms[prec] = dict(ms_per_solve=ms, final_cost=info.final_cost,
+                               initial_cost=info.initial_cost, iterations=info.iterations,
+                               pcg_iterations=info.pcg_iterations, final_rms=info.final_rms,
+                               kernel_launches=info.kernel_launches, clocks=clk.summary())
+            # one profiled solve (phase timing; not part of the timed region)
+            prof = ctx.solve(args.max_iter, SIGMA_PX, Options(precision=prec, profile=True))[0]
+            profile_info[prec] = prof
+    if "fp64" in forms and "mixed" in forms:
+        rel = abs(forms["mixed"]["final_cost"] - forms["fp64"]["final_cost"]) / abs(
+            forms["fp64"]["final_cost"])
+        forms["mixed"]["rel_final_cost_vs_fp64"] = rel
+        chosen = "mixed" if rel <= 1e-6 else "fp64"
+        forms["chosen"] = chosen
+    head = forms[chosen]
+
+    # End to end through the reference-facing C ABI (host buffers, H2D + D2H inside).
+    pp = pin_problem(p)
+    init = pp.state()
+    e2e_times = []
+    e2e_info = None
+    opts = Options(precision=chosen, stream=stream.cuda_stream)
+    for i in range(args.warmup + args.steps):
+        pp.set_state(init)
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st, e2e_info = stitch_ba.bundle_adjust(pp, args.max_iter, SIGMA_PX, opts, return_info=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_times))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank != 0:
+        return None
+    # Roofline of the dominant phase.
+    prof = profile_info[chosen]
+    phases = {k: v for k, v in prof.phases.items() if k != "setup"}
+    dom = max(phases, key=lambda k: phases[k][0])
+    dom_ms, dom_n = phases[dom]
+    zs = prof.sizes
+    sz = dict(n_obs=p.n_obs, n_points=p.n_points, n_cams=p.n_cams, nb=zs["blocks"],
+              nz_blocks=zs["nonzero_blocks"], pairs=zs["schur_pairs"],
+              subsegments=zs["schur_pairs"] // 512 + (zs["nonzero_blocks"] + zs["blocks"]) // 2)
+    s = 8 if chosen == "fp64" else 4
+    per_launch_ms = dom_ms / max(dom_n, 1)
+    if dom == "pcg":
+        bytes_per_launch = algorithmic_bytes("pcg", sz, s, prof.pcg_iterations / max(dom_n, 1))
+    else:
+        bytes_per_launch = algorithmic_bytes(dom, sz, s)
+    peak, peak_kind = load_peaks()
+    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr_path):
+        try:
+            with open(tr_path) as f:
+                traffic = json.load(f).get(f"{args.workload}:{chosen}:{dom}")
+        except Exception:
+            traffic = None
+
+    value = ws * 1000.0 / head["ms_per_solve"]
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": head["ms_per_solve"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if chosen == "fp64" else "f32+f64",
+        "data": "synthetic (seeded survey generator, reference camera model)",
+        "config": {"workload": args.workload, "cameras": p.n_cams, "points": p.n_points,
+                   "observations": p.n_obs, "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
+                   "loss": "cauchy", "precision": chosen, "parallelism": f"replicas{ws}",
+                   "l2": "flushed between steps (256 MiB write)"},
+        "forms": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} if isinstance(v, dict) else v
+                  for k, v in forms.items()},
+        "e2e": {"value": ws / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(e2e_info.h2d_bytes),
+                "d2h_bytes_per_step": int(e2e_info.d2h_bytes),
+                "ms_per_step": e2e_s * 1000.0},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch,
+                     "ms_per_launch": per_launch_ms,
+                     "phases_ms_per_solve": {k: round(v[0], 3) for k, v in prof.phases.items()}},
+        "clocks": head["clocks"],
+        "gpu_launches": int(head["kernel_launches"]) * args.steps,
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(p, head["iterations"], args.cpu_sample_iters)
+    return out
+
+
+def cpu_baseline(p, full_iters: int, sample_iters: int):
+    """Oracle (CPU restatement of the reference, OpenMP on all host cores) on
+    the first `sample_iters` LM iterations of the same solve."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ba_oracle
+    ba_oracle.build()
+    q = p.copy()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    r = ba_oracle.bundle_adjust(q, sample_iters, SIGMA_PX, n_threads=threads)
+    dt = time.perf_counter() - t0
+    per_iter = dt / max(r.iterations, 1)
+    est = per_iter * max(full_iters, 1)
+    return {"value": 1.0 / est, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {r.iterations} LM iterations of the same solve "
+                      f"({dt:.1f} s), scaled by the full solve's {full_iters} iterations",
+            "s_per_lm_iteration": per_iter}
+
+
+def reference_arm(args, ws, rank):
+    """CPU reference solver (oracle port, all host cores), same workload and unit."""
+    if rank != 0:
+        return None
+    p = make_workload(args.workload, args.seed)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ba_oracle
+    ba_oracle.build()
+    threads = os.cpu_count() or 1
+    times = []
+    iters = 0
+    for i in range(args.warmup + args.steps):
+        q = p.copy()
+        t0 = time.perf_counter()
+        r = ba_oracle.bundle_adjust(q, args.cpu_sample_iters, SIGMA_PX, n_threads=threads)
+        dt = time.perf_counter() - t0
+        iters = r.iterations
+        if i >= args.warmup:
+            times.append(dt / max(r.iterations, 1))
+    per_iter = float(np.mean(times))
+    est = per_iter * args.full_iters
+    v = 1.0 / est
+    return {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": est * 1000.0,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded survey generator, reference camera model)",
+        "config": {"workload": args.workload, "cameras": p.n_cams, "points": p.n_points,
+                   "observations": p.n_obs, "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
+                   "loss": "cauchy", "precision": "fp64", "parallelism": "cpu"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"each step = first {iters} LM iterations of the solve, "
+                                   f"scaled by the full solve's {args.full_iters} iterations"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="single500")
+    ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--max-iter", type=int, default=MAX_ITER)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-sample-iters", type=int, default=2)
+    ap.add_argument("--full-iters", type=int, default=int(os.environ.get("BA_FULL_ITERS", "0")) or None)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank = dist_env()
+    if args.impl == "reference":
+        if args.full_iters is None:
+            args.full_iters = FULL_ITERS.get(args.workload, MAX_ITER)
+        out = reference_arm(args, ws, rank)
+    else:
+        out = gpu_arm(args, ws, rank)
+    if out is not None and rank == 0:
+        print(json.dumps(out))
+
+
+# LM iterations the full solve of each workload takes (FP64, measured on the
+# GPU plain form, which matches the CPU solver's iteration count); used to
+# scale the CPU reference arm's per-iteration sample to solves/s.
+FULL_ITERS = {"single500": MAX_ITER, "lawnmower77": 43}
+
+if __name__ == "__main__":
+    main()

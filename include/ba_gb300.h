@@ -1,0 +1,246 @@
+/*
+ * ba_gb300.h — C ABI of the GB300 (sm_103a) bundle-adjustment solver.
+ *
+ * Drop-in for stitch-core's
+ *     pub fn bundle_adjust(p: &mut Problem, max_iter: usize, sigma_px: f64) -> BaStats
+ * (crates/stitch-core/src/recon/ba.rs:198), with the reference's types
+ * `Obs`, `Problem` and `BaStats` (ba.rs:21-46) flattened to
+ * structure-of-arrays.  Plain pointers and sizes only; no torch or CUDA types
+ * in the signatures (a CUDA stream is passed as `void*`).
+ *
+ * Semantics follow the reference: Levenberg–Marquardt over camera poses,
+ * shared lens intrinsics (f, k1, k2) and points, a robust loss on
+ * reprojection residuals and GPS priors on camera centres, points eliminated
+ * by the Schur complement, the reduced camera(+lens) system solved by
+ * block-Jacobi PCG (ba.rs:155-196), then point back-substitution.  The state
+ * (`rot`, `center`, `points`, and `intr` when refining) is updated in place;
+ * observations, groups and priors are read only.
+ *
+ * Unlike the reference, which cannot fail, every entry point returns a
+ * status; the message of the last failure on the calling thread is available
+ * from ba_last_error().  There is no CPU fallback: without a usable GPU the
+ * calls fail with BA_CUDA_ERROR.
+ *
+ * Layouts (host or device memory as stated per call):
+ *   obs_cam   u32[n_obs]          camera of each observation
+ *   obs_pt    u32[n_obs]          point of each observation, non-decreasing
+ *                                 (ba.rs:36: "Sorted by point")
+ *   obs_uv    f64[2*n_obs]        measured pixel (u, v)
+ *   cam_group u32[n_cams]         lens group of each camera (ba.rs:31-32)
+ *   prior_mask u8[n_cams]         1 = camera has a GPS prior (may be NULL)
+ *   prior     f64[6*n_cams]       prior centre xyz, then sigma xyz (ba.rs:33-34)
+ *   rot       f64[9*n_cams]       world->camera rotation, ROW-major
+ *                                 (nalgebra stores column-major: transpose)
+ *   center    f64[3*n_cams]       camera centre in world coordinates
+ *   intr      f64[5*n_groups]     f, cx, cy, k1, k2 (geometry.rs:15-23)
+ *   points    f64[3*n_points]
+ */
+#ifndef BA_GB300_H
+#define BA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BA_GB300_ABI_VERSION 1
+
+typedef enum ba_status {
+  BA_OK = 0,
+  BA_BAD_INPUT = 1,     /* sizes, indices, ordering or options rejected   */
+  BA_OOM = 2,           /* device memory could not be allocated           */
+  BA_CUDA_ERROR = 3,    /* no device, launch failure, or device error     */
+  BA_TIMEOUT = 4,       /* a device-side wait gave up (error flag)        */
+  BA_NOT_SUPPORTED = 5  /* option combination not implemented             */
+} ba_status;
+
+typedef enum ba_loss {
+  BA_LOSS_CAUCHY = 0, /* the reference's loss: s^2 ln(1 + e^2/s^2) (ba.rs:99,114) */
+  BA_LOSS_HUBER = 1   /* Huber with delta = sigma_px (not in the reference)       */
+} ba_loss;
+
+typedef enum ba_precision {
+  BA_PRECISION_FP64 = 0,  /* plain form: FP64 throughout                     */
+  BA_PRECISION_MIXED = 1  /* FP32 Jacobians / Schur blocks / PCG vectors;
+                             FP64 cost, PCG inner products, block inverses */
+} ba_precision;
+
+/* ba.rs:28-39 (`Problem`, read-only parts). */
+typedef struct ba_problem {
+  int64_t n_cams, n_points, n_obs, n_groups;
+  const uint32_t* obs_cam;
+  const uint32_t* obs_pt;
+  const double* obs_uv;
+  const uint32_t* cam_group;
+  const uint8_t* prior_mask; /* NULL: no camera has a prior */
+  const double* prior;
+  int32_t refine_intrinsics; /* ba.rs:38 */
+} ba_problem;
+
+/* ba.rs:28-39 (`Problem`, the parts bundle_adjust mutates). */
+typedef struct ba_state {
+  double* rot;
+  double* center;
+  double* intr;
+  double* points;
+} ba_state;
+
+/* Optional per-LM-iteration log, caller-owned arrays of `cap` entries. */
+typedef struct ba_log {
+  int32_t cap;
+  double* new_cost;   /* robust cost of the trial state                 */
+  double* lambda;     /* damping used to build the iteration's system   */
+  int32_t* pcg_iters; /* PCG matrix-vector products                     */
+  int32_t* accepted;  /* 1 if the trial state was accepted              */
+} ba_log;
+
+typedef struct ba_options {
+  int32_t max_iter;     /* ba.rs:198 `max_iter`                            */
+  double sigma_px;      /* ba.rs:198 `sigma_px` (loss scale, pixels)       */
+  int32_t loss;         /* ba_loss, default BA_LOSS_CAUCHY                 */
+  int32_t precision;    /* ba_precision, default BA_PRECISION_FP64         */
+  int32_t pcg_max_iter; /* <=0: 400 (ba.rs:334)                            */
+  double pcg_tol;       /* <=0: 1e-20, on |r|^2 / |b|^2 (ba.rs:182)        */
+  int32_t matrix_free;  /* 0: auto (by memory cap), 1: stored S, 2: matrix-free */
+  int64_t memory_cap_bytes; /* auto mode: go matrix-free above this (<=0: no cap) */
+  void* stream;         /* cudaStream_t to run on, NULL: the library's own */
+  ba_log* log;          /* NULL or per-iteration log (single-model calls)  */
+  int32_t profile;      /* 1: time each kernel phase with CUDA events      */
+} ba_options;
+
+/* Kernel phases timed when ba_options.profile is set (ba_stats.ms_phase). */
+enum {
+  BA_PHASE_POINT = 0,    /* linearise + per-point blocks (ba.rs:222-268)   */
+  BA_PHASE_CAMERA = 1,   /* per-camera and per-lens sums (ba.rs:273-292)   */
+  BA_PHASE_SCHUR = 2,    /* Schur products (ba.rs:320-331)                 */
+  BA_PHASE_ASSEMBLE = 3, /* reduced matrix, rhs, damping, preconditioner   */
+  BA_PHASE_PCG = 4,      /* block-Jacobi PCG (ba.rs:155-196)               */
+  BA_PHASE_UPDATE = 5,   /* pose update + back-substitution (ba.rs:338-366)*/
+  BA_PHASE_COST = 6,     /* robust cost of the trial state (ba.rs:367)     */
+  BA_PHASE_CONTROL = 7,  /* accept / reject (ba.rs:368-383)                */
+  BA_PHASE_SETUP = 8,    /* per-call structure build                       */
+  BA_N_PHASES = 9
+};
+
+/* ba.rs:41-46 (`BaStats`) plus solver diagnostics. */
+typedef struct ba_stats {
+  int64_t iterations;  /* ba.rs:43 */
+  double initial_rms;  /* ba.rs:44 */
+  double final_rms;    /* ba.rs:45 */
+  double initial_cost, final_cost;
+  int64_t pcg_iterations; /* total PCG matrix-vector products              */
+  int64_t kernel_launches;/* kernels launched by this call                 */
+  double ms_total;        /* wall time of the call (host clock)            */
+  double ms_h2d, ms_d2h;  /* host<->device copies inside the call          */
+  int64_t h2d_bytes, d2h_bytes;
+  int64_t device_bytes;   /* peak device workspace of the call             */
+  double ms_phase[9];     /* per-phase device time (profile only)          */
+  int64_t n_phase[9];     /* launches timed per phase (profile only)       */
+  /* Size of the reduced system the call built (whole batch). */
+  int64_t n_blocks;       /* block rows: cameras + lens groups             */
+  int64_t n_nonzero_blocks;  /* 6x6 blocks of the symmetric matrix (full)  */
+  int64_t n_schur_pairs;  /* point-entry pairs summed into upper blocks    */
+  int64_t n_lens_entries; /* per-point lens entries                        */
+} ba_stats;
+
+/* Defaults: max_iter 60, sigma_px 1, Cauchy, FP64, PCG 400 / 1e-20. */
+void ba_default_options(ba_options* opt);
+
+/* Solve one problem from HOST memory, updating `state` in place.
+ * Replaces ba.rs:198 `bundle_adjust`. */
+ba_status ba_solve(const ba_problem* problem, ba_state* state,
+                   const ba_options* opt, ba_stats* stats);
+
+/* Solve `n_models` independent problems (host memory) in one batched launch
+ * sequence: every kernel covers all models, each model keeps its own damping,
+ * PCG scalars and stopping state.  `stats` has n_models entries (may be NULL).
+ * No counterpart in the reference, which solves one Problem per call
+ * (sparse.rs:450); each model gives the same result as its own ba_solve. */
+ba_status ba_solve_batch(const ba_problem* problems, ba_state* states,
+                         int32_t n_models, const ba_options* opt,
+                         ba_stats* stats);
+
+/* ---- device-resident context (inputs stay in HBM between calls) ---------- */
+
+typedef struct ba_context ba_context;
+
+/* device < 0: the current device.  stream: NULL for a library-owned stream. */
+ba_status ba_context_create(int32_t device, void* stream, ba_context** out);
+void ba_context_destroy(ba_context* ctx);
+
+/* Copy problems and initial states from host memory into the context. */
+ba_status ba_context_upload(ba_context* ctx, const ba_problem* problems,
+                            const ba_state* states, int32_t n_models);
+
+/* Solve the uploaded problems starting from their uploaded initial states
+ * (the initial states stay intact, so repeated calls solve the same problem).
+ * Everything — structure, linearisation, Schur complement, PCG, updates —
+ * runs on the device; only per-iteration control scalars are read back. */
+ba_status ba_context_solve(ba_context* ctx, const ba_options* opt,
+                           ba_stats* stats);
+
+/* Copy the solved states back into host memory. */
+ba_status ba_context_download(ba_context* ctx, ba_state* states,
+                              int32_t n_models);
+
+/* Gradient of the robust cost at the context's current (solved) state with
+ * respect to each lens group's intrinsics (f, cx, cy, k1, k2): the adjoint
+ * (vector-Jacobian product) of reprojection + distortion residuals; GPS
+ * priors do not depend on intrinsics.  At a converged solve in which the
+ * intrinsics were held fixed this is also the total derivative of the final
+ * cost (the poses and points are stationary).  grad: f64[5 * total groups],
+ * host memory.  No counterpart in the reference. */
+ba_status ba_context_intrinsics_grad(ba_context* ctx, const ba_options* opt,
+                                     double* grad);
+
+/* Vector-Jacobian product of the residuals at the context's current state.
+ * Residuals: e_k = u_k − pred_k per observation in front of its camera
+ * (ba.rs:56-101) and r_c = (C_c − prior_c) / sigma_c per prior axis
+ * (ba.rs:120-126).  With cotangents lambda (f64[2*n_obs]) and mu
+ * (f64[3*n_cams]) it returns sum (de/dθ)^T lambda + sum (dr/dθ)^T mu for
+ * θ = camera (rotation as the left perturbation R <- exp(w) R, then centre;
+ * f64[6*n_cams]), points (f64[3*n_points]) and lens intrinsics
+ * (f, cx, cy, k1, k2; f64[5*n_groups]).  lambda == NULL and mu == NULL give
+ * the gradient of the robust cost.  Host arrays; outputs may be NULL.
+ * No counterpart in the reference. */
+ba_status ba_context_vjp(ba_context* ctx, const ba_options* opt,
+                        const double* cot_obs, const double* cot_prior,
+                        double* g_cam, double* g_points, double* g_intr);
+
+/* Per-observation residual and Jacobians at the context's current state,
+ * as the reference's linearise (ba.rs:56-101) defines them, written to host
+ * arrays: e f64[2n], jc f64[12n] (2x6 row-major: rotation | centre),
+ * jg f64[6n] (2x3: f, k1, k2), jp f64[6n], w f64[n], valid u8[n]. */
+ba_status ba_context_linearise(ba_context* ctx, const ba_options* opt,
+                               double* e, double* jc, double* jg, double* jp,
+                               double* w, uint8_t* valid);
+
+/* Robust cost (ba.rs:103-128) at the context's current state, per model:
+ * cost (incl. priors), rms and in-front count; host arrays of n_models. */
+ba_status ba_context_cost(ba_context* ctx, const ba_options* opt,
+                          double* cost, double* rms, int64_t* n_in_front);
+
+/* One LM system at damping `lambda` built at the context's uploaded state
+ * (single model), solved by PCG and applied, without the accept step:
+ * the dense reduced matrix S f64[(6 nb)^2] (row-major, may be NULL; for small
+ * problems), the right-hand side g f64[6 nb], the step dx f64[6 nb], the PCG
+ * iteration count and the robust cost of the trial state.  nb = n_cams +
+ * n_groups, blocks ordered as in ba.rs:199-201.  A diagnostic for
+ * element-wise checks of ba.rs:221-367; no counterpart in the reference. */
+ba_status ba_context_debug_step(ba_context* ctx, const ba_options* opt,
+                                double lambda, double* S_dense, double* g,
+                                double* dx, int32_t* pcg_iters,
+                                double* trial_cost);
+
+/* ---- misc ----------------------------------------------------------------- */
+
+const char* ba_last_error(void);
+int32_t ba_abi_version(void);
+const char* ba_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BA_GB300_H */

@@ -1,0 +1,1012 @@
+// ORACLE — test infrastructure only.
+//
+// A CPU, FP64 restatement of stitch-core's bundle adjustment
+// (crates/stitch-core/src/recon/ba.rs:56-391) and of the camera model it uses
+// (crates/stitch-core/src/recon/geometry.rs:15-112).  It is the checker that
+// the CUDA solver is compared against, and the timed CPU baseline; it is never
+// linked into, called by, or shipped with the product library.
+//
+// Parity pin: the reference cannot be built here (Rust toolchain absent), so
+// this restatement is pinned by the reference's own known-answer test
+// `recovers_perturbed_survey` (ba.rs:400-493), restated as
+// `oracle_make_ref_survey` below, and by its geometry tests
+// (geometry.rs:318-351).  Third-party arithmetic (nalgebra 0.33.3
+// `try_inverse`, Cargo.lock) is restated with textbook algorithms: a 3x3
+// adjugate inverse and a 6x6 LU with partial pivoting.
+//
+// Data structures follow the reference on purpose, because this file is also
+// the CPU baseline: the reduced camera system is a row-wise hash map of 6x6
+// blocks (ba.rs:130-153), assembled serially (ba.rs:270-331); the per-
+// observation and per-point phases run in parallel with OpenMP where the
+// reference uses rayon `par_iter` (ba.rs:107,145,224,235,352).
+//
+// Build: see oracle/Makefile (compiled with -ffp-contract=off so that, like
+// Rust, no multiply-add is fused).
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" {
+
+// Flat SoA problem, the same field meaning as the product's C ABI.
+typedef struct oracle_problem {
+  int32_t n_cams, n_points, n_obs, n_groups;
+  const uint32_t* obs_cam;    // [n_obs]
+  const uint32_t* obs_pt;     // [n_obs], sorted ascending (ba.rs:36)
+  const double* obs_uv;       // [2*n_obs]
+  const uint32_t* cam_group;  // [n_cams]
+  const uint8_t* prior_mask;  // [n_cams] or NULL (no priors)
+  const double* prior;        // [6*n_cams]: centre xyz, sigma xyz
+  int32_t refine_intrinsics;
+} oracle_problem;
+
+typedef struct oracle_state {
+  double* rot;     // [9*n_cams] world->camera R, row-major
+  double* center;  // [3*n_cams]
+  double* intr;    // [5*n_groups]: f, cx, cy, k1, k2
+  double* points;  // [3*n_points]
+} oracle_state;
+
+typedef struct oracle_stats {
+  int64_t iterations;
+  double initial_rms, final_rms;
+  double initial_cost, final_cost;
+  // Optional per-iteration log (caller-owned, log_cap entries each).
+  int32_t log_cap;
+  double* log_new_cost;  // cost of the trial state
+  double* log_lambda;    // lambda used to build the system
+  int32_t* log_pcg;      // PCG iterations
+  int32_t* log_accept;   // 1 if accepted
+  // Per-phase wall time, seconds.
+  double t_linearise, t_point, t_assembly, t_schur, t_pcg, t_backsub, t_cost,
+      t_total;
+} oracle_stats;
+
+}  // extern "C"
+
+namespace {
+
+enum { LOSS_CAUCHY = 0, LOSS_HUBER = 1 };
+
+using M6 = std::array<double, 36>;  // row-major 6x6
+using V6 = std::array<double, 6>;
+
+double now_s() {
+  return std::chrono::duration<double>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// ---- camera model (geometry.rs) -------------------------------------------
+
+// R·(X − C)   (geometry.rs:57-59)
+inline void to_cam(const double* R, const double* C, const double* X,
+                   double* xc) {
+  const double d0 = X[0] - C[0], d1 = X[1] - C[1], d2 = X[2] - C[2];
+  xc[0] = R[0] * d0 + R[1] * d1 + R[2] * d2;
+  xc[1] = R[3] * d0 + R[4] * d1 + R[5] * d2;
+  xc[2] = R[6] * d0 + R[7] * d1 + R[8] * d2;
+}
+
+// Pose::project (geometry.rs:66-72) with Intrinsics::distort (:28-32).
+inline bool project(const double* R, const double* C, const double* K,
+                    const double* X, double* u) {
+  double xc[3];
+  to_cam(R, C, X, xc);
+  if (xc[2] <= 1e-6) return false;
+  const double px = xc[0] / xc[2], py = xc[1] / xc[2];
+  const double r2 = px * px + py * py;
+  const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
+  u[0] = K[0] * d * px + K[1];
+  u[1] = K[0] * d * py + K[2];
+  return true;
+}
+
+// skew (geometry.rs:95-97), row-major.
+inline void skew(const double* v, double* S) {
+  S[0] = 0.0;   S[1] = -v[2]; S[2] = v[1];
+  S[3] = v[2];  S[4] = 0.0;   S[5] = -v[0];
+  S[6] = -v[1]; S[7] = v[0];  S[8] = 0.0;
+}
+
+inline void matmul3(const double* A, const double* B, double* C) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      C[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] +
+                     A[3 * i + 2] * B[6 + j];
+}
+
+// rot_axis (geometry.rs:100-103): I + K sin(a) + K² (1 − cos(a)).
+void rot_axis(const double* axis, double angle, double* R) {
+  double K[9], K2[9];
+  skew(axis, K);
+  matmul3(K, K, K2);
+  const double s = std::sin(angle), c1 = 1.0 - std::cos(angle);
+  for (int i = 0; i < 9; ++i)
+    R[i] = ((i % 4 == 0) ? 1.0 : 0.0) + K[i] * s + K2[i] * c1;
+}
+
+// exp_so3 (geometry.rs:106-112).
+void exp_so3(const double* w, double* R) {
+  const double th = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+  if (th < 1e-12) {
+    double K[9];
+    skew(w, K);
+    for (int i = 0; i < 9; ++i) R[i] = ((i % 4 == 0) ? 1.0 : 0.0) + K[i];
+    return;
+  }
+  const double a[3] = {w[0] / th, w[1] / th, w[2] / th};
+  rot_axis(a, th, R);
+}
+
+// Pose::from_angles (geometry.rs:76-92): R (world->camera) and nothing else.
+void from_angles(double yaw_deg, double pitch_deg, double roll_deg,
+                 double* R) {
+  const double dr = M_PI / 180.0;
+  const double sy = std::sin(yaw_deg * dr), cy = std::cos(yaw_deg * dr);
+  const double sp = std::sin(pitch_deg * dr), cp = std::cos(pitch_deg * dr);
+  const double heading[3] = {sy, cy, 0.0};
+  const double x[3] = {cy, -sy, 0.0};  // right
+  double z[3] = {heading[0] * cp, heading[1] * cp, heading[2] * cp + sp};
+  double y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2],
+                 z[0] * x[1] - z[1] * x[0]};  // z × x
+  double rwc[9] = {x[0], y[0], z[0], x[1], y[1], z[1], x[2], y[2], z[2]};
+  if (std::fabs(roll_deg) > 1e-9) {
+    const double ax[3] = {0.0, 0.0, 1.0};
+    double Rr[9], T[9];
+    rot_axis(ax, roll_deg * dr, Rr);
+    matmul3(rwc, Rr, T);
+    std::memcpy(rwc, T, sizeof T);
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = rwc[3 * j + i];
+}
+
+// ---- small dense algebra ----------------------------------------------------
+
+// 3x3 inverse via the adjugate; false iff the determinant is exactly zero
+// (the behaviour ba.rs:265 relies on: a singular point block is skipped).
+bool inv3(const double* A, double* Ai) {
+  const double c00 = A[4] * A[8] - A[5] * A[7];
+  const double c01 = A[5] * A[6] - A[3] * A[8];
+  const double c02 = A[3] * A[7] - A[4] * A[6];
+  const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+  if (det == 0.0) return false;
+  Ai[0] = c00 / det;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) / det;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) / det;
+  Ai[3] = c01 / det;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) / det;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) / det;
+  Ai[6] = c02 / det;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) / det;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) / det;
+  return true;
+}
+
+// 6x6 inverse, LU with partial pivoting; false on an exactly zero pivot
+// (ba.rs:160 then falls back to the identity).
+bool inv6(const M6& A, M6& Ai) {
+  double a[36];
+  std::memcpy(a, A.data(), sizeof a);
+  int perm[6] = {0, 1, 2, 3, 4, 5};
+  for (int k = 0; k < 6; ++k) {
+    int piv = k;
+    double best = std::fabs(a[6 * k + k]);
+    for (int i = k + 1; i < 6; ++i)
+      if (std::fabs(a[6 * i + k]) > best) best = std::fabs(a[6 * i + k]), piv = i;
+    if (best == 0.0) return false;
+    if (piv != k) {
+      for (int j = 0; j < 6; ++j) std::swap(a[6 * k + j], a[6 * piv + j]);
+      std::swap(perm[k], perm[piv]);
+    }
+    for (int i = k + 1; i < 6; ++i) {
+      const double l = a[6 * i + k] / a[6 * k + k];
+      a[6 * i + k] = l;
+      for (int j = k + 1; j < 6; ++j) a[6 * i + j] -= l * a[6 * k + j];
+    }
+  }
+  // Solve L U x = P e_j for each column j.
+  for (int j = 0; j < 6; ++j) {
+    double x[6];
+    for (int i = 0; i < 6; ++i) x[i] = (perm[i] == j) ? 1.0 : 0.0;
+    for (int i = 0; i < 6; ++i)
+      for (int k = 0; k < i; ++k) x[i] -= a[6 * i + k] * x[k];
+    for (int i = 5; i >= 0; --i) {
+      for (int k = i + 1; k < 6; ++k) x[i] -= a[6 * i + k] * x[k];
+      x[i] /= a[6 * i + i];
+    }
+    for (int i = 0; i < 6; ++i) Ai[6 * i + j] = x[i];
+  }
+  return true;
+}
+
+// ---- linearisation (ba.rs:48-101) -----------------------------------------
+
+struct Lin {
+  double e[2];
+  double jc[12];  // 2x6 row-major: [d/drot | d/dcentre]
+  double jg[6];   // 2x3 row-major: d pred / d(f, k1, k2)
+  double jp[6];   // 2x3 row-major
+  double w;
+};
+
+inline double robust_weight(double e2, double sigma, int loss) {
+  if (loss == LOSS_HUBER) {
+    const double a = std::sqrt(e2);
+    return a <= sigma ? 1.0 : sigma / a;
+  }
+  return 1.0 / (1.0 + e2 / (sigma * sigma));  // ba.rs:99
+}
+
+inline double robust_rho(double e2, double sigma, int loss) {
+  if (loss == LOSS_HUBER) {
+    const double a = std::sqrt(e2);
+    return a <= sigma ? e2 : 2.0 * sigma * a - sigma * sigma;
+  }
+  const double s2 = sigma * sigma;
+  return s2 * std::log(1.0 + e2 / s2);  // ba.rs:114
+}
+
+bool linearise(const oracle_problem& P, const oracle_state& S, int k,
+               double sigma, int loss, Lin& l) {
+  const uint32_t cam = P.obs_cam[k];
+  const double* R = S.rot + 9 * cam;
+  const double* C = S.center + 3 * cam;
+  const double* K = S.intr + 5 * P.cam_group[cam];
+  const double* X = S.points + 3 * (size_t)P.obs_pt[k];
+  double xc[3];
+  to_cam(R, C, X, xc);
+  if (xc[2] <= 1e-6) return false;  // ba.rs:61
+  const double f = K[0], k1 = K[3], k2 = K[4];
+  const double iz = 1.0 / xc[2];
+  const double px = xc[0] * iz, py = xc[1] * iz;
+  const double r2 = px * px + py * py;
+  const double d = 1.0 + k1 * r2 + k2 * r2 * r2;
+  const double qx = px * d, qy = py * d;
+  const double predx = f * qx + K[1], predy = f * qy + K[2];
+  l.e[0] = P.obs_uv[2 * k] - predx;
+  l.e[1] = P.obs_uv[2 * k + 1] - predy;
+  // du/dp = f (d I + c p pᵀ), c = 2 (k1 + 2 k2 r2)   (ba.rs:71-78)
+  const double c = 2.0 * (k1 + 2.0 * k2 * r2);
+  const double a00 = (d + c * px * px) * f, a01 = (c * px * py) * f;
+  const double a10 = (c * px * py) * f, a11 = (d + c * py * py) * f;
+  // dp/dx (ba.rs:79)
+  const double b02 = -xc[0] * iz * iz, b12 = -xc[1] * iz * iz;
+  double dudx[6];
+  dudx[0] = a00 * iz;
+  dudx[1] = a01 * iz;
+  dudx[2] = a00 * b02 + a01 * b12;
+  dudx[3] = a10 * iz;
+  dudx[4] = a11 * iz;
+  dudx[5] = a10 * b02 + a11 * b12;
+  double sk[9];
+  skew(xc, sk);
+  for (int r = 0; r < 2; ++r)
+    for (int j = 0; j < 3; ++j) {
+      double rot = 0.0, cc = 0.0, pp = 0.0;
+      for (int t = 0; t < 3; ++t) {
+        rot += dudx[3 * r + t] * (-sk[3 * t + j]);
+        cc += dudx[3 * r + t] * (-R[3 * t + j]);
+        pp += dudx[3 * r + t] * R[3 * t + j];
+      }
+      l.jc[6 * r + j] = rot;
+      l.jc[6 * r + 3 + j] = cc;
+      l.jp[3 * r + j] = pp;
+    }
+  if (P.refine_intrinsics) {  // ba.rs:87-98
+    l.jg[0] = qx;
+    l.jg[1] = f * px * r2;
+    l.jg[2] = f * px * r2 * r2;
+    l.jg[3] = qy;
+    l.jg[4] = f * py * r2;
+    l.jg[5] = f * py * r2 * r2;
+  } else {
+    for (int i = 0; i < 6; ++i) l.jg[i] = 0.0;
+  }
+  l.w = robust_weight(l.e[0] * l.e[0] + l.e[1] * l.e[1], sigma, loss);
+  return true;
+}
+
+// ---- robust cost (ba.rs:103-128) -------------------------------------------
+
+struct CostOut {
+  double cost, rms;
+  int64_t n;
+};
+
+CostOut robust_cost(const oracle_problem& P, const oracle_state& S,
+                    double sigma, int loss) {
+  double cost = 0.0, sq = 0.0;
+  int64_t n = 0;
+  const double behind = sigma * sigma * 10.0;  // ba.rs:116
+#pragma omp parallel for reduction(+ : cost, sq, n) schedule(static)
+  for (int k = 0; k < P.n_obs; ++k) {
+    const uint32_t cam = P.obs_cam[k];
+    double u[2];
+    if (project(S.rot + 9 * cam, S.center + 3 * cam,
+                S.intr + 5 * P.cam_group[cam],
+                S.points + 3 * (size_t)P.obs_pt[k], u)) {
+      const double ex = P.obs_uv[2 * k] - u[0], ey = P.obs_uv[2 * k + 1] - u[1];
+      const double e2 = ex * ex + ey * ey;
+      cost += robust_rho(e2, sigma, loss);
+      sq += e2;
+      n += 1;
+    } else {
+      cost += behind;
+    }
+  }
+  double prior = 0.0;  // serial, ba.rs:120-126
+  if (P.prior_mask) {
+    for (int i = 0; i < P.n_cams; ++i) {
+      if (!P.prior_mask[i]) continue;
+      const double* pr = P.prior + 6 * i;
+      const double dx = S.center[3 * i] - pr[0], dy = S.center[3 * i + 1] - pr[1],
+                   dz = S.center[3 * i + 2] - pr[2];
+      prior += (dx / pr[3]) * (dx / pr[3]) + (dy / pr[4]) * (dy / pr[4]) +
+               (dz / pr[5]) * (dz / pr[5]);
+    }
+  }
+  CostOut o;
+  o.cost = cost + prior;
+  o.rms = std::sqrt(sq / (double)std::max<int64_t>(n, 1));
+  o.n = n;
+  return o;
+}
+
+// ---- sparse block matrix (ba.rs:130-153) ------------------------------------
+
+struct Sparse {
+  std::vector<std::unordered_map<size_t, M6>> rows;
+  explicit Sparse(size_t n) : rows(n) {}
+  M6& at(size_t i, size_t k) {
+    auto it = rows[i].find(k);
+    if (it == rows[i].end()) it = rows[i].emplace(k, M6{}).first;
+    return it->second;
+  }
+  void add(size_t i, size_t k, const M6& m) {
+    M6& d = at(i, k);
+    for (int t = 0; t < 36; ++t) d[t] += m[t];
+  }
+  void mul(const std::vector<V6>& x, std::vector<V6>& out) const {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)rows.size(); ++i) {
+      V6 s{};
+      for (const auto& kv : rows[i]) {
+        const M6& m = kv.second;
+        const V6& xv = x[kv.first];
+        for (int r = 0; r < 6; ++r) {
+          double acc = 0.0;
+          for (int c = 0; c < 6; ++c) acc += m[6 * r + c] * xv[c];
+          s[r] += acc;
+        }
+      }
+      out[i] = s;
+    }
+  }
+};
+
+double dot(const std::vector<V6>& a, const std::vector<V6>& b) {
+  double s = 0.0;
+  for (size_t i = 0; i < a.size(); ++i) {
+    double d = 0.0;
+    for (int t = 0; t < 6; ++t) d += a[i][t] * b[i][t];
+    s += d;
+  }
+  return s;
+}
+
+// Block-Jacobi PCG (ba.rs:155-196).
+std::vector<V6> pcg(const Sparse& s, const std::vector<V6>& b, int max_iter,
+                    int* iters_out) {
+  const size_t n = b.size();
+  std::vector<M6> pre(n);
+  for (size_t i = 0; i < n; ++i) {
+    M6 d{};
+    auto it = s.rows[i].find(i);
+    if (it != s.rows[i].end())
+      d = it->second;
+    else
+      for (int t = 0; t < 6; ++t) d[7 * t] = 1.0;
+    if (!inv6(d, pre[i])) {
+      pre[i] = M6{};
+      for (int t = 0; t < 6; ++t) pre[i][7 * t] = 1.0;
+    }
+  }
+  auto apply = [&](const std::vector<V6>& r, std::vector<V6>& z) {
+    for (size_t i = 0; i < n; ++i)
+      for (int rr = 0; rr < 6; ++rr) {
+        double acc = 0.0;
+        for (int c = 0; c < 6; ++c) acc += pre[i][6 * rr + c] * r[i][c];
+        z[i][rr] = acc;
+      }
+  };
+  std::vector<V6> x(n, V6{}), r = b, z(n), p, q(n, V6{});
+  apply(r, z);
+  p = z;
+  double rz = dot(r, z);
+  const double b2 = std::max(dot(b, b), 1e-300);
+  int spmv = 0;  // iterations = matrix-vector products performed
+  for (int it = 0; it < max_iter; ++it) {
+    s.mul(p, q);
+    ++spmv;
+    const double pq = dot(p, q);
+    if (std::fabs(pq) < 1e-300) break;
+    const double a = rz / pq;
+    for (size_t i = 0; i < n; ++i)
+      for (int t = 0; t < 6; ++t) {
+        x[i][t] += p[i][t] * a;
+        r[i][t] -= q[i][t] * a;
+      }
+    if (dot(r, r) < 1e-20 * b2) break;
+    apply(r, z);
+    const double rz2 = dot(r, z);
+    const double beta = rz2 / rz;
+    rz = rz2;
+    for (size_t i = 0; i < n; ++i)
+      for (int t = 0; t < 6; ++t) p[i][t] = z[i][t] + p[i][t] * beta;
+  }
+  if (iters_out) *iters_out = spmv;
+  return x;
+}
+
+// ---- one reduced system (ba.rs:221-331) ------------------------------------
+
+struct PointSys {
+  double vinv[9];
+  double v[3];
+  std::vector<std::pair<size_t, std::array<double, 18>>> y;  // (block, 6x3)
+};
+
+struct System {
+  std::vector<Lin> lins;
+  std::vector<uint8_t> valid;
+  std::vector<uint8_t> has_sys;
+  std::vector<PointSys> point_sys;
+  Sparse s;
+  std::vector<V6> g;
+  explicit System(size_t nb) : s(nb), g(nb, V6{}) {}
+};
+
+struct Timing {
+  double lin = 0, point = 0, assembly = 0, schur = 0;
+};
+
+void build_system(const oracle_problem& P, const oracle_state& S,
+                  const std::vector<std::pair<size_t, size_t>>& ranges,
+                  double lambda, double sigma, int loss, System& sys,
+                  Timing& tm) {
+  const int nc = P.n_cams, np = P.n_points, no = P.n_obs;
+  const bool refine = P.refine_intrinsics != 0;
+  double t0 = now_s();
+  // Linearise, parallel over observations (ba.rs:222-226).
+  sys.lins.assign(no, Lin{});
+  sys.valid.assign(no, 0);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < no; ++k)
+    sys.valid[k] = linearise(P, S, k, sigma, loss, sys.lins[k]) ? 1 : 0;
+  double t1 = now_s();
+  tm.lin += t1 - t0;
+
+  // Per-point blocks, parallel over points (ba.rs:229-268).
+  sys.point_sys.assign(np, PointSys{});
+  sys.has_sys.assign(np, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int j = 0; j < np; ++j) {
+    const size_t s0 = ranges[j].first, e0 = ranges[j].second;
+    if (e0 - s0 < 2) continue;
+    double vm[9] = {0}, v[3] = {0};
+    PointSys ps;
+    ps.y.reserve(e0 - s0 + 1);
+    for (size_t k = s0; k < e0; ++k) {
+      if (!sys.valid[k]) continue;
+      const Lin& l = sys.lins[k];
+      for (int a = 0; a < 3; ++a) {
+        for (int b = 0; b < 3; ++b)
+          vm[3 * a + b] += (l.jp[a] * l.jp[b] + l.jp[3 + a] * l.jp[3 + b]) * l.w;
+        v[a] += (l.jp[a] * l.e[0] + l.jp[3 + a] * l.e[1]) * l.w;
+      }
+      std::array<double, 18> yc;
+      for (int a = 0; a < 6; ++a)
+        for (int b = 0; b < 3; ++b)
+          yc[3 * a + b] =
+              (l.jc[a] * l.jp[b] + l.jc[6 + a] * l.jp[3 + b]) * l.w;
+      const uint32_t cam = P.obs_cam[k];
+      ps.y.emplace_back((size_t)cam, yc);
+      if (refine) {
+        std::array<double, 18> yg{};
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b)
+            yg[3 * a + b] =
+                (l.jg[a] * l.jp[b] + l.jg[3 + a] * l.jp[3 + b]) * l.w;
+        const size_t g = (size_t)nc + P.cam_group[cam];
+        bool found = false;
+        for (auto& ent : ps.y)
+          if (ent.first == g) {
+            for (int t = 0; t < 18; ++t) ent.second[t] += yg[t];
+            found = true;
+            break;
+          }
+        if (!found) ps.y.emplace_back(g, yg);
+      }
+    }
+    for (int d = 0; d < 3; ++d) vm[4 * d] = vm[4 * d] * (1.0 + lambda) + 1e-9;
+    if (!inv3(vm, ps.vinv)) continue;  // ba.rs:265
+    std::memcpy(ps.v, v, sizeof v);
+    sys.point_sys[j] = std::move(ps);
+    sys.has_sys[j] = 1;
+  }
+  double t2 = now_s();
+  tm.point += t2 - t1;
+
+  // Reduced system, serial (ba.rs:270-319).
+  for (int k = 0; k < no; ++k) {
+    if (!sys.valid[k]) continue;
+    if (!sys.has_sys[P.obs_pt[k]]) continue;
+    const Lin& l = sys.lins[k];
+    const size_t ci = P.obs_cam[k];
+    M6 u;
+    for (int a = 0; a < 6; ++a)
+      for (int b = 0; b < 6; ++b)
+        u[6 * a + b] = (l.jc[a] * l.jc[b] + l.jc[6 + a] * l.jc[6 + b]) * l.w;
+    sys.s.add(ci, ci, u);
+    for (int a = 0; a < 6; ++a)
+      sys.g[ci][a] += (l.jc[a] * l.e[0] + l.jc[6 + a] * l.e[1]) * l.w;
+    if (refine) {
+      const size_t gi = (size_t)nc + P.cam_group[ci];
+      // jg6 = [jg | 0]  (2x6)
+      M6 gg{};
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          gg[6 * a + b] = (l.jg[a] * l.jg[b] + l.jg[3 + a] * l.jg[3 + b]) * l.w;
+      sys.s.add(gi, gi, gg);
+      for (int a = 0; a < 3; ++a)
+        sys.g[gi][a] += (l.jg[a] * l.e[0] + l.jg[3 + a] * l.e[1]) * l.w;
+      M6 cg{}, gc{};
+      for (int a = 0; a < 6; ++a)
+        for (int b = 0; b < 3; ++b) {
+          const double m = (l.jc[a] * l.jg[b] + l.jc[6 + a] * l.jg[3 + b]) * l.w;
+          cg[6 * a + b] = m;
+          gc[6 * b + a] = m;
+        }
+      sys.s.add(ci, gi, cg);
+      sys.s.add(gi, ci, gc);
+    }
+  }
+  if (P.prior_mask) {  // ba.rs:293-304
+    for (int i = 0; i < nc; ++i) {
+      if (!P.prior_mask[i]) continue;
+      const double* pr = P.prior + 6 * i;
+      M6 m{};
+      for (int a = 0; a < 3; ++a) {
+        const double w = 1.0 / (pr[3 + a] * pr[3 + a]);
+        m[6 * (3 + a) + 3 + a] = w;
+        sys.g[i][3 + a] += w * (pr[a] - S.center[3 * i + a]);
+      }
+      sys.s.add(i, i, m);
+    }
+  }
+  const size_t nb = sys.g.size();
+  for (size_t b = 0; b < nb; ++b) {  // ba.rs:305-319
+    M6& d = sys.s.at(b, b);
+    for (int k = 0; k < 6; ++k) d[7 * k] = d[7 * k] * (1.0 + lambda) + 1e-9;
+    if (b >= (size_t)nc) {
+      for (int k = 3; k < 6; ++k) d[7 * k] = 1.0;
+      if (!refine) {
+        d = M6{};
+        for (int k = 0; k < 6; ++k) d[7 * k] = 1.0;
+      }
+    }
+  }
+  double t3 = now_s();
+  tm.assembly += t3 - t2;
+
+  // Schur subtraction, serial (ba.rs:320-331).
+  for (int j = 0; j < np; ++j) {
+    if (!sys.has_sys[j]) continue;
+    const PointSys& ps = sys.point_sys[j];
+    const size_t m = ps.y.size();
+    // vy_b = vinv · y_bᵀ (3x6)
+    std::vector<std::array<double, 18>> vy(m);
+    for (size_t b = 0; b < m; ++b)
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 6; ++c)
+          vy[b][6 * r + c] = ps.vinv[3 * r] * ps.y[b].second[3 * c] +
+                             ps.vinv[3 * r + 1] * ps.y[b].second[3 * c + 1] +
+                             ps.vinv[3 * r + 2] * ps.y[b].second[3 * c + 2];
+    double vv[3];
+    for (int r = 0; r < 3; ++r)
+      vv[r] = ps.vinv[3 * r] * ps.v[0] + ps.vinv[3 * r + 1] * ps.v[1] +
+              ps.vinv[3 * r + 2] * ps.v[2];
+    for (size_t a = 0; a < m; ++a) {
+      const auto& ya = ps.y[a].second;
+      V6& ga = sys.g[ps.y[a].first];
+      for (int r = 0; r < 6; ++r)
+        ga[r] -= ya[3 * r] * vv[0] + ya[3 * r + 1] * vv[1] + ya[3 * r + 2] * vv[2];
+      for (size_t b = 0; b < m; ++b) {
+        M6 mm;
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c)
+            mm[6 * r + c] = -(ya[3 * r] * vy[b][c] + ya[3 * r + 1] * vy[b][6 + c] +
+                              ya[3 * r + 2] * vy[b][12 + c]);
+        sys.s.add(ps.y[a].first, ps.y[b].first, mm);
+      }
+    }
+  }
+  tm.schur += now_s() - t3;
+}
+
+// Apply dx to a copy of the state (ba.rs:338-366).
+void apply_update(const oracle_problem& P, const System& sys,
+                  const std::vector<V6>& dx, const oracle_state& cur,
+                  oracle_state& out) {
+  const int nc = P.n_cams, ng = P.n_groups, np = P.n_points;
+  for (int i = 0; i < nc; ++i) {
+    const double w[3] = {dx[i][0], dx[i][1], dx[i][2]};
+    double E[9], Rn[9];
+    exp_so3(w, E);
+    matmul3(E, cur.rot + 9 * i, Rn);
+    std::memcpy(out.rot + 9 * i, Rn, sizeof Rn);
+    for (int a = 0; a < 3; ++a)
+      out.center[3 * i + a] = cur.center[3 * i + a] + dx[i][3 + a];
+  }
+  std::memcpy(out.intr, cur.intr, sizeof(double) * 5 * ng);
+  if (P.refine_intrinsics) {
+    for (int g = 0; g < ng; ++g) {
+      const V6& d = dx[nc + g];
+      out.intr[5 * g + 0] += d[0];
+      out.intr[5 * g + 3] += d[1];
+      out.intr[5 * g + 4] += d[2];
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int j = 0; j < np; ++j) {
+    double* X = out.points + 3 * (size_t)j;
+    const double* X0 = cur.points + 3 * (size_t)j;
+    if (!sys.has_sys[j]) {
+      X[0] = X0[0], X[1] = X0[1], X[2] = X0[2];
+      continue;
+    }
+    const PointSys& ps = sys.point_sys[j];
+    double rhs[3] = {ps.v[0], ps.v[1], ps.v[2]};
+    for (const auto& ent : ps.y) {
+      const V6& d = dx[ent.first];
+      for (int r = 0; r < 3; ++r) {
+        double acc = 0.0;
+        for (int c = 0; c < 6; ++c) acc += ent.second[3 * c + r] * d[c];
+        rhs[r] -= acc;
+      }
+    }
+    for (int r = 0; r < 3; ++r)
+      X[r] = X0[r] + (ps.vinv[3 * r] * rhs[0] + ps.vinv[3 * r + 1] * rhs[1] +
+                      ps.vinv[3 * r + 2] * rhs[2]);
+  }
+}
+
+std::vector<std::pair<size_t, size_t>> point_ranges(const oracle_problem& P) {
+  // ba.rs:203-214
+  std::vector<std::pair<size_t, size_t>> ranges(P.n_points, {0, 0});
+  size_t i = 0;
+  const size_t no = P.n_obs;
+  while (i < no) {
+    const uint32_t pt = P.obs_pt[i];
+    const size_t s = i;
+    while (i < no && P.obs_pt[i] == pt) ++i;
+    ranges[pt] = {s, i};
+  }
+  return ranges;
+}
+
+struct OwnedState {
+  std::vector<double> rot, center, intr, points;
+  OwnedState(const oracle_problem& P)
+      : rot(9 * (size_t)P.n_cams), center(3 * (size_t)P.n_cams),
+        intr(5 * (size_t)P.n_groups), points(3 * (size_t)P.n_points) {}
+  oracle_state view() {
+    return oracle_state{rot.data(), center.data(), intr.data(), points.data()};
+  }
+};
+
+void copy_state(const oracle_problem& P, const oracle_state& a,
+                oracle_state& b) {
+  std::memcpy(b.rot, a.rot, sizeof(double) * 9 * P.n_cams);
+  std::memcpy(b.center, a.center, sizeof(double) * 3 * P.n_cams);
+  std::memcpy(b.intr, a.intr, sizeof(double) * 5 * P.n_groups);
+  std::memcpy(b.points, a.points, sizeof(double) * 3 * (size_t)P.n_points);
+}
+
+struct ThreadScope {
+#ifdef _OPENMP
+  int saved;
+  explicit ThreadScope(int n) : saved(omp_get_max_threads()) {
+    if (n > 0) omp_set_num_threads(n);
+  }
+  ~ThreadScope() { omp_set_num_threads(saved); }
+#else
+  explicit ThreadScope(int) {}
+#endif
+};
+
+}  // namespace
+
+extern "C" {
+
+int oracle_version(void) { return 1; }
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+// bundle_adjust (ba.rs:198-391).  Mutates `st` in place.
+int oracle_bundle_adjust(const oracle_problem* P, oracle_state* st,
+                         int32_t max_iter, double sigma_px, int32_t loss,
+                         int32_t pcg_max_iter, int32_t n_threads,
+                         oracle_stats* out) {
+  ThreadScope ts(n_threads);
+  const double T0 = now_s();
+  const int nc = P->n_cams, ng = P->n_groups;
+  const size_t nb = (size_t)nc + ng;
+  const auto ranges = point_ranges(*P);
+  Timing tm;
+  double t_pcg = 0, t_back = 0, t_cost = 0;
+  double tc = now_s();
+  CostOut c0 = robust_cost(*P, *st, sigma_px, loss);
+  t_cost += now_s() - tc;
+  double cost = c0.cost;
+  double lambda = 1e-4;
+  int64_t iterations = 0;
+  OwnedState old(*P);
+  oracle_state oldv = old.view();
+  for (int it = 0; it < max_iter; ++it) {
+    ++iterations;
+    System sys(nb);
+    build_system(*P, *st, ranges, lambda, sigma_px, loss, sys, tm);
+    double tp = now_s();
+    int pcg_iters = 0;
+    std::vector<V6> dx = pcg(sys.s, sys.g, pcg_max_iter, &pcg_iters);
+    t_pcg += now_s() - tp;
+    double tb = now_s();
+    copy_state(*P, *st, oldv);  // snapshot (ba.rs:335-337)
+    apply_update(*P, sys, dx, oldv, *st);
+    t_back += now_s() - tb;
+    tc = now_s();
+    const double new_cost = robust_cost(*P, *st, sigma_px, loss).cost;
+    t_cost += now_s() - tc;
+    bool accepted = false;
+    bool stop = false;
+    const double lambda_used = lambda;
+    if (new_cost < cost) {  // ba.rs:368-383
+      accepted = true;
+      const double rel = (cost - new_cost) / std::max(cost, 1e-12);
+      cost = new_cost;
+      lambda = std::max(lambda / 3.0, 1e-9);
+      if (rel < 1e-6) stop = true;
+    } else {
+      copy_state(*P, oldv, *st);
+      lambda *= 5.0;
+      if (lambda > 1e6) stop = true;
+    }
+    if (out && out->log_cap > it) {
+      if (out->log_new_cost) out->log_new_cost[it] = new_cost;
+      if (out->log_lambda) out->log_lambda[it] = lambda_used;
+      if (out->log_pcg) out->log_pcg[it] = pcg_iters;
+      if (out->log_accept) out->log_accept[it] = accepted ? 1 : 0;
+    }
+    if (stop) break;
+  }
+  tc = now_s();
+  CostOut c1 = robust_cost(*P, *st, sigma_px, loss);
+  t_cost += now_s() - tc;
+  if (out) {
+    out->iterations = iterations;
+    out->initial_rms = c0.rms;
+    out->final_rms = c1.rms;
+    out->initial_cost = c0.cost;
+    out->final_cost = c1.cost;
+    out->t_linearise = tm.lin;
+    out->t_point = tm.point;
+    out->t_assembly = tm.assembly;
+    out->t_schur = tm.schur;
+    out->t_pcg = t_pcg;
+    out->t_backsub = t_back;
+    out->t_cost = t_cost;
+    out->t_total = now_s() - T0;
+  }
+  return 0;
+}
+
+// robust_cost (ba.rs:103-128): writes cost, rms, count.
+int oracle_robust_cost(const oracle_problem* P, const oracle_state* st,
+                       double sigma_px, int32_t loss, double* cost,
+                       double* rms, int64_t* n) {
+  CostOut c = robust_cost(*P, *st, sigma_px, loss);
+  *cost = c.cost;
+  *rms = c.rms;
+  *n = c.n;
+  return 0;
+}
+
+// linearise (ba.rs:56-101) for every observation.  e[2n], jc[12n], jg[6n],
+// jp[6n], w[n], valid[n]; invalid rows are zero.
+int oracle_linearise(const oracle_problem* P, const oracle_state* st,
+                     double sigma_px, int32_t loss, double* e, double* jc,
+                     double* jg, double* jp, double* w, uint8_t* valid) {
+  for (int k = 0; k < P->n_obs; ++k) {
+    Lin l{};
+    const bool ok = linearise(*P, *st, k, sigma_px, loss, l);
+    if (!ok) l = Lin{};
+    valid[k] = ok ? 1 : 0;
+    std::memcpy(e + 2 * (size_t)k, l.e, sizeof l.e);
+    std::memcpy(jc + 12 * (size_t)k, l.jc, sizeof l.jc);
+    std::memcpy(jg + 6 * (size_t)k, l.jg, sizeof l.jg);
+    std::memcpy(jp + 6 * (size_t)k, l.jp, sizeof l.jp);
+    w[k] = l.w;
+  }
+  return 0;
+}
+
+// One LM system at damping `lambda` (ba.rs:221-366) without the accept step:
+// the dense reduced matrix S[(6 nb)^2] (row-major; may be NULL), g[6 nb], the
+// PCG solution dx[6 nb], per-point flag `has_sys`, the trial state `trial`
+// and its cost.  For small problems (tests).
+int oracle_lm_step(const oracle_problem* P, const oracle_state* st,
+                   double lambda, double sigma_px, int32_t loss,
+                   int32_t pcg_max_iter, double* S_dense, double* g_out,
+                   double* dx_out, uint8_t* has_sys, int32_t* pcg_iters,
+                   oracle_state* trial, double* trial_cost) {
+  const size_t nb = (size_t)P->n_cams + P->n_groups;
+  const auto ranges = point_ranges(*P);
+  System sys(nb);
+  Timing tm;
+  build_system(*P, *st, ranges, lambda, sigma_px, loss, sys, tm);
+  if (S_dense) {
+    std::memset(S_dense, 0, sizeof(double) * 36 * nb * nb);
+    for (size_t i = 0; i < nb; ++i)
+      for (const auto& kv : sys.s.rows[i])
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c)
+            S_dense[(6 * i + r) * 6 * nb + 6 * kv.first + c] = kv.second[6 * r + c];
+  }
+  for (size_t i = 0; i < nb; ++i)
+    for (int t = 0; t < 6; ++t) g_out[6 * i + t] = sys.g[i][t];
+  int it = 0;
+  std::vector<V6> dx = pcg(sys.s, sys.g, pcg_max_iter, &it);
+  if (pcg_iters) *pcg_iters = it;
+  for (size_t i = 0; i < nb; ++i)
+    for (int t = 0; t < 6; ++t) dx_out[6 * i + t] = dx[i][t];
+  for (int j = 0; j < P->n_points; ++j) has_sys[j] = sys.has_sys[j];
+  apply_update(*P, sys, dx, *st, *trial);
+  *trial_cost = robust_cost(*P, *trial, sigma_px, loss).cost;
+  return 0;
+}
+
+// exp_so3 / from_angles / project exposed for the geometry pins.
+void oracle_exp_so3(const double* w, double* R) { exp_so3(w, R); }
+void oracle_from_angles(double yaw, double pitch, double roll, double* R) {
+  from_angles(yaw, pitch, roll, R);
+}
+int oracle_project(const double* R, const double* C, const double* K,
+                   const double* X, double* u) {
+  return project(R, C, K, X, u) ? 1 : 0;
+}
+// Intrinsics::undistort (geometry.rs:35-44), 8 fixed-point steps.
+void oracle_undistort(const double* K, const double* u, double* p) {
+  const double qx = (u[0] - K[1]) / K[0], qy = (u[1] - K[2]) / K[0];
+  double px = qx, py = qy;
+  for (int i = 0; i < 8; ++i) {
+    const double r2 = px * px + py * py;
+    const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
+    px = qx / d;
+    py = qy / d;
+  }
+  p[0] = px;
+  p[1] = py;
+}
+
+// The reference's own known-answer problem, `recovers_perturbed_survey`
+// (ba.rs:400-481): 3x4 nadir cameras at 80 m, 1500 candidate ground points,
+// LCG seeded 99 drawing U(−0.5, 0.5) from the top 53 bits (ba.rs:422-428).
+// Capacities: cams 12, points 1500, obs 18000.  Returns the counts through
+// n_points/n_obs; the initial (perturbed) state goes to `st`, the true focal
+// length to *f_true.
+int oracle_make_ref_survey(uint32_t* obs_cam, uint32_t* obs_pt, double* obs_uv,
+                           uint8_t* prior_mask, double* prior,
+                           oracle_state* st, int32_t* n_points,
+                           int32_t* n_obs, double* f_true) {
+  const double K[5] = {3000.0, 2000.0, 1500.0, -0.03, 0.0};
+  double truthR[12][9], truthC[12][3];
+  int nc = 0;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 4; ++c) {
+      const double yaw = (r % 2 == 0) ? 90.0 : 270.0;
+      from_angles(yaw, -90.0, 0.0, truthR[nc]);
+      truthC[nc][0] = c * 25.0;
+      truthC[nc][1] = r * 35.0;
+      truthC[nc][2] = 80.0;
+      ++nc;
+    }
+  uint64_t s = 99;
+  auto rnd = [&s]() {
+    s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+    return ((double)(s >> 11) / (double)(1ULL << 53)) - 0.5;
+  };
+  int npt = 0, nobs = 0;
+  for (int it = 0; it < 1500; ++it) {
+    // Rust evaluates constructor arguments left to right.
+    const double x0 = rnd() * 120.0 + 37.0;
+    const double x1 = rnd() * 110.0 + 35.0;
+    const double x2 = rnd() * 8.0;
+    const double X[3] = {x0, x1, x2};
+    int vi[12];
+    double vu[12][2];
+    int nv = 0;
+    for (int i = 0; i < nc; ++i) {
+      double u[2];
+      if (!project(truthR[i], truthC[i], K, X, u)) continue;
+      if (u[0] > 0.0 && u[1] > 0.0 && u[0] < 4000.0 && u[1] < 3000.0) {
+        vi[nv] = i;
+        vu[nv][0] = u[0];
+        vu[nv][1] = u[1];
+        ++nv;
+      }
+    }
+    if (nv < 2) continue;
+    const int pt = npt++;
+    const double p0 = rnd(), p1 = rnd(), p2 = rnd();
+    st->points[3 * pt] = X[0] + p0 * 2.0;
+    st->points[3 * pt + 1] = X[1] + p1 * 2.0;
+    st->points[3 * pt + 2] = X[2] + p2 * 2.0;
+    for (int v = 0; v < nv; ++v) {
+      const double n0 = rnd(), n1 = rnd();
+      obs_cam[nobs] = (uint32_t)vi[v];
+      obs_pt[nobs] = (uint32_t)pt;
+      obs_uv[2 * nobs] = vu[v][0] + n0 * 0.5;
+      obs_uv[2 * nobs + 1] = vu[v][1] + n1 * 0.5;
+      ++nobs;
+    }
+  }
+  for (int i = 0; i < nc; ++i) {  // ba.rs:454-460
+    const double w[3] = {rnd() * 0.02, rnd() * 0.02, rnd() * 0.02};
+    double E[9];
+    exp_so3(w, E);
+    matmul3(E, truthR[i], st->rot + 9 * i);
+    const double c0 = rnd(), c1 = rnd(), c2 = rnd();
+    st->center[3 * i] = truthC[i][0] + c0 * 3.0;
+    st->center[3 * i + 1] = truthC[i][1] + c1 * 3.0;
+    st->center[3 * i + 2] = truthC[i][2] + c2 * 3.0;
+  }
+  for (int i = 0; i < nc; ++i) {  // ba.rs:461-469
+    const double c0 = rnd(), c1 = rnd(), c2 = rnd();
+    prior_mask[i] = 1;
+    prior[6 * i] = truthC[i][0] + c0 * 1.0;
+    prior[6 * i + 1] = truthC[i][1] + c1 * 1.0;
+    prior[6 * i + 2] = truthC[i][2] + c2 * 1.0;
+    prior[6 * i + 3] = 2.0;
+    prior[6 * i + 4] = 2.0;
+    prior[6 * i + 5] = 3.0;
+  }
+  st->intr[0] = K[0] * 1.03;  // ba.rs:470-472
+  st->intr[1] = K[1];
+  st->intr[2] = K[2];
+  st->intr[3] = 0.0;
+  st->intr[4] = K[4];
+  *n_points = npt;
+  *n_obs = nobs;
+  *f_true = K[0];
+  return 0;
+}
+
+}  // extern "C"
