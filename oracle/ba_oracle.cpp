@@ -365,9 +365,24 @@ CostOut robust_cost(const oracle_problem& P, const oracle_state& S,
 
 // ---- sparse block matrix (ba.rs:130-153) ------------------------------------
 
+// Non-zero: visit each row's blocks in a seeded random order inside the
+// matrix-vector product, the way the reference's HashMap (RandomState, a
+// fresh hash key per map) orders them differently from run to run.  Used to
+// measure the reference's own rounding sensitivity; 0 keeps one fixed order.
+uint64_t g_spmv_seed = 0;
+uint64_t g_sparse_instances = 0;
+
+inline uint64_t mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ULL;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+  return x ^ (x >> 31);
+}
+
 struct Sparse {
   std::vector<std::unordered_map<size_t, M6>> rows;
-  explicit Sparse(size_t n) : rows(n) {}
+  uint64_t instance;
+  explicit Sparse(size_t n) : rows(n), instance(++g_sparse_instances) {}
   M6& at(size_t i, size_t k) {
     auto it = rows[i].find(k);
     if (it == rows[i].end()) it = rows[i].emplace(k, M6{}).first;
@@ -381,14 +396,28 @@ struct Sparse {
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)rows.size(); ++i) {
       V6 s{};
-      for (const auto& kv : rows[i]) {
-        const M6& m = kv.second;
-        const V6& xv = x[kv.first];
+      auto add = [&](size_t k, const M6& m) {
+        const V6& xv = x[k];
         for (int r = 0; r < 6; ++r) {
           double acc = 0.0;
           for (int c = 0; c < 6; ++c) acc += m[6 * r + c] * xv[c];
           s[r] += acc;
         }
+      };
+      if (g_spmv_seed == 0) {
+        for (const auto& kv : rows[i]) add(kv.first, kv.second);
+      } else {
+        std::vector<std::pair<size_t, const M6*>> e;
+        e.reserve(rows[i].size());
+        for (const auto& kv : rows[i]) e.emplace_back(kv.first, &kv.second);
+        std::sort(e.begin(), e.end(),
+                  [](const auto& a, const auto& b) { return a.first < b.first; });
+        uint64_t h = mix64(g_spmv_seed ^ mix64(instance * 1315423911ULL + (uint64_t)i));
+        for (size_t j = e.size(); j > 1; --j) {
+          h = mix64(h);
+          std::swap(e[j - 1], e[h % j]);
+        }
+        for (const auto& kv : e) add(kv.first, *kv.second);
       }
       out[i] = s;
     }
@@ -741,6 +770,8 @@ struct ThreadScope {
 extern "C" {
 
 int oracle_version(void) { return 1; }
+
+void oracle_set_spmv_shuffle(uint64_t seed) { g_spmv_seed = seed; }
 
 int oracle_max_threads(void) {
 #ifdef _OPENMP

@@ -91,6 +91,8 @@ def lib():
             C.POINTER(_State), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
             C.POINTER(C.c_double)]
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_set_spmv_shuffle.argtypes = [C.c_uint64]
+        L.oracle_set_spmv_shuffle.restype = None
         _lib = L
     return _lib
 
@@ -171,6 +173,12 @@ def bundle_adjust(p, max_iter: int, sigma_px: float, *, loss: int = LOSS_CAUCHY,
         dict(linearise=st.t_linearise, point=st.t_point, assembly=st.t_assembly,
              schur=st.t_schur, pcg=st.t_pcg, backsub=st.t_backsub, cost=st.t_cost,
              total=st.t_total))
+
+
+def set_spmv_shuffle(seed: int) -> None:
+    """Permute each row's block order in the PCG product (seeded), emulating
+    the reference's per-run HashMap order; 0 restores the fixed order."""
+    lib().oracle_set_spmv_shuffle(int(seed))
 
 
 def robust_cost(p, sigma_px: float, loss: int = LOSS_CAUCHY):

@@ -1,0 +1,56 @@
+"""The C-ABI library: builds, loads without a GPU, and exports exactly what
+include/ba_gb300.h declares.  CPU only (no compute calls)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from stitch_ba import _build, native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "ba_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(ba_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_header_matches_binding_list():
+    assert declared_functions() == sorted(native.EXPORTS)
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    path = _build.build_solver()
+    lib = ctypes.CDLL(path)  # loads without a GPU
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (ba_\w+)", out))
+    assert set(declared_functions()) <= exported
+
+
+def test_static_queries_work_without_gpu():
+    L = native.load()
+    assert L.ba_abi_version() == 1
+    assert b"sm_103a" in L.ba_version()
+    o = native.BaOptions()
+    L.ba_default_options(ctypes.byref(o))
+    assert o.max_iter == 60 and o.sigma_px == 1.0 and o.pcg_max_iter == 400
+    assert o.pcg_tol == 1e-20
+
+
+def test_null_context_is_rejected_without_gpu():
+    L = native.load()
+    assert L.ba_context_solve(None, None, None) == native.BAD_INPUT
+    assert b"null context" in L.ba_last_error()
+
+
+def test_header_compiles_as_c():
+    src = '#include "ba_gb300.h"\nint main(void){ ba_options o; ba_default_options(&o); return 0; }\n'
+    p = subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-I", os.path.dirname(HEADER), "-x", "c",
+                        "-"], input=src, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
