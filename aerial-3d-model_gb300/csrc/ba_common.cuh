@@ -36,8 +36,8 @@ __device__ __forceinline__ float warp_sum(float v) {
 // Deterministic block sum of N values per thread (fixed tree: lanes by
 // butterfly, then warps in index order).  Result valid in thread 0.
 // `scratch` holds N * 32 doubles.
-template <int N>
-__device__ __forceinline__ void block_sum(double (&v)[N], double* scratch) {
+template <int N, typename T>
+__device__ __forceinline__ void block_sum(T (&v)[N], T* scratch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = (blockDim.x + 31) >> 5;
 #pragma unroll
@@ -50,7 +50,7 @@ __device__ __forceinline__ void block_sum(double (&v)[N], double* scratch) {
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      double s = 0.0;
+      T s = (T)0;
       for (int w = 0; w < nw; ++w) s += scratch[i * 32 + w];
       v[i] = s;
     }

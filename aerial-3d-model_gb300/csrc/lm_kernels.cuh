@@ -31,7 +31,7 @@ struct IterBufs {
   double* grpg;   // [ng][3]
   R* part;        // [nsub][36]
   R* S;           // [nz][36] full symmetric BSR
-  double* pre;    // [nb][36]
+  R* pre;         // [nb][36] block-Jacobi inverses (computed in FP64)
   R* g;           // [nb][6]
   R* x;           // [nb][6] (dx)
   R *r, *z, *p, *q;  // PCG work vectors [nb][6]
@@ -76,38 +76,42 @@ __device__ __forceinline__ bool linearise(const Prob& P, const StateView& st, in
   const double qx = px * d, qy = py * d;
   const double ex = P.obs_uv[2 * k] - (f * qx + K[1]);
   const double ey = P.obs_uv[2 * k + 1] - (f * qy + K[2]);
-  const double c = 2.0 * (k1 + 2.0 * k2 * r2);
-  const double a00 = (d + c * px * px) * f, a01 = (c * px * py) * f;
-  const double a11 = (d + c * py * py) * f;
-  const double b02 = -xc[0] * iz * iz, b12 = -xc[1] * iz * iz;
-  double du[6];
-  du[0] = a00 * iz;
-  du[1] = a01 * iz;
+  // Jacobians in the storage precision R (FP32 in the mixed form; the
+  // residual above stays FP64).
+  const R fR = (R)f, iz_ = (R)iz, px_ = (R)px, py_ = (R)py, r2_ = (R)r2, d_ = (R)d;
+  const R x0 = (R)xc[0], x1 = (R)xc[1], x2 = (R)xc[2];
+  const R c = (R)2 * ((R)k1 + (R)2 * (R)k2 * r2_);
+  const R a00 = (d_ + c * px_ * px_) * fR, a01 = (c * px_ * py_) * fR;
+  const R a11 = (d_ + c * py_ * py_) * fR;
+  const R b02 = -x0 * iz_ * iz_, b12 = -x1 * iz_ * iz_;
+  R du[6];
+  du[0] = a00 * iz_;
+  du[1] = a01 * iz_;
   du[2] = a00 * b02 + a01 * b12;
-  du[3] = a01 * iz;
-  du[4] = a11 * iz;
+  du[3] = a01 * iz_;
+  du[4] = a11 * iz_;
   du[5] = a01 * b02 + a11 * b12;
   // Jc = [dudx · (−[xc]x) | dudx · (−R)], Jp = dudx · R.
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
-    const double u0 = du[3 * r], u1 = du[3 * r + 1], u2 = du[3 * r + 2];
-    out[6 * r + 0] = (R)(u2 * xc[1] - u1 * xc[2]);
-    out[6 * r + 1] = (R)(u0 * xc[2] - u2 * xc[0]);
-    out[6 * r + 2] = (R)(u1 * xc[0] - u0 * xc[1]);
+    const R u0 = du[3 * r], u1 = du[3 * r + 1], u2 = du[3 * r + 2];
+    out[6 * r + 0] = u2 * x1 - u1 * x2;
+    out[6 * r + 1] = u0 * x2 - u2 * x0;
+    out[6 * r + 2] = u1 * x0 - u0 * x1;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const double pp = u0 * Rm[j] + u1 * Rm[3 + j] + u2 * Rm[6 + j];
-      out[6 * r + 3 + j] = (R)(-pp);
-      out[12 + 3 * r + j] = (R)pp;
+      const R pp = u0 * (R)Rm[j] + u1 * (R)Rm[3 + j] + u2 * (R)Rm[6 + j];
+      out[6 * r + 3 + j] = -pp;
+      out[12 + 3 * r + j] = pp;
     }
   }
   if (refine) {  // ba.rs:87-95
     out[18] = (R)qx;
-    out[19] = (R)(f * px * r2);
-    out[20] = (R)(f * px * r2 * r2);
+    out[19] = fR * px_ * r2_;
+    out[20] = fR * px_ * r2_ * r2_;
     out[21] = (R)qy;
-    out[22] = (R)(f * py * r2);
-    out[23] = (R)(f * py * r2 * r2);
+    out[22] = fR * py_ * r2_;
+    out[23] = fR * py_ * r2_ * r2_;
   } else {
 #pragma unroll
     for (int i = 18; i < 24; ++i) out[i] = (R)0;
@@ -156,16 +160,18 @@ __global__ void __launch_bounds__(128)
     }
     return;
   }
-  double V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
+  // V, v and the Y / Z products accumulate in the storage precision R (FP32 in
+  // the mixed form); the 3x3 inversion and its Cholesky factor are FP64.
+  R V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
   for (uint32_t k = s; k < e; ++k) {
     R* o = B.lin + (size_t)k * kLinW;
     if (!linearise<R>(P, st, k, sg, refine, o)) {
       for (int i = 0; i < kLinW; ++i) o[i] = (R)0;
       continue;
     }
-    const double w = (double)o[26];
-    const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
-    const double e0 = o[24], e1 = o[25];
+    const R w = o[26];
+    const R j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+    const R e0 = o[24], e1 = o[25];
     V[0] += (j0 * j0 + j3 * j3) * w;
     V[1] += (j0 * j1 + j3 * j4) * w;
     V[2] += (j0 * j2 + j3 * j5) * w;
@@ -176,8 +182,10 @@ __global__ void __launch_bounds__(128)
     v[1] += (j1 * e0 + j4 * e1) * w;
     v[2] += (j2 * e0 + j5 * e1) * w;
   }
-  double A[9], Ai[9];
-  sym3_full(V, A);
+  double A[9], Ai[9], Vd[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) Vd[i] = (double)V[i];
+  sym3_full(Vd, A);
   A[0] = A[0] * (1.0 + lam) + 1e-9;  // ba.rs:262-264
   A[4] = A[4] * (1.0 + lam) + 1e-9;
   A[8] = A[8] * (1.0 + lam) + 1e-9;
@@ -185,16 +193,17 @@ __global__ void __launch_bounds__(128)
   B.kept[p] = ok ? 1 : 0;
   double L[6] = {0, 0, 0, 0, 0, 0};
   if (ok) chol3(Ai, L);
-  const double l00 = L[0], l10 = L[1], l11 = L[2], l20 = L[3], l21 = L[4], l22 = L[5];
-  const double zv0 = l00 * v[0] + l10 * v[1] + l20 * v[2];
-  const double zv1 = l11 * v[1] + l21 * v[2];
-  const double zv2 = l22 * v[2];
+  const double zv0d = L[0] * (double)v[0] + L[1] * (double)v[1] + L[3] * (double)v[2];
+  const double zv1d = L[2] * (double)v[1] + L[4] * (double)v[2];
+  const double zv2d = L[5] * (double)v[2];
   // t = V^-1 v = L zv
-  const double t0 = l00 * zv0, t1 = l10 * zv0 + l11 * zv1, t2 = l20 * zv0 + l21 * zv1 + l22 * zv2;
+  const R l00 = (R)L[0], l10 = (R)L[1], l11 = (R)L[2], l20 = (R)L[3], l21 = (R)L[4], l22 = (R)L[5];
+  const R t0 = (R)(L[0] * zv0d), t1 = (R)(L[1] * zv0d + L[2] * zv1d),
+          t2 = (R)(L[3] * zv0d + L[4] * zv1d + L[5] * zv2d);
   R* pl = B.ptL + 6 * (size_t)p;
 #pragma unroll
   for (int i = 0; i < 6; ++i) pl[i] = (R)L[i];
-  B.ptzv[3 * p] = (R)zv0, B.ptzv[3 * p + 1] = (R)zv1, B.ptzv[3 * p + 2] = (R)zv2;
+  B.ptzv[3 * p] = (R)zv0d, B.ptzv[3 * p + 1] = (R)zv1d, B.ptzv[3 * p + 2] = (R)zv2d;
   for (uint32_t k = s; k < e; ++k) {
     const R* o = B.lin + (size_t)k * kLinW;
     R* Z = B.Z + (size_t)k * 18;
@@ -206,39 +215,38 @@ __global__ void __launch_bounds__(128)
       for (int i = 0; i < 9; ++i) gs[i] = (R)0;
       continue;
     }
-    const double w = (double)o[26];
-    const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+    const R w = o[26];
+    const R j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-      const double ca = o[r], cb = o[6 + r];
+      const R ca = o[r], cb = o[6 + r];
       // Y = (Jc^T Jp) w   (ba.rs:249)
-      const double y0 = (ca * j0 + cb * j3) * w;
-      const double y1 = (ca * j1 + cb * j4) * w;
-      const double y2 = (ca * j2 + cb * j5) * w;
-      Z[3 * r + 0] = (R)(y0 * l00 + y1 * l10 + y2 * l20);
-      Z[3 * r + 1] = (R)(y1 * l11 + y2 * l21);
-      Z[3 * r + 2] = (R)(y2 * l22);
-      gs[r] = (R)(y0 * t0 + y1 * t1 + y2 * t2);
+      const R y0 = (ca * j0 + cb * j3) * w;
+      const R y1 = (ca * j1 + cb * j4) * w;
+      const R y2 = (ca * j2 + cb * j5) * w;
+      Z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
+      Z[3 * r + 1] = y1 * l11 + y2 * l21;
+      Z[3 * r + 2] = y2 * l22;
+      gs[r] = y0 * t0 + y1 * t1 + y2 * t2;
     }
     // w Jg^T (Jp t)
-    const double pt0 = j0 * t0 + j1 * t1 + j2 * t2, pt1 = j3 * t0 + j4 * t1 + j5 * t2;
+    const R pt0 = j0 * t0 + j1 * t1 + j2 * t2, pt1 = j3 * t0 + j4 * t1 + j5 * t2;
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
-      gs[6 + a] = (R)(((double)o[18 + a] * pt0 + (double)o[21 + a] * pt1) * w);
+    for (int a = 0; a < 3; ++a) gs[6 + a] = (o[18 + a] * pt0 + o[21 + a] * pt1) * w;
   }
   // Lens entries: Y_g = sum over the point's observations in group g (ba.rs:251-259).
   const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
   for (uint32_t j = l0; j < l1; ++j) {
-    double Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    R Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (uint32_t k = s; k < e; ++k) {
       if (S.obs_lens[k] != j) continue;
       const R* o = B.lin + (size_t)k * kLinW;
       if (o[27] == (R)0) continue;
-      const double w = (double)o[26];
-      const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+      const R w = o[26];
+      const R j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        const double ga = o[18 + a], gb = o[21 + a];
+        const R ga = o[18 + a], gb = o[21 + a];
         Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
         Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
         Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
@@ -247,10 +255,10 @@ __global__ void __launch_bounds__(128)
     R* Zl = B.Zl + (size_t)j * 9;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      const double y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
-      Zl[3 * a + 0] = (R)(ok ? y0 * l00 + y1 * l10 + y2 * l20 : 0.0);
-      Zl[3 * a + 1] = (R)(ok ? y1 * l11 + y2 * l21 : 0.0);
-      Zl[3 * a + 2] = (R)(ok ? y2 * l22 : 0.0);
+      const R y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
+      Zl[3 * a + 0] = ok ? y0 * l00 + y1 * l10 + y2 * l20 : (R)0;
+      Zl[3 * a + 1] = ok ? y1 * l11 + y2 * l21 : (R)0;
+      Zl[3 * a + 2] = ok ? y2 * l22 : (R)0;
     }
   }
 }
@@ -258,28 +266,36 @@ __global__ void __launch_bounds__(128)
 // ---- per camera: U, g, lens terms (ba.rs:273-292) ----------------------------
 
 constexpr int kCamThreads = 128;
-constexpr int kCamN = 63;  // 21 U | 6 gj | 6 gs | 18 X | 6 lU | 3 lg | 3 ls
+constexpr int kCamN = 45;  // 21 U | 18 X | 6 lens U     (storage precision)
+constexpr int kCamG = 18;  // 6 gj | 6 gs | 3 lg | 3 ls  (FP64)
 
 template <typename R>
 __global__ void __launch_bounds__(kCamThreads)
     camera_kernel(Prob P, StructView S, IterBufs<R> B, const int32_t* active) {
-  __shared__ double scratch[kCamN * 32];
+  // Matrix sums in the storage precision R (FP32 accumulation in the mixed
+  // form); the gradient sums (J^T W e and the Schur correction) in FP64, so
+  // the LM outer loop refines against an FP64 gradient.
+  __shared__ R scratch[kCamN * 32];
+  __shared__ double gscratch[kCamG * 32];
   const int64_t c = blockIdx.x;
   if (c >= P.nc) return;
   const uint32_t m = P.cam_model[c];
   if (!active[m]) return;
   const bool refine = P.model_refine[m] != 0;
-  double acc[kCamN];
+  R acc[kCamN];
+  double gacc[kCamG];
 #pragma unroll
-  for (int i = 0; i < kCamN; ++i) acc[i] = 0.0;
+  for (int i = 0; i < kCamN; ++i) acc[i] = (R)0;
+#pragma unroll
+  for (int i = 0; i < kCamG; ++i) gacc[i] = 0.0;
   const uint32_t b = S.cam_ptr[c], e = S.cam_ptr[c + 1];
   for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     const uint32_t k = S.cam_obs[i];
     const R* o = B.lin + (size_t)k * kLinW;
     if (o[27] == (R)0 || !B.kept[P.obs_pt[k]]) continue;  // ba.rs:274-277
-    const double w = (double)o[26];
-    const double e0 = o[24], e1 = o[25];
-    double jc[12];
+    const R w = o[26];
+    const double e0 = (double)o[24], e1 = (double)o[25], wd = (double)w;
+    R jc[12];
 #pragma unroll
     for (int t = 0; t < 12; ++t) jc[t] = o[t];
     int u = 0;
@@ -290,36 +306,37 @@ __global__ void __launch_bounds__(kCamThreads)
     const R* gs = B.gsub + (size_t)k * 9;
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
-      acc[21 + a] += (jc[a] * e0 + jc[6 + a] * e1) * w;
-      acc[27 + a] += (double)gs[a];
+      gacc[a] += ((double)jc[a] * e0 + (double)jc[6 + a] * e1) * wd;
+      gacc[6 + a] += (double)gs[a];
     }
     if (refine) {
-      const double g0 = o[18], g1 = o[19], g2 = o[20], g3 = o[21], g4 = o[22], g5 = o[23];
-      const double jg[6] = {g0, g1, g2, g3, g4, g5};
+      const R jg[6] = {o[18], o[19], o[20], o[21], o[22], o[23]};
 #pragma unroll
       for (int a = 0; a < 6; ++a)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb)
-          acc[33 + 3 * a + bb] += (jc[a] * jg[bb] + jc[6 + a] * jg[3 + bb]) * w;
+          acc[21 + 3 * a + bb] += (jc[a] * jg[bb] + jc[6 + a] * jg[3 + bb]) * w;
       int v = 0;
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int bb = a; bb < 3; ++bb) acc[51 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
+        for (int bb = a; bb < 3; ++bb) acc[39 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        acc[57 + a] += (jg[a] * e0 + jg[3 + a] * e1) * w;
-        acc[60 + a] += (double)gs[6 + a];
+        gacc[12 + a] += ((double)jg[a] * e0 + (double)jg[3 + a] * e1) * wd;
+        gacc[15 + a] += (double)gs[6 + a];
       }
     }
   }
   block_sum<kCamN>(acc, scratch);
+  block_sum<kCamG>(gacc, gscratch);
   if (threadIdx.x == 0) {
     double* U = B.camU + 21 * c;
-    for (int i = 0; i < 21; ++i) U[i] = acc[i];
-    for (int i = 0; i < 6; ++i) B.camgj[6 * c + i] = acc[21 + i], B.camgs[6 * c + i] = acc[27 + i];
-    for (int i = 0; i < 18; ++i) B.camX[18 * c + i] = acc[33 + i];
-    for (int i = 0; i < 12; ++i) B.caml[12 * c + i] = acc[51 + i];
+    for (int i = 0; i < 21; ++i) U[i] = (double)acc[i];
+    for (int i = 0; i < 6; ++i) B.camgj[6 * c + i] = gacc[i], B.camgs[6 * c + i] = gacc[6 + i];
+    for (int i = 0; i < 18; ++i) B.camX[18 * c + i] = (double)acc[21 + i];
+    for (int i = 0; i < 6; ++i) B.caml[12 * c + i] = (double)acc[39 + i];
+    for (int i = 0; i < 6; ++i) B.caml[12 * c + 6 + i] = gacc[12 + i];
   }
 }
 
@@ -606,9 +623,9 @@ __global__ void precond_kernel(Prob P, StructView S, IterBufs<R> B, const int32_
 #pragma unroll
     for (int i = 0; i < 36; ++i) Ai[i] = (i % 7 == 0) ? 1.0 : 0.0;
   }
-  double* o = B.pre + 36 * (size_t)b;
+  R* o = B.pre + 36 * (size_t)b;
 #pragma unroll
-  for (int i = 0; i < 36; ++i) o[i] = Ai[i];
+  for (int i = 0; i < 36; ++i) o[i] = (R)Ai[i];
 }
 
 // ---- update (ba.rs:338-366) ---------------------------------------------------
@@ -652,17 +669,17 @@ __global__ void backsub_kernel(Prob P, StructView S, StateView cur, StateView tr
     Xt[0] = X[0], Xt[1] = X[1], Xt[2] = X[2];
     return;
   }
-  double a0 = B.ptzv[3 * p], a1 = B.ptzv[3 * p + 1], a2 = B.ptzv[3 * p + 2];
+  R a0 = B.ptzv[3 * p], a1 = B.ptzv[3 * p + 1], a2 = B.ptzv[3 * p + 2];
   const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
   for (uint32_t k = s; k < e; ++k) {
     const R* Z = B.Z + (size_t)k * 18;
     const R* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-      const double dr = (double)d[r];
-      a0 -= (double)Z[3 * r] * dr;
-      a1 -= (double)Z[3 * r + 1] * dr;
-      a2 -= (double)Z[3 * r + 2] * dr;
+      const R dr = d[r];
+      a0 -= Z[3 * r] * dr;
+      a1 -= Z[3 * r + 1] * dr;
+      a2 -= Z[3 * r + 2] * dr;
     }
   }
   for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j) {
@@ -670,17 +687,17 @@ __global__ void backsub_kernel(Prob P, StructView S, StateView cur, StateView tr
     const R* d = B.x + 6 * (size_t)P.grp_blk[S.lens_grp[j]];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      const double dr = (double)d[r];
-      a0 -= (double)Z[3 * r] * dr;
-      a1 -= (double)Z[3 * r + 1] * dr;
-      a2 -= (double)Z[3 * r + 2] * dr;
+      const R dr = d[r];
+      a0 -= Z[3 * r] * dr;
+      a1 -= Z[3 * r + 1] * dr;
+      a2 -= Z[3 * r + 2] * dr;
     }
   }
   const R* L = B.ptL + 6 * p;
-  const double l00 = L[0], l10 = L[1], l11 = L[2], l20 = L[3], l21 = L[4], l22 = L[5];
-  Xt[0] = X[0] + l00 * a0;
-  Xt[1] = X[1] + (l10 * a0 + l11 * a1);
-  Xt[2] = X[2] + (l20 * a0 + l21 * a1 + l22 * a2);
+  const R l00 = L[0], l10 = L[1], l11 = L[2], l20 = L[3], l21 = L[4], l22 = L[5];
+  Xt[0] = X[0] + (double)(l00 * a0);
+  Xt[1] = X[1] + (double)(l10 * a0 + l11 * a1);
+  Xt[2] = X[2] + (double)(l20 * a0 + l21 * a1 + l22 * a2);
 }
 
 }  // namespace ba

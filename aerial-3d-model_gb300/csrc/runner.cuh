@@ -22,10 +22,22 @@ struct PcgPlan {
 
 // Split the block rows of each model over a group of CTAs, balancing
 // (blocks + 1) per row; models with fewer blocks get fewer CTAs.
-inline PcgPlan plan_pcg(const Context& ctx, const std::vector<uint32_t>& row_ptr, int max_ctas,
+inline PcgPlan plan_pcg(const Context& ctx, const std::vector<uint32_t>& row_ptr_in,
+                        const std::vector<int32_t>& lens_row, int max_ctas,
                         int64_t blocks_per_cta) {
   PcgPlan pl;
   const int64_t nm = ctx.nm;
+  // Work per row: its blocks, except a transposed lens row (its camera blocks
+  // are multiplied by the camera rows' CTAs).
+  std::vector<uint32_t> row_ptr(row_ptr_in.size());
+  row_ptr[0] = 0;
+  {
+    std::vector<uint8_t> is_lens(row_ptr_in.size(), 0);
+    for (int32_t r : lens_row)
+      if (r >= 0) is_lens[r] = 1;
+    for (size_t r = 0; r + 1 < row_ptr_in.size(); ++r)
+      row_ptr[r + 1] = row_ptr[r] + (is_lens[r] ? 1u : row_ptr_in[r + 1] - row_ptr_in[r]);
+  }
   std::vector<int64_t> cost(nm);
   for (int64_t m = 0; m < nm; ++m) {
     const uint32_t r0 = ctx.h_blk0[m], r1 = ctx.h_blk0[m + 1];
@@ -153,9 +165,9 @@ struct LmEngine {
   Prob P;
   StructBufs SB;
   StructView SV;
-  DevBuf<R> lin, gsub, Z, Zl, ptL, ptzv, part, S, g, x, r, z, p, q;
+  DevBuf<R> lin, gsub, Z, Zl, ptL, ptzv, part, S, pre, g, x, r, z, p, q;
   DevBuf<uint8_t> kept;
-  DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, pre, cost_part;
+  DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
   DevBuf<int64_t> n_front, pcg_total;
@@ -168,6 +180,7 @@ struct LmEngine {
   DevBuf<PcgJob> jobs;
   DevBuf<int32_t> cta_job0;
   DevBuf<unsigned long long> bar;
+  DevBuf<int32_t> lens_row;
   DevBuf<double> pcg_part;
   PcgArgs<R> pa{};
   PhaseTimer T;
@@ -228,15 +241,21 @@ struct LmEngine {
           "occupancy");
     const int max_ctas = std::max(1, occ) * ctx.n_sm;
     const int64_t per_cta = sizeof(R) == 8 ? 96 : 192;
-    plan = detail::plan_pcg(ctx, SB.h_row_ptr, max_ctas, per_cta);
+    std::vector<int32_t> h_lens(nm, -1);
+    for (int64_t m = 0; m < nm; ++m)
+      if (ctx.h_grp0[m + 1] - ctx.h_grp0[m] == 1)
+        h_lens[m] = (int32_t)(ctx.h_blk0[m] + (ctx.h_cam0[m + 1] - ctx.h_cam0[m]));
+    plan = detail::plan_pcg(ctx, SB.h_row_ptr, h_lens, max_ctas, per_cta);
+    detail::h2d(lens_row, h_lens, s);
     detail::h2d(jobs, plan.jobs, s);
     detail::h2d(cta_job0, plan.cta_job0, s);
     bar.alloc(nm, s);
     bar.zero();
-    pcg_part.alloc(5 * (size_t)plan.ncta, s);
+    pcg_part.alloc(kParts * (size_t)plan.ncta, s);
     check(cudaStreamSynchronize(s), "sync");  // host plan vectors
     pa = PcgArgs<R>{jobs, cta_job0, bar, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx, S, pre, g,
-                    x, r, z, q, p, nb, active, pcg_iters, o.pcg_max_iter, o.pcg_tol, ctx.err};
+                    x, r, z, q, p, nb, lens_row, active, pcg_iters, o.pcg_max_iter, o.pcg_tol,
+                    ctx.err};
   }
 
   void set_lambda(double lam) {
