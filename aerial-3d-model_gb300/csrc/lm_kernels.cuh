@@ -34,7 +34,6 @@ struct IterBufs {
   R* pre;         // [nb][36] block-Jacobi inverses (computed in FP64)
   R* g;           // [nb][6]
   R* x;           // [nb][6] (dx)
-  R *r, *z, *p, *q;  // PCG work vectors [nb][6]
   double* cost_part;  // [ncost][3]
 };
 

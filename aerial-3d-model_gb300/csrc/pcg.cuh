@@ -1,23 +1,27 @@
 // Block-Jacobi preconditioned conjugate gradients on the reduced camera
 // system (ba.rs:155-196), as one persistent cooperative kernel.
 //
-// Each model's block rows are split over a group of CTAs.  The reference's
-// iteration
+// Each model's block rows are split over a group of CTAs and, inside a CTA,
+// over its warps: a warp owns whole block rows.  The reference's iteration
 //     q = S p;  a = rz / p·q;  x += a p;  r -= a q;  stop if r·r < tol b·b;
 //     z = M r;  β = r·z / rz;  p = z + β p
 // needs three group-wide exchanges (p, p·q, r·r and r·z).  Here p is never
-// exchanged: every CTA forms p_j = z_j + β p_j(prev) on the fly for the columns
-// its matrix-vector product touches (z and the previous p are double-buffered
-// and visible after the previous exchange), so an iteration costs two group
-// barriers.
+// exchanged: every warp forms p_j = z_j + β p_j(prev) on the fly for the
+// columns its rows touch (z and the previous p are double-buffered in global
+// memory and visible after the previous exchange), so an iteration costs two
+// group barriers.
+//
+// A CTA keeps its rows' state (x, r, z, p, q and the 6x6 block-Jacobi
+// inverse) in shared memory for the whole solve, and its S blocks too when
+// they fit; only the gathered neighbour z / p come from L2 each iteration.
 //
 // The lens block row of a model couples to every camera, so it is not
-// multiplied by one CTA: every camera row c adds S_cg^T p_c to a lens partial,
-// which travels with the p·q partial sums (S is symmetric, S_gc = S_cg^T).
+// multiplied by one warp: every camera row c adds S_cg^T p_c to a lens
+// partial that travels with the p·q partial sums (S is symmetric).
 //
 // FP64 instructions on this GPU cost ~64 cycles per SM sub-partition whatever
-// the number of active lanes, so reductions pack several values per
-// instruction (recursive halving) instead of one butterfly per value.
+// the number of active lanes, so row vectors live one component per lane and
+// reductions pack several values per instruction.
 //
 // Inner products are FP64 and summed in a fixed order (fixed lane trees, CTA
 // partials in rank order), so every CTA of a group sees bit-identical scalars
@@ -30,7 +34,6 @@ namespace ba {
 
 constexpr int kPcgThreads = 256;
 constexpr int kPcgWarps = kPcgThreads / 32;
-constexpr uint32_t kLongRow = 64;  // blocks; longer rows (other than the lens row) use all warps
 
 struct PcgJob {
   int32_t model, rank, gsize, base;  // base: first CTA of the group
@@ -49,10 +52,14 @@ struct PcgArgs {
   const R* S;
   const R* pre;  // block-Jacobi inverses, computed in FP64, stored in R
   const R* b;
-  R *x, *r, *z, *q;
+  R* x;
+  R* z;   // [nb][6] z = M r, gathered by neighbours
   R* p2;  // [2][nb][6] double-buffered search direction
   int64_t nb;
   const int32_t* lens_row;  // [nm]: the model's single lens block row, or -1
+  const int32_t* lens_pos;  // [nb]: block index of (row, lens row), or -1
+  uint32_t smem_rows;       // row-state capacity of the dynamic shared memory
+  uint32_t smem_blocks;     // S-block capacity (0: S read from global)
   const int32_t* active;
   int32_t* iters;
   int32_t max_iter;
@@ -62,6 +69,15 @@ struct PcgArgs {
 
 // partial slots: 0,1 init (rz, bb) | 2..5 (pq, lens q 0..2) | 6,7 (rr, rz)
 constexpr int kParts = 8;
+
+// Row state per local row in shared memory: x, r, z, p, q (6 each), M (36),
+// padded to a multiple of 16 bytes in both precisions.
+constexpr int kRowState = 68;
+
+template <typename R>
+constexpr size_t pcg_smem_bytes(uint32_t rows, uint32_t blocks) {
+  return (size_t)rows * kRowState * sizeof(R) + (size_t)blocks * (36 * sizeof(R) + 4);
+}
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
   unsigned long long v;
@@ -142,21 +158,31 @@ __device__ __forceinline__ void warp_sum8(T (&v)[8]) {
   v[0] += __shfl_xor_sync(kFull, v[0], 1);
 }
 
-// Sum N (<= 8) per-warp values over the CTA's warps, then over the group's
-// CTAs in rank order; every thread receives the totals in tot[].
+// Sum over lanes 0..7 (lanes >= 8 must hold 0): result in lanes 0..7.
+__device__ __forceinline__ double sum8(double v) {
+  v += __shfl_xor_sync(kFull, v, 1);
+  v += __shfl_xor_sync(kFull, v, 2);
+  v += __shfl_xor_sync(kFull, v, 4);
+  return v;
+}
+
+// N (<= 4) values per warp (held by lane 0) summed over the CTA's warps with
+// one shuffle tree, then over the group's CTAs in rank order; every thread
+// receives the totals in tot[].
 template <int N, typename R>
 __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm, double* tot,
                                              const PcgArgs<R>& A, const PcgJob& J, int slot) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
-    for (int i = 0; i < N; ++i) wsm[warp * 8 + i] = wv[i];
+    for (int i = 0; i < 4; ++i) wsm[warp * 4 + i] = i < N ? wv[i < N ? i : 0] : 0.0;
   __syncthreads();
   if (warp == 0) {
-    // CTA partial: value i summed over the warps in order.
-    double c = 0.0;
-    if (lane < N)
-      for (int w = 0; w < kPcgWarps; ++w) c += wsm[w * 8 + lane];
+    // lane = 4 w + i: warp w, value i; sum over w in a fixed tree.
+    double c = wsm[lane];
+    c += __shfl_xor_sync(kFull, c, 4);
+    c += __shfl_xor_sync(kFull, c, 8);
+    c += __shfl_xor_sync(kFull, c, 16);
     if (J.gsize > 1) {
       if (lane < N) A.part[(size_t)(slot + lane) * A.ncta + J.base + J.rank] = c;
       __threadfence();
@@ -185,13 +211,13 @@ __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm,
   return true;
 }
 
-// A 6x6 block into registers with 16-byte loads.
+// A 6x6 block into registers with 16-byte loads (global or shared).
 template <typename A>
 __device__ __forceinline__ void load_block(const double* blk, A* m) {
   const double2* v = reinterpret_cast<const double2*>(blk);
 #pragma unroll
   for (int i = 0; i < 18; ++i) {
-    const double2 t = __ldg(v + i);
+    const double2 t = v[i];
     m[2 * i] = (A)t.x, m[2 * i + 1] = (A)t.y;
   }
 }
@@ -200,7 +226,7 @@ __device__ __forceinline__ void load_block(const float* blk, A* m) {
   const float4* v = reinterpret_cast<const float4*>(blk);
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
-    const float4 t = __ldg(v + i);
+    const float4 t = v[i];
     m[4 * i] = (A)t.x, m[4 * i + 1] = (A)t.y, m[4 * i + 2] = (A)t.z, m[4 * i + 3] = (A)t.w;
   }
 }
@@ -213,51 +239,63 @@ __device__ __forceinline__ R p_of(R zj, R pj, double beta) {
 }
 
 template <typename R>
-__device__ __forceinline__ void gather_p(const PcgArgs<R>& A, const R* pprev, uint32_t col,
-                                         double beta, R* pp) {
-  const R* zv = A.z + 6 * (size_t)col;
-  const R* pv = pprev + 6 * (size_t)col;
-#pragma unroll
-  for (int j = 0; j < 6; ++j) pp[j] = p_of<R>(__ldcg(zv + j), __ldcg(pv + j), beta);
-}
-
-template <typename R>
 __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, double* tot,
-                        double* long_part) {
+                        R* rs) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nrows = J.row1 - J.row0;
+  const uint32_t B0 = A.row_ptr[J.row0];
+  const uint32_t nblk = A.row_ptr[J.row1] - B0;
+  if (nrows > A.smem_rows) {  // the planner never does this; fail loudly
+    if (threadIdx.x == 0) atomicOr(A.err, ERR_STRUCTURE);
+    return false;
+  }
+  const bool cached = nblk <= A.smem_blocks;
+  // Shared-memory carve-up: row state, then cached S blocks and columns.
+  R* sS = rs + (size_t)A.smem_rows * kRowState;
+  uint32_t* sC = reinterpret_cast<uint32_t*>(sS + (size_t)A.smem_blocks * 36);
   const int32_t lens = A.lens_row[J.model];  // -1: no transposed lens row
-  // Six threads per block row for the vector phases: lanes 6s..6s+5 of a
-  // warp hold row (warp*5 + s), component lane%6.
-  const int sub = lane / 6, comp = lane - 6 * sub;
-  const bool vlane = sub < 5;
+  if (cached) {
+    const uint32_t chunks = nblk * (uint32_t)(36 * sizeof(R) / 16);
+    const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
+    float4* dst = reinterpret_cast<float4*>(sS);
+    for (uint32_t c = threadIdx.x; c < chunks; c += blockDim.x) dst[c] = src[c];
+    for (uint32_t t = threadIdx.x; t < nblk; t += blockDim.x) sC[t] = A.col_idx[B0 + t];
+  }
+  for (uint32_t t = threadIdx.x; t < nrows * 36; t += blockDim.x)
+    rs[(t / 36) * kRowState + 30 + (t % 36)] = A.pre[36 * (size_t)J.row0 + t];
+  __syncthreads();
+  const bool vl = lane < 6;
+  const int ci = vl ? lane : 0;
+  // row state: x 0..5 | r 6..11 | z 12..17 | p 18..23 | q 24..29 | M 30..65
+#define ROW(lr) (rs + (size_t)(lr) * kRowState)
+
   // x = 0, r = b, z = M r, p(prev) = 0 (ba.rs:164-168; β = 0 gives p = z)
-  double acc2[2] = {0.0, 0.0};
-  for (uint32_t grp = warp; grp * 5 < J.row1 - J.row0; grp += kPcgWarps) {
-    const uint32_t row = J.row0 + grp * 5 + sub;
-    const bool on = vlane && row < J.row1;
-    const size_t o = 6 * (size_t)row + comp;
-    const R rb = on ? A.b[o] : (R)0;
+  double w2[2] = {0.0, 0.0};
+  for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps) {
+    const uint32_t row = J.row0 + lr;
+    R* st = ROW(lr);
+    const R ri = vl ? A.b[6 * (size_t)row + ci] : (R)0;
     R zi = (R)0;
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      const R rj = __shfl_sync(kFull, rb, min(6 * sub + j, 31));
-      if (on) zi += A.pre[36 * (size_t)row + 6 * comp + j] * rj;
+      const R rj = __shfl_sync(kFull, ri, j);
+      zi += st[30 + 6 * ci + j] * rj;
     }
-    if (on) {
-      A.x[o] = (R)0;
-      A.r[o] = rb;
-      A.z[o] = zi;
-      A.p2[(size_t)6 * A.nb + o] = (R)0;
-      acc2[0] += (double)rb * (double)zi;
-      acc2[1] += (double)rb * (double)rb;
+    double a = 0.0, bb = 0.0;
+    if (vl) {
+      st[ci] = (R)0;
+      st[6 + ci] = ri;
+      st[12 + ci] = zi;
+      st[18 + ci] = (R)0;
+      A.z[6 * (size_t)row + ci] = zi;
+      A.p2[(size_t)6 * A.nb + 6 * (size_t)row + ci] = (R)0;
+      a = (double)ri * (double)zi;
+      bb = (double)ri * (double)ri;
     }
+    w2[0] += sum8(a);
+    w2[1] += sum8(bb);
   }
-  {
-    double v[8] = {acc2[0], acc2[1], 0, 0, 0, 0, 0, 0};
-    warp_sum8(v);
-    double wv[2] = {__shfl_sync(kFull, v[0], 0), __shfl_sync(kFull, v[0], 4)};
-    if (!group_reduce<2>(wv, wsm, tot, A, J, 0)) return false;
-  }
+  if (!group_reduce<2>(w2, wsm, tot, A, J, 0)) return false;
   double rz = tot[0];
   const double b2 = fmax(tot[1], 1e-300);
   double beta = 0.0;
@@ -265,181 +303,152 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
   for (int32_t it = 0; it < A.max_iter; ++it) {
     R* pcur = A.p2 + (size_t)(it & 1) * 6 * A.nb;
     const R* pprev = A.p2 + (size_t)((it + 1) & 1) * 6 * A.nb;
-    // q = S p (ba.rs:144-152), warp per camera block row; per warp: p·q and
-    // the lens partial Σ S_cg^T p_c (3 components; the rest of S_cg^T is 0).
-    double wpq = 0.0, wl0 = 0.0, wl1 = 0.0, wl2 = 0.0;
-    for (uint32_t row = J.row0 + warp; row < J.row1; row += kPcgWarps) {
+    // q = S p (ba.rs:144-152) for the warp's rows.
+    double w4[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps) {
+      const uint32_t row = J.row0 + lr;
+      R* st = ROW(lr);
       const uint32_t b0 = A.row_ptr[row], b1 = A.row_ptr[row + 1];
       const bool is_lens = (int32_t)row == lens;
-      if (!is_lens && b1 - b0 > kLongRow) continue;
-      R pown[6];
-#pragma unroll
-      for (int j = 0; j < 6; ++j) pown[j] = p_of<R>(A.z[6 * (size_t)row + j], pprev[6 * (size_t)row + j], beta);
       R acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      R tl0 = 0, tl1 = 0, tl2 = 0;
       for (uint32_t k = b0 + lane; k < b1; k += 32) {
-        const uint32_t col = A.col_idx[k];
-        // Lens row: only its blocks with the lens column (the diagonal);
+        const uint32_t col = cached ? sC[k - B0] : A.col_idx[k];
+        // Lens row: only its block with the lens column (the diagonal);
         // camera columns arrive through the camera rows' transposed terms.
         if (is_lens && (int32_t)col != lens) continue;
         R m[36], pp[6];
-        load_block(A.S + (size_t)k * 36, m);
-        gather_p<R>(A, pprev, col, beta, pp);
+        load_block(cached ? sS + (size_t)(k - B0) * 36 : A.S + (size_t)k * 36, m);
+        const R* zv = A.z + 6 * (size_t)col;
+        const R* pv = pprev + 6 * (size_t)col;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) pp[j] = p_of<R>(__ldcg(zv + j), __ldcg(pv + j), beta);
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
-          R a = 0;
+          R s = acc[i];
 #pragma unroll
-          for (int j = 0; j < 6; ++j) a += m[6 * i + j] * pp[j];
-          acc[i] += a;
-        }
-        if (!is_lens && (int32_t)col == lens) {
-#pragma unroll
-          for (int t = 0; t < 6; ++t) {
-            tl0 += m[6 * t + 0] * pown[t];
-            tl1 += m[6 * t + 1] * pown[t];
-            tl2 += m[6 * t + 2] * pown[t];
-          }
+          for (int j = 0; j < 6; ++j) s += m[6 * i + j] * pp[j];
+          acc[i] = s;
         }
       }
-      acc[6] = tl0, acc[7] = tl1;
-      warp_sum8(acc);  // lane 4i holds q_i (i < 6) and lens terms 0, 1
-      R tl2s = tl2;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) tl2s += __shfl_xor_sync(kFull, tl2s, o);
-      // q_i lives in lane 4i; p·q = Σ p_i q_i over lanes 0, 4, .., 20.
-      const int qi = lane >> 2;
-      const bool qlane = (lane & 3) == 0 && qi < 6;
-      if (qlane) A.q[6 * (size_t)row + qi] = acc[0];
-      double d = 0.0;
-      if (qlane)
-        d = (double)p_of<R>(A.z[6 * (size_t)row + qi], pprev[6 * (size_t)row + qi], beta) *
-            (double)acc[0];
-      d += __shfl_xor_sync(kFull, d, 4);
-      d += __shfl_xor_sync(kFull, d, 8);
-      d += __shfl_xor_sync(kFull, d, 16);
-      wpq += __shfl_sync(kFull, d, 0);
-      wl0 += (double)__shfl_sync(kFull, acc[0], 24);
-      wl1 += (double)__shfl_sync(kFull, acc[0], 28);
-      wl2 += (double)tl2s;
-    }
-    // Rows longer than kLongRow that are not a transposed lens row: all warps.
-    for (uint32_t row = J.row0; row < J.row1; ++row) {  // CTA-uniform
-      const uint32_t b0 = A.row_ptr[row], b1 = A.row_ptr[row + 1];
-      if ((int32_t)row == lens || b1 - b0 <= kLongRow) continue;
-      const uint32_t chunk = (b1 - b0 + kPcgWarps - 1) / kPcgWarps;
-      const uint32_t k0 = b0 + warp * chunk, k1 = min(b1, k0 + chunk);
-      R acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      for (uint32_t k = k0 + lane; k < k1; k += 32) {
-        R m[36], pp[6];
-        load_block(A.S + (size_t)k * 36, m);
-        gather_p<R>(A, pprev, A.col_idx[k], beta, pp);
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-          R a = 0;
-#pragma unroll
-          for (int j = 0; j < 6; ++j) a += m[6 * i + j] * pp[j];
-          acc[i] += a;
+      warp_sum8(acc);  // lane 4i holds q_i
+      const R qi = __shfl_sync(kFull, acc[0], 4 * ci);
+      // own p = z + β p(prev)
+      const R pi = p_of<R>(st[12 + ci], st[18 + ci], beta);
+      __syncwarp();
+      if (vl) {
+        st[24 + ci] = qi;
+        st[18 + ci] = pi;
+        pcur[6 * (size_t)row + ci] = pi;
+      }
+      w4[0] += sum8(vl ? (double)pi * (double)qi : 0.0);
+      // S_cg^T p_c for the lens column: lane 3t + j multiplies S_cg[t][j] p_t.
+      const int32_t lp = is_lens ? -1 : A.lens_pos[row];
+      if (lp >= 0) {
+        const int t = lane / 3, j = lane - 3 * (lane / 3);
+        const R pt = __shfl_sync(kFull, pi, t < 6 ? t : 0);
+        R v = (R)0;
+        if (lane < 18) {
+          const R* blk = cached ? sS + (size_t)(lp - B0) * 36 : A.S + (size_t)lp * 36;
+          v = blk[6 * t + j] * pt;
         }
-      }
-      warp_sum8(acc);
-      if ((lane & 3) == 0 && (lane >> 2) < 6) long_part[6 * warp + (lane >> 2)] = (double)acc[0];
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double d = 0.0;
-        for (int i = 0; i < 6; ++i) {
-          R s = 0;
-          for (int w = 0; w < kPcgWarps; ++w) s += (R)long_part[6 * w + i];
-          A.q[6 * (size_t)row + i] = s;
-          d += (double)p_of<R>(A.z[6 * (size_t)row + i], pprev[6 * (size_t)row + i], beta) *
-               (double)s;
-        }
-        wpq += d;
-      }
-      __syncthreads();
-    }
-    // own rows: p = z + β p(prev) for the update below and the next gather
-    for (uint32_t grp = warp; grp * 5 < J.row1 - J.row0; grp += kPcgWarps) {
-      const uint32_t row = J.row0 + grp * 5 + sub;
-      if (vlane && row < J.row1) {
-        const size_t o = 6 * (size_t)row + comp;
-        pcur[o] = p_of<R>(A.z[o], pprev[o], beta);
+        v += __shfl_down_sync(kFull, v, 3);
+        v += __shfl_down_sync(kFull, v, 6);
+        v += __shfl_down_sync(kFull, v, 12);
+        // lanes 0, 1, 2 hold the three components; every lane adds the same
+        w4[1] += (double)__shfl_sync(kFull, v, 0);
+        w4[2] += (double)__shfl_sync(kFull, v, 1);
+        w4[3] += (double)__shfl_sync(kFull, v, 2);
       }
     }
-    {
-      double wv[4] = {wpq, wl0, wl1, wl2};
-      if (!group_reduce<4>(wv, wsm, tot, A, J, 2)) return false;
-    }
+    if (!group_reduce<4>(w4, wsm, tot, A, J, 2)) return false;
     ++spmv;
     double pq = tot[0];
-    // The lens row's q: its diagonal product (computed by its owner in the
-    // row loop above) plus the reduced transposed partials.
-    if (lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1 && threadIdx.x < 3) {
-      const size_t o = 6 * (size_t)lens + threadIdx.x;
-      A.q[o] = (R)((double)A.q[o] + tot[1 + threadIdx.x]);
-    }
     if (lens >= 0) {
-      // p_g · (Σ S_cg^T p_c): the lens row's share of p·q.
-      const R* pg = pcur + 6 * (size_t)lens;
+      // The lens row's q: its diagonal product plus the transposed partials;
+      // its share of p·q: p_g · (Σ S_cg^T p_c).
       const R* zg = A.z + 6 * (size_t)lens;
-      const R* pgp = pprev + 6 * (size_t)lens;
-      (void)pg;
-      pq += (double)p_of<R>(__ldcg(zg + 0), __ldcg(pgp + 0), beta) * tot[1] +
-            (double)p_of<R>(__ldcg(zg + 1), __ldcg(pgp + 1), beta) * tot[2] +
-            (double)p_of<R>(__ldcg(zg + 2), __ldcg(pgp + 2), beta) * tot[3];
+      const R* pg = pprev + 6 * (size_t)lens;
+      pq += (double)p_of<R>(__ldcg(zg + 0), __ldcg(pg + 0), beta) * tot[1] +
+            (double)p_of<R>(__ldcg(zg + 1), __ldcg(pg + 1), beta) * tot[2] +
+            (double)p_of<R>(__ldcg(zg + 2), __ldcg(pg + 2), beta) * tot[3];
+      if ((uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1 && threadIdx.x < 3) {
+        R* q = ROW((uint32_t)lens - J.row0) + 24;
+        q[threadIdx.x] = (R)((double)q[threadIdx.x] + tot[1 + threadIdx.x]);
+      }
     }
     __syncthreads();
     if (fabs(pq) < 1e-300) break;  // ba.rs:174
     const double a = rz / pq;
-    // x += a p, r -= a q, z = M r (ba.rs:178-188), six threads per row.
-    double acc3[2] = {0.0, 0.0};
-    for (uint32_t grp = warp; grp * 5 < J.row1 - J.row0; grp += kPcgWarps) {
-      const uint32_t row = J.row0 + grp * 5 + sub;
-      const bool on = vlane && row < J.row1;
-      const size_t o = 6 * (size_t)row + comp;
+    // x += a p, r -= a q, z = M r (ba.rs:178-188), one component per lane.
+    double w2b[2] = {0.0, 0.0};
+    for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps) {
+      const uint32_t row = J.row0 + lr;
+      R* st = ROW(lr);
       R ri = (R)0;
-      if (on) {
-        A.x[o] = A.x[o] + pcur[o] * (R)a;
-        ri = A.r[o] - A.q[o] * (R)a;
-        A.r[o] = ri;
+      if (vl) {
+        st[ci] = st[ci] + st[18 + ci] * (R)a;
+        ri = st[6 + ci] - st[24 + ci] * (R)a;
+        st[6 + ci] = ri;
       }
       R zi = (R)0;
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
-        const R rj = __shfl_sync(kFull, ri, min(6 * sub + j, 31));
-        if (on) zi += A.pre[36 * (size_t)row + 6 * comp + j] * rj;
+        const R rj = __shfl_sync(kFull, ri, j);
+        zi += st[30 + 6 * ci + j] * rj;
       }
-      if (on) {
-        A.z[o] = zi;
-        acc3[0] += (double)ri * (double)ri;
-        acc3[1] += (double)ri * (double)zi;
+      double rr = 0.0, rzl = 0.0;
+      if (vl) {
+        st[12 + ci] = zi;
+        A.z[6 * (size_t)row + ci] = zi;
+        rr = (double)ri * (double)ri;
+        rzl = (double)ri * (double)zi;
       }
+      w2b[0] += sum8(rr);
+      w2b[1] += sum8(rzl);
     }
-    {
-      double v[8] = {acc3[0], acc3[1], 0, 0, 0, 0, 0, 0};
-      warp_sum8(v);
-      double wv[2] = {__shfl_sync(kFull, v[0], 0), __shfl_sync(kFull, v[0], 4)};
-      if (!group_reduce<2>(wv, wsm, tot, A, J, 6)) return false;
-    }
+    if (!group_reduce<2>(w2b, wsm, tot, A, J, 6)) return false;
     const double rr = tot[0], rz2 = tot[1];
     __syncthreads();
     if (rr < A.tol * b2) break;  // ba.rs:182
     beta = rz2 / rz;             // ba.rs:189-190
     rz = rz2;
   }
+  for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps)
+    if (vl) A.x[6 * (size_t)(J.row0 + lr) + ci] = ROW(lr)[ci];
+#undef ROW
   if (J.rank == 0 && threadIdx.x == 0) A.iters[J.model] = spmv;
+  __syncthreads();
   return true;
 }
 
 template <typename R>
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<R> A) {
-  __shared__ double wsm[kPcgWarps * 8];
-  __shared__ double tot[8];
-  __shared__ double long_part[6 * kPcgWarps];
+  __shared__ double wsm[kPcgWarps * 4];
+  __shared__ double tot[4];
+  extern __shared__ __align__(16) unsigned char pcg_smem[];
+  R* rs = reinterpret_cast<R*>(pcg_smem);
   for (int jb = A.cta_job0[blockIdx.x]; jb < A.cta_job0[blockIdx.x + 1]; ++jb) {
     const PcgJob J = A.jobs[jb];
     if (!A.active[J.model]) continue;
-    if (!pcg_job<R>(A, J, wsm, tot, long_part)) return;
+    if (!pcg_job<R>(A, J, wsm, tot, rs)) return;
   }
+}
+
+// lens_pos[row] = index of the block (row, lens row of its model), or -1.
+__global__ static void lens_pos_kernel(int64_t nb, const uint32_t* row_ptr,
+                                       const uint32_t* col_idx, const uint32_t* blk_model,
+                                       const int32_t* lens_row, int32_t* lens_pos) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nb) return;
+  const int32_t L = lens_row[blk_model[r]];
+  int32_t pos = -1;
+  if (L >= 0 && L != (int32_t)r)
+    for (uint32_t k = row_ptr[r]; k < row_ptr[r + 1]; ++k)
+      if ((int32_t)col_idx[k] == L) {
+        pos = (int32_t)k;
+        break;
+      }
+  lens_pos[r] = pos;
 }
 
 }  // namespace ba

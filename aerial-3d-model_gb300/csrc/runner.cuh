@@ -12,6 +12,8 @@
 
 namespace ba {
 
+constexpr size_t kPcgSmemBudget = 96 * 1024;  // dynamic shared memory per PCG CTA
+
 namespace detail {
 
 struct PcgPlan {
@@ -20,88 +22,91 @@ struct PcgPlan {
   int32_t ncta = 0;
 };
 
-// Split the block rows of each model over a group of CTAs, balancing
-// (blocks + 1) per row; models with fewer blocks get fewer CTAs.
+// Split the block rows of each model over a group of CTAs, a CTA's rows
+// over its warps.  Each CTA gets about `rows_target` rows (never more than
+// `rows_cap`, its shared-memory row capacity), balanced by blocks (a
+// transposed lens row counts one block: its camera blocks are multiplied by
+// the camera rows).  Models with more rows get more CTAs.
 inline PcgPlan plan_pcg(const Context& ctx, const std::vector<uint32_t>& row_ptr_in,
-                        const std::vector<int32_t>& lens_row, int max_ctas,
-                        int64_t blocks_per_cta) {
+                        const std::vector<int32_t>& lens_row, int max_ctas, int rows_target,
+                        int rows_cap) {
   PcgPlan pl;
   const int64_t nm = ctx.nm;
-  // Work per row: its blocks, except a transposed lens row (its camera blocks
-  // are multiplied by the camera rows' CTAs).
-  std::vector<uint32_t> row_ptr(row_ptr_in.size());
-  row_ptr[0] = 0;
+  std::vector<int64_t> rc(row_ptr_in.size() - 1);  // per-row cost
   {
     std::vector<uint8_t> is_lens(row_ptr_in.size(), 0);
     for (int32_t r : lens_row)
       if (r >= 0) is_lens[r] = 1;
-    for (size_t r = 0; r + 1 < row_ptr_in.size(); ++r)
-      row_ptr[r + 1] = row_ptr[r] + (is_lens[r] ? 1u : row_ptr_in[r + 1] - row_ptr_in[r]);
+    for (size_t r = 0; r < rc.size(); ++r)
+      rc[r] = (is_lens[r] ? 1 : (int64_t)(row_ptr_in[r + 1] - row_ptr_in[r])) + 8;
   }
-  std::vector<int64_t> cost(nm);
+  std::vector<int64_t> G(nm), rows(nm);
+  int64_t tot = 0, need = 0;
   for (int64_t m = 0; m < nm; ++m) {
-    const uint32_t r0 = ctx.h_blk0[m], r1 = ctx.h_blk0[m + 1];
-    cost[m] = (int64_t)(row_ptr[r1] - row_ptr[r0]) + (r1 - r0);
+    rows[m] = ctx.h_blk0[m + 1] - ctx.h_blk0[m];
+    G[m] = std::max<int64_t>(1, (rows[m] + rows_target - 1) / rows_target);
+    tot += G[m];
+    need += std::max<int64_t>(1, (rows[m] + rows_cap - 1) / rows_cap);
   }
-  if (nm <= max_ctas) {
-    std::vector<int64_t> G(nm);
-    int64_t tot = 0;
-    for (int64_t m = 0; m < nm; ++m) {
-      G[m] = std::max<int64_t>(1, std::min<int64_t>(max_ctas, (cost[m] + blocks_per_cta - 1) / blocks_per_cta));
-      tot += G[m];
-    }
-    if (tot > max_ctas) {  // scale down, every model keeps at least one CTA
-      int64_t t2 = 0;
-      for (int64_t m = 0; m < nm; ++m) {
-        G[m] = std::max<int64_t>(1, (G[m] * max_ctas) / tot);
-        t2 += G[m];
-      }
-      while (t2 > max_ctas) {
-        const int64_t best = std::max_element(G.begin(), G.end()) - G.begin();
-        if (G[best] <= 1) break;
-        --G[best];
-        --t2;
-      }
-    }
-    int32_t cta = 0;
-    for (int64_t m = 0; m < nm; ++m) {
-      const uint32_t r0 = ctx.h_blk0[m], r1 = ctx.h_blk0[m + 1];
-      const int64_t g = G[m];
-      uint32_t row = r0;
-      int64_t acc = 0;
-      for (int64_t k = 0; k < g; ++k) {
-        const uint32_t start = row;
-        const int64_t target = (cost[m] * (k + 1)) / g;
-        while (row < r1 && (acc + (int64_t)(row_ptr[row + 1] - row_ptr[row]) + 1 <= target ||
-                            k == g - 1)) {
-          acc += (int64_t)(row_ptr[row + 1] - row_ptr[row]) + 1;
-          ++row;
-        }
-        pl.cta_job0.push_back((int32_t)pl.jobs.size());
-        pl.jobs.push_back(PcgJob{(int32_t)m, (int32_t)k, (int32_t)g, cta, start, row});
-      }
-      cta += (int32_t)g;
-    }
-    pl.ncta = cta;
-  } else {
-    // More models than resident CTAs: one CTA per model, models dealt out
-    // greedily to the least-loaded CTA (largest first).
+  if (need > max_ctas) {
+    // More models than resident CTAs: one CTA per model, dealt greedily to
+    // the least-loaded CTA (largest first); a CTA solves its models in turn.
+    for (int64_t m = 0; m < nm; ++m)
+      if (rows[m] > rows_cap) throw std::runtime_error("batch too large for the PCG plan");
     pl.ncta = max_ctas;
     std::vector<std::vector<int64_t>> lists(max_ctas);
     std::vector<int64_t> load(max_ctas, 0), order(nm);
     for (int64_t m = 0; m < nm; ++m) order[m] = m;
-    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cost[a] > cost[b]; });
+    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return rows[a] > rows[b]; });
     for (int64_t m : order) {
       const int64_t c = std::min_element(load.begin(), load.end()) - load.begin();
       lists[c].push_back(m);
-      load[c] += cost[m];
+      load[c] += rows[m];
     }
     for (int c = 0; c < max_ctas; ++c) {
       pl.cta_job0.push_back((int32_t)pl.jobs.size());
       for (int64_t m : lists[c])
         pl.jobs.push_back(PcgJob{(int32_t)m, 0, 1, c, ctx.h_blk0[m], ctx.h_blk0[m + 1]});
     }
+    pl.cta_job0.push_back((int32_t)pl.jobs.size());
+    return pl;
   }
+  while (tot > max_ctas) {  // shrink the largest groups, keep the row cap
+    int64_t best = -1;
+    for (int64_t m = 0; m < nm; ++m)
+      if (G[m] > (rows[m] + rows_cap - 1) / rows_cap && (best < 0 || G[m] > G[best])) best = m;
+    if (best < 0) break;
+    --G[best];
+    --tot;
+  }
+  int32_t cta = 0;
+  for (int64_t m = 0; m < nm; ++m) {
+    const uint32_t r0 = ctx.h_blk0[m], r1 = ctx.h_blk0[m + 1];
+    const int64_t g = G[m];
+    int64_t total = 0;
+    for (uint32_t r = r0; r < r1; ++r) total += rc[r];
+    uint32_t row = r0;
+    int64_t acc = 0;
+    for (int64_t k = 0; k < g; ++k) {
+      const uint32_t start = row;
+      const int64_t target = (total * (k + 1)) / g;
+      const int64_t left_after = (int64_t)(g - k - 1) * rows_cap;
+      while (row < r1) {
+        const int64_t taken = row - start;
+        const int64_t remaining = r1 - row;
+        if (taken >= rows_cap) break;
+        const bool must = remaining > left_after;  // the rest would not fit
+        if (!must && k < g - 1 && acc + rc[row] > target && taken > 0) break;
+        acc += rc[row];
+        ++row;
+      }
+      pl.cta_job0.push_back((int32_t)pl.jobs.size());
+      pl.jobs.push_back(PcgJob{(int32_t)m, (int32_t)k, (int32_t)g, cta, start, row});
+    }
+    if (row != r1) throw std::runtime_error("PCG plan left rows unassigned");
+    cta += (int32_t)g;
+  }
+  pl.ncta = cta;
   pl.cta_job0.push_back((int32_t)pl.jobs.size());
   return pl;
 }
@@ -165,7 +170,7 @@ struct LmEngine {
   Prob P;
   StructBufs SB;
   StructView SV;
-  DevBuf<R> lin, gsub, Z, Zl, ptL, ptzv, part, S, pre, g, x, r, z, p, q;
+  DevBuf<R> lin, gsub, Z, Zl, ptL, ptzv, part, S, pre, g, x, z, p;
   DevBuf<uint8_t> kept;
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
@@ -180,7 +185,10 @@ struct LmEngine {
   DevBuf<PcgJob> jobs;
   DevBuf<int32_t> cta_job0;
   DevBuf<unsigned long long> bar;
-  DevBuf<int32_t> lens_row;
+  DevBuf<int32_t> lens_row, lens_pos;
+  uint32_t smem_rows = 0, smem_blocks = 0;
+  size_t smem_bytes = 0;
+  int pcg_rows_target = 0;
   DevBuf<double> pcg_part;
   PcgArgs<R> pa{};
   PhaseTimer T;
@@ -209,14 +217,14 @@ struct LmEngine {
     grpg.alloc(at_least_1(ng) * 3, s);
     part.alloc(at_least_1(SB.nsub) * 36, s), S.alloc(at_least_1(SB.nz) * 36, s);
     pre.alloc(at_least_1(nb) * 36, s);
-    g.alloc(at_least_1(nb) * 6, s), x.alloc(at_least_1(nb) * 6, s), r.alloc(at_least_1(nb) * 6, s);
-    z.alloc(at_least_1(nb) * 6, s), p.alloc(at_least_1(nb) * 12, s), q.alloc(at_least_1(nb) * 6, s);
+    g.alloc(at_least_1(nb) * 6, s), x.alloc(at_least_1(nb) * 6, s);
+    z.alloc(at_least_1(nb) * 6, s), p.alloc(at_least_1(nb) * 12, s);
     cost_part.alloc(at_least_1(SB.ncost) * 3, s);
     // Camera sums are read for every camera, including ones without observations.
     camU.zero(), camgj.zero(), camgs.zero(), camX.zero(), caml.zero(), grpU.zero(), grpg.zero();
     x.zero();
     B = IterBufs<R>{lin, gsub, Z, Zl, ptL, ptzv, kept, camU, camgj, camgs, camX, caml,
-                    grpU, grpg, part, S, pre, g, x, r, z, p, q, cost_part};
+                    grpU, grpg, part, S, pre, g, x, cost_part};
     lambda.alloc(nm, s), cost.alloc(nm, s), new_cost.alloc(nm, s), rms.alloc(nm, s);
     sq.alloc(nm, s), sigma.alloc(nm, s), n_front.alloc(nm, s), pcg_total.alloc(nm, s);
     active.alloc(nm, s), accepted.alloc(nm, s), iters.alloc(nm, s), pcg_iters.alloc(nm, s);
@@ -235,18 +243,33 @@ struct LmEngine {
     }
     C = Control{lambda, cost, new_cost, rms, sq, n_front, active, accepted, iters, pcg_iters,
                 pcg_total, any, sigma, o.max_iter, log_cap, log_cost, log_lam, log_pcg, log_acc};
-    // PCG plan (cooperative launch: all CTAs co-resident).
+    // PCG plan (cooperative launch: all CTAs co-resident).  Shared memory per
+    // CTA: row state for up to kSmemRows rows, then as many S blocks as fit.
+    smem_rows = 64;
+    smem_blocks = (uint32_t)((kPcgSmemBudget - (size_t)smem_rows * kRowState * sizeof(R)) /
+                             (36 * sizeof(R) + 4));
+    smem_bytes = pcg_smem_bytes<R>(smem_rows, smem_blocks);
+    check(cudaFuncSetAttribute(pcg_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem_bytes),
+          "pcg smem");
     int occ = 0;
-    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_kernel<R>, kPcgThreads, 0),
+    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_kernel<R>, kPcgThreads,
+                                                        smem_bytes),
           "occupancy");
     const int max_ctas = std::max(1, occ) * ctx.n_sm;
-    const int64_t per_cta = sizeof(R) == 8 ? 96 : 192;
     std::vector<int32_t> h_lens(nm, -1);
     for (int64_t m = 0; m < nm; ++m)
       if (ctx.h_grp0[m + 1] - ctx.h_grp0[m] == 1)
         h_lens[m] = (int32_t)(ctx.h_blk0[m] + (ctx.h_cam0[m + 1] - ctx.h_cam0[m]));
-    plan = detail::plan_pcg(ctx, SB.h_row_ptr, h_lens, max_ctas, per_cta);
+    // FP64 instructions serialise per SM sub-partition: one row per warp on
+    // four warps; FP32 rows are cheap: one per warp on all eight.
+    const int rows_target = pcg_rows_target > 0 ? pcg_rows_target : (sizeof(R) == 8 ? 4 : 8);
+    plan = detail::plan_pcg(ctx, SB.h_row_ptr, h_lens, max_ctas, rows_target, (int)smem_rows);
     detail::h2d(lens_row, h_lens, s);
+    lens_pos.alloc(detail::at_least_1(nb), s);
+    if (nb > 0)
+      BA_LAUNCH(lens_pos_kernel<<<grid_for(nb, 256), 256, 0, s>>>(nb, SB.row_ptr, SB.col_idx,
+                                                                 P.blk_model, lens_row, lens_pos));
     detail::h2d(jobs, plan.jobs, s);
     detail::h2d(cta_job0, plan.cta_job0, s);
     bar.alloc(nm, s);
@@ -254,8 +277,8 @@ struct LmEngine {
     pcg_part.alloc(kParts * (size_t)plan.ncta, s);
     check(cudaStreamSynchronize(s), "sync");  // host plan vectors
     pa = PcgArgs<R>{jobs, cta_job0, bar, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx, S, pre, g,
-                    x, r, z, q, p, nb, lens_row, active, pcg_iters, o.pcg_max_iter, o.pcg_tol,
-                    ctx.err};
+                    x, z, p, nb, lens_row, lens_pos, smem_rows, smem_blocks, active, pcg_iters,
+                    o.pcg_max_iter, o.pcg_tol, ctx.err};
   }
 
   void set_lambda(double lam) {
@@ -299,7 +322,7 @@ struct LmEngine {
   void solve_pcg() {
     void* args[] = {&pa};
     check(cudaLaunchCooperativeKernel((void*)pcg_kernel<R>, dim3(plan.ncta), dim3(kPcgThreads),
-                                      args, 0, s),
+                                      args, smem_bytes, s),
           "pcg launch");
     g_launches++;
     T.mark(BA_PHASE_PCG);
