@@ -61,7 +61,7 @@ EXPORTS = [
     "ba_default_options", "ba_solve", "ba_solve_batch", "ba_context_create",
     "ba_context_destroy", "ba_context_upload", "ba_context_solve", "ba_context_download",
     "ba_context_intrinsics_grad", "ba_context_vjp", "ba_context_linearise", "ba_context_cost",
-    "ba_context_debug_step", "ba_last_error",
+    "ba_context_debug_step", "ba_robust_cost_noalloc", "ba_last_error",
     "ba_abi_version", "ba_version",
 ]
 
@@ -107,11 +107,14 @@ def load(build_if_missing: bool = True):
     L.ba_context_cost.argtypes = [C.c_void_p, O, C.c_void_p, C.c_void_p, C.c_void_p]
     L.ba_context_debug_step.argtypes = [C.c_void_p, O, C.c_double, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+    L.ba_robust_cost_noalloc.argtypes = [P, S, C.c_double, C.c_int32, C.c_void_p,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_int64)]
     L.ba_last_error.restype = C.c_char_p
     L.ba_version.restype = C.c_char_p
     for name in ("ba_solve", "ba_solve_batch", "ba_context_create", "ba_context_upload",
                  "ba_context_solve", "ba_context_download", "ba_context_intrinsics_grad",
-                 "ba_context_vjp", "ba_context_debug_step",
+                 "ba_context_vjp", "ba_context_debug_step", "ba_robust_cost_noalloc",
                  "ba_context_linearise", "ba_context_cost"):
         getattr(L, name).restype = C.c_int
     _lib = L

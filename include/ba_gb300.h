@@ -233,6 +233,22 @@ ba_status ba_context_debug_step(ba_context* ctx, const ba_options* opt,
                                 double* dx, int32_t* pcg_iters,
                                 double* trial_cost);
 
+/* Robust cost (ba.rs:103-128) of one problem whose arrays (every pointer in
+ * `problem` and `state`) are already in DEVICE memory, computed without
+ * allocating: for callers that cannot call cudaMalloc — a host whose device
+ * memory is all held by another runtime's caching allocator, or a
+ * latency-critical loop where cudaMalloc / cudaFree would synchronise the
+ * whole device.  Runs on `stream` (NULL: the legacy default stream) on the
+ * current device and waits for it.  Scratch: a fixed 196,632-byte device
+ * array per device, looked up on the first call on that device (make that
+ * first call before any stream capture); at most 33,554,432 observations
+ * per call (BA_BAD_INPUT beyond).  Calls share the scratch: calls that overlap
+ * on the GPU race.  Results go to host memory.  No counterpart in the
+ * reference. */
+ba_status ba_robust_cost_noalloc(const ba_problem* problem, const ba_state* state,
+                                 double sigma_px, int32_t loss, void* stream,
+                                 double* cost, double* rms, int64_t* n_in_front);
+
 /* ---- misc ----------------------------------------------------------------- */
 
 const char* ba_last_error(void);
