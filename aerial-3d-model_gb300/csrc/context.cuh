@@ -49,6 +49,7 @@ struct Context {
   double phase_ms[kPhases] = {0};
   int64_t phase_n[kPhases] = {0};
   int64_t last_nz = 0, last_pairs = 0, last_nl = 0;
+  int32_t last_pcg_kernel = 0, last_pcg_cluster = 0;
   double last_h2d_ms = 0, last_d2h_ms = 0;
   int64_t last_h2d_bytes = 0, last_d2h_bytes = 0;
 
@@ -91,6 +92,7 @@ struct Opts {
   int64_t memory_cap = 0;
   ba_log* log = nullptr;
   int32_t profile = 0;
+  int32_t pcg_kernel = 0;  // 0 auto, 1 grid, 2 cluster
 };
 
 // One solve of the uploaded batch from its initial states, in precision R.

@@ -16,12 +16,15 @@ enum { LOSS_CAUCHY = 0, LOSS_HUBER = 1 };
 template <typename R>
 struct IterBufs {
   R* lin;      // [no][kLinW]
-  R* gsub;     // [no][9]: Y_k V^-1 v (6) | w Jg^T Jp V^-1 v (3)
+  // [no][9]: FP64 form: Y_k V^-1 v (6) | w Jg^T Jp V^-1 v (3).  Mixed form:
+  // the observation's whole share of the reduced gradient, Jc^T r' (6) |
+  // Jg^T r' (3) with r' = w (e - Jp V^-1 v), computed from FP64 values.
+  R* gsub;
   R* Z;        // [no][18]: Y_k L (L L^T = V^-1)
   R* Zl;       // [nl][9]: lens entry, top 3x3
-  R* ptL;      // [np][6]: l00 l10 l11 l20 l21 l22
-  R* ptzv;     // [np][3]: L^T v
-  uint8_t* kept;  // [np]
+  double* ptL;   // [np][6]: l00 l10 l11 l20 l21 l22
+  double* ptzv;  // [np][3]: L^T v
+  uint8_t* kept;  // [np]: 0 skipped, 1 kept, 2 kept and ill-conditioned (mixed form)
   double* camU;   // [nc][21] upper triangle of sum w Jc^T Jc
   double* camgj;  // [nc][6] sum w Jc^T e
   double* camgs;  // [nc][6] sum Y V^-1 v
@@ -29,7 +32,7 @@ struct IterBufs {
   double* caml;   // [nc][12]: lens U upper (6) | sum w Jg^T e (3) | lens Schur g (3)
   double* grpU;   // [ng][6]
   double* grpg;   // [ng][3]
-  R* part;        // [nsub][36]
+  double* part;   // [nsub][36] Schur sub-segment sums
   R* S;           // [nz][36] full symmetric BSR
   R* pre;         // [nb][36] block-Jacobi inverses (computed in FP64)
   R* g;           // [nb][6]
@@ -140,16 +143,10 @@ __device__ __forceinline__ void chol3(const double* A, double* L) {
 // ---- per point: linearise its observations, V, v, V^-1, Z (ba.rs:222-268) ----
 
 template <typename R>
-__global__ void __launch_bounds__(128)
-    point_kernel(Prob P, StateView st, StructView S, IterBufs<R> B, const int32_t* active,
-                 const double* lambda, const double* sigma) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.np) return;
-  const uint32_t m = P.pt_model[p];
-  if (!active[m]) return;
+__device__ __forceinline__ void point_system(const Prob& P, const StateView& st,
+                                             const StructView& S, const IterBufs<R>& B,
+                                             int64_t p, bool refine, double sg, double lam) {
   const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
-  const bool refine = P.model_refine[m] != 0;
-  const double sg = sigma[m], lam = lambda[m];
   if (e - s < 2) {  // ba.rs:238
     B.kept[p] = 0;
     for (uint32_t k = s; k < e; ++k) {
@@ -199,10 +196,10 @@ __global__ void __launch_bounds__(128)
   const R l00 = (R)L[0], l10 = (R)L[1], l11 = (R)L[2], l20 = (R)L[3], l21 = (R)L[4], l22 = (R)L[5];
   const R t0 = (R)(L[0] * zv0d), t1 = (R)(L[1] * zv0d + L[2] * zv1d),
           t2 = (R)(L[3] * zv0d + L[4] * zv1d + L[5] * zv2d);
-  R* pl = B.ptL + 6 * (size_t)p;
+  double* pl = B.ptL + 6 * (size_t)p;
 #pragma unroll
-  for (int i = 0; i < 6; ++i) pl[i] = (R)L[i];
-  B.ptzv[3 * p] = (R)zv0d, B.ptzv[3 * p + 1] = (R)zv1d, B.ptzv[3 * p + 2] = (R)zv2d;
+  for (int i = 0; i < 6; ++i) pl[i] = L[i];
+  B.ptzv[3 * p] = zv0d, B.ptzv[3 * p + 1] = zv1d, B.ptzv[3 * p + 2] = zv2d;
   for (uint32_t k = s; k < e; ++k) {
     const R* o = B.lin + (size_t)k * kLinW;
     R* Z = B.Z + (size_t)k * 18;
@@ -262,6 +259,263 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Mixed form, first pass over an observation: the residual, dudx and Jp in
+// FP64 (the point system V, v and its inverse must be exact: a point whose
+// rays are nearly parallel has a nearly singular V, and FP32 noise in V or v
+// would be amplified by V^-1); the record keeps FP32 Jc, Jp, Jg, e and w.
+__device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& st, int64_t k,
+                                                double sigma, bool refine, float* out,
+                                                double (&jp)[6], double (&ev)[2], double& w) {
+  const uint32_t cam = P.obs_cam[k];
+  const double* Rm = st.rot + 9 * (size_t)cam;
+  const double* C = st.center + 3 * (size_t)cam;
+  const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
+  const double* X = st.points + 3 * (size_t)P.obs_pt[k];
+  double xc[3];
+  bacam::to_cam(Rm, C, X, xc);
+  if (xc[2] <= 1e-6) return false;
+  const double f = K[0], k1 = K[3], k2 = K[4];
+  const double iz = 1.0 / xc[2];
+  const double px = xc[0] * iz, py = xc[1] * iz;
+  const double r2 = px * px + py * py;
+  const double d = 1.0 + k1 * r2 + k2 * r2 * r2;
+  const double qx = px * d, qy = py * d;
+  ev[0] = P.obs_uv[2 * k] - (f * qx + K[1]);
+  ev[1] = P.obs_uv[2 * k + 1] - (f * qy + K[2]);
+  const double c = 2.0 * (k1 + 2.0 * k2 * r2);
+  const double a00 = (d + c * px * px) * f, a01 = (c * px * py) * f;
+  const double a11 = (d + c * py * py) * f;
+  const double b02 = -xc[0] * iz * iz, b12 = -xc[1] * iz * iz;
+  double du[6];
+  du[0] = a00 * iz;
+  du[1] = a01 * iz;
+  du[2] = a00 * b02 + a01 * b12;
+  du[3] = a01 * iz;
+  du[4] = a11 * iz;
+  du[5] = a01 * b02 + a11 * b12;
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const double u0 = du[3 * r], u1 = du[3 * r + 1], u2 = du[3 * r + 2];
+    const float f0 = (float)u0, f1 = (float)u1, f2 = (float)u2;
+    const float x0 = (float)xc[0], x1 = (float)xc[1], x2 = (float)xc[2];
+    out[6 * r + 0] = f2 * x1 - f1 * x2;
+    out[6 * r + 1] = f0 * x2 - f2 * x0;
+    out[6 * r + 2] = f1 * x0 - f0 * x1;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      jp[3 * r + j] = u0 * Rm[j] + u1 * Rm[3 + j] + u2 * Rm[6 + j];
+      out[6 * r + 3 + j] = -(float)jp[3 * r + j];
+      out[12 + 3 * r + j] = (float)jp[3 * r + j];
+    }
+  }
+  if (refine) {  // ba.rs:87-95
+    out[18] = (float)qx;
+    out[19] = (float)(f * px * r2);
+    out[20] = (float)(f * px * r2 * r2);
+    out[21] = (float)qy;
+    out[22] = (float)(f * py * r2);
+    out[23] = (float)(f * py * r2 * r2);
+  } else {
+#pragma unroll
+    for (int i = 18; i < 24; ++i) out[i] = 0.0f;
+  }
+  w = robust_weight(ev[0] * ev[0] + ev[1] * ev[1], sigma, P.loss);
+  out[24] = (float)ev[0];
+  out[25] = (float)ev[1];
+  out[26] = (float)w;
+  out[27] = 1.0f;
+  return true;
+}
+
+// Above this bound on cond(V) a point's second pass runs in FP64 (its V^-1
+// would amplify FP32 rounding of Jc, Jp beyond the accuracy the reduced
+// system needs).  cond(V) <= tr^3 / (4 det) for a 3x3 SPD matrix.
+constexpr double kMixedCondLimit = 1e4;
+
+// Mixed form (R = float): point system in FP64, storage in FP32.  Z and the
+// per-observation reduced gradient r' are formed in FP32 for well-conditioned
+// points and from an FP64 re-linearisation for the rest.
+__device__ __forceinline__ void point_system_mixed(const Prob& P, const StateView& st,
+                                                   const StructView& S, const IterBufs<float>& B,
+                                                   int64_t p, bool refine, double sg, double lam) {
+  const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
+  double V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
+  for (uint32_t k = s; k < e; ++k) {
+    float* o = B.lin + (size_t)k * kLinW;
+    double jp[6], ev[2], w;
+    if (!linearise_mixed(P, st, k, sg, refine, o, jp, ev, w)) {
+      for (int i = 0; i < kLinW; ++i) o[i] = 0.0f;
+      continue;
+    }
+    V[0] += (jp[0] * jp[0] + jp[3] * jp[3]) * w;
+    V[1] += (jp[0] * jp[1] + jp[3] * jp[4]) * w;
+    V[2] += (jp[0] * jp[2] + jp[3] * jp[5]) * w;
+    V[3] += (jp[1] * jp[1] + jp[4] * jp[4]) * w;
+    V[4] += (jp[1] * jp[2] + jp[4] * jp[5]) * w;
+    V[5] += (jp[2] * jp[2] + jp[5] * jp[5]) * w;
+    v[0] += (jp[0] * ev[0] + jp[3] * ev[1]) * w;
+    v[1] += (jp[1] * ev[0] + jp[4] * ev[1]) * w;
+    v[2] += (jp[2] * ev[0] + jp[5] * ev[1]) * w;
+  }
+  if (e - s < 2) {  // ba.rs:238
+    B.kept[p] = 0;
+    return;
+  }
+  double A[9], Ai[9];
+  sym3_full(V, A);
+  A[0] = A[0] * (1.0 + lam) + 1e-9;  // ba.rs:262-264
+  A[4] = A[4] * (1.0 + lam) + 1e-9;
+  A[8] = A[8] * (1.0 + lam) + 1e-9;
+  const bool ok = inv3(A, Ai);  // ba.rs:265
+  double L[6] = {0, 0, 0, 0, 0, 0};
+  if (ok) chol3(Ai, L);
+  const double tr = A[0] + A[4] + A[8];
+  const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                     A[2] * (A[3] * A[7] - A[4] * A[6]);
+  const bool ill = !(det > 0.0) || tr * tr * tr > 4.0 * kMixedCondLimit * det;
+  B.kept[p] = ok ? (ill ? 2 : 1) : 0;
+  const double zv0 = L[0] * v[0] + L[1] * v[1] + L[3] * v[2];
+  const double zv1 = L[2] * v[1] + L[4] * v[2];
+  const double zv2 = L[5] * v[2];
+  const double t0 = L[0] * zv0, t1 = L[1] * zv0 + L[2] * zv1, t2 = L[3] * zv0 + L[4] * zv1 + L[5] * zv2;
+  double* pl = B.ptL + 6 * (size_t)p;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) pl[i] = L[i];
+  B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
+  const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
+  if (!ok || !ill) {
+    const float l00 = (float)L[0], l10 = (float)L[1], l11 = (float)L[2], l20 = (float)L[3],
+                l21 = (float)L[4], l22 = (float)L[5];
+    const float tf0 = (float)t0, tf1 = (float)t1, tf2 = (float)t2;
+    for (uint32_t k = s; k < e; ++k) {
+      const float* o = B.lin + (size_t)k * kLinW;
+      float* Z = B.Z + (size_t)k * 18;
+      float* gs = B.gsub + (size_t)k * 9;
+      if (!ok || o[27] == 0.0f) {
+#pragma unroll
+        for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
+        continue;
+      }
+      const float w = o[26];
+      const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+      // r' = w (e - Jp t)
+      const float r0 = (o[24] - (j0 * tf0 + j1 * tf1 + j2 * tf2)) * w;
+      const float r1 = (o[25] - (j3 * tf0 + j4 * tf1 + j5 * tf2)) * w;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        const float ca = o[r], cb = o[6 + r];
+        const float y0 = (ca * j0 + cb * j3) * w;
+        const float y1 = (ca * j1 + cb * j4) * w;
+        const float y2 = (ca * j2 + cb * j5) * w;
+        Z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
+        Z[3 * r + 1] = y1 * l11 + y2 * l21;
+        Z[3 * r + 2] = y2 * l22;
+        gs[r] = ca * r0 + cb * r1;
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) gs[6 + a] = o[18 + a] * r0 + o[21 + a] * r1;
+    }
+    for (uint32_t j = l0; j < l1; ++j) {
+      float Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (uint32_t k = s; k < e; ++k) {
+        if (S.obs_lens[k] != j) continue;
+        const float* o = B.lin + (size_t)k * kLinW;
+        if (o[27] == 0.0f) continue;
+        const float w = o[26];
+        const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float ga = o[18 + a], gb = o[21 + a];
+          Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
+          Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
+          Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
+        }
+      }
+      float* Zl = B.Zl + (size_t)j * 9;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
+        Zl[3 * a + 0] = ok ? y0 * l00 + y1 * l10 + y2 * l20 : 0.0f;
+        Zl[3 * a + 1] = ok ? y1 * l11 + y2 * l21 : 0.0f;
+        Zl[3 * a + 2] = ok ? y2 * l22 : 0.0f;
+      }
+    }
+    return;
+  }
+  // Ill-conditioned point: second pass from an FP64 re-linearisation.
+  for (uint32_t k = s; k < e; ++k) {
+    float* Z = B.Z + (size_t)k * 18;
+    float* gs = B.gsub + (size_t)k * 9;
+    double o[kLinW];
+    if (!linearise<double>(P, st, k, sg, refine, o)) {
+#pragma unroll
+      for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
+      continue;
+    }
+    const double w = o[26];
+    const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+    const double r0 = (o[24] - (j0 * t0 + j1 * t1 + j2 * t2)) * w;
+    const double r1 = (o[25] - (j3 * t0 + j4 * t1 + j5 * t2)) * w;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      const double ca = o[r], cb = o[6 + r];
+      const double y0 = (ca * j0 + cb * j3) * w;
+      const double y1 = (ca * j1 + cb * j4) * w;
+      const double y2 = (ca * j2 + cb * j5) * w;
+      Z[3 * r + 0] = (float)(y0 * L[0] + y1 * L[1] + y2 * L[3]);
+      Z[3 * r + 1] = (float)(y1 * L[2] + y2 * L[4]);
+      Z[3 * r + 2] = (float)(y2 * L[5]);
+      gs[r] = (float)(ca * r0 + cb * r1);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) gs[6 + a] = (float)(o[18 + a] * r0 + o[21 + a] * r1);
+  }
+  for (uint32_t j = l0; j < l1; ++j) {
+    double Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t k = s; k < e; ++k) {
+      if (S.obs_lens[k] != j) continue;
+      double o[kLinW];
+      if (!linearise<double>(P, st, k, sg, refine, o)) continue;
+      const double w = o[26];
+      const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const double ga = o[18 + a], gb = o[21 + a];
+        Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
+        Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
+        Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
+      }
+    }
+    float* Zl = B.Zl + (size_t)j * 9;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
+      Zl[3 * a + 0] = (float)(y0 * L[0] + y1 * L[1] + y2 * L[3]);
+      Zl[3 * a + 1] = (float)(y1 * L[2] + y2 * L[4]);
+      Zl[3 * a + 2] = (float)(y2 * L[5]);
+    }
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128)
+    point_kernel(Prob P, StateView st, StructView S, IterBufs<R> B, const int32_t* active,
+                 const double* lambda, const double* sigma) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.np) return;
+  const uint32_t m = P.pt_model[p];
+  if (!active[m]) return;
+  const bool refine = P.model_refine[m] != 0;
+  if constexpr (sizeof(R) == 8)
+    point_system<R>(P, st, S, B, p, refine, sigma[m], lambda[m]);
+  else
+    point_system_mixed(P, st, S, B, p, refine, sigma[m], lambda[m]);
+}
+
 // ---- per camera: U, g, lens terms (ba.rs:273-292) ----------------------------
 
 constexpr int kCamThreads = 128;
@@ -271,10 +525,14 @@ constexpr int kCamG = 18;  // 6 gj | 6 gs | 3 lg | 3 ls  (FP64)
 template <typename R>
 __global__ void __launch_bounds__(kCamThreads)
     camera_kernel(Prob P, StructView S, IterBufs<R> B, const int32_t* active) {
-  // Matrix sums in the storage precision R (FP32 accumulation in the mixed
-  // form); the gradient sums (J^T W e and the Schur correction) in FP64, so
-  // the LM outer loop refines against an FP64 gradient.
-  __shared__ R scratch[kCamN * 32];
+  // FP64 form: every sum in FP64.  Mixed form: products in FP32, summed in
+  // FP32 over runs of kCamChunk observations and then folded into FP64 (a
+  // camera sees thousands of observations: plain FP32 accumulation would
+  // bury the weak, prior-only directions of the reduced system); the
+  // gradient is the FP64 sum of the observations' reduced-gradient shares.
+  constexpr int kCamChunk = 8;
+  constexpr bool kMixed = sizeof(R) == 4;
+  __shared__ double scratch[kCamN * 32];
   __shared__ double gscratch[kCamG * 32];
   const int64_t c = blockIdx.x;
   if (c >= P.nc) return;
@@ -282,18 +540,19 @@ __global__ void __launch_bounds__(kCamThreads)
   if (!active[m]) return;
   const bool refine = P.model_refine[m] != 0;
   R acc[kCamN];
+  double accd[kCamN];
   double gacc[kCamG];
 #pragma unroll
-  for (int i = 0; i < kCamN; ++i) acc[i] = (R)0;
+  for (int i = 0; i < kCamN; ++i) acc[i] = (R)0, accd[i] = 0.0;
 #pragma unroll
   for (int i = 0; i < kCamG; ++i) gacc[i] = 0.0;
+  int run = 0;
   const uint32_t b = S.cam_ptr[c], e = S.cam_ptr[c + 1];
   for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     const uint32_t k = S.cam_obs[i];
     const R* o = B.lin + (size_t)k * kLinW;
     if (o[27] == (R)0 || !B.kept[P.obs_pt[k]]) continue;  // ba.rs:274-277
     const R w = o[26];
-    const double e0 = (double)o[24], e1 = (double)o[25], wd = (double)w;
     R jc[12];
 #pragma unroll
     for (int t = 0; t < 12; ++t) jc[t] = o[t];
@@ -303,10 +562,16 @@ __global__ void __launch_bounds__(kCamThreads)
 #pragma unroll
       for (int bb = a; bb < 6; ++bb) acc[u++] += (jc[a] * jc[bb] + jc[6 + a] * jc[6 + bb]) * w;
     const R* gs = B.gsub + (size_t)k * 9;
+    if constexpr (kMixed) {
 #pragma unroll
-    for (int a = 0; a < 6; ++a) {
-      gacc[a] += ((double)jc[a] * e0 + (double)jc[6 + a] * e1) * wd;
-      gacc[6 + a] += (double)gs[a];
+      for (int a = 0; a < 6; ++a) gacc[a] += (double)gs[a];
+    } else {
+      const double e0 = (double)o[24], e1 = (double)o[25], wd = (double)w;
+#pragma unroll
+      for (int a = 0; a < 6; ++a) {
+        gacc[a] += ((double)jc[a] * e0 + (double)jc[6 + a] * e1) * wd;
+        gacc[6 + a] += (double)gs[a];
+      }
     }
     if (refine) {
       const R jg[6] = {o[18], o[19], o[20], o[21], o[22], o[23]};
@@ -320,21 +585,41 @@ __global__ void __launch_bounds__(kCamThreads)
       for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int bb = a; bb < 3; ++bb) acc[39 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
+      if constexpr (kMixed) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        gacc[12 + a] += ((double)jg[a] * e0 + (double)jg[3 + a] * e1) * wd;
-        gacc[15 + a] += (double)gs[6 + a];
+        for (int a = 0; a < 3; ++a) gacc[12 + a] += (double)gs[6 + a];
+      } else {
+        const double e0 = (double)o[24], e1 = (double)o[25], wd = (double)w;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          gacc[12 + a] += ((double)jg[a] * e0 + (double)jg[3 + a] * e1) * wd;
+          gacc[15 + a] += (double)gs[6 + a];
+        }
+      }
+    }
+    if constexpr (kMixed) {
+      if (++run == kCamChunk) {
+        run = 0;
+#pragma unroll
+        for (int t = 0; t < kCamN; ++t) accd[t] += (double)acc[t], acc[t] = (R)0;
       }
     }
   }
-  block_sum<kCamN>(acc, scratch);
+  if constexpr (kMixed) {
+#pragma unroll
+    for (int t = 0; t < kCamN; ++t) accd[t] += (double)acc[t];
+  } else {
+#pragma unroll
+    for (int t = 0; t < kCamN; ++t) accd[t] = acc[t];
+  }
+  block_sum<kCamN>(accd, scratch);
   block_sum<kCamG>(gacc, gscratch);
   if (threadIdx.x == 0) {
     double* U = B.camU + 21 * c;
-    for (int i = 0; i < 21; ++i) U[i] = (double)acc[i];
+    for (int i = 0; i < 21; ++i) U[i] = accd[i];
     for (int i = 0; i < 6; ++i) B.camgj[6 * c + i] = gacc[i], B.camgs[6 * c + i] = gacc[6 + i];
-    for (int i = 0; i < 18; ++i) B.camX[18 * c + i] = (double)acc[21 + i];
-    for (int i = 0; i < 6; ++i) B.caml[12 * c + i] = (double)acc[39 + i];
+    for (int i = 0; i < 18; ++i) B.camX[18 * c + i] = accd[21 + i];
+    for (int i = 0; i < 6; ++i) B.caml[12 * c + i] = accd[39 + i];
     for (int i = 0; i < 6; ++i) B.caml[12 * c + 6 + i] = gacc[12 + i];
   }
 }
@@ -530,9 +815,9 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int i = 0; i < 36; ++i) acc[i] = warp_sum(acc[i]);
   if (lane == 0) {
-    R* o = B.part + (size_t)sub * 36;
+    double* o = B.part + (size_t)sub * 36;
 #pragma unroll
-    for (int i = 0; i < 36; ++i) o[i] = acc[i];
+    for (int i = 0; i < 36; ++i) o[i] = (double)acc[i];
   }
 }
 
@@ -548,7 +833,7 @@ __global__ void assemble_kernel(Prob P, StateView st, StructView S, IterBufs<R> 
   const uint32_t a = S.slot_row[s], bcol = S.slot_col[s];
   const uint32_t m = P.blk_model[a];
   if (!active[m]) return;
-  R sum = (R)0;
+  double sum = 0.0;  // sub-segment sums in FP64 in both forms
   for (uint32_t u = S.slot_sub_ptr[s]; u < S.slot_sub_ptr[s + 1]; ++u)
     sum += B.part[(size_t)u * 36 + el];
   double val;
@@ -658,45 +943,75 @@ __global__ void update_cameras_kernel(Prob P, StateView cur, StateView trial, It
 
 template <typename R>
 __global__ void backsub_kernel(Prob P, StructView S, StateView cur, StateView trial,
-                               IterBufs<R> B, const int32_t* active) {
+                               IterBufs<R> B, const double* sigma, const int32_t* active) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P.np) return;
-  if (!active[P.pt_model[p]]) return;
+  const uint32_t m = P.pt_model[p];
+  if (!active[m]) return;
   const double* X = cur.points + 3 * p;
   double* Xt = trial.points + 3 * p;
-  if (!B.kept[p]) {
+  const uint8_t kept = B.kept[p];
+  if (!kept) {
     Xt[0] = X[0], Xt[1] = X[1], Xt[2] = X[2];
     return;
   }
-  R a0 = B.ptzv[3 * p], a1 = B.ptzv[3 * p + 1], a2 = B.ptzv[3 * p + 2];
   const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
-  for (uint32_t k = s; k < e; ++k) {
-    const R* Z = B.Z + (size_t)k * 18;
-    const R* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
+  const double* L = B.ptL + 6 * p;
+  double a0, a1, a2;
+  if (sizeof(R) == 4 && kept == 2) {
+    // Mixed form, ill-conditioned point: u = sum_k Y_k^T dx from an FP64
+    // re-linearisation, then a = zv - L^T u.
+    const bool refine = P.model_refine[m] != 0;
+    double u0 = 0.0, u1 = 0.0, u2 = 0.0;
+    for (uint32_t k = s; k < e; ++k) {
+      double o[kLinW];
+      if (!linearise<double>(P, cur, k, sigma[m], refine, o)) continue;
+      const R* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
+      double jd0 = 0.0, jd1 = 0.0;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-      const R dr = d[r];
-      a0 -= Z[3 * r] * dr;
-      a1 -= Z[3 * r + 1] * dr;
-      a2 -= Z[3 * r + 2] * dr;
-    }
-  }
-  for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j) {
-    const R* Z = B.Zl + (size_t)j * 9;
-    const R* d = B.x + 6 * (size_t)P.grp_blk[S.lens_grp[j]];
+      for (int r = 0; r < 6; ++r) jd0 += o[r] * (double)d[r], jd1 += o[6 + r] * (double)d[r];
+      if (refine) {
+        const R* dg = B.x + 6 * (size_t)P.grp_blk[P.cam_group[P.obs_cam[k]]];
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const R dr = d[r];
-      a0 -= Z[3 * r] * dr;
-      a1 -= Z[3 * r + 1] * dr;
-      a2 -= Z[3 * r + 2] * dr;
+        for (int r = 0; r < 3; ++r) jd0 += o[18 + r] * (double)dg[r], jd1 += o[21 + r] * (double)dg[r];
+      }
+      const double w = o[26];
+      u0 += (o[12] * jd0 + o[15] * jd1) * w;
+      u1 += (o[13] * jd0 + o[16] * jd1) * w;
+      u2 += (o[14] * jd0 + o[17] * jd1) * w;
     }
+    a0 = B.ptzv[3 * p] - (L[0] * u0 + L[1] * u1 + L[3] * u2);
+    a1 = B.ptzv[3 * p + 1] - (L[2] * u1 + L[4] * u2);
+    a2 = B.ptzv[3 * p + 2] - L[5] * u2;
+  } else {
+    R b0 = (R)B.ptzv[3 * p], b1 = (R)B.ptzv[3 * p + 1], b2 = (R)B.ptzv[3 * p + 2];
+    for (uint32_t k = s; k < e; ++k) {
+      const R* Z = B.Z + (size_t)k * 18;
+      const R* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        const R dr = d[r];
+        b0 -= Z[3 * r] * dr;
+        b1 -= Z[3 * r + 1] * dr;
+        b2 -= Z[3 * r + 2] * dr;
+      }
+    }
+    for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j) {
+      const R* Z = B.Zl + (size_t)j * 9;
+      const R* d = B.x + 6 * (size_t)P.grp_blk[S.lens_grp[j]];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const R dr = d[r];
+        b0 -= Z[3 * r] * dr;
+        b1 -= Z[3 * r + 1] * dr;
+        b2 -= Z[3 * r + 2] * dr;
+      }
+    }
+    a0 = (double)b0, a1 = (double)b1, a2 = (double)b2;
   }
-  const R* L = B.ptL + 6 * p;
-  const R l00 = L[0], l10 = L[1], l11 = L[2], l20 = L[3], l21 = L[4], l22 = L[5];
-  Xt[0] = X[0] + (double)(l00 * a0);
-  Xt[1] = X[1] + (double)(l10 * a0 + l11 * a1);
-  Xt[2] = X[2] + (double)(l20 * a0 + l21 * a1 + l22 * a2);
+  Xt[0] = X[0] + L[0] * a0;
+  Xt[1] = X[1] + (L[1] * a0 + L[2] * a1);
+  Xt[2] = X[2] + (L[3] * a0 + L[4] * a1 + L[5] * a2);
 }
 
 }  // namespace ba

@@ -44,8 +44,9 @@ template <typename R>
 struct PcgArgs {
   const PcgJob* jobs;
   const int32_t* cta_job0;  // [ncta+1]
-  unsigned long long* bar;  // [nm] arrival counters
-  double* part;             // [kParts][ncta]
+  unsigned long long* bar;       // [nm] arrival counter of each model's group
+  unsigned long long* bar_base;  // [nm] counter value when the next launch starts
+  double* part;                  // [kParts][ncta] partial sums
   int32_t ncta;
   const uint32_t* row_ptr;
   const uint32_t* col_idx;
@@ -69,6 +70,9 @@ struct PcgArgs {
 
 // partial slots: 0,1 init (rz, bb) | 2..5 (pq, lens q 0..2) | 6,7 (rr, rz)
 constexpr int kParts = 8;
+// A reader lane loads up to kReadUnroll members' partials at once.
+constexpr int kReadUnroll = 4;
+constexpr int kMaxGroupCtas = 32 * kReadUnroll * 4;
 
 // Row state per local row in shared memory: x, r, z, p, q (6 each), M (36),
 // padded to a multiple of 16 bytes in both precisions.
@@ -84,45 +88,8 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ unsigned long long atom_add_release_u64(unsigned long long* p,
-                                                                   unsigned long long v) {
-  unsigned long long old;
-  asm volatile("atom.add.release.gpu.global.u64 %0, [%1], %2;"
-               : "=l"(old)
-               : "l"(p), "l"(v)
-               : "memory");
-  return old;
-}
-
-// Barrier over the n CTAs of a group: a monotonic 64-bit arrival counter
-// (release on arrival, acquire while polling).  Bounded: after kSpinCycles
-// the waiter sets ERR_BARRIER_TIMEOUT; every CTA leaves at its next wait.
-__device__ __forceinline__ bool counter_sync(unsigned long long* ctr, unsigned n,
-                                             unsigned* err) {
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    if (n > 1) {
-      const unsigned long long old = atom_add_release_u64(ctr, 1ULL);
-      const unsigned long long target = (old / n + 1) * n;
-      const long long t0 = clock64();
-      while (ld_acquire_u64(ctr) < target) {
-        if ((*(volatile unsigned*)err) & ERR_BARRIER_TIMEOUT) {
-          ok = 0;
-          break;
-        }
-        if (clock64() - t0 > kSpinCycles) {
-          atomicOr(err, ERR_BARRIER_TIMEOUT);
-          ok = 0;
-          break;
-        }
-      }
-    }
-    ok_s = ok;
-  }
-  __syncthreads();
-  return ok_s != 0;
+__device__ __forceinline__ void red_add_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 // Warp sum of 8 values per lane by recursive halving: afterwards lane 4k
@@ -169,9 +136,18 @@ __device__ __forceinline__ double sum8(double v) {
 // N (<= 4) values per warp (held by lane 0) summed over the CTA's warps with
 // one shuffle tree, then over the group's CTAs in rank order; every thread
 // receives the totals in tot[].
+//
+// Group barrier: every member adds 1 to the group's monotonic 64-bit counter
+// (release) after publishing its partials, and waits (acquire) until the
+// counter reaches `target`, which grows by the group size per exchange from
+// the launch's base value.  Only warp 0 of a CTA takes part; the partials are
+// then read with all loads in flight at once.  Bounded: after kSpinCycles the
+// waiter sets ERR_BARRIER_TIMEOUT; every CTA leaves at its next exchange.
 template <int N, typename R>
 __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm, double* tot,
-                                             const PcgArgs<R>& A, const PcgJob& J, int slot) {
+                                             const PcgArgs<R>& A, const PcgJob& J, int slot,
+                                             unsigned long long& target) {
+  __shared__ int ok_s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
@@ -183,32 +159,56 @@ __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm,
     c += __shfl_xor_sync(kFull, c, 4);
     c += __shfl_xor_sync(kFull, c, 8);
     c += __shfl_xor_sync(kFull, c, 16);
-    if (J.gsize > 1) {
+    if (J.gsize == 1) {
+      if (lane < N) tot[lane] = c;
+      if (lane == 0) ok_s = 1;
+    } else {
       if (lane < N) A.part[(size_t)(slot + lane) * A.ncta + J.base + J.rank] = c;
       __threadfence();
-    } else if (lane < N) {
-      tot[lane] = c;
-    }
-  }
-  if (J.gsize > 1) {
-    if (!counter_sync(A.bar + J.model, (unsigned)J.gsize, A.err)) return false;
-    if (warp == 0) {
-      double v[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        double s = 0.0;
-        if (i < N) {
-          const double* src = A.part + (size_t)(slot + i) * A.ncta + J.base;
-          for (int k = lane; k < J.gsize; k += 32) s += __ldcg(src + k);
+      __syncwarp();
+      int ok = 1;
+      if (lane == 0) {
+        target += (unsigned long long)J.gsize;
+        unsigned long long* ctr = A.bar + J.model;
+        red_add_release_u64(ctr, 1ULL);
+        const long long t0 = clock64();
+        while (ld_acquire_u64(ctr) < target) {
+          if ((*(volatile unsigned*)A.err) & ERR_BARRIER_TIMEOUT) {
+            ok = 0;
+            break;
+          }
+          if (clock64() - t0 > kSpinCycles) {
+            atomicOr(A.err, ERR_BARRIER_TIMEOUT);
+            ok = 0;
+            break;
+          }
         }
-        v[i] = s;
+        ok_s = ok;
       }
-      warp_sum8(v);
+      __syncwarp();
+      double v[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      for (int k0 = 0; k0 < J.gsize; k0 += 32 * kReadUnroll) {
+        double t[4][kReadUnroll];
+#pragma unroll
+        for (int u = 0; u < kReadUnroll; ++u) {
+          const int k = k0 + lane + 32 * u;
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            t[i][u] = (i < N && k < J.gsize)
+                          ? __ldcg(A.part + (size_t)(slot + i) * A.ncta + J.base + k)
+                          : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kReadUnroll; ++u)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) v[i] += t[i][u];
+      }
+      warp_sum8(v);  // lane 4i holds value i
       if ((lane & 3) == 0 && (lane >> 2) < N) tot[lane >> 2] = v[0];
     }
   }
   __syncthreads();
-  return true;
+  return ok_s != 0;
 }
 
 // A 6x6 block into registers with 16-byte loads (global or shared).
@@ -250,6 +250,9 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
     return false;
   }
   const bool cached = nblk <= A.smem_blocks;
+  // Barrier counter value at this launch's start (written by the previous
+  // launch's rank 0: every member made the same number of arrivals).
+  unsigned long long target = A.bar_base[J.model];
   // Shared-memory carve-up: row state, then cached S blocks and columns.
   R* sS = rs + (size_t)A.smem_rows * kRowState;
   uint32_t* sC = reinterpret_cast<uint32_t*>(sS + (size_t)A.smem_blocks * 36);
@@ -295,7 +298,7 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
     w2[0] += sum8(a);
     w2[1] += sum8(bb);
   }
-  if (!group_reduce<2>(w2, wsm, tot, A, J, 0)) return false;
+  if (!group_reduce<2>(w2, wsm, tot, A, J, 0, target)) return false;
   double rz = tot[0];
   const double b2 = fmax(tot[1], 1e-300);
   double beta = 0.0;
@@ -360,7 +363,7 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
         w4[3] += (double)__shfl_sync(kFull, v, 2);
       }
     }
-    if (!group_reduce<4>(w4, wsm, tot, A, J, 2)) return false;
+    if (!group_reduce<4>(w4, wsm, tot, A, J, 2, target)) return false;
     ++spmv;
     double pq = tot[0];
     if (lens >= 0) {
@@ -406,7 +409,7 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
       w2b[0] += sum8(rr);
       w2b[1] += sum8(rzl);
     }
-    if (!group_reduce<2>(w2b, wsm, tot, A, J, 6)) return false;
+    if (!group_reduce<2>(w2b, wsm, tot, A, J, 6, target)) return false;
     const double rr = tot[0], rz2 = tot[1];
     __syncthreads();
     if (rr < A.tol * b2) break;  // ba.rs:182
@@ -416,7 +419,10 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
   for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps)
     if (vl) A.x[6 * (size_t)(J.row0 + lr) + ci] = ROW(lr)[ci];
 #undef ROW
-  if (J.rank == 0 && threadIdx.x == 0) A.iters[J.model] = spmv;
+  if (J.rank == 0 && threadIdx.x == 0) {
+    A.iters[J.model] = spmv;
+    A.bar_base[J.model] = target;  // every member made the same arrivals
+  }
   __syncthreads();
   return true;
 }

@@ -1,0 +1,287 @@
+// Block-Jacobi PCG of the reduced camera system (ba.rs:155-196) with one
+// thread-block cluster per model and the whole solve in the cluster's
+// distributed shared memory: mixed form only (FP32 matrix and vectors, FP64
+// inner products).
+//
+// A model's block rows are split over the CTAs of its cluster (balanced by
+// blocks); each CTA keeps its rows' state (x, r, z, two buffers of p, q and
+// the block-Jacobi inverse) and its rows' S blocks in shared memory for the
+// whole solve.  A row's neighbour values z_j and p_j(prev) are read straight
+// from the owning CTA's shared memory (DSMEM), and the two reductions of an
+// iteration meet at hardware cluster barriers: no global memory traffic and
+// no software spin inside the iteration.  The iteration is the reference's,
+// with p_j = z_j + β p_j(prev) formed on the fly as in the grid kernel.
+//
+// Every CTA of a cluster executes the same sequence of cluster barriers:
+// loop exits depend only on reduced scalars, which every CTA computes from
+// the same partials in the same order (bit-identical), and the kernel has no
+// early return after its first barrier.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "pcg.cuh"
+
+namespace ba {
+
+namespace cgx = cooperative_groups;
+
+constexpr int kCgThreads = 256;
+constexpr int kCgWarps = kCgThreads / 32;
+constexpr int kCgMaxCluster = 16;
+// Row state in floats: x r z p0 p1 q (8 each, 6 used) | M (36) | the row's
+// first and end block and its lens block (int bits) | pad.
+constexpr int kCgX = 0, kCgR = 8, kCgZ = 16, kCgP = 24, kCgQ = 40, kCgM = 48, kCgIdx = 84;
+constexpr int kCgRow = 88;
+
+struct CgJob {
+  int32_t model;
+  uint32_t row0, row1;  // this CTA's block rows
+};
+
+struct CgArgs {
+  const CgJob* jobs;        // [grid]
+  const uint32_t* row_loc;  // [nb]: owner rank << 16 | local row index
+  const uint32_t* row_ptr;
+  const uint32_t* col_idx;
+  const float* S;
+  const float* pre;
+  const float* b;
+  float* x;
+  const int32_t* lens_row;  // [nm]
+  const int32_t* lens_pos;  // [nb]
+  const uint32_t* diag_pos; // [nb]
+  uint32_t cap_rows;        // row-state capacity (same in every CTA)
+  uint32_t cap_blocks;      // cached S blocks per CTA (the rest read from global)
+  const int32_t* active;
+  int32_t* iters;
+  int32_t max_iter;
+  double tol;
+};
+
+inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks) {
+  return (size_t)cap_rows * kCgRow * 4 + (size_t)cap_blocks * (36 * 4 + 4);
+}
+
+// Sum over lanes 0..7 of a float (lanes >= 8 hold 0): all lanes get it.
+__device__ __forceinline__ double cg_sum8(double v) {
+  v += __shfl_xor_sync(kFull, v, 1);
+  v += __shfl_xor_sync(kFull, v, 2);
+  v += __shfl_xor_sync(kFull, v, 4);
+  return v;
+}
+
+// N (<= 4) per-warp values (every lane holds them) summed over the CTA, then
+// over the cluster's CTAs: every lane of every warp receives the totals.
+// `part` is this CTA's slot (static shared memory, same offset everywhere).
+template <int N>
+__device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const double (&wv)[N],
+                                          double* wsm, double* part, double (&tot)[4]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) wsm[warp * 4 + i] = i < N ? wv[i < N ? i : 0] : 0.0;
+  __syncthreads();
+  if (warp == 0) {
+    double c = wsm[lane];  // lane = 4 w + i
+    c += __shfl_xor_sync(kFull, c, 4);
+    c += __shfl_xor_sync(kFull, c, 8);
+    c += __shfl_xor_sync(kFull, c, 16);
+    if (lane < 4) part[lane] = c;
+  }
+  cl.sync();
+  const int csize = (int)cl.num_blocks();
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  if (lane < csize) {
+    const double* rp = cl.map_shared_rank(part, (unsigned)lane);
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = rp[i];
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    double t = v[i];
+    t += __shfl_xor_sync(kFull, t, 1);
+    t += __shfl_xor_sync(kFull, t, 2);
+    t += __shfl_xor_sync(kFull, t, 4);
+    t += __shfl_xor_sync(kFull, t, 8);
+    t += __shfl_xor_sync(kFull, t, 16);
+    tot[i] = t;
+  }
+}
+
+static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A) {
+  __shared__ double wsm[kCgWarps * 4];
+  __shared__ double part[2][4];
+  extern __shared__ __align__(16) unsigned char cg_smem[];
+  cgx::cluster_group cl = cgx::this_cluster();
+  const CgJob J = A.jobs[blockIdx.x];
+  if (!A.active[J.model]) return;  // uniform over the cluster
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nrows = J.row1 - J.row0;
+  const uint32_t B0 = A.row_ptr[J.row0];
+  const uint32_t nblk = A.row_ptr[J.row1] - B0;
+  const uint32_t ncached = nblk < A.cap_blocks ? nblk : A.cap_blocks;
+  float* rs = reinterpret_cast<float*>(cg_smem);
+  float* sS = rs + (size_t)A.cap_rows * kCgRow;
+  uint32_t* sL = reinterpret_cast<uint32_t*>(sS + (size_t)A.cap_blocks * 36);
+  const int32_t lens = A.lens_row[J.model];
+  {
+    const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
+    float4* dst = reinterpret_cast<float4*>(sS);
+    for (uint32_t c = threadIdx.x; c < ncached * 9; c += blockDim.x) dst[c] = src[c];
+    for (uint32_t t = threadIdx.x; t < ncached; t += blockDim.x)
+      sL[t] = A.row_loc[A.col_idx[B0 + t]];
+    for (uint32_t t = threadIdx.x; t < nrows * 36; t += blockDim.x)
+      rs[(size_t)(t / 36) * kCgRow + kCgM + (t % 36)] = A.pre[36 * (size_t)J.row0 + t];
+    // Per row: its block range (the lens row: its diagonal block only; its
+    // camera columns arrive through the camera rows' transposed terms) and
+    // the position of its lens block.
+    for (uint32_t lr = threadIdx.x; lr < nrows; lr += blockDim.x) {
+      const uint32_t row = J.row0 + lr;
+      float* st = rs + (size_t)lr * kCgRow;
+      uint32_t b0 = A.row_ptr[row], b1 = A.row_ptr[row + 1];
+      if ((int32_t)row == lens) b0 = A.diag_pos[row], b1 = b0 + 1;
+      st[kCgIdx] = __int_as_float((int)b0);
+      st[kCgIdx + 1] = __int_as_float((int)b1);
+      st[kCgIdx + 2] = __int_as_float((int32_t)row == lens ? -1 : A.lens_pos[row]);
+    }
+  }
+  __syncthreads();
+  const bool vl = lane < 6;
+  const int ci = vl ? lane : 0;
+#define CGROW(lr) (rs + (size_t)(lr) * kCgRow)
+  // x = 0, r = b, z = M r, p(prev) = 0 (ba.rs:164-168)
+  double w2[2] = {0.0, 0.0};
+  for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
+    float* st = CGROW(lr);
+    const float ri = vl ? A.b[6 * (size_t)(J.row0 + lr) + ci] : 0.0f;
+    float zi = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
+    double a = 0.0, bb = 0.0;
+    if (vl) {
+      st[kCgX + ci] = 0.0f;
+      st[kCgR + ci] = ri;
+      st[kCgZ + ci] = zi;
+      st[kCgP + 8 + ci] = 0.0f;  // p buffer 1 = p(prev) of iteration 0
+      a = (double)ri * (double)zi;
+      bb = (double)ri * (double)ri;
+    }
+    w2[0] += cg_sum8(a);
+    w2[1] += cg_sum8(bb);
+  }
+  // The first barrier also makes every CTA's shared memory live for DSMEM.
+  double tot[4];
+  cg_reduce<2>(cl, w2, wsm, part[1], tot);
+  double rz = tot[0];
+  const double b2 = fmax(tot[1], 1e-300);
+  double beta = 0.0;
+  int32_t spmv = 0;
+  for (int32_t it = 0; it < A.max_iter; ++it) {
+    const int cur = it & 1, prv = cur ^ 1;
+    const float bf = (float)beta;
+    double w4[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
+      float* st = CGROW(lr);
+      const uint32_t b0 = (uint32_t)__float_as_int(st[kCgIdx]);
+      const uint32_t b1 = (uint32_t)__float_as_int(st[kCgIdx + 1]);
+      float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (uint32_t k = b0 + lane; k < b1; k += 32) {
+        const uint32_t kk = k - B0;
+        const uint32_t loc = kk < ncached ? sL[kk] : A.row_loc[A.col_idx[k]];
+        const float* rrow = cl.map_shared_rank(rs, loc >> 16) + (size_t)(loc & 0xffffu) * kCgRow;
+        const float4 z0 = *reinterpret_cast<const float4*>(rrow + kCgZ);
+        const float4 z1 = *reinterpret_cast<const float4*>(rrow + kCgZ + 4);
+        const float4 q0 = *reinterpret_cast<const float4*>(rrow + kCgP + 8 * prv);
+        const float4 q1 = *reinterpret_cast<const float4*>(rrow + kCgP + 8 * prv + 4);
+        const float pp[6] = {z0.x + q0.x * bf, z0.y + q0.y * bf, z0.z + q0.z * bf,
+                             z0.w + q0.w * bf, z1.x + q1.x * bf, z1.y + q1.y * bf};
+        float m[36];
+        load_block(kk < ncached ? sS + (size_t)kk * 36 : A.S + (size_t)k * 36, m);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+          float s = acc[i];
+#pragma unroll
+          for (int j = 0; j < 6; ++j) s += m[6 * i + j] * pp[j];
+          acc[i] = s;
+        }
+      }
+      warp_sum8(acc);  // lane 4i holds q_i
+      const float qi = __shfl_sync(kFull, acc[0], 4 * ci);
+      const float pi = st[kCgZ + ci] + st[kCgP + 8 * prv + ci] * bf;
+      __syncwarp();
+      if (vl) {
+        st[kCgQ + ci] = qi;
+        st[kCgP + 8 * cur + ci] = pi;
+      }
+      w4[0] += cg_sum8(vl ? (double)pi * (double)qi : 0.0);
+      const int32_t lp = __float_as_int(st[kCgIdx + 2]);
+      if (lp >= 0) {  // S_cg^T p_c for the lens column
+        const int t = lane / 3, j = lane - 3 * (lane / 3);
+        const float pt = __shfl_sync(kFull, pi, t < 6 ? t : 0);
+        float v = 0.0f;
+        if (lane < 18) {
+          const uint32_t kk = (uint32_t)lp - B0;
+          const float* blk = kk < ncached ? sS + (size_t)kk * 36 : A.S + (size_t)lp * 36;
+          v = blk[6 * t + j] * pt;
+        }
+        v += __shfl_down_sync(kFull, v, 3);
+        v += __shfl_down_sync(kFull, v, 6);
+        v += __shfl_down_sync(kFull, v, 12);
+        w4[1] += (double)__shfl_sync(kFull, v, 0);
+        w4[2] += (double)__shfl_sync(kFull, v, 1);
+        w4[3] += (double)__shfl_sync(kFull, v, 2);
+      }
+    }
+    cg_reduce<4>(cl, w4, wsm, part[0], tot);
+    ++spmv;
+    double pq = tot[0];
+    if (lens >= 0) {
+      const uint32_t lloc = A.row_loc[lens];
+      const float* lrow = cl.map_shared_rank(rs, lloc >> 16) + (size_t)(lloc & 0xffffu) * kCgRow;
+      // the lens row's p of this iteration (its owner stored it before the barrier)
+      pq += (double)lrow[kCgP + 8 * cur + 0] * tot[1] + (double)lrow[kCgP + 8 * cur + 1] * tot[2] +
+            (double)lrow[kCgP + 8 * cur + 2] * tot[3];
+      if ((uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1 && threadIdx.x < 3) {
+        float* q = CGROW((uint32_t)lens - J.row0) + kCgQ;
+        q[threadIdx.x] = (float)((double)q[threadIdx.x] + tot[1 + threadIdx.x]);
+      }
+    }
+    __syncthreads();
+    if (fabs(pq) < 1e-300) break;  // ba.rs:174
+    const double a = rz / pq;
+    const float af = (float)a;
+    double w2b[2] = {0.0, 0.0};
+    for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
+      float* st = CGROW(lr);
+      float ri = 0.0f;
+      if (vl) {
+        st[kCgX + ci] += st[kCgP + 8 * cur + ci] * af;
+        ri = st[kCgR + ci] - st[kCgQ + ci] * af;
+        st[kCgR + ci] = ri;
+      }
+      float zi = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
+      double rr = 0.0, rzl = 0.0;
+      if (vl) {
+        st[kCgZ + ci] = zi;
+        rr = (double)ri * (double)ri;
+        rzl = (double)ri * (double)zi;
+      }
+      w2b[0] += cg_sum8(rr);
+      w2b[1] += cg_sum8(rzl);
+    }
+    cg_reduce<2>(cl, w2b, wsm, part[1], tot);
+    if (tot[0] < A.tol * b2) break;  // ba.rs:182
+    beta = tot[1] / rz;               // ba.rs:189-190
+    rz = tot[1];
+  }
+  for (uint32_t lr = warp; lr < nrows; lr += kCgWarps)
+    if (vl) A.x[6 * (size_t)(J.row0 + lr) + ci] = CGROW(lr)[kCgX + ci];
+#undef CGROW
+  if (cl.block_rank() == 0 && threadIdx.x == 0) A.iters[J.model] = spmv;
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+}  // namespace ba

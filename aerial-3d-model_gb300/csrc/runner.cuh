@@ -8,6 +8,7 @@
 
 #include "context.cuh"
 #include "pcg.cuh"
+#include "pcg_cluster.cuh"
 #include "structure.cuh"
 
 namespace ba {
@@ -48,6 +49,7 @@ inline PcgPlan plan_pcg(const Context& ctx, const std::vector<uint32_t>& row_ptr
     tot += G[m];
     need += std::max<int64_t>(1, (rows[m] + rows_cap - 1) / rows_cap);
   }
+  max_ctas = std::min(max_ctas, kMaxGroupCtas);
   if (need > max_ctas) {
     // More models than resident CTAs: one CTA per model, dealt greedily to
     // the least-loaded CTA (largest first); a CTA solves its models in turn.
@@ -111,6 +113,50 @@ inline PcgPlan plan_pcg(const Context& ctx, const std::vector<uint32_t>& row_ptr
   return pl;
 }
 
+// Cluster plan (mixed form): every model gets one cluster of `csize` CTAs,
+// its block rows split over them balanced by blocks.  row_loc[row] = owning
+// rank << 16 | local row.  Returns false if a CTA would exceed the row cap.
+struct ClusterPlan {
+  std::vector<CgJob> jobs;
+  std::vector<uint32_t> row_loc;
+  uint32_t max_rows = 0, max_blocks = 0;
+};
+
+inline bool plan_cluster(const Context& ctx, const std::vector<uint32_t>& row_ptr,
+                         const std::vector<int32_t>& lens_row, int csize, uint32_t rows_cap,
+                         ClusterPlan& pl) {
+  pl.jobs.clear();
+  pl.row_loc.assign(row_ptr.size() - 1, 0);
+  pl.max_rows = pl.max_blocks = 0;
+  for (int64_t m = 0; m < ctx.nm; ++m) {
+    const uint32_t r0 = ctx.h_blk0[m], r1 = ctx.h_blk0[m + 1];
+    std::vector<int64_t> rc(r1 - r0);
+    int64_t total = 0;
+    for (uint32_t r = r0; r < r1; ++r) {
+      rc[r - r0] = ((int32_t)r == lens_row[m] ? 1 : (int64_t)(row_ptr[r + 1] - row_ptr[r])) + 8;
+      total += rc[r - r0];
+    }
+    uint32_t row = r0;
+    int64_t acc = 0;
+    for (int k = 0; k < csize; ++k) {
+      const uint32_t start = row;
+      const int64_t target = (total * (k + 1)) / csize;
+      while (row < r1 && (k == csize - 1 || acc + rc[row - r0] <= target || row == start)) {
+        acc += rc[row - r0];
+        ++row;
+        if (k < csize - 1 && acc >= target) break;
+      }
+      if (row - start > rows_cap || row - start > 0xffffu) return false;
+      for (uint32_t r = start; r < row; ++r) pl.row_loc[r] = ((uint32_t)k << 16) | (r - start);
+      pl.jobs.push_back(CgJob{(int32_t)m, start, row});
+      pl.max_rows = std::max(pl.max_rows, row - start);
+      pl.max_blocks = std::max(pl.max_blocks, row_ptr[row] - row_ptr[start]);
+    }
+    if (row != r1) return false;
+  }
+  return true;
+}
+
 template <typename T>
 void h2d(DevBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
   d.alloc(h.size(), s);
@@ -170,7 +216,8 @@ struct LmEngine {
   Prob P;
   StructBufs SB;
   StructView SV;
-  DevBuf<R> lin, gsub, Z, Zl, ptL, ptzv, part, S, pre, g, x, z, p;
+  DevBuf<R> lin, gsub, Z, Zl, S, pre, g, x, z, p;
+  DevBuf<double> ptL, ptzv, part;
   DevBuf<uint8_t> kept;
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
@@ -184,13 +231,20 @@ struct LmEngine {
   detail::PcgPlan plan;
   DevBuf<PcgJob> jobs;
   DevBuf<int32_t> cta_job0;
-  DevBuf<unsigned long long> bar;
+  DevBuf<unsigned long long> bar, bar_base;
+  DevBuf<double> pcg_part;
   DevBuf<int32_t> lens_row, lens_pos;
   uint32_t smem_rows = 0, smem_blocks = 0;
   size_t smem_bytes = 0;
   int pcg_rows_target = 0;
-  DevBuf<double> pcg_part;
   PcgArgs<R> pa{};
+  // Cluster-resident PCG (mixed form).
+  bool use_cluster = false;
+  int cl_size = 0;
+  DevBuf<CgJob> cg_jobs;
+  DevBuf<uint32_t> cg_loc;
+  CgArgs ca{};
+  size_t cg_smem = 0;
   PhaseTimer T;
 
   LmEngine(Context& c, const Opts& opts) : ctx(c), o(opts), s(c.stream) {
@@ -274,11 +328,83 @@ struct LmEngine {
     detail::h2d(cta_job0, plan.cta_job0, s);
     bar.alloc(nm, s);
     bar.zero();
+    bar_base.alloc(nm, s);
+    bar_base.zero();
     pcg_part.alloc(kParts * (size_t)plan.ncta, s);
     check(cudaStreamSynchronize(s), "sync");  // host plan vectors
-    pa = PcgArgs<R>{jobs, cta_job0, bar, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx, S, pre, g,
+    pa = PcgArgs<R>{jobs, cta_job0, bar, bar_base, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx, S, pre, g,
                     x, z, p, nb, lens_row, lens_pos, smem_rows, smem_blocks, active, pcg_iters,
                     o.pcg_max_iter, o.pcg_tol, ctx.err};
+    ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0;
+    if constexpr (sizeof(R) == 4) setup_cluster(h_lens);
+    else if (o.pcg_kernel == 2)
+      throw CudaError(cudaErrorNotSupported, "cluster PCG: the FP64 form uses the grid kernel");
+  }
+
+  // Mixed form: one cluster of up to 16 CTAs per model with the whole PCG in
+  // distributed shared memory, if every model fits; else the grid kernel.
+  void setup_cluster(const std::vector<int32_t>& h_lens) {
+    use_cluster = false;
+    ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0;
+    if (o.pcg_kernel == 1) return;  // grid kernel requested
+    const bool required = o.pcg_kernel == 2;
+    auto unusable = [&](const std::string& why) {
+      if (required) throw CudaError(cudaErrorNotSupported, "cluster PCG: " + why);
+    };
+    int64_t max_rows = 0;
+    for (int64_t m = 0; m < ctx.nm; ++m)
+      max_rows = std::max<int64_t>(max_rows, ctx.h_blk0[m + 1] - ctx.h_blk0[m]);
+    const int csize = (int)std::min<int64_t>(kCgMaxCluster, std::max<int64_t>(1, (max_rows + 31) / 32));
+    int smem_optin = 0;
+    check(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx.device),
+          "attr");
+    cudaFuncAttributes fa{};
+    check(cudaFuncGetAttributes(&fa, pcg_cluster_kernel), "func attr");
+    const size_t avail = (size_t)smem_optin - fa.sharedSizeBytes;
+    const uint32_t rows_cap = (uint32_t)std::min<size_t>(avail / 2 / (kCgRow * 4), 4096);
+    detail::ClusterPlan cp;
+    if (!detail::plan_cluster(ctx, SB.h_row_ptr, h_lens, csize, rows_cap, cp))
+      return unusable("a model has too many block rows for one cluster");
+    const size_t row_bytes = (size_t)cp.max_rows * kCgRow * 4;
+    const uint32_t cap_blocks = (uint32_t)std::min<size_t>(cp.max_blocks, (avail - row_bytes) / (36 * 4 + 4));
+    const size_t smem = cg_smem_bytes(cp.max_rows, cap_blocks);
+    check(cudaFuncSetAttribute(pcg_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem),
+          "cluster smem");
+    if (csize > 8)
+      check(cudaFuncSetAttribute(pcg_cluster_kernel,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+            "cluster size");
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)cp.jobs.size());
+    cfg.blockDim = dim3(kCgThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    const cudaError_t oe = cudaOccupancyMaxActiveClusters(&nclusters, pcg_cluster_kernel, &cfg);
+    if (oe != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      return unusable(std::string("no cluster of ") + std::to_string(csize) + " CTAs with " +
+                      std::to_string(smem) + " bytes of shared memory fits (" +
+                      cudaGetErrorString(oe) + ")");
+    }
+    detail::h2d(cg_jobs, cp.jobs, s);
+    detail::h2d(cg_loc, cp.row_loc, s);
+    check(cudaStreamSynchronize(s), "sync");
+    ca = CgArgs{cg_jobs, cg_loc, SB.row_ptr, SB.col_idx, (const float*)S.p, (const float*)pre.p,
+                (const float*)g.p, (float*)x.p, lens_row, lens_pos, SB.diag_pos, cp.max_rows,
+                cap_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol};
+    cg_smem = smem;
+    cl_size = csize;
+    use_cluster = true;
+    ctx.last_pcg_kernel = 2, ctx.last_pcg_cluster = csize;
   }
 
   void set_lambda(double lam) {
@@ -320,10 +446,26 @@ struct LmEngine {
 
   // Block-Jacobi PCG (ba.rs:155-196).
   void solve_pcg() {
-    void* args[] = {&pa};
-    check(cudaLaunchCooperativeKernel((void*)pcg_kernel<R>, dim3(plan.ncta), dim3(kPcgThreads),
-                                      args, smem_bytes, s),
-          "pcg launch");
+    if (use_cluster) {
+      cudaLaunchConfig_t cfg{};
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)cl_size;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)(ctx.nm * cl_size));
+      cfg.blockDim = dim3(kCgThreads);
+      cfg.dynamicSmemBytes = cg_smem;
+      cfg.stream = s;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      check(cudaLaunchKernelEx(&cfg, pcg_cluster_kernel, ca), "pcg cluster launch");
+    } else {
+      void* args[] = {&pa};
+      check(cudaLaunchCooperativeKernel((void*)pcg_kernel<R>, dim3(plan.ncta), dim3(kPcgThreads),
+                                        args, smem_bytes, s),
+            "pcg launch");
+    }
     g_launches++;
     T.mark(BA_PHASE_PCG);
   }
@@ -333,7 +475,8 @@ struct LmEngine {
     const StateView cur = ctx.cur(), tri = ctx.trial();
     BA_LAUNCH(update_cameras_kernel<R><<<grid_for(std::max(ctx.nc, ctx.ng), 256), 256, 0, s>>>(
         P, cur, tri, B, active));
-    BA_LAUNCH(backsub_kernel<R><<<grid_for(ctx.np, 256), 256, 0, s>>>(P, SV, cur, tri, B, active));
+    BA_LAUNCH(backsub_kernel<R><<<grid_for(ctx.np, 256), 256, 0, s>>>(P, SV, cur, tri, B, sigma,
+                                                                     active));
     T.mark(BA_PHASE_UPDATE);
   }
 

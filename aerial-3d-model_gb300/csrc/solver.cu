@@ -223,12 +223,14 @@ Opts resolve_options(const ba_options* o) {
     r.memory_cap = o->memory_cap_bytes;
     r.log = o->log;
     r.profile = o->profile;
+    r.pcg_kernel = o->pcg_kernel;
   }
   if (r.max_iter < 0) throw BadInput("max_iter must be >= 0");
   if (!(r.sigma > 0.0) || !std::isfinite(r.sigma)) throw BadInput("sigma_px must be finite and > 0");
   if (r.loss != 0 && r.loss != 1) throw BadInput("unknown loss");
   if (r.precision != 0 && r.precision != 1) throw BadInput("unknown precision");
   if (r.matrix_free < 0 || r.matrix_free > 2) throw BadInput("unknown matrix_free mode");
+  if (r.pcg_kernel < 0 || r.pcg_kernel > 2) throw BadInput("unknown pcg_kernel");
   return r;
 }
 
@@ -330,6 +332,8 @@ void solve(Context& c, const ba_options* opt, ba_stats* stats) {
       for (int k = 0; k < kPhases; ++k) st.ms_phase[k] = c.phase_ms[k], st.n_phase[k] = c.phase_n[k];
       st.n_blocks = c.nb, st.n_nonzero_blocks = c.last_nz, st.n_schur_pairs = c.last_pairs;
       st.n_lens_entries = c.last_nl;
+      st.pcg_kernel = c.last_pcg_kernel;
+      st.pcg_cluster = c.last_pcg_cluster;
     }
   }
 }

@@ -33,6 +33,7 @@ class Options:
     memory_cap_bytes: int = 0
     stream: int | None = None     # cudaStream_t as an integer handle
     profile: bool = False         # per-phase CUDA-event timing (SolveInfo.phases)
+    pcg_kernel: str = "auto"      # "auto" | "grid" | "cluster" (mixed form)
 
 
 @dataclass
@@ -57,6 +58,8 @@ class SolveInfo:
     accepted: np.ndarray = field(default=None, repr=False)
     phases: dict = field(default_factory=dict, repr=False)  # name -> (ms, launches)
     sizes: dict = field(default_factory=dict, repr=False)   # reduced-system sizes
+    pcg_kernel: str = "none"      # PCG kernel that ran: "grid" | "cluster"
+    pcg_cluster: int = 0          # CTAs per cluster when the cluster kernel ran
 
     def stats(self) -> BaStats:
         return BaStats(self.iterations, self.initial_rms, self.final_rms)
@@ -79,6 +82,7 @@ def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> n
     c.memory_cap_bytes = int(o.memory_cap_bytes)
     c.stream = o.stream
     c.profile = 1 if o.profile else 0
+    c.pcg_kernel = {"auto": 0, "grid": 1, "cluster": 2}[o.pcg_kernel]
     c.log = C.cast(C.pointer(log), C.c_void_p) if log is not None else None
     return c
 
@@ -116,6 +120,8 @@ def _info(s: native.BaStatsC) -> SolveInfo:
                    if s.n_phase[i]}
     info.sizes = dict(blocks=s.n_blocks, nonzero_blocks=s.n_nonzero_blocks,
                       schur_pairs=s.n_schur_pairs, lens_entries=s.n_lens_entries)
+    info.pcg_kernel = {1: "grid", 2: "cluster"}.get(s.pcg_kernel, "none")
+    info.pcg_cluster = s.pcg_cluster
     return info
 
 

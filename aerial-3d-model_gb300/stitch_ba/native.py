@@ -39,7 +39,8 @@ class BaOptions(C.Structure):
     _fields_ = [("max_iter", C.c_int32), ("sigma_px", C.c_double), ("loss", C.c_int32),
                 ("precision", C.c_int32), ("pcg_max_iter", C.c_int32), ("pcg_tol", C.c_double),
                 ("matrix_free", C.c_int32), ("memory_cap_bytes", C.c_int64),
-                ("stream", C.c_void_p), ("log", C.c_void_p), ("profile", C.c_int32)]
+                ("stream", C.c_void_p), ("log", C.c_void_p), ("profile", C.c_int32),
+                ("pcg_kernel", C.c_int32)]
 
 
 class BaStatsC(C.Structure):
@@ -51,7 +52,8 @@ class BaStatsC(C.Structure):
                 ("d2h_bytes", C.c_int64), ("device_bytes", C.c_int64),
                 ("ms_phase", C.c_double * 9), ("n_phase", C.c_int64 * 9),
                 ("n_blocks", C.c_int64), ("n_nonzero_blocks", C.c_int64),
-                ("n_schur_pairs", C.c_int64), ("n_lens_entries", C.c_int64)]
+                ("n_schur_pairs", C.c_int64), ("n_lens_entries", C.c_int64),
+                ("pcg_kernel", C.c_int32), ("pcg_cluster", C.c_int32)]
 
 PHASES = ["point", "camera", "schur", "assemble", "pcg", "update", "cost", "control", "setup"]
 

@@ -107,6 +107,9 @@ typedef struct ba_options {
   void* stream;         /* cudaStream_t to run on, NULL: the library's own */
   ba_log* log;          /* NULL or per-iteration log (single-model calls)  */
   int32_t profile;      /* 1: time each kernel phase with CUDA events      */
+  int32_t pcg_kernel;   /* 0: auto, 1: grid-wide kernel, 2: one thread-block
+                           cluster per model (mixed form; falls back to the
+                           grid kernel when a model does not fit)          */
 } ba_options;
 
 /* Kernel phases timed when ba_options.profile is set (ba_stats.ms_phase). */
@@ -142,6 +145,8 @@ typedef struct ba_stats {
   int64_t n_nonzero_blocks;  /* 6x6 blocks of the symmetric matrix (full)  */
   int64_t n_schur_pairs;  /* point-entry pairs summed into upper blocks    */
   int64_t n_lens_entries; /* per-point lens entries                        */
+  int32_t pcg_kernel;     /* PCG kernel that ran: 1 grid-wide, 2 cluster   */
+  int32_t pcg_cluster;    /* CTAs per cluster (cluster kernel), else 0     */
 } ba_stats;
 
 /* Defaults: max_iter 60, sigma_px 1, Cauchy, FP64, PCG 400 / 1e-20. */
