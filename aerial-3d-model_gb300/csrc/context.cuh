@@ -19,6 +19,15 @@ struct ModelResult {
 
 constexpr int kPhases = 9;
 
+// PCG configuration chosen by the autotuner for one form (FP64 / mixed).
+struct PcgTuning {
+  bool valid = false;
+  int kernel = 1;       // 1 grid, 2 cluster
+  int rows_target = 4;  // grid kernel: block rows per CTA
+  int cluster = 0;      // cluster kernel: CTAs per cluster
+  double us_per_iter = 0.0;
+};
+
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -49,7 +58,9 @@ struct Context {
   double phase_ms[kPhases] = {0};
   int64_t phase_n[kPhases] = {0};
   int64_t last_nz = 0, last_pairs = 0, last_nl = 0;
-  int32_t last_pcg_kernel = 0, last_pcg_cluster = 0;
+  int32_t last_pcg_kernel = 0, last_pcg_cluster = 0, last_pcg_ctas = 0;
+  PcgTuning tuning[2];  // [0] FP64 form, [1] mixed form
+  bool last_graph = false;
   double last_h2d_ms = 0, last_d2h_ms = 0;
   int64_t last_h2d_bytes = 0, last_d2h_bytes = 0;
 
@@ -93,6 +104,9 @@ struct Opts {
   ba_log* log = nullptr;
   int32_t profile = 0;
   int32_t pcg_kernel = 0;  // 0 auto, 1 grid, 2 cluster
+  int32_t graph = 1;       // capture each LM iteration as a CUDA graph
+  int32_t autotune = 0;    // tune the PCG configuration before solving
+  int32_t stop_patience = 0;  // 0 or 1: the reference's stop rule
 };
 
 // One solve of the uploaded batch from its initial states, in precision R.

@@ -738,7 +738,14 @@ static __global__ void control_kernel(int64_t nm, Control C) {
     const double rel = (c - nc) / fmax(c, 1e-12);
     C.cost[m] = nc;
     C.lambda[m] = fmax(lam / 3.0, 1e-9);
-    if (rel < 1e-6) act = 0;
+    // ba.rs:372-374 stops on the first such step (patience 1, the default);
+    // a larger patience waits for that many consecutive ones, for inexact
+    // inner solves that can give one small decrease before the minimum.
+    if (rel < 1e-6) {
+      if (++C.small[m] >= C.patience) act = 0;
+    } else {
+      C.small[m] = 0;
+    }
   } else {
     C.lambda[m] = lam * 5.0;
     if (C.lambda[m] > 1e6) act = 0;

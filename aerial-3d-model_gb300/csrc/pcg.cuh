@@ -59,8 +59,9 @@ struct PcgArgs {
   int64_t nb;
   const int32_t* lens_row;  // [nm]: the model's single lens block row, or -1
   const int32_t* lens_pos;  // [nb]: block index of (row, lens row), or -1
+  const uint32_t* diag_pos; // [nb]: block index of the diagonal block
   uint32_t smem_rows;       // row-state capacity of the dynamic shared memory
-  uint32_t smem_blocks;     // S-block capacity (0: S read from global)
+  uint32_t smem_blocks;     // S blocks cached per CTA (the rest read from global)
   const int32_t* active;
   int32_t* iters;
   int32_t max_iter;
@@ -78,9 +79,12 @@ constexpr int kMaxGroupCtas = 32 * kReadUnroll * 4;
 // padded to a multiple of 16 bytes in both precisions.
 constexpr int kRowState = 68;
 
+// Dynamic shared memory: row state, cached S blocks, their columns, and per
+// row its block range and lens block (3 words).
 template <typename R>
 constexpr size_t pcg_smem_bytes(uint32_t rows, uint32_t blocks) {
-  return (size_t)rows * kRowState * sizeof(R) + (size_t)blocks * (36 * sizeof(R) + 4);
+  return (size_t)rows * kRowState * sizeof(R) + (size_t)blocks * (36 * sizeof(R) + 4) +
+         (size_t)rows * 12;
 }
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
@@ -143,10 +147,10 @@ __device__ __forceinline__ double sum8(double v) {
 // the launch's base value.  Only warp 0 of a CTA takes part; the partials are
 // then read with all loads in flight at once.  Bounded: after kSpinCycles the
 // waiter sets ERR_BARRIER_TIMEOUT; every CTA leaves at its next exchange.
-template <int N, typename R>
+template <int N, typename R, typename Post>
 __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm, double* tot,
                                              const PcgArgs<R>& A, const PcgJob& J, int slot,
-                                             unsigned long long& target) {
+                                             unsigned long long& target, Post&& post) {
   __shared__ int ok_s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
@@ -161,7 +165,11 @@ __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm,
     c += __shfl_xor_sync(kFull, c, 16);
     if (J.gsize == 1) {
       if (lane < N) tot[lane] = c;
-      if (lane == 0) ok_s = 1;
+      __syncwarp();
+      if (lane == 0) {
+        ok_s = 1;
+        post();  // the iteration's scalars, once per CTA
+      }
     } else {
       if (lane < N) A.part[(size_t)(slot + lane) * A.ncta + J.base + J.rank] = c;
       __threadfence();
@@ -205,11 +213,22 @@ __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm,
       }
       warp_sum8(v);  // lane 4i holds value i
       if ((lane & 3) == 0 && (lane >> 2) < N) tot[lane >> 2] = v[0];
+      __syncwarp();
+      if (lane == 0) post();  // the iteration's scalars, once per CTA
     }
   }
   __syncthreads();
   return ok_s != 0;
 }
+
+// Scalars of an iteration, computed once per CTA by thread 0 (FP64 division
+// and conversions would otherwise run on every warp's FP64 pipe).
+template <typename R>
+struct PcgScalars {
+  double rz, b2, beta, a;
+  R beta_r, a_r;  // beta and a in storage precision
+  int stop;
+};
 
 // A 6x6 block into registers with 16-byte loads (global or shared).
 template <typename A>
@@ -234,13 +253,13 @@ __device__ __forceinline__ void load_block(const float* blk, A* m) {
 // p_j = z_j + β p_j(prev), the reference's update (ba.rs:192), in storage
 // precision; the same expression for own rows and for gathered columns.
 template <typename R>
-__device__ __forceinline__ R p_of(R zj, R pj, double beta) {
-  return (R)(zj + pj * (R)beta);
+__device__ __forceinline__ R p_of(R zj, R pj, R beta_r) {
+  return (R)(zj + pj * beta_r);
 }
 
 template <typename R>
 __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, double* tot,
-                        R* rs) {
+                        PcgScalars<R>& sc, R* rs) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nrows = J.row1 - J.row0;
   const uint32_t B0 = A.row_ptr[J.row0];
@@ -249,20 +268,34 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
     if (threadIdx.x == 0) atomicOr(A.err, ERR_STRUCTURE);
     return false;
   }
-  const bool cached = nblk <= A.smem_blocks;
+  // The first ncached blocks of the CTA's rows (camera rows come first; the
+  // lens row, last, uses only its diagonal block) live in shared memory.
+  const uint32_t ncached = nblk < A.smem_blocks ? nblk : A.smem_blocks;
   // Barrier counter value at this launch's start (written by the previous
   // launch's rank 0: every member made the same number of arrivals).
   unsigned long long target = A.bar_base[J.model];
   // Shared-memory carve-up: row state, then cached S blocks and columns.
   R* sS = rs + (size_t)A.smem_rows * kRowState;
   uint32_t* sC = reinterpret_cast<uint32_t*>(sS + (size_t)A.smem_blocks * 36);
+  int32_t* sM = reinterpret_cast<int32_t*>(sC + A.smem_blocks);
   const int32_t lens = A.lens_row[J.model];  // -1: no transposed lens row
-  if (cached) {
-    const uint32_t chunks = nblk * (uint32_t)(36 * sizeof(R) / 16);
+  {
+    const uint32_t chunks = ncached * (uint32_t)(36 * sizeof(R) / 16);
     const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
     float4* dst = reinterpret_cast<float4*>(sS);
     for (uint32_t c = threadIdx.x; c < chunks; c += blockDim.x) dst[c] = src[c];
-    for (uint32_t t = threadIdx.x; t < nblk; t += blockDim.x) sC[t] = A.col_idx[B0 + t];
+    for (uint32_t t = threadIdx.x; t < ncached; t += blockDim.x) sC[t] = A.col_idx[B0 + t];
+    // Per row: its block range (the lens row: only its diagonal block; its
+    // camera columns arrive through the camera rows' transposed terms) and
+    // the position of its lens block.
+    for (uint32_t lr = threadIdx.x; lr < nrows; lr += blockDim.x) {
+      const uint32_t row = J.row0 + lr;
+      uint32_t b0 = A.row_ptr[row], b1 = A.row_ptr[row + 1];
+      if ((int32_t)row == lens) b0 = A.diag_pos[row], b1 = b0 + 1;
+      sM[3 * lr] = (int32_t)b0;
+      sM[3 * lr + 1] = (int32_t)b1;
+      sM[3 * lr + 2] = (int32_t)row == lens ? -1 : A.lens_pos[row];
+    }
   }
   for (uint32_t t = threadIdx.x; t < nrows * 36; t += blockDim.x)
     rs[(t / 36) * kRowState + 30 + (t % 36)] = A.pre[36 * (size_t)J.row0 + t];
@@ -298,29 +331,32 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
     w2[0] += sum8(a);
     w2[1] += sum8(bb);
   }
-  if (!group_reduce<2>(w2, wsm, tot, A, J, 0, target)) return false;
-  double rz = tot[0];
-  const double b2 = fmax(tot[1], 1e-300);
-  double beta = 0.0;
+  if (!group_reduce<2>(w2, wsm, tot, A, J, 0, target, [&] {
+        sc.rz = tot[0];
+        sc.b2 = fmax(tot[1], 1e-300);
+        sc.beta = 0.0;
+        sc.beta_r = (R)0;
+        sc.stop = 0;
+      }))
+    return false;
   int32_t spmv = 0;
   for (int32_t it = 0; it < A.max_iter; ++it) {
     R* pcur = A.p2 + (size_t)(it & 1) * 6 * A.nb;
     const R* pprev = A.p2 + (size_t)((it + 1) & 1) * 6 * A.nb;
+    const R beta = sc.beta_r;
     // q = S p (ba.rs:144-152) for the warp's rows.
     double w4[4] = {0.0, 0.0, 0.0, 0.0};
     for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps) {
       const uint32_t row = J.row0 + lr;
       R* st = ROW(lr);
-      const uint32_t b0 = A.row_ptr[row], b1 = A.row_ptr[row + 1];
-      const bool is_lens = (int32_t)row == lens;
+      const uint32_t b0 = (uint32_t)sM[3 * lr], b1 = (uint32_t)sM[3 * lr + 1];
       R acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       for (uint32_t k = b0 + lane; k < b1; k += 32) {
-        const uint32_t col = cached ? sC[k - B0] : A.col_idx[k];
-        // Lens row: only its block with the lens column (the diagonal);
-        // camera columns arrive through the camera rows' transposed terms.
-        if (is_lens && (int32_t)col != lens) continue;
+        const uint32_t kk = k - B0;
+        const bool in_smem = kk < ncached;
+        const uint32_t col = in_smem ? sC[kk] : A.col_idx[k];
         R m[36], pp[6];
-        load_block(cached ? sS + (size_t)(k - B0) * 36 : A.S + (size_t)k * 36, m);
+        load_block(in_smem ? sS + (size_t)kk * 36 : A.S + (size_t)k * 36, m);
         const R* zv = A.z + 6 * (size_t)col;
         const R* pv = pprev + 6 * (size_t)col;
 #pragma unroll
@@ -345,13 +381,14 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
       }
       w4[0] += sum8(vl ? (double)pi * (double)qi : 0.0);
       // S_cg^T p_c for the lens column: lane 3t + j multiplies S_cg[t][j] p_t.
-      const int32_t lp = is_lens ? -1 : A.lens_pos[row];
+      const int32_t lp = sM[3 * lr + 2];
       if (lp >= 0) {
         const int t = lane / 3, j = lane - 3 * (lane / 3);
         const R pt = __shfl_sync(kFull, pi, t < 6 ? t : 0);
         R v = (R)0;
         if (lane < 18) {
-          const R* blk = cached ? sS + (size_t)(lp - B0) * 36 : A.S + (size_t)lp * 36;
+          const uint32_t kk = (uint32_t)lp - B0;
+          const R* blk = kk < ncached ? sS + (size_t)kk * 36 : A.S + (size_t)lp * 36;
           v = blk[6 * t + j] * pt;
         }
         v += __shfl_down_sync(kFull, v, 3);
@@ -363,25 +400,30 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
         w4[3] += (double)__shfl_sync(kFull, v, 2);
       }
     }
-    if (!group_reduce<4>(w4, wsm, tot, A, J, 2, target)) return false;
+    const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
+    if (!group_reduce<4>(w4, wsm, tot, A, J, 2, target, [&] {
+          double pq = tot[0];
+          if (lens >= 0) {
+            // The lens row's q: its diagonal product plus the transposed
+            // partials; its share of p·q: p_g · (Σ S_cg^T p_c).
+            const R* zg = A.z + 6 * (size_t)lens;
+            const R* pg = pprev + 6 * (size_t)lens;
+            pq += (double)p_of<R>(__ldcg(zg + 0), __ldcg(pg + 0), beta) * tot[1] +
+                  (double)p_of<R>(__ldcg(zg + 1), __ldcg(pg + 1), beta) * tot[2] +
+                  (double)p_of<R>(__ldcg(zg + 2), __ldcg(pg + 2), beta) * tot[3];
+            if (lens_here) {
+              R* q = ROW((uint32_t)lens - J.row0) + 24;
+              for (int c = 0; c < 3; ++c) q[c] = (R)((double)q[c] + tot[1 + c]);
+            }
+          }
+          sc.stop = fabs(pq) < 1e-300 ? 1 : 0;  // ba.rs:174
+          sc.a = sc.stop ? 0.0 : sc.rz / pq;
+          sc.a_r = (R)sc.a;
+        }))
+      return false;
     ++spmv;
-    double pq = tot[0];
-    if (lens >= 0) {
-      // The lens row's q: its diagonal product plus the transposed partials;
-      // its share of p·q: p_g · (Σ S_cg^T p_c).
-      const R* zg = A.z + 6 * (size_t)lens;
-      const R* pg = pprev + 6 * (size_t)lens;
-      pq += (double)p_of<R>(__ldcg(zg + 0), __ldcg(pg + 0), beta) * tot[1] +
-            (double)p_of<R>(__ldcg(zg + 1), __ldcg(pg + 1), beta) * tot[2] +
-            (double)p_of<R>(__ldcg(zg + 2), __ldcg(pg + 2), beta) * tot[3];
-      if ((uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1 && threadIdx.x < 3) {
-        R* q = ROW((uint32_t)lens - J.row0) + 24;
-        q[threadIdx.x] = (R)((double)q[threadIdx.x] + tot[1 + threadIdx.x]);
-      }
-    }
-    __syncthreads();
-    if (fabs(pq) < 1e-300) break;  // ba.rs:174
-    const double a = rz / pq;
+    if (sc.stop) break;
+    const R a = sc.a_r;
     // x += a p, r -= a q, z = M r (ba.rs:178-188), one component per lane.
     double w2b[2] = {0.0, 0.0};
     for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps) {
@@ -389,8 +431,8 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
       R* st = ROW(lr);
       R ri = (R)0;
       if (vl) {
-        st[ci] = st[ci] + st[18 + ci] * (R)a;
-        ri = st[6 + ci] - st[24 + ci] * (R)a;
+        st[ci] = st[ci] + st[18 + ci] * a;
+        ri = st[6 + ci] - st[24 + ci] * a;
         st[6 + ci] = ri;
       }
       R zi = (R)0;
@@ -409,12 +451,14 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
       w2b[0] += sum8(rr);
       w2b[1] += sum8(rzl);
     }
-    if (!group_reduce<2>(w2b, wsm, tot, A, J, 6, target)) return false;
-    const double rr = tot[0], rz2 = tot[1];
-    __syncthreads();
-    if (rr < A.tol * b2) break;  // ba.rs:182
-    beta = rz2 / rz;             // ba.rs:189-190
-    rz = rz2;
+    if (!group_reduce<2>(w2b, wsm, tot, A, J, 6, target, [&] {
+          sc.stop = tot[0] < A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
+          sc.beta = tot[1] / sc.rz;                    // ba.rs:189-190
+          sc.beta_r = (R)sc.beta;
+          sc.rz = tot[1];
+        }))
+      return false;
+    if (sc.stop) break;
   }
   for (uint32_t lr = warp; lr < nrows; lr += kPcgWarps)
     if (vl) A.x[6 * (size_t)(J.row0 + lr) + ci] = ROW(lr)[ci];
@@ -431,12 +475,13 @@ template <typename R>
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<R> A) {
   __shared__ double wsm[kPcgWarps * 4];
   __shared__ double tot[4];
+  __shared__ PcgScalars<R> sc;
   extern __shared__ __align__(16) unsigned char pcg_smem[];
   R* rs = reinterpret_cast<R*>(pcg_smem);
   for (int jb = A.cta_job0[blockIdx.x]; jb < A.cta_job0[blockIdx.x + 1]; ++jb) {
     const PcgJob J = A.jobs[jb];
     if (!A.active[J.model]) continue;
-    if (!pcg_job<R>(A, J, wsm, tot, rs)) return;
+    if (!pcg_job<R>(A, J, wsm, tot, sc, rs)) return;
   }
 }
 

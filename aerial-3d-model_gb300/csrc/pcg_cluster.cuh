@@ -26,7 +26,7 @@ namespace ba {
 
 namespace cgx = cooperative_groups;
 
-constexpr int kCgThreads = 256;
+constexpr int kCgThreads = 512;
 constexpr int kCgWarps = kCgThreads / 32;
 constexpr int kCgMaxCluster = 16;
 // Row state in floats: x r z p0 p1 q (8 each, 6 used) | M (36) | the row's
@@ -63,55 +63,83 @@ inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks) {
   return (size_t)cap_rows * kCgRow * 4 + (size_t)cap_blocks * (36 * 4 + 4);
 }
 
-// Sum over lanes 0..7 of a float (lanes >= 8 hold 0): all lanes get it.
-__device__ __forceinline__ double cg_sum8(double v) {
+// Sum over lanes 0..7 (lanes >= 8 hold 0); lanes 0..7 receive it.
+__device__ __forceinline__ float cg_sum8f(float v) {
   v += __shfl_xor_sync(kFull, v, 1);
   v += __shfl_xor_sync(kFull, v, 2);
   v += __shfl_xor_sync(kFull, v, 4);
   return v;
 }
 
-// N (<= 4) per-warp values (every lane holds them) summed over the CTA, then
-// over the cluster's CTAs: every lane of every warp receives the totals.
-// `part` is this CTA's slot (static shared memory, same offset everywhere).
-template <int N>
-__device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const double (&wv)[N],
-                                          double* wsm, double* part, double (&tot)[4]) {
+// Inner products: a warp sums its rows' products in FP32 (a few rows of six
+// components); the warps' partials are summed in FP64 over the CTA and then
+// over the cluster's CTAs, in a fixed order, by warp 0 alone (an FP64 warp
+// instruction occupies its SM sub-partition for ~64 cycles on this GPU, so
+// FP64 work stays off the other warps).  wv: N (<= 4) values held by lane 0
+// of every warp; all threads receive the totals in tot (shared memory).
+template <int N, typename Post>
+__device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&wv)[N],
+                                          float* wsm, double* part, double* tot, Post&& post) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) wsm[warp * 4 + i] = i < N ? wv[i < N ? i : 0] : 0.0;
+    for (int i = 0; i < 4; ++i) wsm[warp * 4 + i] = i < N ? wv[i < N ? i : 0] : 0.0f;
   __syncthreads();
   if (warp == 0) {
-    double c = wsm[lane];  // lane = 4 w + i
+    double c = 0.0;  // lane = 4 w + i (mod 32): warps w, w + 8, ... in order
+#pragma unroll
+    for (int o = 0; o < kCgWarps * 4; o += 32) c += (double)wsm[o + lane];
     c += __shfl_xor_sync(kFull, c, 4);
     c += __shfl_xor_sync(kFull, c, 8);
     c += __shfl_xor_sync(kFull, c, 16);
     if (lane < 4) part[lane] = c;
   }
   cl.sync();
-  const int csize = (int)cl.num_blocks();
-  double v[4] = {0.0, 0.0, 0.0, 0.0};
-  if (lane < csize) {
-    const double* rp = cl.map_shared_rank(part, (unsigned)lane);
+  if (warp == 0) {
+    // lane r < cluster size holds CTA r's values; recursive halving leaves
+    // the sum of value i in lanes 4i..4i+3.
+    const int csize = (int)cl.num_blocks();
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    if (lane < csize) {
+      const double* rp = cl.map_shared_rank(part, (unsigned)lane);
 #pragma unroll
-    for (int i = 0; i < N; ++i) v[i] = rp[i];
+      for (int i = 0; i < N; ++i) v[i] = rp[i];
+    }
+    {
+      const bool up = lane & 8;
+      const double s0 = up ? v[0] : v[2], s1 = up ? v[1] : v[3];
+      const double r0 = __shfl_xor_sync(kFull, s0, 8), r1 = __shfl_xor_sync(kFull, s1, 8);
+      v[0] = (up ? v[2] : v[0]) + r0;
+      v[1] = (up ? v[3] : v[1]) + r1;
+    }
+    {
+      const bool up = lane & 4;
+      const double s0 = up ? v[0] : v[1];
+      const double r0 = __shfl_xor_sync(kFull, s0, 4);
+      v[0] = (up ? v[1] : v[0]) + r0;
+    }
+    v[0] += __shfl_xor_sync(kFull, v[0], 2);
+    v[0] += __shfl_xor_sync(kFull, v[0], 1);
+    v[0] += __shfl_xor_sync(kFull, v[0], 16);  // lanes >= 16 hold zeros
+    if ((lane & 3) == 0 && lane < 16) tot[lane >> 2] = v[0];
+    __syncwarp();
+    if (lane == 0) post();  // the iteration's scalars, once per CTA
   }
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    double t = v[i];
-    t += __shfl_xor_sync(kFull, t, 1);
-    t += __shfl_xor_sync(kFull, t, 2);
-    t += __shfl_xor_sync(kFull, t, 4);
-    t += __shfl_xor_sync(kFull, t, 8);
-    t += __shfl_xor_sync(kFull, t, 16);
-    tot[i] = t;
-  }
+  __syncthreads();
 }
 
+// Scalars of the iteration, computed by thread 0 and read by every thread.
+struct CgScalars {
+  double rz, b2, pq, beta;
+  float af, bf;
+  int stop;
+};
+
 static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A) {
-  __shared__ double wsm[kCgWarps * 4];
+  __shared__ float wsm[kCgWarps * 4];
   __shared__ double part[2][4];
+  __shared__ double tot[4];
+  __shared__ CgScalars sc;
   extern __shared__ __align__(16) unsigned char cg_smem[];
   cgx::cluster_group cl = cgx::this_cluster();
   const CgJob J = A.jobs[blockIdx.x];
@@ -125,6 +153,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   float* sS = rs + (size_t)A.cap_rows * kCgRow;
   uint32_t* sL = reinterpret_cast<uint32_t*>(sS + (size_t)A.cap_blocks * 36);
   const int32_t lens = A.lens_row[J.model];
+  const uint32_t lens_loc = lens >= 0 ? A.row_loc[lens] : 0u;
   {
     const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
     float4* dst = reinterpret_cast<float4*>(sS);
@@ -150,37 +179,39 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   const bool vl = lane < 6;
   const int ci = vl ? lane : 0;
 #define CGROW(lr) (rs + (size_t)(lr) * kCgRow)
-  // x = 0, r = b, z = M r, p(prev) = 0 (ba.rs:164-168)
-  double w2[2] = {0.0, 0.0};
+  // x = 0, r = b, z = M r, p(prev) = 0 (ba.rs:164-168).  Inner products:
+  // each lane accumulates its component's FP64 products over the warp's rows;
+  // the lanes are summed once per phase.
+  float drz = 0.0f, dbb = 0.0f;
   for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
     float* st = CGROW(lr);
     const float ri = vl ? A.b[6 * (size_t)(J.row0 + lr) + ci] : 0.0f;
     float zi = 0.0f;
 #pragma unroll
     for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
-    double a = 0.0, bb = 0.0;
     if (vl) {
       st[kCgX + ci] = 0.0f;
       st[kCgR + ci] = ri;
       st[kCgZ + ci] = zi;
       st[kCgP + 8 + ci] = 0.0f;  // p buffer 1 = p(prev) of iteration 0
-      a = (double)ri * (double)zi;
-      bb = (double)ri * (double)ri;
+      drz += ri * zi;
+      dbb += ri * ri;
     }
-    w2[0] += cg_sum8(a);
-    w2[1] += cg_sum8(bb);
   }
+  const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
   // The first barrier also makes every CTA's shared memory live for DSMEM.
-  double tot[4];
-  cg_reduce<2>(cl, w2, wsm, part[1], tot);
-  double rz = tot[0];
-  const double b2 = fmax(tot[1], 1e-300);
-  double beta = 0.0;
+  cg_reduce<2>(cl, w2, wsm, part[1], tot, [&] {
+    sc.rz = tot[0];
+    sc.b2 = fmax(tot[1], 1e-300);
+    sc.beta = 0.0;
+    sc.bf = 0.0f;
+    sc.stop = 0;
+  });
   int32_t spmv = 0;
   for (int32_t it = 0; it < A.max_iter; ++it) {
     const int cur = it & 1, prv = cur ^ 1;
-    const float bf = (float)beta;
-    double w4[4] = {0.0, 0.0, 0.0, 0.0};
+    const float bf = sc.bf;
+    float dpq = 0.0f, dlens = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
       const uint32_t b0 = (uint32_t)__float_as_int(st[kCgIdx]);
@@ -214,7 +245,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         st[kCgQ + ci] = qi;
         st[kCgP + 8 * cur + ci] = pi;
       }
-      w4[0] += cg_sum8(vl ? (double)pi * (double)qi : 0.0);
+      if (vl) dpq += pi * qi;
       const int32_t lp = __float_as_int(st[kCgIdx + 2]);
       if (lp >= 0) {  // S_cg^T p_c for the lens column
         const int t = lane / 3, j = lane - 3 * (lane / 3);
@@ -228,30 +259,35 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         v += __shfl_down_sync(kFull, v, 3);
         v += __shfl_down_sync(kFull, v, 6);
         v += __shfl_down_sync(kFull, v, 12);
-        w4[1] += (double)__shfl_sync(kFull, v, 0);
-        w4[2] += (double)__shfl_sync(kFull, v, 1);
-        w4[3] += (double)__shfl_sync(kFull, v, 2);
+        if (lane < 3) dlens += v;  // lanes 0, 1, 2: components 0, 1, 2
       }
     }
-    cg_reduce<4>(cl, w4, wsm, part[0], tot);
+    const float w4[4] = {cg_sum8f(dpq), __shfl_sync(kFull, dlens, 0), __shfl_sync(kFull, dlens, 1),
+                         __shfl_sync(kFull, dlens, 2)};
+    const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
+    cg_reduce<4>(cl, w4, wsm, part[0], tot, [&] {
+      double pq = tot[0];
+      if (lens >= 0) {
+        // The lens row's q gets the transposed camera terms; its share of
+        // p.q is p_g . (sum S_cg^T p_c), with p_g stored by its owner before
+        // the barrier.
+        const float* lrow =
+            cl.map_shared_rank(rs, lens_loc >> 16) + (size_t)(lens_loc & 0xffffu) * kCgRow;
+        pq += (double)lrow[kCgP + 8 * cur + 0] * tot[1] + (double)lrow[kCgP + 8 * cur + 1] * tot[2] +
+              (double)lrow[kCgP + 8 * cur + 2] * tot[3];
+        if (lens_here) {
+          float* q = CGROW((uint32_t)lens - J.row0) + kCgQ;
+          for (int c = 0; c < 3; ++c) q[c] = (float)((double)q[c] + tot[1 + c]);
+        }
+      }
+      sc.pq = pq;
+      sc.stop = fabs(pq) < 1e-300 ? 1 : 0;  // ba.rs:174
+      sc.af = sc.stop ? 0.0f : (float)(sc.rz / pq);
+    });
     ++spmv;
-    double pq = tot[0];
-    if (lens >= 0) {
-      const uint32_t lloc = A.row_loc[lens];
-      const float* lrow = cl.map_shared_rank(rs, lloc >> 16) + (size_t)(lloc & 0xffffu) * kCgRow;
-      // the lens row's p of this iteration (its owner stored it before the barrier)
-      pq += (double)lrow[kCgP + 8 * cur + 0] * tot[1] + (double)lrow[kCgP + 8 * cur + 1] * tot[2] +
-            (double)lrow[kCgP + 8 * cur + 2] * tot[3];
-      if ((uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1 && threadIdx.x < 3) {
-        float* q = CGROW((uint32_t)lens - J.row0) + kCgQ;
-        q[threadIdx.x] = (float)((double)q[threadIdx.x] + tot[1 + threadIdx.x]);
-      }
-    }
-    __syncthreads();
-    if (fabs(pq) < 1e-300) break;  // ba.rs:174
-    const double a = rz / pq;
-    const float af = (float)a;
-    double w2b[2] = {0.0, 0.0};
+    if (sc.stop) break;
+    const float af = sc.af;
+    float drr = 0.0f, drz2 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
       float ri = 0.0f;
@@ -263,19 +299,20 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       float zi = 0.0f;
 #pragma unroll
       for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
-      double rr = 0.0, rzl = 0.0;
       if (vl) {
         st[kCgZ + ci] = zi;
-        rr = (double)ri * (double)ri;
-        rzl = (double)ri * (double)zi;
+        drr += ri * ri;
+        drz2 += ri * zi;
       }
-      w2b[0] += cg_sum8(rr);
-      w2b[1] += cg_sum8(rzl);
     }
-    cg_reduce<2>(cl, w2b, wsm, part[1], tot);
-    if (tot[0] < A.tol * b2) break;  // ba.rs:182
-    beta = tot[1] / rz;               // ba.rs:189-190
-    rz = tot[1];
+    const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};
+    cg_reduce<2>(cl, w2b, wsm, part[1], tot, [&] {
+      sc.stop = tot[0] < A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
+      sc.beta = tot[1] / sc.rz;                    // ba.rs:189-190
+      sc.bf = (float)sc.beta;
+      sc.rz = tot[1];
+    });
+    if (sc.stop) break;
   }
   for (uint32_t lr = warp; lr < nrows; lr += kCgWarps)
     if (vl) A.x[6 * (size_t)(J.row0 + lr) + ci] = CGROW(lr)[kCgX + ci];

@@ -43,18 +43,22 @@ inline PcgPlan plan_pcg(const Context& ctx, const std::vector<uint32_t>& row_ptr
   }
   std::vector<int64_t> G(nm), rows(nm);
   int64_t tot = 0, need = 0;
+  bool all_small = true;
   for (int64_t m = 0; m < nm; ++m) {
     rows[m] = ctx.h_blk0[m + 1] - ctx.h_blk0[m];
     G[m] = std::max<int64_t>(1, (rows[m] + rows_target - 1) / rows_target);
+    G[m] = std::max<int64_t>(G[m], (rows[m] + rows_cap - 1) / rows_cap);
     tot += G[m];
     need += std::max<int64_t>(1, (rows[m] + rows_cap - 1) / rows_cap);
+    all_small = all_small && rows[m] <= rows_cap;
   }
   max_ctas = std::min(max_ctas, kMaxGroupCtas);
+  if (need > max_ctas && !all_small)
+    throw CudaError(cudaErrorNotSupported,
+                    "PCG plan: the batch needs more resident CTAs than the device holds");
   if (need > max_ctas) {
     // More models than resident CTAs: one CTA per model, dealt greedily to
     // the least-loaded CTA (largest first); a CTA solves its models in turn.
-    for (int64_t m = 0; m < nm; ++m)
-      if (rows[m] > rows_cap) throw std::runtime_error("batch too large for the PCG plan");
     pl.ncta = max_ctas;
     std::vector<std::vector<int64_t>> lists(max_ctas);
     std::vector<int64_t> load(max_ctas, 0), order(nm);
@@ -206,6 +210,68 @@ struct PhaseTimer {
   }
 };
 
+// CUDA graph of one LM iteration, captured from the engine's stream on first
+// use.  If the stream cannot be captured (the legacy default stream, or a
+// capture error), the engine launches the kernels directly.
+struct IterationGraph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t kernels = 0;  // kernel nodes, counted into the launch statistics
+  bool tried = false;
+
+  template <typename Engine>
+  bool ok(Engine* e) {
+    if (tried) return exec != nullptr;
+    tried = true;
+    cudaStream_t s = e->s;
+    if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) return false;
+    const int64_t l0 = g_launches;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    bool captured = true;
+    try {
+      e->iteration();
+    } catch (...) {
+      captured = false;
+    }
+    cudaGraph_t gr = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+    g_launches = l0;
+    if (!captured || ce != cudaSuccess || gr == nullptr) {
+      cudaGetLastError();
+      if (gr) cudaGraphDestroy(gr);
+      return false;
+    }
+    if (cudaGraphInstantiate(&exec, gr, 0) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphDestroy(gr);
+      exec = nullptr;
+      return false;
+    }
+    g = gr;
+    size_t n = 0;
+    check(cudaGraphGetNodes(g, nullptr, &n), "graph nodes");
+    std::vector<cudaGraphNode_t> nodes(n);
+    check(cudaGraphGetNodes(g, nodes.data(), &n), "graph nodes");
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType t;
+      check(cudaGraphNodeGetType(nd, &t), "graph node type");
+      if (t == cudaGraphNodeTypeKernel) ++kernels;
+    }
+    return true;
+  }
+  void launch(cudaStream_t s) {
+    check(cudaGraphLaunch(exec, s), "graph launch");
+    g_launches += kernels;
+  }
+  ~IterationGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+  }
+};
+
 // All device state of one solve: structure, per-iteration buffers, LM
 // control scalars and the PCG plan.
 template <typename R>
@@ -223,7 +289,7 @@ struct LmEngine {
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
   DevBuf<int64_t> n_front, pcg_total;
-  DevBuf<int32_t> active, accepted, iters, pcg_iters, any;
+  DevBuf<int32_t> active, accepted, iters, pcg_iters, any, small;
   DevBuf<double> log_cost, log_lam;
   DevBuf<int32_t> log_pcg, log_acc;
   int32_t log_cap = 0;
@@ -236,7 +302,8 @@ struct LmEngine {
   DevBuf<int32_t> lens_row, lens_pos;
   uint32_t smem_rows = 0, smem_blocks = 0;
   size_t smem_bytes = 0;
-  int pcg_rows_target = 0;
+  int pcg_rows_target = 0, grid_rows_target = 0, max_ctas = 0;
+  std::vector<int32_t> h_lens;
   PcgArgs<R> pa{};
   // Cluster-resident PCG (mixed form).
   bool use_cluster = false;
@@ -295,66 +362,90 @@ struct LmEngine {
       accepted.zero(), iters.zero(), pcg_iters.zero(), pcg_total.zero();
       check(cudaStreamSynchronize(s), "sync");
     }
+    small.alloc(nm, s);
+    small.zero();
+    const int32_t patience = o.stop_patience > 0 ? o.stop_patience : 1;
     C = Control{lambda, cost, new_cost, rms, sq, n_front, active, accepted, iters, pcg_iters,
-                pcg_total, any, sigma, o.max_iter, log_cap, log_cost, log_lam, log_pcg, log_acc};
-    // PCG plan (cooperative launch: all CTAs co-resident).  Shared memory per
-    // CTA: row state for up to kSmemRows rows, then as many S blocks as fit.
-    smem_rows = 64;
-    smem_blocks = (uint32_t)((kPcgSmemBudget - (size_t)smem_rows * kRowState * sizeof(R)) /
-                             (36 * sizeof(R) + 4));
-    smem_bytes = pcg_smem_bytes<R>(smem_rows, smem_blocks);
+                pcg_total, any, sigma, small, patience, o.max_iter, log_cap, log_cost, log_lam,
+                log_pcg, log_acc};
+    // PCG: shared memory per grid-kernel CTA (a fixed budget) holds row state
+    // for up to smem_rows rows, then as many S blocks as fit.  A large batch
+    // needs more rows per CTA: all CTAs of the cooperative launch must be
+    // resident at once.
     check(cudaFuncSetAttribute(pcg_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem_bytes),
+                               (int)kPcgSmemBudget),
           "pcg smem");
     int occ = 0;
     check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_kernel<R>, kPcgThreads,
-                                                        smem_bytes),
+                                                        kPcgSmemBudget),
           "occupancy");
-    const int max_ctas = std::max(1, occ) * ctx.n_sm;
-    std::vector<int32_t> h_lens(nm, -1);
+    max_ctas = std::min(std::max(1, occ) * ctx.n_sm, kMaxGroupCtas);
+    const size_t row_bytes = kRowState * sizeof(R) + 12;
+    const int64_t rows_fit = (int64_t)(kPcgSmemBudget / row_bytes);
+    const int64_t rows_need = (nb * 5 / 4 + max_ctas - 1) / max_ctas + 8;
+    smem_rows = (uint32_t)std::min<int64_t>(rows_fit, std::max<int64_t>(64, rows_need));
+    smem_blocks = (uint32_t)((kPcgSmemBudget - (size_t)smem_rows * row_bytes) / (36 * sizeof(R) + 4));
+    smem_bytes = pcg_smem_bytes<R>(smem_rows, smem_blocks);
+    h_lens.assign(nm, -1);
     for (int64_t m = 0; m < nm; ++m)
       if (ctx.h_grp0[m + 1] - ctx.h_grp0[m] == 1)
         h_lens[m] = (int32_t)(ctx.h_blk0[m] + (ctx.h_cam0[m + 1] - ctx.h_cam0[m]));
-    // FP64 instructions serialise per SM sub-partition: one row per warp on
-    // four warps; FP32 rows are cheap: one per warp on all eight.
-    const int rows_target = pcg_rows_target > 0 ? pcg_rows_target : (sizeof(R) == 8 ? 4 : 8);
-    plan = detail::plan_pcg(ctx, SB.h_row_ptr, h_lens, max_ctas, rows_target, (int)smem_rows);
     detail::h2d(lens_row, h_lens, s);
     lens_pos.alloc(detail::at_least_1(nb), s);
     if (nb > 0)
       BA_LAUNCH(lens_pos_kernel<<<grid_for(nb, 256), 256, 0, s>>>(nb, SB.row_ptr, SB.col_idx,
                                                                  P.blk_model, lens_row, lens_pos));
+    bar.alloc(nm, s);
+    bar_base.alloc(nm, s);
+    if (sizeof(R) == 8 && o.pcg_kernel == 2)
+      throw CudaError(cudaErrorNotSupported, "cluster PCG: the FP64 form uses the grid kernel");
+    // Configuration: an earlier tuning of this context for this form, or the
+    // defaults (FP64 instructions serialise per SM sub-partition: one row per
+    // warp on four warps; FP32 rows are cheap: one per warp on all eight).
+    const PcgTuning& tu = ctx.tuning[sizeof(R) == 8 ? 0 : 1];
+    if (tu.valid && o.pcg_kernel == 0) {
+      if (tu.kernel != 2 || !try_cluster(tu.cluster, false, true)) plan_grid(tu.rows_target);
+    } else if (o.pcg_kernel == 2) {
+      try_cluster(0, true);
+    } else if (sizeof(R) == 4 && o.pcg_kernel == 0 && try_cluster(0, false)) {
+      // mixed form: the cluster kernel when every model fits
+    } else {
+      plan_grid(pcg_rows_target > 0 ? pcg_rows_target : (sizeof(R) == 8 ? 4 : 8));
+    }
+  }
+
+  // Grid kernel plan: about rows_target block rows per CTA.
+  void plan_grid(int rows_target) {
+    use_cluster = false;
+    plan = detail::plan_pcg(ctx, SB.h_row_ptr, h_lens, max_ctas, rows_target, (int)smem_rows);
     detail::h2d(jobs, plan.jobs, s);
     detail::h2d(cta_job0, plan.cta_job0, s);
-    bar.alloc(nm, s);
     bar.zero();
-    bar_base.alloc(nm, s);
     bar_base.zero();
     pcg_part.alloc(kParts * (size_t)plan.ncta, s);
     check(cudaStreamSynchronize(s), "sync");  // host plan vectors
-    pa = PcgArgs<R>{jobs, cta_job0, bar, bar_base, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx, S, pre, g,
-                    x, z, p, nb, lens_row, lens_pos, smem_rows, smem_blocks, active, pcg_iters,
-                    o.pcg_max_iter, o.pcg_tol, ctx.err};
-    ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0;
-    if constexpr (sizeof(R) == 4) setup_cluster(h_lens);
-    else if (o.pcg_kernel == 2)
-      throw CudaError(cudaErrorNotSupported, "cluster PCG: the FP64 form uses the grid kernel");
+    pa = PcgArgs<R>{jobs, cta_job0, bar, bar_base, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx,
+                    S, pre, g, x, z, p, ctx.nb, lens_row, lens_pos, SB.diag_pos, smem_rows,
+                    smem_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol, ctx.err};
+    grid_rows_target = rows_target;
+    ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = plan.ncta;
   }
 
-  // Mixed form: one cluster of up to 16 CTAs per model with the whole PCG in
-  // distributed shared memory, if every model fits; else the grid kernel.
-  void setup_cluster(const std::vector<int32_t>& h_lens) {
-    use_cluster = false;
-    ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0;
-    if (o.pcg_kernel == 1) return;  // grid kernel requested
-    const bool required = o.pcg_kernel == 2;
+  // Mixed form: one cluster of `csize` CTAs (0: by size, up to 16) per model
+  // with the whole PCG in distributed shared memory.  Returns false (or throws
+  // BA_NOT_SUPPORTED when `required`) if a model does not fit.
+  bool try_cluster(int csize_req, bool required, bool prefer_cluster = false) {
+    if constexpr (sizeof(R) == 8) return false;
     auto unusable = [&](const std::string& why) {
       if (required) throw CudaError(cudaErrorNotSupported, "cluster PCG: " + why);
+      return false;
     };
     int64_t max_rows = 0;
     for (int64_t m = 0; m < ctx.nm; ++m)
       max_rows = std::max<int64_t>(max_rows, ctx.h_blk0[m + 1] - ctx.h_blk0[m]);
-    const int csize = (int)std::min<int64_t>(kCgMaxCluster, std::max<int64_t>(1, (max_rows + 31) / 32));
+    const int csize = csize_req > 0 ? std::min(csize_req, kCgMaxCluster)
+                                    : (int)std::min<int64_t>(kCgMaxCluster,
+                                                             std::max<int64_t>(1, (max_rows + 31) / 32));
     int smem_optin = 0;
     check(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx.device),
           "attr");
@@ -365,6 +456,7 @@ struct LmEngine {
     detail::ClusterPlan cp;
     if (!detail::plan_cluster(ctx, SB.h_row_ptr, h_lens, csize, rows_cap, cp))
       return unusable("a model has too many block rows for one cluster");
+    if (cp.max_blocks == 0 && cp.max_rows == 0) return unusable("empty plan");
     const size_t row_bytes = (size_t)cp.max_rows * kCgRow * 4;
     const uint32_t cap_blocks = (uint32_t)std::min<size_t>(cp.max_blocks, (avail - row_bytes) / (36 * 4 + 4));
     const size_t smem = cg_smem_bytes(cp.max_rows, cap_blocks);
@@ -395,6 +487,10 @@ struct LmEngine {
                       std::to_string(smem) + " bytes of shared memory fits (" +
                       cudaGetErrorString(oe) + ")");
     }
+    // Unless asked for, use clusters only when every model's cluster is
+    // resident at once (one wave); otherwise models would queue behind each
+    // other while the grid kernel runs them all together.
+    if (!required && !prefer_cluster && (int64_t)nclusters < ctx.nm) return false;
     detail::h2d(cg_jobs, cp.jobs, s);
     detail::h2d(cg_loc, cp.row_loc, s);
     check(cudaStreamSynchronize(s), "sync");
@@ -405,6 +501,70 @@ struct LmEngine {
     cl_size = csize;
     use_cluster = true;
     ctx.last_pcg_kernel = 2, ctx.last_pcg_cluster = csize;
+    ctx.last_pcg_ctas = (int32_t)cp.jobs.size();
+    return true;
+  }
+
+  // Autotuner: time a short PCG run of every candidate configuration on the
+  // system of the first iteration and keep the fastest per iteration.  The
+  // choice is stored in the context and reused by later solves of this form.
+  void autotune() {
+    constexpr int kTuneIters = 40;
+    const bool timing = T.on;
+    T.on = false;  // tuning time is not a solve phase
+    struct Restore {
+      PhaseTimer& t;
+      bool v;
+      ~Restore() { t.on = v; }
+    } restore{T, timing};
+    build_system();
+    std::vector<std::pair<int, int>> cand;  // (kernel, rows_target or cluster size)
+    for (int rt : {2, 3, 4, 6, 8, 12, 16}) cand.push_back({1, rt});
+    if constexpr (sizeof(R) == 4)
+      for (int cs : {4, 8, 12, 16}) cand.push_back({2, cs});
+    cudaEvent_t e0, e1;
+    check(cudaEventCreate(&e0), "event");
+    check(cudaEventCreate(&e1), "event");
+    struct Ev {
+      cudaEvent_t a, b;
+      ~Ev() { cudaEventDestroy(a), cudaEventDestroy(b); }
+    } ev{e0, e1};
+    double best = 1e300;
+    std::pair<int, int> best_c{1, 4};
+    std::vector<int32_t> hit(ctx.nm);
+    for (const auto& c : cand) {
+      if (c.first == 1) {
+        plan_grid(c.second);
+      } else if (!try_cluster(c.second, false, true)) {
+        continue;
+      }
+      const int32_t mi = pa.max_iter;
+      pa.max_iter = ca.max_iter = kTuneIters;
+      float tbest = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        check(cudaEventRecord(e0, s), "event");
+        solve_pcg();
+        check(cudaEventRecord(e1, s), "event");
+        check(cudaEventSynchronize(e1), "tune");
+        float ms = 0;
+        check(cudaEventElapsedTime(&ms, e0, e1), "event");
+        tbest = std::min(tbest, ms);
+      }
+      pa.max_iter = ca.max_iter = mi;
+      check(cudaMemcpy(hit.data(), pcg_iters.p, 4 * ctx.nm, cudaMemcpyDeviceToHost), "d2h");
+      int32_t its = 1;
+      for (int32_t v : hit) its = std::max(its, v);
+      const double per = (double)tbest / its;
+      if (per < best) best = per, best_c = c;
+    }
+    PcgTuning& tu = ctx.tuning[sizeof(R) == 8 ? 0 : 1];
+    tu.valid = true;
+    tu.kernel = best_c.first;
+    tu.rows_target = best_c.first == 1 ? best_c.second : 4;
+    tu.cluster = best_c.first == 2 ? best_c.second : 0;
+    tu.us_per_iter = best * 1000.0;
+    if (best_c.first == 2 && try_cluster(best_c.second, false, true)) return;
+    plan_grid(tu.rows_target);
   }
 
   void set_lambda(double lam) {
@@ -503,6 +663,7 @@ struct LmEngine {
     T.mark(-1);
     setup();
     T.mark(BA_PHASE_SETUP);
+    if (o.autotune && !ctx.tuning[sizeof(R) == 8 ? 0 : 1].valid) autotune();
     eval_cost(ctx.cur(), nullptr, cost, sq, n_front);  // ba.rs:216
     std::vector<double> h_cost0(nm), h_sq0(nm);
     std::vector<int64_t> h_n0(nm);
@@ -515,13 +676,24 @@ struct LmEngine {
       int32_t* p;
       ~PinnedFree() { cudaFreeHost(p); }
     } pf{h_any};
+    // One LM iteration is a fixed sequence of kernels over device-resident
+    // data, so it is captured once as a CUDA graph and replayed; the host only
+    // reads the "any model active" flag between iterations.  Phase timing
+    // needs events between kernels and runs without the graph.
+    IterationGraph graph;
+    const bool use_graph = !T.on && o.graph != 0;
     for (int32_t it = 0; it < o.max_iter; ++it) {
-      iteration();
+      if (use_graph && graph.ok(this)) {
+        graph.launch(s);
+      } else {
+        iteration();
+      }
       check(cudaMemcpyAsync(h_any, any.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
       check(cudaStreamSynchronize(s), "lm iteration");
       T.flush(ctx.phase_ms, ctx.phase_n);
       if (!*h_any) break;
     }
+    ctx.last_graph = graph.exec != nullptr;
     eval_cost(ctx.cur(), nullptr, cost, sq, n_front);  // ba.rs:385
     std::vector<double> h_cost1(nm), h_sq1(nm);
     std::vector<int64_t> h_n1(nm), h_pcg(nm);

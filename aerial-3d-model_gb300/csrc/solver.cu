@@ -224,6 +224,9 @@ Opts resolve_options(const ba_options* o) {
     r.log = o->log;
     r.profile = o->profile;
     r.pcg_kernel = o->pcg_kernel;
+    r.graph = o->no_graph ? 0 : 1;
+    r.autotune = o->autotune;
+    r.stop_patience = o->stop_patience;
   }
   if (r.max_iter < 0) throw BadInput("max_iter must be >= 0");
   if (!(r.sigma > 0.0) || !std::isfinite(r.sigma)) throw BadInput("sigma_px must be finite and > 0");
@@ -231,6 +234,7 @@ Opts resolve_options(const ba_options* o) {
   if (r.precision != 0 && r.precision != 1) throw BadInput("unknown precision");
   if (r.matrix_free < 0 || r.matrix_free > 2) throw BadInput("unknown matrix_free mode");
   if (r.pcg_kernel < 0 || r.pcg_kernel > 2) throw BadInput("unknown pcg_kernel");
+  if (r.stop_patience < 0) throw BadInput("stop_patience must be >= 0");
   return r;
 }
 
@@ -334,6 +338,11 @@ void solve(Context& c, const ba_options* opt, ba_stats* stats) {
       st.n_lens_entries = c.last_nl;
       st.pcg_kernel = c.last_pcg_kernel;
       st.pcg_cluster = c.last_pcg_cluster;
+      st.graph = c.last_graph ? 1 : 0;
+      st.pcg_ctas = c.last_pcg_ctas;
+      st.pcg_tuned_us = c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].valid
+                            ? c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].us_per_iter
+                            : 0.0;
     }
   }
 }

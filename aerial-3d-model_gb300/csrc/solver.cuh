@@ -95,6 +95,8 @@ struct Control {
   int64_t* pcg_total;
   int32_t* any_active;
   double* sigma;      // per model
+  int32_t* small;     // consecutive accepted steps below the 1e-6 decrease
+  int32_t patience;   // stop after this many (1: the reference's rule)
   int32_t max_iter;
   // per-iteration log of model 0 (device arrays, log_cap entries)
   int32_t log_cap;

@@ -34,6 +34,9 @@ class Options:
     stream: int | None = None     # cudaStream_t as an integer handle
     profile: bool = False         # per-phase CUDA-event timing (SolveInfo.phases)
     pcg_kernel: str = "auto"      # "auto" | "grid" | "cluster" (mixed form)
+    graph: bool = True            # replay a CUDA graph per LM iteration
+    autotune: bool = False        # time PCG configurations on the first solve of a form
+    stop_patience: int = 0        # consecutive small accepted steps before stopping (0/1: ba.rs rule)
 
 
 @dataclass
@@ -60,6 +63,9 @@ class SolveInfo:
     sizes: dict = field(default_factory=dict, repr=False)   # reduced-system sizes
     pcg_kernel: str = "none"      # PCG kernel that ran: "grid" | "cluster"
     pcg_cluster: int = 0          # CTAs per cluster when the cluster kernel ran
+    graph: bool = False           # LM iterations replayed a CUDA graph
+    pcg_ctas: int = 0             # CTAs of the PCG launch
+    pcg_tuned_us: float = 0.0     # autotuned time per PCG iteration (0: not tuned)
 
     def stats(self) -> BaStats:
         return BaStats(self.iterations, self.initial_rms, self.final_rms)
@@ -83,6 +89,9 @@ def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> n
     c.stream = o.stream
     c.profile = 1 if o.profile else 0
     c.pcg_kernel = {"auto": 0, "grid": 1, "cluster": 2}[o.pcg_kernel]
+    c.no_graph = 0 if o.graph else 1
+    c.autotune = 1 if o.autotune else 0
+    c.stop_patience = int(o.stop_patience)
     c.log = C.cast(C.pointer(log), C.c_void_p) if log is not None else None
     return c
 
@@ -122,6 +131,9 @@ def _info(s: native.BaStatsC) -> SolveInfo:
                       schur_pairs=s.n_schur_pairs, lens_entries=s.n_lens_entries)
     info.pcg_kernel = {1: "grid", 2: "cluster"}.get(s.pcg_kernel, "none")
     info.pcg_cluster = s.pcg_cluster
+    info.graph = bool(s.graph)
+    info.pcg_ctas = s.pcg_ctas
+    info.pcg_tuned_us = s.pcg_tuned_us
     return info
 
 

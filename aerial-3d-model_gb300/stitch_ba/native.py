@@ -40,7 +40,8 @@ class BaOptions(C.Structure):
                 ("precision", C.c_int32), ("pcg_max_iter", C.c_int32), ("pcg_tol", C.c_double),
                 ("matrix_free", C.c_int32), ("memory_cap_bytes", C.c_int64),
                 ("stream", C.c_void_p), ("log", C.c_void_p), ("profile", C.c_int32),
-                ("pcg_kernel", C.c_int32)]
+                ("pcg_kernel", C.c_int32), ("no_graph", C.c_int32), ("autotune", C.c_int32),
+                ("stop_patience", C.c_int32)]
 
 
 class BaStatsC(C.Structure):
@@ -53,7 +54,8 @@ class BaStatsC(C.Structure):
                 ("ms_phase", C.c_double * 9), ("n_phase", C.c_int64 * 9),
                 ("n_blocks", C.c_int64), ("n_nonzero_blocks", C.c_int64),
                 ("n_schur_pairs", C.c_int64), ("n_lens_entries", C.c_int64),
-                ("pcg_kernel", C.c_int32), ("pcg_cluster", C.c_int32)]
+                ("pcg_kernel", C.c_int32), ("pcg_cluster", C.c_int32), ("graph", C.c_int32),
+                ("pcg_ctas", C.c_int32), ("pcg_tuned_us", C.c_double)]
 
 PHASES = ["point", "camera", "schur", "assemble", "pcg", "update", "cost", "control", "setup"]
 

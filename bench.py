@@ -43,6 +43,10 @@ METRIC = "BA solve time & kernel HBM GB/s, mixed vs FP64 GPU at equal final cost
 UNIT = "solves/s"
 SIGMA_PX = 1.0
 MAX_ITER = 60
+# The mixed form caps its FP32 PCG at this many iterations per LM step (the
+# FP64 form keeps the reference's 400): FP32 vectors cannot resolve the
+# system's weakest directions any further, and the LM outer loop refines.
+MIXED_PCG_ITERS = 200
 # Per LM iteration, algorithmic bytes of each phase, written as a function of
 # the problem sizes and the storage width s (8 FP64 / 4 FP32): reads and writes
 # each kernel must make at minimum.
@@ -132,16 +136,36 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def form_options(prec: str, **kw):
+    from stitch_ba import Options
+    if prec == "mixed":
+        return Options(precision="mixed", pcg_max_iter=MIXED_PCG_ITERS, **kw)
+    return Options(precision="fp64", **kw)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     return ws, rank
 
 
+# Batched workload: 64 independent lawnmower models of uneven size (cameras
+# ~U[20, 800], 500-1000 points per camera), solved together.
+BATCH_MODELS = 64
+
+
 def make_workload(name: str, seed: int):
+    """A list of problems: one for a single survey, BATCH_MODELS for batch64."""
     from stitch_ba import survey
+    if name == "batch64":
+        return [m[0] for m in survey.batched_models(BATCH_MODELS, seed=seed)]
     p, truth = survey.generate(name, seed=seed)
-    return p
+    return [p]
+
+
+def totals(ps):
+    return dict(n_cams=sum(q.n_cams for q in ps), n_points=sum(q.n_points for q in ps),
+                n_obs=sum(q.n_obs for q in ps))
 
 
 def pin_problem(p):
@@ -169,7 +193,9 @@ def gpu_arm(args, ws, rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     native.load()
-    p = make_workload(args.workload, args.seed + rank)
+    ps = make_workload(args.workload, args.seed + rank)
+    nmod = len(ps)
+    tot = totals(ps)
     stream = torch.cuda.current_stream()
     flush = torch.empty(int(256 * 2**20) // 4, dtype=torch.float32, device="cuda")
 
@@ -183,10 +209,11 @@ def gpu_arm(args, ws, rank):
     chosen = args.precision
     precisions = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
     profile_info = {}
+    infos_by_form = {}
     with stitch_ba.Context(device=dev, stream=stream.cuda_stream) as ctx:
-        ctx.upload(p)
+        ctx.upload(ps)
         for prec in precisions:
-            opts = Options(precision=prec)
+            opts = form_options(prec)
             for _ in range(args.warmup):
                 ctx.solve(args.max_iter, SIGMA_PX, opts)
             torch.cuda.synchronize()
@@ -199,7 +226,8 @@ def gpu_arm(args, ws, rank):
                     a = torch.cuda.Event(enable_timing=True)
                     b = torch.cuda.Event(enable_timing=True)
                     a.record(stream)
-                    info = ctx.solve(args.max_iter, SIGMA_PX, opts)[0]
+                    infos = ctx.solve(args.max_iter, SIGMA_PX, opts)
+                    info = infos[0]
                     b.record(stream)
                     b.synchronize()
                     times.append(a.elapsed_time(b))
@@ -210,33 +238,68 @@ def gpu_arm(args, ws, rank):
                 t = torch.tensor([ms], device="cuda")
                 dist.all_reduce(t, op=dist.ReduceOp.MAX)
                 ms = float(t.item())
-            forms[prec] = dict(ms_per_solve=ms, final_cost=info.final_cost,
-                               initial_cost=info.initial_cost, iterations=info.iterations,
-                               pcg_iterations=info.pcg_iterations, final_rms=info.final_rms,
+            forms[prec] = dict(ms_per_solve=ms, final_cost=sum(i.final_cost for i in infos),
+                               initial_cost=sum(i.initial_cost for i in infos),
+                               iterations=max(i.iterations for i in infos),
+                               pcg_iterations=sum(i.pcg_iterations for i in infos),
+                               final_rms=info.final_rms,
                                kernel_launches=info.kernel_launches, clocks=clk.summary())
-            # one profiled solve (phase timing; not part of the timed region)
-            prof = ctx.solve(args.max_iter, SIGMA_PX, Options(precision=prec, profile=True))[0]
+            forms[prec]["model_final_costs"] = [i.final_cost for i in infos] if nmod > 1 else None
+            forms[prec]["model_iterations"] = [i.iterations for i in infos] if nmod > 1 else None
+            # one profiled solve with the per-iteration log (phase timing; not
+            # part of the timed region)
+            prof = ctx.solve(args.max_iter, SIGMA_PX, form_options(prec, profile=True),
+                             log=(nmod == 1))[0]
             profile_info[prec] = prof
+            infos_by_form[prec] = infos
+            forms[prec]["pcg_kernel"] = prof.pcg_kernel
+            forms[prec]["pcg_max_iter"] = opts.pcg_max_iter
+            forms[prec]["graph"] = bool(info.graph)
     if "fp64" in forms and "mixed" in forms:
-        rel = abs(forms["mixed"]["final_cost"] - forms["fp64"]["final_cost"]) / abs(
-            forms["fp64"]["final_cost"])
-        forms["mixed"]["rel_final_cost_vs_fp64"] = rel
-        chosen = "mixed" if rel <= 1e-6 else "fp64"
+        # Equal final cost: the mixed solve reaches the FP64 solve's final cost
+        # to within 1e-6 relative (or ends below it).
+        f64, fm = forms["fp64"]["final_cost"], forms["mixed"]["final_cost"]
+        forms["mixed"]["rel_final_cost_vs_fp64"] = (fm - f64) / abs(f64)
+        reaches = fm <= f64 * (1.0 + 1e-6)
+        forms["mixed"]["reaches_fp64_final_cost"] = bool(reaches)
+        # First LM iteration whose accepted cost is within 1e-6 of the FP64
+        # final cost, and the share of the solve's time spent until then.
+        log = profile_info["mixed"]
+        hit = None
+        for i in range(int(log.iterations) if nmod == 1 else 0):
+            if log.accepted[i] and log.new_cost[i] <= f64 * (1.0 + 1e-6):
+                hit = i
+                break
+        if hit is not None:
+            forms["mixed"]["iteration_reaching_fp64_cost"] = hit + 1
+            forms["mixed"]["ms_to_fp64_cost_est"] = forms["mixed"]["ms_per_solve"] * (hit + 1) / max(
+                int(log.iterations), 1)
+        if nmod > 1:
+            a, b = forms["fp64"]["model_final_costs"], forms["mixed"]["model_final_costs"]
+            forms["mixed"]["models_reaching_fp64_cost"] = int(sum(
+                1 for x, y in zip(a, b) if y <= x * (1.0 + 1e-6)))
+        forms["mixed"]["speedup_vs_fp64"] = forms["fp64"]["ms_per_solve"] / forms["mixed"]["ms_per_solve"]
+        chosen = "mixed" if reaches else "fp64"
         forms["chosen"] = chosen
     head = forms[chosen]
 
     # End to end through the reference-facing C ABI (host buffers, H2D + D2H inside).
-    pp = pin_problem(p)
-    init = pp.state()
+    pps = [pin_problem(q) for q in ps]
+    inits = [q.state() for q in pps]
     e2e_times = []
     e2e_info = None
-    opts = Options(precision=chosen, stream=stream.cuda_stream)
+    opts = form_options(chosen, stream=stream.cuda_stream)
     for i in range(args.warmup + args.steps):
-        pp.set_state(init)
+        for q, st0 in zip(pps, inits):
+            q.set_state(st0)
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st, e2e_info = stitch_ba.bundle_adjust(pp, args.max_iter, SIGMA_PX, opts, return_info=True)
+        if nmod == 1:
+            st, e2e_info = stitch_ba.bundle_adjust(pps[0], args.max_iter, SIGMA_PX, opts,
+                                                   return_info=True)
+        else:
+            e2e_info = stitch_ba.bundle_adjust_batch(pps, args.max_iter, SIGMA_PX, opts)[0]
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
@@ -255,7 +318,7 @@ def gpu_arm(args, ws, rank):
     dom = max(phases, key=lambda k: phases[k][0])
     dom_ms, dom_n = phases[dom]
     zs = prof.sizes
-    sz = dict(n_obs=p.n_obs, n_points=p.n_points, n_cams=p.n_cams, nb=zs["blocks"],
+    sz = dict(n_obs=tot["n_obs"], n_points=tot["n_points"], n_cams=tot["n_cams"], nb=zs["blocks"],
               nz_blocks=zs["nonzero_blocks"], pairs=zs["schur_pairs"],
               subsegments=zs["schur_pairs"] // 512 + (zs["nonzero_blocks"] + zs["blocks"]) // 2)
     s = 8 if chosen == "fp64" else 4
@@ -275,7 +338,7 @@ def gpu_arm(args, ws, rank):
         except Exception:
             traffic = None
 
-    value = ws * 1000.0 / head["ms_per_solve"]
+    value = ws * nmod * 1000.0 / head["ms_per_solve"]
     out = {
         "metric": METRIC,
         "value": value,
@@ -289,13 +352,14 @@ def gpu_arm(args, ws, rank):
         "vs_baseline": None,
         "dtype": "f64" if chosen == "fp64" else "f32+f64",
         "data": "synthetic (seeded survey generator, reference camera model)",
-        "config": {"workload": args.workload, "cameras": p.n_cams, "points": p.n_points,
-                   "observations": p.n_obs, "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
+        "config": {"workload": args.workload, "models": nmod, "cameras": tot["n_cams"],
+                   "points": tot["n_points"], "observations": tot["n_obs"],
+                   "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
                    "loss": "cauchy", "precision": chosen, "parallelism": f"replicas{ws}",
                    "l2": "flushed between steps (256 MiB write)"},
         "forms": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} if isinstance(v, dict) else v
                   for k, v in forms.items()},
-        "e2e": {"value": ws / e2e_s, "unit": UNIT,
+        "e2e": {"value": ws * nmod / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": int(e2e_info.h2d_bytes),
                 "d2h_bytes_per_step": int(e2e_info.d2h_bytes),
                 "ms_per_step": e2e_s * 1000.0},
@@ -310,34 +374,45 @@ def gpu_arm(args, ws, rank):
         "gpu_launches": int(head["kernel_launches"]) * args.steps,
     }
     if not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(p, head["iterations"], args.cpu_sample_iters)
+        out["cpu_baseline"] = cpu_baseline(ps, [i.iterations for i in infos_by_form[chosen]],
+                                           args.cpu_sample_iters)
     return out
 
 
-def cpu_baseline(p, full_iters: int, sample_iters: int):
+def cpu_baseline(ps, full_iters, sample_iters: int):
     """Oracle (CPU restatement of the reference, OpenMP on all host cores) on
-    the first `sample_iters` LM iterations of the same solve."""
+    the first `sample_iters` LM iterations of one model (the largest), scaled
+    to the whole job by observations x LM iterations."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ba_oracle
     ba_oracle.build()
-    q = p.copy()
+    k = max(range(len(ps)), key=lambda i: ps[i].n_obs)
+    q = ps[k].copy()
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     r = ba_oracle.bundle_adjust(q, sample_iters, SIGMA_PX, n_threads=threads)
     dt = time.perf_counter() - t0
     per_iter = dt / max(r.iterations, 1)
-    est = per_iter * max(full_iters, 1)
-    return {"value": 1.0 / est, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {r.iterations} LM iterations of the same solve "
-                      f"({dt:.1f} s), scaled by the full solve's {full_iters} iterations",
+    work = sum(p.n_obs * max(it, 1) for p, it in zip(ps, full_iters))
+    est = per_iter * work / ps[k].n_obs
+    solves = len(ps)
+    what = "the survey" if solves == 1 else f"the largest of {solves} models"
+    return {"value": solves / est, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {r.iterations} LM iterations of {what} ({dt:.1f} s), scaled by "
+                      f"observations x the GPU solve's LM iterations ({max(full_iters)} max)",
             "s_per_lm_iteration": per_iter}
 
 
 def reference_arm(args, ws, rank):
-    """CPU reference solver (oracle port, all host cores), same workload and unit."""
+    """CPU reference solver (oracle port, all host cores), same workload and unit.
+    A step solves the first `cpu_sample_iters` LM iterations of the survey (of
+    the largest model for batch64), scaled to whole solves by the LM
+    iteration count of the full solve and, for batch64, by observations."""
     if rank != 0:
         return None
-    p = make_workload(args.workload, args.seed)
+    ps = make_workload(args.workload, args.seed)
+    tot = totals(ps)
+    k = max(range(len(ps)), key=lambda i: ps[i].n_obs)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ba_oracle
     ba_oracle.build()
@@ -345,7 +420,7 @@ def reference_arm(args, ws, rank):
     times = []
     iters = 0
     for i in range(args.warmup + args.steps):
-        q = p.copy()
+        q = ps[k].copy()
         t0 = time.perf_counter()
         r = ba_oracle.bundle_adjust(q, args.cpu_sample_iters, SIGMA_PX, n_threads=threads)
         dt = time.perf_counter() - t0
@@ -353,19 +428,22 @@ def reference_arm(args, ws, rank):
         if i >= args.warmup:
             times.append(dt / max(r.iterations, 1))
     per_iter = float(np.mean(times))
-    est = per_iter * args.full_iters
-    v = 1.0 / est
+    est = per_iter * args.full_iters * tot["n_obs"] / ps[k].n_obs
+    v = len(ps) / est
     return {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": est * 1000.0,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded survey generator, reference camera model)",
-        "config": {"workload": args.workload, "cameras": p.n_cams, "points": p.n_points,
-                   "observations": p.n_obs, "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
+        "config": {"workload": args.workload, "models": len(ps), "cameras": tot["n_cams"],
+                   "points": tot["n_points"], "observations": tot["n_obs"],
+                   "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
                    "loss": "cauchy", "precision": "fp64", "parallelism": "cpu"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"each step = first {iters} LM iterations of the solve, "
-                                   f"scaled by the full solve's {args.full_iters} iterations"},
+                         "sample": f"each step = first {iters} LM iterations of the "
+                                   f"{'survey' if len(ps) == 1 else 'largest model'}, scaled by "
+                                   f"{args.full_iters} LM iterations per solve"
+                                   + ("" if len(ps) == 1 else " and by observations")},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

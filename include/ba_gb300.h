@@ -107,9 +107,19 @@ typedef struct ba_options {
   void* stream;         /* cudaStream_t to run on, NULL: the library's own */
   ba_log* log;          /* NULL or per-iteration log (single-model calls)  */
   int32_t profile;      /* 1: time each kernel phase with CUDA events      */
-  int32_t pcg_kernel;   /* 0: auto, 1: grid-wide kernel, 2: one thread-block
-                           cluster per model (mixed form; falls back to the
-                           grid kernel when a model does not fit)          */
+  int32_t pcg_kernel;   /* 0: auto (mixed form: cluster kernel when every
+                           model fits, else grid), 1: grid-wide kernel,
+                           2: one thread-block cluster per model (mixed
+                           form; BA_NOT_SUPPORTED when a model does not fit) */
+  int32_t no_graph;     /* 1: launch each kernel directly instead of replaying
+                           a CUDA graph of the LM iteration                */
+  int32_t autotune;     /* 1: before the first solve of a form on a context,
+                           time the PCG configurations (grid rows per CTA,
+                           cluster sizes) on its first system and keep the
+                           fastest for this and later solves               */
+  int32_t stop_patience; /* LM stops after this many consecutive accepted
+                           steps with relative decrease < 1e-6; 0 or 1:
+                           the reference's rule (ba.rs:372-374)          */
 } ba_options;
 
 /* Kernel phases timed when ba_options.profile is set (ba_stats.ms_phase). */
@@ -147,6 +157,9 @@ typedef struct ba_stats {
   int64_t n_lens_entries; /* per-point lens entries                        */
   int32_t pcg_kernel;     /* PCG kernel that ran: 1 grid-wide, 2 cluster   */
   int32_t pcg_cluster;    /* CTAs per cluster (cluster kernel), else 0     */
+  int32_t graph;          /* 1 if the LM iterations replayed a CUDA graph  */
+  int32_t pcg_ctas;       /* CTAs of the PCG launch                        */
+  double pcg_tuned_us;    /* autotuner's time per PCG iteration (0: none)  */
 } ba_stats;
 
 /* Defaults: max_iter 60, sigma_px 1, Cauchy, FP64, PCG 400 / 1e-20. */
