@@ -61,6 +61,7 @@ struct Context {
   int32_t last_pcg_kernel = 0, last_pcg_cluster = 0, last_pcg_ctas = 0;
   PcgTuning tuning[2];  // [0] FP64 form, [1] mixed form
   bool last_graph = false;
+  bool last_matrix_free = false;
   double last_h2d_ms = 0, last_d2h_ms = 0;
   int64_t last_h2d_bytes = 0, last_d2h_bytes = 0;
 

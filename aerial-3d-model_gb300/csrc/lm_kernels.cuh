@@ -153,7 +153,11 @@ __device__ __forceinline__ void point_system(const Prob& P, const StateView& st,
       R* o = B.lin + (size_t)k * kLinW;
       if (!linearise<R>(P, st, k, sg, refine, o))
         for (int i = 0; i < kLinW; ++i) o[i] = (R)0;
+      for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = (R)0;
+      for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = (R)0;
     }
+    for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j)
+      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = (R)0;
     return;
   }
   // V, v and the Y / Z products accumulate in the storage precision R (FP32 in
@@ -359,6 +363,12 @@ __device__ __forceinline__ void point_system_mixed(const Prob& P, const StateVie
   }
   if (e - s < 2) {  // ba.rs:238
     B.kept[p] = 0;
+    for (uint32_t k = s; k < e; ++k) {
+      for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = 0.0f;
+      for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = 0.0f;
+    }
+    for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j)
+      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
     return;
   }
   double A[9], Ai[9];
@@ -778,12 +788,30 @@ static __global__ void commit_kernel(Prob P, const uint32_t* grp_model, StateVie
 
 // ---- Schur sums: warp per sub-segment of one destination block ---------------
 
+// An observation's Z (18 values) with vector loads: 144-byte records are
+// 16-byte aligned (FP64: 9 x 16 B), 72-byte records 8-byte aligned (FP32:
+// 9 x 8 B).
+__device__ __forceinline__ void load_Z18(const double* s, double* z) {
+  const double2* v = reinterpret_cast<const double2*>(s);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const double2 t = __ldg(v + i);
+    z[2 * i] = t.x, z[2 * i + 1] = t.y;
+  }
+}
+__device__ __forceinline__ void load_Z18(const float* s, float* z) {
+  const float2* v = reinterpret_cast<const float2*>(s);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const float2 t = __ldg(v + i);
+    z[2 * i] = t.x, z[2 * i + 1] = t.y;
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ void load_Z(const IterBufs<R>& B, int64_t no, uint32_t eid, R* z) {
   if ((int64_t)eid < no) {
-    const R* s = B.Z + (size_t)eid * 18;
-#pragma unroll
-    for (int i = 0; i < 18; ++i) z[i] = s[i];
+    load_Z18(B.Z + (size_t)eid * 18, z);
   } else {
     const R* s = B.Zl + (size_t)(eid - no) * 9;
 #pragma unroll
@@ -819,12 +847,38 @@ __global__ void __launch_bounds__(256)
         acc[6 * r + c] += za[3 * r] * zb[3 * c] + za[3 * r + 1] * zb[3 * c + 1] +
                           za[3 * r + 2] * zb[3 * c + 2];
   }
+  // Warp sum of the 36 entries, halving twice (36 -> 18 -> 9 values per lane)
+  // before a butterfly on the last 9: 54 adds per lane instead of 180 (the
+  // adds are FP64 warp instructions in the plain form).  Lanes 0, 8, 16, 24
+  // then hold entries 0-8, 9-17, 18-26, 27-35.
+  R a[18];
+  {
+    const bool up = lane & 16;
 #pragma unroll
-  for (int i = 0; i < 36; ++i) acc[i] = warp_sum(acc[i]);
-  if (lane == 0) {
-    double* o = B.part + (size_t)sub * 36;
+    for (int i = 0; i < 18; ++i) {
+      const R recv = __shfl_xor_sync(kFull, up ? acc[i] : acc[18 + i], 16);
+      a[i] = (up ? acc[18 + i] : acc[i]) + recv;
+    }
+  }
+  R v[9];
+  {
+    const bool up = lane & 8;
 #pragma unroll
-    for (int i = 0; i < 36; ++i) o[i] = (double)acc[i];
+    for (int i = 0; i < 9; ++i) {
+      const R recv = __shfl_xor_sync(kFull, up ? a[i] : a[9 + i], 8);
+      v[i] = (up ? a[9 + i] : a[i]) + recv;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    v[i] += __shfl_xor_sync(kFull, v[i], 4);
+    v[i] += __shfl_xor_sync(kFull, v[i], 2);
+    v[i] += __shfl_xor_sync(kFull, v[i], 1);
+  }
+  if ((lane & 7) == 0) {
+    double* o = B.part + (size_t)sub * 36 + ((lane & 16) ? 18 : 0) + ((lane & 8) ? 9 : 0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) o[i] = (double)v[i];
   }
 }
 

@@ -147,9 +147,10 @@ __device__ __forceinline__ double sum8(double v) {
 // the launch's base value.  Only warp 0 of a CTA takes part; the partials are
 // then read with all loads in flight at once.  Bounded: after kSpinCycles the
 // waiter sets ERR_BARRIER_TIMEOUT; every CTA leaves at its next exchange.
-template <int N, typename R, typename Post>
+// Args: any type with part, ncta, bar and err as in PcgArgs.
+template <int N, typename Args, typename Post>
 __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm, double* tot,
-                                             const PcgArgs<R>& A, const PcgJob& J, int slot,
+                                             const Args& A, const PcgJob& J, int slot,
                                              unsigned long long& target, Post&& post) {
   __shared__ int ok_s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

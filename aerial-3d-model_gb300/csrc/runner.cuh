@@ -9,6 +9,7 @@
 #include "context.cuh"
 #include "pcg.cuh"
 #include "pcg_cluster.cuh"
+#include "pcg_implicit.cuh"
 #include "structure.cuh"
 
 namespace ba {
@@ -305,6 +306,11 @@ struct LmEngine {
   int pcg_rows_target = 0, grid_rows_target = 0, max_ctas = 0;
   std::vector<int32_t> h_lens;
   PcgArgs<R> pa{};
+  // Matrix-free PCG.
+  bool implicit = false;
+  DevBuf<R> own, tbuf, rbuf, qbuf;
+  ImpArgs<R> ia{};
+  int32_t imp_ncta = 0;
   // Cluster-resident PCG (mixed form).
   bool use_cluster = false;
   int cl_size = 0;
@@ -325,7 +331,19 @@ struct LmEngine {
     const int64_t nc = ctx.nc, np = ctx.np, no = ctx.no, ng = ctx.ng, nb = ctx.nb, nm = ctx.nm;
     reset_states(ctx);
     P = ctx.prob(o.loss);
-    build_structure(P, ctx.h_obs0, SB, ctx.err, s);
+    // Matrix-free PCG (no pair list, no reduced matrix): when asked for, or in
+    // auto mode when the explicit layout would exceed the memory cap.  One
+    // model with at most one lens group.
+    const bool mf_ok = nm == 1 && ng <= 1;
+    if (o.matrix_free == 2 && !mf_ok)
+      throw CudaError(cudaErrorNotSupported,
+                      "matrix-free PCG: one model with at most one lens group per call");
+    const int64_t cap = o.matrix_free == 2 ? 0
+                        : (o.matrix_free == 0 && mf_ok && o.memory_cap > 0) ? o.memory_cap
+                                                                            : -1;
+    build_structure(P, ctx.h_obs0, SB, ctx.err, s, cap);
+    implicit = SB.implicit;
+    ctx.last_matrix_free = implicit;
     SV = SB.view();
     ctx.last_nz = SB.nz, ctx.last_pairs = SB.npairs - nb, ctx.last_nl = SB.nl;
     lin.alloc(at_least_1(no) * kLinW, s), gsub.alloc(at_least_1(no) * 9, s);
@@ -337,6 +355,10 @@ struct LmEngine {
     caml.alloc(at_least_1(nc) * 12, s), grpU.alloc(at_least_1(ng) * 6, s);
     grpg.alloc(at_least_1(ng) * 3, s);
     part.alloc(at_least_1(SB.nsub) * 36, s), S.alloc(at_least_1(SB.nz) * 36, s);
+    if (implicit) {
+      own.alloc(at_least_1(nb) * 36, s), tbuf.alloc(at_least_1(np) * 3, s);
+      rbuf.alloc(at_least_1(nb) * 6, s), qbuf.alloc(at_least_1(nb) * 6, s);
+    }
     pre.alloc(at_least_1(nb) * 36, s);
     g.alloc(at_least_1(nb) * 6, s), x.alloc(at_least_1(nb) * 6, s);
     z.alloc(at_least_1(nb) * 6, s), p.alloc(at_least_1(nb) * 12, s);
@@ -392,11 +414,15 @@ struct LmEngine {
         h_lens[m] = (int32_t)(ctx.h_blk0[m] + (ctx.h_cam0[m + 1] - ctx.h_cam0[m]));
     detail::h2d(lens_row, h_lens, s);
     lens_pos.alloc(detail::at_least_1(nb), s);
+    bar.alloc(nm, s);
+    bar_base.alloc(nm, s);
+    if (implicit) {
+      setup_implicit();
+      return;
+    }
     if (nb > 0)
       BA_LAUNCH(lens_pos_kernel<<<grid_for(nb, 256), 256, 0, s>>>(nb, SB.row_ptr, SB.col_idx,
                                                                  P.blk_model, lens_row, lens_pos));
-    bar.alloc(nm, s);
-    bar_base.alloc(nm, s);
     if (sizeof(R) == 8 && o.pcg_kernel == 2)
       throw CudaError(cudaErrorNotSupported, "cluster PCG: the FP64 form uses the grid kernel");
     // Configuration: an earlier tuning of this context for this form, or the
@@ -412,6 +438,23 @@ struct LmEngine {
     } else {
       plan_grid(pcg_rows_target > 0 ? pcg_rows_target : (sizeof(R) == 8 ? 4 : 8));
     }
+  }
+
+  // Matrix-free PCG: one cooperative launch over every SM, one group.
+  void setup_implicit() {
+    use_cluster = false;
+    int occ = 0;
+    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_implicit_kernel<R>, kPcgThreads,
+                                                        0),
+          "occupancy");
+    imp_ncta = std::min(std::max(1, occ) * ctx.n_sm, kMaxGroupCtas);
+    bar.zero();
+    bar_base.zero();
+    pcg_part.alloc(kParts * (size_t)imp_ncta, s);
+    ia = ImpArgs<R>{bar, bar_base, pcg_part, imp_ncta, ctx.err, P, SV, Z, Zl, kept, own, camX,
+                    pre, g, x, rbuf, z, p, qbuf, tbuf, h_lens[0], (int32_t)ctx.nb, pcg_iters,
+                    o.pcg_max_iter, o.pcg_tol};
+    ctx.last_pcg_kernel = 3, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = imp_ncta;
   }
 
   // Grid kernel plan: about rows_target block rows per CTA.
@@ -509,6 +552,7 @@ struct LmEngine {
   // system of the first iteration and keep the fastest per iteration.  The
   // choice is stored in the context and reused by later solves of this form.
   void autotune() {
+    if (implicit) return;
     constexpr int kTuneIters = 40;
     const bool timing = T.on;
     T.on = false;  // tuning time is not a solve phase
@@ -593,6 +637,14 @@ struct LmEngine {
     BA_LAUNCH(group_kernel<<<grid_for(ctx.ng * 32, 128), 128, 0, s>>>(P, SV, caml, grpU, grpg,
                                                                      active));
     T.mark(BA_PHASE_CAMERA);
+    if (implicit) {
+      T.mark(BA_PHASE_SCHUR);
+      BA_LAUNCH(implicit_blocks_kernel<R><<<(unsigned)ctx.nb, 256, 0, s>>>(P, cur, SV, B, Z, own,
+                                                                          active, lambda));
+      BA_LAUNCH(rhs_kernel<R><<<grid_for(ctx.nb * 6, 256), 256, 0, s>>>(P, cur, B, active));
+      T.mark(BA_PHASE_ASSEMBLE);
+      return;
+    }
     if (SB.nsub > 0)
       BA_LAUNCH(schur_kernel<R><<<grid_for(SB.nsub * 32, 256), 256, 0, s>>>(P, SV, B, active));
     T.mark(BA_PHASE_SCHUR);
@@ -606,7 +658,12 @@ struct LmEngine {
 
   // Block-Jacobi PCG (ba.rs:155-196).
   void solve_pcg() {
-    if (use_cluster) {
+    if (implicit) {
+      void* args[] = {&ia};
+      check(cudaLaunchCooperativeKernel((void*)pcg_implicit_kernel<R>, dim3(imp_ncta),
+                                        dim3(kPcgThreads), args, 0, s),
+            "pcg launch");
+    } else if (use_cluster) {
       cudaLaunchConfig_t cfg{};
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;

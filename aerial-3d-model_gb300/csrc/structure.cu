@@ -370,7 +370,7 @@ void build_cam_index(const Prob& P, StructBufs& S, cudaStream_t s) {
 }
 
 void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, StructBufs& S,
-                     uint32_t* err, cudaStream_t s) {
+                     uint32_t* err, cudaStream_t s, int64_t pair_bytes_cap) {
   const int64_t nc = P.nc, np = P.np, no = P.no, ng = P.ng, nb = P.nb, nm = P.nm;
 
   // Point ranges (obs are sorted by point).
@@ -395,14 +395,19 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
   // Schur pair list, sorted by destination block.
   DevBuf<uint64_t> keys;
   int64_t npairs = 0;
-  {
-    DevBuf<uint32_t> cnt(np + 1, s), off(np + 1, s);
-    cnt.zero();
-    if (np > 0)
-      BA_LAUNCH(pair_count_kernel<<<grid_for(np, T), T, 0, s>>>(P, S.pt_ptr, S.lens_ptr,
-                                                              S.lens_grp, cnt));
-    const uint64_t npt = exclusive_scan_u32(cnt, off, np + 1, s);
-    const uint64_t total = npt + (uint64_t)nb;
+  S.implicit = false;
+  DevBuf<uint32_t> cnt(np + 1, s), off(np + 1, s);
+  cnt.zero();
+  if (np > 0)
+    BA_LAUNCH(pair_count_kernel<<<grid_for(np, T), T, 0, s>>>(P, S.pt_ptr, S.lens_ptr,
+                                                            S.lens_grp, cnt));
+  const uint64_t npt = exclusive_scan_u32(cnt, off, np + 1, s);
+  const uint64_t total = npt + (uint64_t)nb;
+  // Matrix-free calls (cap 0), or a pair list (with its sort buffers and the
+  // Schur partial sums) above the memory cap: no pair list, no S.
+  if (pair_bytes_cap == 0 || (pair_bytes_cap > 0 && (int64_t)total * 40 > pair_bytes_cap))
+    S.implicit = true;
+  if (!S.implicit) {
     if (total >= 0xffffffffULL)
       throw std::runtime_error("too many Schur pair contributions for one call");
     npairs = (int64_t)total;
@@ -415,68 +420,76 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
     DevBuf<uint64_t> kt(npairs, s), vt(npairs, s);
     radix_sort_u64_u64(keys, S.pairs, kt, vt, npairs, bits_for((uint64_t)nb * nb - 1), s);
   }
+  cnt.release();
+  off.release();
   S.npairs = npairs;
-  // Slots = distinct destination blocks (upper triangle incl. diagonal).
-  DevBuf<uint64_t> slot_key;
-  {
-    DevBuf<uint32_t> head(npairs, s), sid(npairs, s);
-    BA_LAUNCH(head_flags_kernel<<<grid_for(npairs, T), T, 0, s>>>(keys, npairs, head));
-    S.ns = (int64_t)exclusive_scan_u32(head, sid, npairs, s);
-    S.slot_ptr.alloc(S.ns + 1, s);
-    slot_key.alloc(S.ns, s);
-    BA_LAUNCH(slot_fill_kernel<<<grid_for(npairs, T), T, 0, s>>>(keys, npairs, head, sid, nb,
-                                                               S.slot_ptr, slot_key));
-    const uint32_t np32 = (uint32_t)npairs;
-    check(cudaMemcpyAsync(S.slot_ptr.p + S.ns, &np32, 4, cudaMemcpyHostToDevice, s), "slot");
-  }
-  keys.release();
-  const int64_t ns = S.ns;
-  // Full symmetric BSR.
-  S.slot_row.alloc(ns, s);
-  S.slot_col.alloc(ns, s);
-  S.slot_pos_ab.alloc(ns, s);
-  S.slot_pos_ba.alloc(ns, s);
-  S.diag_pos.alloc(nb, s);
-  {
-    DevBuf<uint32_t> offd(ns + 1, s), toff(ns + 1, s);
-    BA_LAUNCH(slot_rowcol_kernel<<<grid_for(ns, T), T, 0, s>>>(slot_key, ns, nb, S.slot_row,
-                                                             S.slot_col, offd));
-    check(cudaMemsetAsync(offd.p + ns, 0, 4, s), "memset");
-    const int64_t nt = (int64_t)exclusive_scan_u32(offd, toff, ns + 1, s);
-    DevBuf<uint64_t> tk(std::max<int64_t>(nt, 1), s), tkt(std::max<int64_t>(nt, 1), s);
-    DevBuf<uint32_t> tv(std::max<int64_t>(nt, 1), s), tvt(std::max<int64_t>(nt, 1), s);
-    BA_LAUNCH(transpose_keys_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_row, S.slot_col, offd,
-                                                                toff, ns, nb, tk, tv));
-    if (nt > 1) radix_sort_u64_u32(tk, tv, tkt, tvt, nt, bits_for((uint64_t)nb * nb - 1), s);
-    DevBuf<uint32_t> up_first(nb + 1, s), lo_first(nb + 1, s), cnt(nb + 1, s);
-    lower_bounds_u64(slot_key, ns, up_first, nb, (uint64_t)nb, s);
-    lower_bounds_u64(tk, nt, lo_first, nb, (uint64_t)nb, s);
-    BA_LAUNCH(row_count_kernel<<<grid_for(nb, T), T, 0, s>>>(up_first, lo_first, nb, cnt));
-    check(cudaMemsetAsync(cnt.p + nb, 0, 4, s), "memset");
-    S.row_ptr.alloc(nb + 1, s);
-    S.nz = (int64_t)exclusive_scan_u32(cnt, S.row_ptr, nb + 1, s);
-    S.col_idx.alloc(S.nz, s);
-    BA_LAUNCH(place_upper_kernel<<<grid_for(ns, T), T, 0, s>>>(
-        S.slot_row, S.slot_col, ns, S.row_ptr, up_first, lo_first, S.col_idx, S.slot_pos_ab,
-        S.slot_pos_ba, S.diag_pos, nb, S.nz, err));
-    if (nt > 0)
-      BA_LAUNCH(place_lower_kernel<<<grid_for(nt, T), T, 0, s>>>(tk, tv, nt, nb, S.row_ptr,
-                                                               lo_first, S.col_idx,
-                                                               S.slot_pos_ba, ns, S.nz, err));
-  }
-  slot_key.release();
-  // Warp sub-segments of the Schur sums.
-  {
-    DevBuf<uint32_t> cnt(ns + 1, s);
-    BA_LAUNCH(sub_count_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, ns, cnt));
-    check(cudaMemsetAsync(cnt.p + ns, 0, 4, s), "memset");
-    S.slot_sub_ptr.alloc(ns + 1, s);
-    S.nsub = (int64_t)exclusive_scan_u32(cnt, S.slot_sub_ptr, ns + 1, s);
-    S.sub_slot.alloc(S.nsub, s);
-    S.sub_begin.alloc(S.nsub, s);
-    S.sub_end.alloc(S.nsub, s);
-    BA_LAUNCH(sub_fill_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, S.slot_sub_ptr, ns,
-                                                          S.sub_slot, S.sub_begin, S.sub_end));
+  if (!S.implicit) {
+    // Slots = distinct destination blocks (upper triangle incl. diagonal).
+    DevBuf<uint64_t> slot_key;
+    {
+      DevBuf<uint32_t> head(npairs, s), sid(npairs, s);
+      BA_LAUNCH(head_flags_kernel<<<grid_for(npairs, T), T, 0, s>>>(keys, npairs, head));
+      S.ns = (int64_t)exclusive_scan_u32(head, sid, npairs, s);
+      S.slot_ptr.alloc(S.ns + 1, s);
+      slot_key.alloc(S.ns, s);
+      BA_LAUNCH(slot_fill_kernel<<<grid_for(npairs, T), T, 0, s>>>(keys, npairs, head, sid, nb,
+                                                                 S.slot_ptr, slot_key));
+      const uint32_t np32 = (uint32_t)npairs;
+      check(cudaMemcpyAsync(S.slot_ptr.p + S.ns, &np32, 4, cudaMemcpyHostToDevice, s), "slot");
+    }
+    keys.release();
+    const int64_t ns = S.ns;
+    // Full symmetric BSR.
+    S.slot_row.alloc(ns, s);
+    S.slot_col.alloc(ns, s);
+    S.slot_pos_ab.alloc(ns, s);
+    S.slot_pos_ba.alloc(ns, s);
+    S.diag_pos.alloc(nb, s);
+    {
+      DevBuf<uint32_t> offd(ns + 1, s), toff(ns + 1, s);
+      BA_LAUNCH(slot_rowcol_kernel<<<grid_for(ns, T), T, 0, s>>>(slot_key, ns, nb, S.slot_row,
+                                                               S.slot_col, offd));
+      check(cudaMemsetAsync(offd.p + ns, 0, 4, s), "memset");
+      const int64_t nt = (int64_t)exclusive_scan_u32(offd, toff, ns + 1, s);
+      DevBuf<uint64_t> tk(std::max<int64_t>(nt, 1), s), tkt(std::max<int64_t>(nt, 1), s);
+      DevBuf<uint32_t> tv(std::max<int64_t>(nt, 1), s), tvt(std::max<int64_t>(nt, 1), s);
+      BA_LAUNCH(transpose_keys_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_row, S.slot_col, offd,
+                                                                  toff, ns, nb, tk, tv));
+      if (nt > 1) radix_sort_u64_u32(tk, tv, tkt, tvt, nt, bits_for((uint64_t)nb * nb - 1), s);
+      DevBuf<uint32_t> up_first(nb + 1, s), lo_first(nb + 1, s), cnt(nb + 1, s);
+      lower_bounds_u64(slot_key, ns, up_first, nb, (uint64_t)nb, s);
+      lower_bounds_u64(tk, nt, lo_first, nb, (uint64_t)nb, s);
+      BA_LAUNCH(row_count_kernel<<<grid_for(nb, T), T, 0, s>>>(up_first, lo_first, nb, cnt));
+      check(cudaMemsetAsync(cnt.p + nb, 0, 4, s), "memset");
+      S.row_ptr.alloc(nb + 1, s);
+      S.nz = (int64_t)exclusive_scan_u32(cnt, S.row_ptr, nb + 1, s);
+      S.col_idx.alloc(S.nz, s);
+      BA_LAUNCH(place_upper_kernel<<<grid_for(ns, T), T, 0, s>>>(
+          S.slot_row, S.slot_col, ns, S.row_ptr, up_first, lo_first, S.col_idx, S.slot_pos_ab,
+          S.slot_pos_ba, S.diag_pos, nb, S.nz, err));
+      if (nt > 0)
+        BA_LAUNCH(place_lower_kernel<<<grid_for(nt, T), T, 0, s>>>(tk, tv, nt, nb, S.row_ptr,
+                                                                 lo_first, S.col_idx,
+                                                                 S.slot_pos_ba, ns, S.nz, err));
+    }
+    slot_key.release();
+    // Warp sub-segments of the Schur sums.
+    {
+      DevBuf<uint32_t> cnt(ns + 1, s);
+      BA_LAUNCH(sub_count_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, ns, cnt));
+      check(cudaMemsetAsync(cnt.p + ns, 0, 4, s), "memset");
+      S.slot_sub_ptr.alloc(ns + 1, s);
+      S.nsub = (int64_t)exclusive_scan_u32(cnt, S.slot_sub_ptr, ns + 1, s);
+      S.sub_slot.alloc(S.nsub, s);
+      S.sub_begin.alloc(S.nsub, s);
+      S.sub_end.alloc(S.nsub, s);
+      BA_LAUNCH(sub_fill_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, S.slot_sub_ptr, ns,
+                                                            S.sub_slot, S.sub_begin, S.sub_end));
+    }
+
+  } else {
+    S.ns = S.nsub = S.nz = 0;
+    S.diag_pos.alloc(1, s);
   }
   // Cost-reduction chunks, aligned to model boundaries (host-side plan).
   {
@@ -506,9 +519,10 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
     // The host vectors must outlive the copies.
     check(cudaStreamSynchronize(s), "sync");
   }
-  S.h_row_ptr.resize(nb + 1);
-  check(cudaMemcpyAsync(S.h_row_ptr.data(), S.row_ptr, 4 * (nb + 1), cudaMemcpyDeviceToHost, s),
-        "d2h");
+  S.h_row_ptr.assign(nb + 1, 0);
+  if (!S.implicit)
+    check(cudaMemcpyAsync(S.h_row_ptr.data(), S.row_ptr, 4 * (nb + 1), cudaMemcpyDeviceToHost, s),
+          "d2h");
   uint32_t e = 0;
   check(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s), "d2h");
   check(cudaStreamSynchronize(s), "sync");

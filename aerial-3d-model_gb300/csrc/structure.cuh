@@ -15,6 +15,7 @@ struct StructBufs {
   DevBuf<uint32_t> row_ptr, col_idx, diag_pos;
   DevBuf<uint32_t> cost_chunk_model, cost_chunk_begin, cost_chunk_end, model_chunk0;
   int64_t nl = 0, npairs = 0, ns = 0, nsub = 0, nz = 0, ncost = 0;
+  bool implicit = false;  // no pair list / reduced matrix (matrix-free PCG)
   std::vector<uint32_t> h_row_ptr;
   StructView view() const;
 };
@@ -24,7 +25,10 @@ void validate_problem(const Prob& P, const uint32_t* grp_model, uint32_t* d_err,
 // Observations by camera (cam_ptr, cam_obs) and cameras by group (grp_ptr,
 // grp_cams), both stable.
 void build_cam_index(const Prob& P, StructBufs& S, cudaStream_t s);
+// pair_bytes_cap: < 0 always build the Schur pair list and the reduced
+// matrix layout; 0 never (matrix-free); > 0 only if they fit in that many
+// bytes.
 void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, StructBufs& S,
-                     uint32_t* err, cudaStream_t s);
+                     uint32_t* err, cudaStream_t s, int64_t pair_bytes_cap = -1);
 
 }  // namespace ba

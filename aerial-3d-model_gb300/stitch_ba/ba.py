@@ -61,7 +61,7 @@ class SolveInfo:
     accepted: np.ndarray = field(default=None, repr=False)
     phases: dict = field(default_factory=dict, repr=False)  # name -> (ms, launches)
     sizes: dict = field(default_factory=dict, repr=False)   # reduced-system sizes
-    pcg_kernel: str = "none"      # PCG kernel that ran: "grid" | "cluster"
+    pcg_kernel: str = "none"      # PCG kernel that ran: "grid" | "cluster" | "matrix_free"
     pcg_cluster: int = 0          # CTAs per cluster when the cluster kernel ran
     graph: bool = False           # LM iterations replayed a CUDA graph
     pcg_ctas: int = 0             # CTAs of the PCG launch
@@ -129,7 +129,7 @@ def _info(s: native.BaStatsC) -> SolveInfo:
                    if s.n_phase[i]}
     info.sizes = dict(blocks=s.n_blocks, nonzero_blocks=s.n_nonzero_blocks,
                       schur_pairs=s.n_schur_pairs, lens_entries=s.n_lens_entries)
-    info.pcg_kernel = {1: "grid", 2: "cluster"}.get(s.pcg_kernel, "none")
+    info.pcg_kernel = {1: "grid", 2: "cluster", 3: "matrix_free"}.get(s.pcg_kernel, "none")
     info.pcg_cluster = s.pcg_cluster
     info.graph = bool(s.graph)
     info.pcg_ctas = s.pcg_ctas

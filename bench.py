@@ -136,11 +136,31 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+MIXED_MATRIX_FREE = False  # --matrix-free: the mixed form applies S without forming it
+
+
 def form_options(prec: str, **kw):
     from stitch_ba import Options
     if prec == "mixed":
-        return Options(precision="mixed", pcg_max_iter=MIXED_PCG_ITERS, **kw)
+        mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
+        return Options(precision="mixed", pcg_max_iter=MIXED_PCG_ITERS, matrix_free=mf, **kw)
     return Options(precision="fp64", **kw)
+
+
+def max_over_ranks(x: float, ws: int, device: str = "cuda") -> float:
+    """Timing of the slowest rank (replicas: every rank solves its own models)."""
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_seed(seed: int, rank: int) -> int:
+    """Each replica solves its own survey (weak scaling: fixed work per GPU)."""
+    return seed + rank
 
 
 def dist_env():
@@ -193,7 +213,7 @@ def gpu_arm(args, ws, rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     native.load()
-    ps = make_workload(args.workload, args.seed + rank)
+    ps = make_workload(args.workload, rank_seed(args.seed, rank))
     nmod = len(ps)
     tot = totals(ps)
     stream = torch.cuda.current_stream()
@@ -232,12 +252,7 @@ def gpu_arm(args, ws, rank):
                     b.synchronize()
                     times.append(a.elapsed_time(b))
                 barrier()
-            ms = float(np.sum(times)) / len(times)
-            if ws > 1:
-                import torch.distributed as dist
-                t = torch.tensor([ms], device="cuda")
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-                ms = float(t.item())
+            ms = max_over_ranks(float(np.sum(times)) / len(times), ws)
             forms[prec] = dict(ms_per_solve=ms, final_cost=sum(i.final_cost for i in infos),
                                initial_cost=sum(i.initial_cost for i in infos),
                                iterations=max(i.iterations for i in infos),
@@ -253,6 +268,7 @@ def gpu_arm(args, ws, rank):
             profile_info[prec] = prof
             infos_by_form[prec] = infos
             forms[prec]["pcg_kernel"] = prof.pcg_kernel
+            forms[prec]["device_bytes"] = int(prof.device_bytes)
             forms[prec]["pcg_max_iter"] = opts.pcg_max_iter
             forms[prec]["graph"] = bool(info.graph)
     if "fp64" in forms and "mixed" in forms:
@@ -303,12 +319,7 @@ def gpu_arm(args, ws, rank):
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_s = float(np.mean(e2e_times))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(float(np.mean(e2e_times)), ws)
 
     if rank != 0:
         return None
@@ -461,7 +472,11 @@ def main():
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
     ap.add_argument("--full-iters", type=int, default=int(os.environ.get("BA_FULL_ITERS", "0")) or None)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--matrix-free", action="store_true",
+                    help="mixed form: matrix-free PCG (S p from per-observation factors)")
     args = ap.parse_args()
+    global MIXED_MATRIX_FREE
+    MIXED_MATRIX_FREE = args.matrix_free
     ws, rank = dist_env()
     if args.impl == "reference":
         if args.full_iters is None:

@@ -102,8 +102,11 @@ typedef struct ba_options {
   int32_t precision;    /* ba_precision, default BA_PRECISION_FP64         */
   int32_t pcg_max_iter; /* <=0: 400 (ba.rs:334)                            */
   double pcg_tol;       /* <=0: 1e-20, on |r|^2 / |b|^2 (ba.rs:182)        */
-  int32_t matrix_free;  /* 0: auto (by memory cap), 1: stored S, 2: matrix-free */
-  int64_t memory_cap_bytes; /* auto mode: go matrix-free above this (<=0: no cap) */
+  int32_t matrix_free;  /* 0: auto (by memory cap), 1: stored S, 2: matrix-free
+                           (S p applied from the per-observation Schur factors;
+                           one model with at most one lens group)          */
+  int64_t memory_cap_bytes; /* auto mode: go matrix-free when the Schur pair list
+                           and reduced matrix would exceed this (<=0: no cap) */
   void* stream;         /* cudaStream_t to run on, NULL: the library's own */
   ba_log* log;          /* NULL or per-iteration log (single-model calls)  */
   int32_t profile;      /* 1: time each kernel phase with CUDA events      */
@@ -155,7 +158,8 @@ typedef struct ba_stats {
   int64_t n_nonzero_blocks;  /* 6x6 blocks of the symmetric matrix (full)  */
   int64_t n_schur_pairs;  /* point-entry pairs summed into upper blocks    */
   int64_t n_lens_entries; /* per-point lens entries                        */
-  int32_t pcg_kernel;     /* PCG kernel that ran: 1 grid-wide, 2 cluster   */
+  int32_t pcg_kernel;     /* PCG kernel that ran: 1 grid-wide, 2 cluster,
+                             3 matrix-free (reduced matrix not formed)     */
   int32_t pcg_cluster;    /* CTAs per cluster (cluster kernel), else 0     */
   int32_t graph;          /* 1 if the LM iterations replayed a CUDA graph  */
   int32_t pcg_ctas;       /* CTAs of the PCG launch                        */

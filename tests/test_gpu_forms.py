@@ -95,3 +95,36 @@ def test_autotuner_picks_a_configuration_and_keeps_the_result(precision):
     assert again.final_cost == tuned.final_cost
     # a different PCG layout only reorders FP64 sums
     assert abs(tuned.final_cost - base.final_cost) <= 1e-6 * base.final_cost
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_matrix_free_pcg_matches_stored_reduced_matrix(precision):
+    """S p applied from the per-observation Schur factors, without forming
+    S: the same LM system gives the same step as the stored-matrix path."""
+    p, _ = survey.generate("lawnmower77", seed=4, n_cams=30, n_points=6000)
+    with stitch_ba.Context() as ctx:
+        ctx.upload(p)
+        a = ctx.debug_step(1e-4, 1.0, Options(precision=precision, matrix_free="stored"),
+                           dense=False)
+        b = ctx.debug_step(1e-4, 1.0, Options(precision=precision, matrix_free="matrix_free"),
+                           dense=False)
+    assert np.linalg.norm(a["g"] - b["g"]) <= 1e-12 * np.linalg.norm(a["g"])
+    rel = np.linalg.norm(a["dx"] - b["dx"]) / np.linalg.norm(a["dx"])
+    if precision == "fp64":
+        assert abs(a["pcg_iters"] - b["pcg_iters"]) <= 3
+        assert rel < 1e-8, rel
+    else:
+        # FP32 products round differently in the two forms of S p, which moves
+        # the |r|^2 < 1e-20 |b|^2 crossing; the steps agree to FP32 accuracy
+        assert rel < 1e-2, rel
+    tol = 1e-6 if precision == "fp64" else 1e-4
+    assert abs(a["trial_cost"] - b["trial_cost"]) <= tol * a["trial_cost"]
+
+
+def test_memory_cap_switches_to_matrix_free():
+    p, _ = survey.generate("lawnmower77", seed=4, n_cams=30, n_points=6000)
+    q, st, info = solve(p, Options(memory_cap_bytes=1), sigma=1.0)
+    assert info.pcg_kernel == "matrix_free"
+    _, st2, info2 = solve(p, Options(), sigma=1.0)
+    assert info2.pcg_kernel == "grid"
+    assert abs(info.final_cost - info2.final_cost) <= 1e-6 * info2.final_cost
