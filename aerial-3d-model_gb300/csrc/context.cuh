@@ -120,6 +120,9 @@ void debug_lm_step(Context& ctx, const Opts& o, double lam, double* S_dense, dou
 
 void reset_states(Context& ctx);
 
+// Copy problems and initial states (host or device arrays) into the context.
+void upload(Context& c, const ba_problem* P, const ba_state* S, int32_t n);
+
 struct BadInput : std::runtime_error {
   using std::runtime_error::runtime_error;
 };

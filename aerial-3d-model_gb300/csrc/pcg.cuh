@@ -69,8 +69,11 @@ struct PcgArgs {
   unsigned* err;
 };
 
-// partial slots: 0,1 init (rz, bb) | 2..5 (pq, lens q 0..2) | 6,7 (rr, rz)
-constexpr int kParts = 8;
+// Partial-sum slots.  Grid kernel: 0,1 init (rz, bb) | 2..5 (pq, lens q
+// 0..2) | 6,7 (rr, rz).  Matrix-free kernel adds 8 (barrier) and 9..11 (lens
+// terms).  Consecutive exchanges must use disjoint slots: a CTA may still be
+// reading one exchange's partials while a faster one writes the next.
+constexpr int kParts = 12;
 // A reader lane loads up to kReadUnroll members' partials at once.
 constexpr int kReadUnroll = 4;
 constexpr int kMaxGroupCtas = 32 * kReadUnroll * 4;

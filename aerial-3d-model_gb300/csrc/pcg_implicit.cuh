@@ -8,10 +8,11 @@
 // (camera pairs) is stored: no pair list, no Schur sums, no S.
 //
 // One persistent cooperative launch per LM iteration; the CTAs form one
-// group.  An iteration has three phases separated by group exchanges:
-//   1. per point: t_p = E_p p (p formed on the fly as z + β p_prev); the
-//      lens entries' shares Zl t_p are summed per CTA;
-//   2. per camera: q_c = A_c p_c + X_c p_g - sum_k Z_k t_p(k); p·q and the
+// group.  An iteration has four phases separated by group exchanges:
+//   0. per row: p = z + β p_prev;
+//   1. per point: t_p = E_p p; the lens entries' shares Zl t_p are summed
+//      per CTA;
+//   2. per camera (a CTA each): q_c = A_c p_c + X_c p_g - sum_k Z_k t_p(k); p·q and the
 //      lens row's transposed terms X_c^T p_c are summed per CTA; the lens row
 //      q_g = A_g p_g + sum_c X_c^T p_c - sum_j Zl_j t_p(j) is formed by every
 //      CTA from the exchanged sums;
@@ -57,22 +58,17 @@ struct ImpArgs {
 // Implicit-product scalars, computed once per CTA by thread 0.
 template <typename R>
 struct ImpScalars {
-  double rz, b2, beta, a, lensq[3], pg[3];
+  double rz, b2, beta, a, lensq[3];
   R beta_r, a_r;
   int stop;
 };
-
-// p_j = z_j + β p_j(prev) for block row j, component i.
-template <typename R>
-__device__ __forceinline__ R imp_p(const ImpArgs<R>& A, const R* pprev, uint32_t j, int i, R br) {
-  return (R)(__ldcg(A.z + 6 * (size_t)j + i) + __ldcg(pprev + 6 * (size_t)j + i) * br);
-}
 
 template <typename R>
 __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A) {
   __shared__ double wsm[kPcgWarps * 4];
   __shared__ double tot[4];
   __shared__ ImpScalars<R> sc;
+  __shared__ R smem_q[kPcgWarps * 6];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gw = blockIdx.x * kPcgWarps + warp, nw = gridDim.x * kPcgWarps;
   const PcgJob J{0, (int32_t)blockIdx.x, (int32_t)gridDim.x, 0, 0, 0};
@@ -115,11 +111,18 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
     R* pcur = A.p2 + (size_t)(it & 1) * 6 * A.nb;
     const R* pprev = A.p2 + (size_t)((it + 1) & 1) * 6 * A.nb;
     const R br = sc.beta_r;
-    // The lens row's p, formed by every thread that needs it.
-    R pg[3] = {(R)0, (R)0, (R)0};
+    // Phase 0: p = z + β p_prev for every block row (thread per component).
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < 6 * (int64_t)A.nb;
+         e += (int64_t)gridDim.x * blockDim.x)
+      pcur[e] = (R)(__ldcg(A.z + e) + __ldcg(pprev + e) * br);
+    {
+      const double w1[1] = {0.0};
+      if (!group_reduce<1>(w1, wsm, tot, A, J, 8, target, [] {})) return;
+    }
+    R pg[3] = {(R)0, (R)0, (R)0};  // the lens row's p
     if (lens >= 0)
 #pragma unroll
-      for (int i = 0; i < 3; ++i) pg[i] = imp_p(A, pprev, (uint32_t)lens, i, br);
+      for (int i = 0; i < 3; ++i) pg[i] = __ldcg(pcur + 6 * (size_t)lens + i);
 
     // Phase 1: t_p = E_p p per point (thread per point).
     double wl[3] = {0.0, 0.0, 0.0};  // sum over lens entries of Zl t
@@ -129,13 +132,15 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
       if (A.kept[pt]) {
         for (uint32_t k = A.SV.pt_ptr[pt]; k < A.SV.pt_ptr[pt + 1]; ++k) {
           const uint32_t cb = A.P.cam_blk[A.P.obs_cam[k]];
-          const R* Zk = A.Z + 18 * (size_t)k;
+          R zk[18], pv[6];
+          load_Z18(A.Z + 18 * (size_t)k, zk);
+#pragma unroll
+          for (int i = 0; i < 6; ++i) pv[i] = __ldcg(pcur + 6 * (size_t)cb + i);
 #pragma unroll
           for (int i = 0; i < 6; ++i) {
-            const R pi = imp_p(A, pprev, cb, i, br);
-            t0 += Zk[3 * i] * pi;
-            t1 += Zk[3 * i + 1] * pi;
-            t2 += Zk[3 * i + 2] * pi;
+            t0 += zk[3 * i] * pv[i];
+            t1 += zk[3 * i + 1] * pv[i];
+            t2 += zk[3 * i + 2] * pv[i];
           }
         }
         for (uint32_t j = A.SV.lens_ptr[pt]; j < A.SV.lens_ptr[pt + 1]; ++j) {
@@ -161,46 +166,52 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
       double w3[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) w3[i] = warp_sum(wl[i]);
-      if (!group_reduce<3>(w3, wsm, tot, A, J, 0, target, [&] {
+      if (!group_reduce<3>(w3, wsm, tot, A, J, 9, target, [&] {
             for (int i = 0; i < 3; ++i) sc.lensq[i] = -tot[i];
           }))
         return;
     }
 
-    // Phase 2: q_c = A_c p_c + X_c p_g - sum_k Z_k t_p(k) (warp per camera).
+    // Phase 2: q_c = A_c p_c + X_c p_g - sum_k Z_k t_p(k), a CTA per camera
+    // (its observations strided over the CTA, summed in a fixed order).
     double w4[4] = {0.0, 0.0, 0.0, 0.0};
-    for (uint32_t c = (uint32_t)gw; c < nc; c += (uint32_t)nw) {
+    for (uint32_t c = blockIdx.x; c < nc; c += gridDim.x) {
       const uint32_t row = A.P.cam_blk[c];
       R acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      for (uint32_t i = A.SV.cam_ptr[c] + lane; i < A.SV.cam_ptr[c + 1]; i += 32) {
+      for (uint32_t i = A.SV.cam_ptr[c] + threadIdx.x; i < A.SV.cam_ptr[c + 1]; i += blockDim.x) {
         const uint32_t k = A.SV.cam_obs[i];
-        const R* Zk = A.Z + 18 * (size_t)k;
+        R zk[18];
+        load_Z18(A.Z + 18 * (size_t)k, zk);
         const R* tp = A.t + 3 * (size_t)A.P.obs_pt[k];
         const R u0 = __ldcg(tp), u1 = __ldcg(tp + 1), u2 = __ldcg(tp + 2);
 #pragma unroll
-        for (int r = 0; r < 6; ++r) acc[r] -= Zk[3 * r] * u0 + Zk[3 * r + 1] * u1 + Zk[3 * r + 2] * u2;
+        for (int r = 0; r < 6; ++r) acc[r] -= zk[3 * r] * u0 + zk[3 * r + 1] * u1 + zk[3 * r + 2] * u2;
       }
-      warp_sum8(acc);  // lane 4i holds the Schur part of q_i
-      const R si = __shfl_sync(kFull, acc[0], 4 * ci);
-      const R pi = imp_p(A, pprev, row, ci, br);
-      const R* Ac = A.own + 36 * (size_t)row;
-      R qi = si;
+      warp_sum8(acc);  // lane 4i holds this warp's Schur part of q_i
+      __syncthreads();  // smem_q of the previous camera has been read
+      if ((lane & 3) == 0 && lane < 24) smem_q[warp * 6 + (lane >> 2)] = acc[0];
+      __syncthreads();
+      if (warp == 0) {
+        R si = (R)0;
+        if (vl)
+          for (int w = 0; w < kPcgWarps; ++w) si += smem_q[w * 6 + ci];
+        const R pi = vl ? __ldcg(pcur + 6 * (size_t)row + ci) : (R)0;
+        const R* Ac = A.own + 36 * (size_t)row;
+        R qi = si;
 #pragma unroll
-      for (int j = 0; j < 6; ++j) qi += Ac[6 * ci + j] * __shfl_sync(kFull, pi, j);
-      const double* X = A.camX + 18 * (size_t)c;
-      if (lens >= 0)
+        for (int j = 0; j < 6; ++j) qi += Ac[6 * ci + j] * __shfl_sync(kFull, pi, j);
+        const double* X = A.camX + 18 * (size_t)c;
+        if (lens >= 0)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) qi += (R)X[3 * ci + j] * pg[j];
-      if (vl) {
-        pcur[6 * (size_t)row + ci] = pi;
-        A.q[6 * (size_t)row + ci] = qi;
-      }
-      w4[0] += sum8(vl ? (double)pi * (double)qi : 0.0);
-      if (lens >= 0) {  // X_c^T p_c for the lens row
-        double xt[3];
+          for (int j = 0; j < 3; ++j) qi += (R)X[3 * ci + j] * pg[j];
+        if (vl) A.q[6 * (size_t)row + ci] = qi;
+        w4[0] += sum8(vl ? (double)pi * (double)qi : 0.0);
+        if (lens >= 0) {  // X_c^T p_c for the lens row
+          double xt[3];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) xt[j] = sum8(vl ? X[3 * ci + j] * (double)pi : 0.0);
-        w4[1] += xt[0], w4[2] += xt[1], w4[3] += xt[2];
+          for (int j = 0; j < 3; ++j) xt[j] = sum8(vl ? X[3 * ci + j] * (double)pi : 0.0);
+          w4[1] += xt[0], w4[2] += xt[1], w4[3] += xt[2];
+        }
       }
     }
     if (!group_reduce<4>(w4, wsm, tot, A, J, 2, target, [&] {
@@ -217,10 +228,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
             }
             for (int i = 0; i < 3; ++i) {
               sc.lensq[i] = qg[i];
-              if (blockIdx.x == 0) {
-                pcur[6 * (size_t)lens + i] = pg[i];
-                A.q[6 * (size_t)lens + i] = (R)qg[i];
-              }
+              if (blockIdx.x == 0) A.q[6 * (size_t)lens + i] = (R)qg[i];
             }
           }
           sc.stop = fabs(pq) < 1e-300 ? 1 : 0;  // ba.rs:174
@@ -239,7 +247,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
       if (vl) {
         const size_t o = 6 * (size_t)row + ci;
         const R qv = row == lens ? (R)sc.lensq[ci < 3 ? ci : 0] * (R)(ci < 3) : __ldcg(A.q + o);
-        const R pv = row == lens ? (ci < 3 ? pg[ci < 3 ? ci : 0] : (R)0) : __ldcg(pcur + o);
+        const R pv = __ldcg(pcur + o);
         A.x[o] = A.x[o] + pv * a;
         ri = A.r[o] - qv * a;
         A.r[o] = ri;
@@ -277,10 +285,36 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
 // its padding, damped); the preconditioner's diagonal block is A_b minus the
 // row's own Schur terms sum Z Z^T (cameras: over their observations; lens
 // row: over all lens entries), inverted in FP64 (ba.rs:159-160).
+// Lens row's own Schur terms sum_j Zl_j Zl_j^T over every lens entry, as
+// kLensChunks partial sums (CTA per chunk, fixed order).
+constexpr int kLensChunks = 256;
+
+template <typename R>
+__global__ void lens_diag_kernel(StructView S, IterBufs<R> B, double* lens_part) {
+  __shared__ double red[9 * 32];
+  const int64_t ch = blockIdx.x;
+  const int64_t j0 = S.nl * ch / kLensChunks, j1 = S.nl * (ch + 1) / kLensChunks;
+  double s[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) s[i] = 0.0;
+  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    const R* Zj = B.Zl + 9 * (size_t)j;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        s[3 * r + c] += (double)(Zj[3 * r] * Zj[3 * c] + Zj[3 * r + 1] * Zj[3 * c + 1] +
+                                 Zj[3 * r + 2] * Zj[3 * c + 2]);
+  }
+  block_sum<9>(s, red);
+  if (threadIdx.x == 0)
+    for (int i = 0; i < 9; ++i) lens_part[9 * ch + i] = s[i];
+}
+
 template <typename R>
 __global__ void implicit_blocks_kernel(Prob P, StateView st, StructView S, IterBufs<R> B,
                                        const R* Z, R* own, const int32_t* active,
-                                       const double* lambda) {
+                                       const double* lambda, const double* lens_part) {
   __shared__ double red[36 * 32];
   const int64_t b = blockIdx.x;
   if (b >= P.nb) return;
@@ -302,17 +336,13 @@ __global__ void implicit_blocks_kernel(Prob P, StateView st, StructView S, IterB
           s[6 * r + c] += (double)(Zk[3 * r] * Zk[3 * c] + Zk[3 * r + 1] * Zk[3 * c + 1] +
                                    Zk[3 * r + 2] * Zk[3 * c + 2]);
     }
-  } else {
-    for (int64_t j = threadIdx.x; j < S.nl; j += blockDim.x) {
-      if (P.grp_blk[S.lens_grp[j]] != (uint32_t)b) continue;
-      const R* Zj = B.Zl + 9 * (size_t)j;
+  } else if (threadIdx.x == 0) {
+    // the lens row (one group per matrix-free call): chunk partials in order
+    for (int ch = 0; ch < kLensChunks; ++ch)
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-          s[6 * r + c] += (double)(Zj[3 * r] * Zj[3 * c] + Zj[3 * r + 1] * Zj[3 * c + 1] +
-                                   Zj[3 * r + 2] * Zj[3 * c + 2]);
-    }
+        for (int c = 0; c < 3; ++c) s[6 * r + c] += lens_part[9 * ch + 3 * r + c];
   }
   block_sum<36>(s, red);
   if (threadIdx.x != 0) return;

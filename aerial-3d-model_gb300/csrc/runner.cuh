@@ -309,6 +309,7 @@ struct LmEngine {
   // Matrix-free PCG.
   bool implicit = false;
   DevBuf<R> own, tbuf, rbuf, qbuf;
+  DevBuf<double> lens_part;
   ImpArgs<R> ia{};
   int32_t imp_ncta = 0;
   // Cluster-resident PCG (mixed form).
@@ -357,6 +358,7 @@ struct LmEngine {
     part.alloc(at_least_1(SB.nsub) * 36, s), S.alloc(at_least_1(SB.nz) * 36, s);
     if (implicit) {
       own.alloc(at_least_1(nb) * 36, s), tbuf.alloc(at_least_1(np) * 3, s);
+      lens_part.alloc(9 * kLensChunks, s);
       rbuf.alloc(at_least_1(nb) * 6, s), qbuf.alloc(at_least_1(nb) * 6, s);
     }
     pre.alloc(at_least_1(nb) * 36, s);
@@ -639,8 +641,10 @@ struct LmEngine {
     T.mark(BA_PHASE_CAMERA);
     if (implicit) {
       T.mark(BA_PHASE_SCHUR);
+      BA_LAUNCH(lens_diag_kernel<R><<<kLensChunks, 256, 0, s>>>(SV, B, lens_part));
       BA_LAUNCH(implicit_blocks_kernel<R><<<(unsigned)ctx.nb, 256, 0, s>>>(P, cur, SV, B, Z, own,
-                                                                          active, lambda));
+                                                                          active, lambda,
+                                                                          lens_part));
       BA_LAUNCH(rhs_kernel<R><<<grid_for(ctx.nb * 6, 256), 256, 0, s>>>(P, cur, B, active));
       T.mark(BA_PHASE_ASSEMBLE);
       return;

@@ -74,9 +74,12 @@ __global__ void fixup_kernel(int64_t nm, const uint32_t* obs0, const uint32_t* c
 
 template <typename T>
 void up(DevBuf<T>& d, const T* h, size_t off, size_t n, cudaStream_t s) {
-  if (n) check(cudaMemcpyAsync(d.p + off, h, n * sizeof(T), cudaMemcpyHostToDevice, s), "h2d");
+  if (n) check(cudaMemcpyAsync(d.p + off, h, n * sizeof(T), cudaMemcpyDefault, s), "h2d");
 }
 
+}  // namespace
+
+// Copies into the context: host or device source arrays (unified addressing).
 void upload(Context& c, const ba_problem* P, const ba_state* S, int32_t n) {
   if (n < 1) throw BadInput("n_models must be >= 1");
   if (!P || !S) throw BadInput("null problem or state");
@@ -184,6 +187,8 @@ void upload(Context& c, const ba_problem* P, const ba_state* S, int32_t n) {
     throw BadInput(msg);
   }
 }
+
+namespace {
 
 void download(Context& c, ba_state* S, int32_t n) {
   if (!c.uploaded) throw BadInput("no problem uploaded");

@@ -291,9 +291,75 @@ class Context:
             g.ctypes.data, dx.ctypes.data, C.byref(it), C.byref(tc)))
         return dict(S=S, g=g, dx=dx, pcg_iters=it.value, trial_cost=tc.value)
 
+    def upload_tracks(self, tracks: "Tracks", rot, center, intr, thr_px: float,
+                      prior_mask=None, prior=None, refine_intrinsics: bool = True):
+        """Triangulate and gate a round's tracks on the device and make the
+        kept tracks the context's problem (sparse.rs:389-449), without a host
+        round trip.  Returns (n_points, n_obs)."""
+        R, Cc, K = _f64(rot), _f64(center), _f64(intr)
+        st = native.BaState(R.ctypes.data, Cc.ctypes.data, K.ctypes.data, None)
+        pm = None if prior_mask is None else np.ascontiguousarray(prior_mask, np.uint8)
+        pr = None if prior is None else _f64(prior)
+        n_pts, n_obs = C.c_int64(), C.c_int64()
+        tv = tracks.c_view()
+        native.check(self._L.ba_context_upload_tracks(
+            self._h, C.byref(tv), C.byref(st), None if pm is None else pm.ctypes.data,
+            None if pr is None else pr.ctypes.data, 1 if refine_intrinsics else 0, float(thr_px),
+            C.byref(n_pts), C.byref(n_obs)))
+        nc, ng = len(tracks.cam_group), int(tracks.n_groups)
+        # A host mirror for download(): the state arrays the context solves.
+        self._problems = [Problem.empty(nc, n_pts.value, n_obs.value, ng,
+                                        refine_intrinsics=refine_intrinsics)]
+        self._n = 1
+        return n_pts.value, n_obs.value
+
     def intrinsics_grad(self, sigma_px: float, options: Options | None = None) -> np.ndarray:
         ng = sum(p.n_groups for p in self._problems)
         g = np.zeros((ng, 5))
         opt = _c_options(0, sigma_px, options)
         native.check(self._L.ba_context_intrinsics_grad(self._h, C.byref(opt), g.ctypes.data))
         return g
+
+
+@dataclass
+class Tracks:
+    """Feature tracks of one sparse-stage round (sparse.rs:389): track t is
+    observed by obs_cam / obs_uv[track_ptr[t]:track_ptr[t + 1]] (full
+    resolution, distorted pixels); cam_group gives each camera's lens group."""
+    track_ptr: np.ndarray  # u32[n_tracks + 1]
+    obs_cam: np.ndarray    # u32[n_obs]
+    obs_uv: np.ndarray     # f64[n_obs, 2]
+    cam_group: np.ndarray  # u32[n_cams]
+    n_groups: int = 1
+
+    def c_view(self) -> native.BaTracks:
+        for name, dt in (("track_ptr", np.uint32), ("obs_cam", np.uint32), ("obs_uv", np.float64),
+                         ("cam_group", np.uint32)):
+            a = getattr(self, name)
+            if not (isinstance(a, np.ndarray) and a.dtype == dt and a.flags.c_contiguous):
+                raise TypeError(f"Tracks.{name} must be a C-contiguous {np.dtype(dt)} array")
+        return native.BaTracks(len(self.track_ptr) - 1, len(self.obs_cam), len(self.cam_group),
+                               int(self.n_groups), self.track_ptr.ctypes.data,
+                               self.obs_cam.ctypes.data, self.obs_uv.ctypes.data,
+                               self.cam_group.ctypes.data)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def triangulate(tracks: Tracks, rot, center, intr, thr_px: float):
+    """One round's triangulation and reprojection gating (sparse.rs:389-421).
+    Returns (kept bool[n_tracks], points f64[n_tracks, 3], good bool[n_obs])."""
+    L = native.load()
+    nt, no = len(tracks.track_ptr) - 1, len(tracks.obs_cam)
+    kept = np.zeros(max(nt, 0), np.uint8)
+    pts = np.zeros((max(nt, 0), 3))
+    good = np.zeros(no, np.uint8)
+    nk = C.c_int64()
+    R, Cc, K = _f64(rot), _f64(center), _f64(intr)
+    tv = tracks.c_view()
+    native.check(L.ba_triangulate(C.byref(tv), R.ctypes.data, Cc.ctypes.data, K.ctypes.data,
+                                  float(thr_px), None, kept.ctypes.data, pts.ctypes.data,
+                                  good.ctypes.data, C.byref(nk)))
+    return kept.astype(bool), pts, good.astype(bool)

@@ -30,6 +30,12 @@ class BaState(C.Structure):
                 ("points", C.c_void_p)]
 
 
+class BaTracks(C.Structure):
+    _fields_ = [("n_tracks", C.c_int64), ("n_obs", C.c_int64), ("n_cams", C.c_int64),
+                ("n_groups", C.c_int64), ("track_ptr", C.c_void_p), ("obs_cam", C.c_void_p),
+                ("obs_uv", C.c_void_p), ("cam_group", C.c_void_p)]
+
+
 class BaLog(C.Structure):
     _fields_ = [("cap", C.c_int32), ("new_cost", C.c_void_p), ("lam", C.c_void_p),
                 ("pcg_iters", C.c_void_p), ("accepted", C.c_void_p)]
@@ -65,7 +71,8 @@ EXPORTS = [
     "ba_default_options", "ba_solve", "ba_solve_batch", "ba_context_create",
     "ba_context_destroy", "ba_context_upload", "ba_context_solve", "ba_context_download",
     "ba_context_intrinsics_grad", "ba_context_vjp", "ba_context_linearise", "ba_context_cost",
-    "ba_context_debug_step", "ba_robust_cost_noalloc", "ba_last_error",
+    "ba_context_debug_step", "ba_robust_cost_noalloc", "ba_triangulate",
+    "ba_context_upload_tracks", "ba_last_error",
     "ba_abi_version", "ba_version",
 ]
 
@@ -114,12 +121,19 @@ def load(build_if_missing: bool = True):
     L.ba_robust_cost_noalloc.argtypes = [P, S, C.c_double, C.c_int32, C.c_void_p,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double),
                                          C.POINTER(C.c_int64)]
+    L.ba_triangulate.argtypes = [C.POINTER(BaTracks), C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.POINTER(C.c_int64)]
+    L.ba_context_upload_tracks.argtypes = [C.c_void_p, C.POINTER(BaTracks), S, C.c_void_p,
+                                           C.c_void_p, C.c_int32, C.c_double,
+                                           C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.ba_last_error.restype = C.c_char_p
     L.ba_version.restype = C.c_char_p
     for name in ("ba_solve", "ba_solve_batch", "ba_context_create", "ba_context_upload",
                  "ba_context_solve", "ba_context_download", "ba_context_intrinsics_grad",
                  "ba_context_vjp", "ba_context_debug_step", "ba_robust_cost_noalloc",
-                 "ba_context_linearise", "ba_context_cost"):
+                 "ba_context_linearise", "ba_context_cost", "ba_triangulate",
+                 "ba_context_upload_tracks"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

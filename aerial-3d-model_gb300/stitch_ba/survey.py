@@ -82,8 +82,8 @@ PRESETS = {
                                 across_overlap=0.45),
     "single500": SurveyParams(n_cams=500, n_points=400_000, along_overlap=0.795,
                               across_overlap=0.44),
-    "oblique2000": SurveyParams(n_cams=2000, n_points=2_000_000, along_overlap=0.78,
-                                across_overlap=0.42, oblique_frac=0.30),
+    "oblique2000": SurveyParams(n_cams=2000, n_points=2_000_000, along_overlap=0.5,
+                                across_overlap=0.2, oblique_frac=0.30),
     "large5000": SurveyParams(n_cams=5000, n_points=6_000_000, along_overlap=0.79,
                               across_overlap=0.42),
 }

@@ -140,7 +140,10 @@ MIXED_MATRIX_FREE = False  # --matrix-free: the mixed form applies S without for
 
 
 def form_options(prec: str, **kw):
+    """Per form: the PCG layout is picked by the solver's autotuner on the
+    first (warm-up) solve of the form and reused by the timed solves."""
     from stitch_ba import Options
+    kw.setdefault("autotune", True)
     if prec == "mixed":
         mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
         return Options(precision="mixed", pcg_max_iter=MIXED_PCG_ITERS, matrix_free=mf, **kw)
@@ -268,6 +271,8 @@ def gpu_arm(args, ws, rank):
             profile_info[prec] = prof
             infos_by_form[prec] = infos
             forms[prec]["pcg_kernel"] = prof.pcg_kernel
+            forms[prec]["pcg_ctas"] = int(prof.pcg_ctas)
+            forms[prec]["pcg_autotuned_us_per_iter"] = prof.pcg_tuned_us
             forms[prec]["device_bytes"] = int(prof.device_bytes)
             forms[prec]["pcg_max_iter"] = opts.pcg_max_iter
             forms[prec]["graph"] = bool(info.graph)

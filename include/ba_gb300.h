@@ -271,6 +271,45 @@ ba_status ba_robust_cost_noalloc(const ba_problem* problem, const ba_state* stat
                                  double sigma_px, int32_t loss, void* stream,
                                  double* cost, double* rms, int64_t* n_in_front);
 
+/* ---- triangulation and gating of a sparse-stage round ---------------------- */
+
+/* Feature tracks of the sparse stage (sparse.rs:389): track t's observations
+ * are obs_cam / obs_uv[track_ptr[t] .. track_ptr[t+1]).  Pixels are full
+ * resolution, distorted (as matched). */
+typedef struct ba_tracks {
+  int64_t n_tracks, n_obs, n_cams, n_groups;
+  const uint32_t* track_ptr; /* n_tracks + 1 */
+  const uint32_t* obs_cam;   /* n_obs */
+  const double* obs_uv;      /* 2 * n_obs */
+  const uint32_t* cam_group; /* n_cams */
+} ba_tracks;
+
+/* One round's triangulation and reprojection gating of every track
+ * (sparse.rs:389-421): linear triangulation from the undistorted observations
+ * (geometry.rs:115-144), observations kept if they reproject within thr_px,
+ * track kept if two or more remain and their rays span more than 2 degrees
+ * (three or more views) or 6 degrees (two views; geometry.rs:146-156).
+ * Cameras: rot f64[9 n_cams] (row-major), center f64[3 n_cams], intr
+ * f64[5 n_groups].  Host (or device) inputs; outputs (host, may be NULL):
+ * kept u8[n_tracks], points f64[3 n_tracks], good u8[n_obs], n_kept.
+ * Replaces the reference's per-round closure at sparse.rs:389-421. */
+ba_status ba_triangulate(const ba_tracks* tracks, const double* rot, const double* center,
+                         const double* intr, double thr_px, void* stream, uint8_t* kept,
+                         double* points, uint8_t* good, int64_t* n_kept);
+
+/* Triangulate and gate as ba_triangulate, then build the round's bundle
+ * adjustment problem in the context's device memory (sparse.rs:429-449:
+ * points of the kept tracks in track order, their kept observations sorted
+ * by point; cameras and groups as given; priors optional) without a round
+ * trip through the host.  `cams`: rot, center, intr (points ignored).  Then
+ * ba_context_solve / ba_context_download as after ba_context_upload.
+ * n_points / n_obs receive the problem's sizes.  No counterpart in the
+ * reference, which builds the Problem on the host. */
+ba_status ba_context_upload_tracks(ba_context* ctx, const ba_tracks* tracks,
+                                   const ba_state* cams, const uint8_t* prior_mask,
+                                   const double* prior, int32_t refine_intrinsics,
+                                   double thr_px, int64_t* n_points, int64_t* n_obs);
+
 /* ---- misc ----------------------------------------------------------------- */
 
 const char* ba_last_error(void);

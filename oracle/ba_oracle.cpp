@@ -947,6 +947,153 @@ void oracle_undistort(const double* K, const double* u, double* p) {
   p[1] = py;
 }
 
+// Symmetric 4x4 eigen-decomposition by cyclic Jacobi rotations (the
+// reference calls nalgebra's symmetric_eigen, a third-party routine not in
+// the reference tree; any accurate symmetric solver gives the same
+// eigenvector of a simple eigenvalue up to sign and rounding).
+static void jacobi4(double A[4][4], double V[4][4]) {
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int i = 0; i < 4; ++i) {
+      diag += A[i][i] * A[i][i];
+      for (int j = i + 1; j < 4; ++j) off += A[i][j] * A[i][j];
+    }
+    if (off <= 1e-34 * diag || off == 0.0) break;
+    for (int p = 0; p < 3; ++p)
+      for (int q = p + 1; q < 4; ++q) {
+        if (A[p][q] == 0.0) continue;
+        const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) /
+                         (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 4; ++k) {  // A <- J^T A J
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - sn * akq;
+          A[k][q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < 4; ++k) {
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - sn * aqk;
+          A[q][k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < 4; ++k) {
+          const double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - sn * vkq;
+          V[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+}
+
+// triangulate (geometry.rs:115-144): linear multi-view triangulation from
+// undistorted normalised coordinates via the smallest eigenvector of A^T A.
+static bool triangulate_track(int n, const double* const* R, const double* const* C,
+                              const double* p, double* X) {
+  if (n < 2) return false;
+  double ata[4][4] = {};
+  for (int i = 0; i < n; ++i) {
+    const double* Ri = R[i];
+    double t[3];
+    for (int k = 0; k < 3; ++k)
+      t[k] = -(Ri[3 * k] * C[i][0] + Ri[3 * k + 1] * C[i][1] + Ri[3 * k + 2] * C[i][2]);
+    const double row0[4] = {Ri[0], Ri[1], Ri[2], t[0]};
+    const double row1[4] = {Ri[3], Ri[4], Ri[5], t[1]};
+    const double row2[4] = {Ri[6], Ri[7], Ri[8], t[2]};
+    double a0[4], a1[4];
+    for (int c = 0; c < 4; ++c) {
+      a0[c] = p[2 * i] * row2[c] - row0[c];
+      a1[c] = p[2 * i + 1] * row2[c] - row1[c];
+    }
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) ata[r][c] += a0[r] * a0[c] + a1[r] * a1[c];
+  }
+  double V[4][4];
+  jacobi4(ata, V);
+  int best = 0;
+  for (int i = 1; i < 4; ++i)
+    if (ata[i][i] < ata[best][best]) best = i;
+  const double v3 = V[3][best];
+  if (std::fabs(v3) < 1e-12) return false;
+  for (int k = 0; k < 3; ++k) X[k] = V[k][best] / v3;
+  return true;
+}
+
+// One round's triangulation and reprojection gating of every track
+// (sparse.rs:389-421): triangulate from undistorted observations, keep the
+// observations that reproject within thr pixels, keep the track if at least
+// two remain and their rays span more than 2 degrees (3+ views) or 6 degrees
+// (2 views; geometry.rs:146-156 max_ray_angle).  Tracks in CSR form
+// (track_ptr[n_tracks + 1], obs_cam, obs_uv); cameras: rot (row-major),
+// center, intr per group, cam_group.  Outputs kept[n_tracks],
+// points[3 * n_tracks], good[n_obs].  Returns the number of kept tracks.
+int64_t oracle_triangulate(int64_t n_tracks, const uint32_t* track_ptr, const uint32_t* obs_cam,
+                           const double* obs_uv, const double* rot, const double* center,
+                           const double* intr, const uint32_t* cam_group, double thr,
+                           uint8_t* kept, double* points, uint8_t* good, int n_threads) {
+  int64_t nk = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : nk) num_threads(n_threads)
+  for (int64_t t = 0; t < n_tracks; ++t) {
+    const uint32_t b = track_ptr[t], e = track_ptr[t + 1];
+    const int n = (int)(e - b);
+    std::vector<const double*> Rs(n), Cs(n);
+    std::vector<double> pn(2 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+      const uint32_t c = obs_cam[b + i];
+      Rs[i] = rot + 9 * (size_t)c;
+      Cs[i] = center + 3 * (size_t)c;
+      oracle_undistort(intr + 5 * (size_t)cam_group[c], obs_uv + 2 * (size_t)(b + i), &pn[2 * i]);
+      good[b + i] = 0;
+    }
+    double X[3] = {0, 0, 0};
+    kept[t] = 0;
+    points[3 * t] = points[3 * t + 1] = points[3 * t + 2] = 0.0;
+    if (!triangulate_track(n, Rs.data(), Cs.data(), pn.data(), X)) continue;
+    int ng = 0;
+    for (int i = 0; i < n; ++i) {
+      const uint32_t c = obs_cam[b + i];
+      double u[2];
+      if (!project(Rs[i], Cs[i], intr + 5 * (size_t)cam_group[c], X, u)) continue;
+      const double dx = u[0] - obs_uv[2 * (size_t)(b + i)], dy = u[1] - obs_uv[2 * (size_t)(b + i) + 1];
+      if (std::sqrt(dx * dx + dy * dy) < thr) good[b + i] = 1, ++ng;
+    }
+    if (ng < 2) {
+      for (int i = 0; i < n; ++i) good[b + i] = 0;
+      continue;
+    }
+    // max_ray_angle over the kept observations' unit rays (geometry.rs:146-156)
+    std::vector<double> ray(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+      double r[3];
+      for (int k = 0; k < 3; ++k) r[k] = X[k] - Cs[i][k];
+      const double l = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+      for (int k = 0; k < 3; ++k) ray[3 * i + k] = r[k] / l;
+    }
+    double best = 0.0;
+    for (int i = 0; i < n; ++i) {
+      if (!good[b + i]) continue;
+      for (int j = i + 1; j < n; ++j) {
+        if (!good[b + j]) continue;
+        double d = ray[3 * i] * ray[3 * j] + ray[3 * i + 1] * ray[3 * j + 1] +
+                   ray[3 * i + 2] * ray[3 * j + 2];
+        d = std::min(1.0, std::max(-1.0, d));
+        best = std::max(best, std::acos(d));
+      }
+    }
+    const double deg = best * 180.0 / M_PI;
+    const bool ok = ng >= 3 ? deg > 2.0 : deg > 6.0;
+    if (!ok) {
+      for (int i = 0; i < n; ++i) good[b + i] = 0;
+      continue;
+    }
+    kept[t] = 1;
+    for (int k = 0; k < 3; ++k) points[3 * t + k] = X[k];
+    ++nk;
+  }
+  return nk;
+}
+
 // The reference's own known-answer problem, `recovers_perturbed_survey`
 // (ba.rs:400-481): 3x4 nadir cameras at 80 m, 1500 candidate ground points,
 // LCG seeded 99 drawing U(−0.5, 0.5) from the top 53 bits (ba.rs:422-428).

@@ -296,3 +296,28 @@ class RefSurvey:
         self.cam_group = np.zeros(12, np.uint32)
         self.refine_intrinsics = True
         self.f_true = ft.value
+
+
+def triangulate(track_ptr, obs_cam, obs_uv, rot, center, intr, cam_group, thr: float,
+                n_threads: int = 0):
+    """sparse.rs:389-421 restated: (kept bool[nt], points [nt, 3], good bool[no])."""
+    L = lib()
+    nt = len(track_ptr) - 1
+    kept = np.zeros(nt, np.uint8)
+    pts = np.zeros((nt, 3))
+    good = np.zeros(len(obs_cam), np.uint8)
+    f = L.oracle_triangulate
+    f.restype = C.c_int64
+    f.argtypes = [C.c_int64] + [C.c_void_p] * 7 + [C.c_double, C.c_void_p, C.c_void_p,
+                                                    C.c_void_p, C.c_int]
+    tp = np.ascontiguousarray(track_ptr, np.uint32)
+    oc = np.ascontiguousarray(obs_cam, np.uint32)
+    uv = np.ascontiguousarray(obs_uv, np.float64)
+    R = np.ascontiguousarray(rot, np.float64)
+    Cc = np.ascontiguousarray(center, np.float64)
+    K = np.ascontiguousarray(intr, np.float64)
+    cg = np.ascontiguousarray(cam_group, np.uint32)
+    f(nt, tp.ctypes.data, oc.ctypes.data, uv.ctypes.data, R.ctypes.data, Cc.ctypes.data,
+      K.ctypes.data, cg.ctypes.data, float(thr), kept.ctypes.data, pts.ctypes.data,
+      good.ctypes.data, int(n_threads or L.oracle_max_threads()))
+    return kept.astype(bool), pts, good.astype(bool)
