@@ -313,6 +313,15 @@ class Context:
         self._n = 1
         return n_pts.value, n_obs.value
 
+    def sparse_summary(self, agl: float, max_neighbours: int = 8) -> "SparseSummary":
+        """sparse_summary() of the context's single model with its current
+        (solved) state, computed where the state lives."""
+        p = self._problems[0]
+        out = SparseSummary.alloc(p.n_cams, p.n_points, max_neighbours)
+        native.check(self._L.ba_context_sparse_summary(self._h, int(max_neighbours), float(agl),
+                                                        *out.pointers()))
+        return out
+
     def intrinsics_grad(self, sigma_px: float, options: Options | None = None) -> np.ndarray:
         ng = sum(p.n_groups for p in self._problems)
         g = np.zeros((ng, 5))
@@ -363,3 +372,43 @@ def triangulate(tracks: Tracks, rot, center, intr, thr_px: float):
                                   float(thr_px), None, kept.ctypes.data, pts.ctypes.data,
                                   good.ctypes.data, C.byref(nk)))
     return kept.astype(bool), pts, good.astype(bool)
+
+
+@dataclass
+class SparseSummary:
+    """Per-camera fields of cameras.json and the f32 points of sparse.ply
+    (sparse.rs:470-483, 515-533; mod.rs:31-35).  Row a of `neighbours` holds
+    camera a's n_neighbours[a] best co-observing cameras, most shared points
+    first (equal counts by ascending index), padded with UINT32_MAX."""
+    neighbours: np.ndarray    # u32[n_cams, max_neighbours]
+    shared: np.ndarray        # u32[n_cams, max_neighbours]
+    n_neighbours: np.ndarray  # i32[n_cams]
+    depth_range: np.ndarray   # f64[n_cams, 2]
+    points_f32: np.ndarray    # f32[n_points, 3]
+
+    @staticmethod
+    def alloc(nc: int, npts: int, k: int) -> "SparseSummary":
+        return SparseSummary(np.zeros((nc, k), np.uint32), np.zeros((nc, k), np.uint32),
+                             np.zeros(nc, np.int32), np.zeros((nc, 2)),
+                             np.zeros((npts, 3), np.float32))
+
+    def pointers(self):
+        return (self.neighbours.ctypes.data, self.shared.ctypes.data,
+                self.n_neighbours.ctypes.data, self.depth_range.ctypes.data,
+                self.points_f32.ctypes.data)
+
+    def neighbour_lists(self) -> list[list[int]]:
+        return [self.neighbours[a, :n].tolist() for a, n in enumerate(self.n_neighbours)]
+
+
+def sparse_summary(problem: Problem, agl: float, max_neighbours: int = 8) -> SparseSummary:
+    """Neighbours, depth ranges and f32 points of a bundle-adjusted problem
+    on the device (replaces the host loops at sparse.rs:470-483, 515-533 and
+    the conversion at mod.rs:31-35).  `agl` is the flying height above
+    ground, the depth range of cameras with fewer than ten points."""
+    L = native.load()
+    prob, st = c_views(problem)
+    out = SparseSummary.alloc(problem.n_cams, problem.n_points, max_neighbours)
+    native.check(L.ba_sparse_summary(C.byref(prob), C.byref(st), int(max_neighbours), float(agl),
+                                     None, *out.pointers()))
+    return out

@@ -72,7 +72,8 @@ EXPORTS = [
     "ba_context_destroy", "ba_context_upload", "ba_context_solve", "ba_context_download",
     "ba_context_intrinsics_grad", "ba_context_vjp", "ba_context_linearise", "ba_context_cost",
     "ba_context_debug_step", "ba_robust_cost_noalloc", "ba_triangulate",
-    "ba_context_upload_tracks", "ba_last_error",
+    "ba_context_upload_tracks", "ba_sparse_summary", "ba_context_sparse_summary",
+    "ba_json_f64", "ba_json_u8", "ba_json_u32", "ba_last_error",
     "ba_abi_version", "ba_version",
 ]
 
@@ -127,13 +128,19 @@ def load(build_if_missing: bool = True):
     L.ba_context_upload_tracks.argtypes = [C.c_void_p, C.POINTER(BaTracks), S, C.c_void_p,
                                            C.c_void_p, C.c_int32, C.c_double,
                                            C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.ba_sparse_summary.argtypes = [P, S, C.c_int32, C.c_double, C.c_void_p] + [C.c_void_p] * 5
+    L.ba_context_sparse_summary.argtypes = [C.c_void_p, C.c_int32, C.c_double] + [C.c_void_p] * 5
+    for name in ("ba_json_f64", "ba_json_u8", "ba_json_u32"):
+        getattr(L, name).argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_char_p, C.c_int64,
+                                     C.POINTER(C.c_int64)]
     L.ba_last_error.restype = C.c_char_p
     L.ba_version.restype = C.c_char_p
     for name in ("ba_solve", "ba_solve_batch", "ba_context_create", "ba_context_upload",
                  "ba_context_solve", "ba_context_download", "ba_context_intrinsics_grad",
                  "ba_context_vjp", "ba_context_debug_step", "ba_robust_cost_noalloc",
                  "ba_context_linearise", "ba_context_cost", "ba_triangulate",
-                 "ba_context_upload_tracks"):
+                 "ba_context_upload_tracks", "ba_sparse_summary", "ba_context_sparse_summary",
+                 "ba_json_f64", "ba_json_u8", "ba_json_u32"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

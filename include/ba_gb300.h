@@ -310,6 +310,51 @@ ba_status ba_context_upload_tracks(ba_context* ctx, const ba_tracks* tracks,
                                    const double* prior, int32_t refine_intrinsics,
                                    double thr_px, int64_t* n_points, int64_t* n_obs);
 
+/* ---- sparse-stage outputs ------------------------------------------------- */
+
+/* Per-camera summary of a finished sparse reconstruction, the fields of
+ * cameras.json that come from the bundle-adjusted problem (sparse.rs:470-483
+ * and 515-533), and the f32 points of sparse.ply (mod.rs:31-35).
+ *   neighbours u32[n_cams * max_neighbours]: the cameras sharing the most
+ *     points with each camera, best first (equal counts by ascending camera
+ *     index, which the reference leaves to HashMap order), UINT32_MAX padded;
+ *   shared u32[n_cams * max_neighbours]: those point counts, 0 padded;
+ *   n_neighbours i32[n_cams];
+ *   depth_range f64[2 n_cams]: (d[n/20] * 0.8, d[19n/20] * 1.25) of the
+ *     sorted camera-frame depths of the camera's observed points when there
+ *     are ten or more, else (0.3 agl, 3 agl);
+ *   points_f32 f32[3 n_points]: the points rounded to f32.
+ * Uses obs_cam, obs_pt (sorted by point) of `problem` and rot, center, points
+ * of `state`; host or device pointers.  Outputs (may be NULL) are host or
+ * device pointers.  max_neighbours in 1..64 (the reference keeps 8).
+ * Replaces the host loops at sparse.rs:470-483 and 515-533 and the f32
+ * conversion at mod.rs:31-35. */
+ba_status ba_sparse_summary(const ba_problem* problem, const ba_state* state,
+                            int32_t max_neighbours, double agl, void* stream,
+                            uint32_t* neighbours, uint32_t* shared, int32_t* n_neighbours,
+                            double* depth_range, float* points_f32);
+
+/* ba_sparse_summary of the single model held by a context, with its current
+ * (solved) state: a round's result summarised without leaving the device. */
+ba_status ba_context_sparse_summary(ba_context* ctx, int32_t max_neighbours, double agl,
+                                    uint32_t* neighbours, uint32_t* shared,
+                                    int32_t* n_neighbours, double* depth_range,
+                                    float* points_f32);
+
+/* JSON text of an array as cameras.json holds it (mod.rs:30,
+ * `serde_json::to_vec(&Sparse)`): "[a,b,c]" when group == 0, else rows of
+ * `group` values "[[a,b,c],[d,e,f]]".  f64 values in the shortest text that
+ * reads back exactly, in serde_json's layout (1.0, 0.001, 1e-7, 1.5e300;
+ * non-finite as null); integers in decimal.  `cap` must be at least
+ * n*(w+1) + 2*(n/group) + 3 bytes, w = 25 (f64), 3 (u8), 10 (u32); the text
+ * is NUL-terminated and *len receives its length.  Host code only. */
+ba_status ba_json_f64(const double* v, int64_t n, int32_t group, char* out, int64_t cap,
+                      int64_t* len);
+ba_status ba_json_u8(const uint8_t* v, int64_t n, int32_t group, char* out, int64_t cap,
+                     int64_t* len);
+ba_status ba_json_u32(const uint32_t* v, int64_t n, int32_t group, char* out, int64_t cap,
+                      int64_t* len);
+
 /* ---- misc ----------------------------------------------------------------- */
 
 const char* ba_last_error(void);

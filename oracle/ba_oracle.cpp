@@ -1094,6 +1094,63 @@ int64_t oracle_triangulate(int64_t n_tracks, const uint32_t* track_ptr, const ui
   return nk;
 }
 
+// Per-camera summary of a finished sparse reconstruction (sparse.rs:470-483,
+// 515-533) and the f32 points of sparse.ply (mod.rs:31-35).  Shared-point
+// counts per ordered pair of distinct cameras of each point and each
+// camera's observed depths, as the reference's loops over `kept` collect
+// them; neighbours sorted by count, best first (equal counts by ascending
+// camera index: the reference takes them in HashMap order), at most max_nb;
+// depth range (d[n/20] * 0.8, d[19n/20] * 1.25) of the depths in total order
+// when n >= 10, else (0.3 agl, 3 agl).  Observations sorted by point.
+void oracle_sparse_summary(int64_t nc, int64_t np, int64_t no, const uint32_t* obs_cam,
+                           const uint32_t* obs_pt, const double* rot, const double* center,
+                           const double* points, int max_nb, double agl, uint32_t* nb,
+                           uint32_t* shared, int32_t* n_nb, double* range, float* pts32) {
+  std::vector<std::unordered_map<uint32_t, uint32_t>> sh(nc);
+  std::vector<std::vector<double>> depths(nc);
+  for (int64_t b = 0, e; b < no; b = e) {
+    for (e = b + 1; e < no && obs_pt[e] == obs_pt[b]; ++e) {
+    }
+    const double* X = points + 3 * (size_t)obs_pt[b];
+    for (int64_t i = b; i < e; ++i) {
+      const uint32_t a = obs_cam[i];
+      double xc[3];
+      to_cam(rot + 9 * (size_t)a, center + 3 * (size_t)a, X, xc);
+      depths[a].push_back(xc[2]);
+      for (int64_t j = b; j < e; ++j)
+        if (obs_cam[j] != a) ++sh[a][obs_cam[j]];
+    }
+  }
+  auto key = [](double z) {
+    uint64_t u;
+    std::memcpy(&u, &z, 8);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+  };
+  for (int64_t a = 0; a < nc; ++a) {
+    std::vector<std::pair<uint32_t, uint32_t>> v(sh[a].begin(), sh[a].end());
+    std::sort(v.begin(), v.end(), [](const auto& x, const auto& y) {
+      return x.second != y.second ? x.second > y.second : x.first < y.first;
+    });
+    const int k = (int)std::min<size_t>(v.size(), (size_t)max_nb);
+    n_nb[a] = k;
+    for (int q = 0; q < max_nb; ++q) {
+      nb[a * max_nb + q] = q < k ? v[q].first : 0xffffffffu;
+      shared[a * max_nb + q] = q < k ? v[q].second : 0u;
+    }
+    auto& d = depths[a];
+    std::sort(d.begin(), d.end(), [&](double x, double y) { return key(x) < key(y); });
+    const size_t n = d.size();
+    if (n >= 10) {
+      range[2 * a] = d[n / 20] * 0.8;
+      range[2 * a + 1] = d[n * 19 / 20] * 1.25;
+    } else {
+      range[2 * a] = agl * 0.3;
+      range[2 * a + 1] = agl * 3.0;
+    }
+  }
+  for (int64_t i = 0; i < 3 * np; ++i) pts32[i] = (float)points[i];
+}
+
 // The reference's own known-answer problem, `recovers_perturbed_survey`
 // (ba.rs:400-481): 3x4 nadir cameras at 80 m, 1500 candidate ground points,
 // LCG seeded 99 drawing U(−0.5, 0.5) from the top 53 bits (ba.rs:422-428).

@@ -321,3 +321,28 @@ def triangulate(track_ptr, obs_cam, obs_uv, rot, center, intr, cam_group, thr: f
       K.ctypes.data, cg.ctypes.data, float(thr), kept.ctypes.data, pts.ctypes.data,
       good.ctypes.data, int(n_threads or L.oracle_max_threads()))
     return kept.astype(bool), pts, good.astype(bool)
+
+
+def sparse_summary(obs_cam, obs_pt, rot, center, points, agl: float, max_neighbours: int = 8):
+    """sparse.rs:470-483, 515-533 and mod.rs:31-35 restated: (neighbours
+    u32[nc, k], shared u32[nc, k], n_neighbours i32[nc], depth_range [nc, 2],
+    points_f32 [np, 3])."""
+    L = lib()
+    f = L.oracle_sparse_summary
+    f.restype = None
+    f.argtypes = [C.c_int64] * 3 + [C.c_void_p] * 5 + [C.c_int, C.c_double] + [C.c_void_p] * 5
+    oc = np.ascontiguousarray(obs_cam, np.uint32)
+    op = np.ascontiguousarray(obs_pt, np.uint32)
+    R = np.ascontiguousarray(rot, np.float64)
+    Cc = np.ascontiguousarray(center, np.float64)
+    X = np.ascontiguousarray(points, np.float64)
+    nc, npts, k = len(Cc.reshape(-1, 3)), len(X.reshape(-1, 3)), int(max_neighbours)
+    nb = np.zeros((nc, k), np.uint32)
+    sh = np.zeros((nc, k), np.uint32)
+    n_nb = np.zeros(nc, np.int32)
+    rng = np.zeros((nc, 2))
+    p32 = np.zeros((npts, 3), np.float32)
+    f(nc, npts, len(oc), oc.ctypes.data, op.ctypes.data, R.ctypes.data, Cc.ctypes.data,
+      X.ctypes.data, k, float(agl), nb.ctypes.data, sh.ctypes.data, n_nb.ctypes.data,
+      rng.ctypes.data, p32.ctypes.data)
+    return nb, sh, n_nb, rng, p32
