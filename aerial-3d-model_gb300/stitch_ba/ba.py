@@ -412,3 +412,58 @@ def sparse_summary(problem: Problem, agl: float, max_neighbours: int = 8) -> Spa
     native.check(L.ba_sparse_summary(C.byref(prob), C.byref(st), int(max_neighbours), float(agl),
                                      None, *out.pointers()))
     return out
+
+
+@dataclass
+class PairMatches:
+    """Matches of photo pairs: pair p joins cameras pair_cam[p] = (i, j) and
+    owns uv[match_ptr[p]:match_ptr[p + 1]], rows (u_i, v_i, u_j, v_j) in
+    pixels.  seed: per-pair RANSAC seeds (default i * 7919 + j,
+    sparse.rs:290)."""
+    pair_cam: np.ndarray   # u32[n_pairs, 2]
+    match_ptr: np.ndarray  # u32[n_pairs + 1]
+    uv: np.ndarray         # f64[n_matches, 4]
+    seed: np.ndarray | None = None  # u64[n_pairs]
+
+    def c_view(self) -> native.BaPairMatches:
+        for name, dt in (("pair_cam", np.uint32), ("match_ptr", np.uint32), ("uv", np.float64),
+                         ("seed", np.uint64)):
+            a = getattr(self, name)
+            if a is None and name == "seed":
+                continue
+            if not (isinstance(a, np.ndarray) and a.dtype == dt and a.flags.c_contiguous):
+                raise TypeError(f"PairMatches.{name} must be a C-contiguous {np.dtype(dt)} array")
+        return native.BaPairMatches(len(self.match_ptr) - 1, len(self.uv.reshape(-1, 4)),
+                                    self.pair_cam.ctypes.data, self.match_ptr.ctypes.data,
+                                    self.uv.ctypes.data,
+                                    None if self.seed is None else self.seed.ctypes.data)
+
+
+def ransac_fundamental(pairs: PairMatches, thresh_px: float = 1.5, iters: int = 600):
+    """Fundamental-matrix RANSAC of every pair on the device (geometry.rs:
+    248-300 as sparse.rs:290 calls it).  Returns (inlier bool[n_matches],
+    n_inliers i32[n_pairs], best_hypothesis i32[n_pairs], refit bool[n_pairs])."""
+    L = native.load()
+    v = pairs.c_view()
+    inl = np.zeros(v.n_matches, np.uint8)
+    n = np.zeros(v.n_pairs, np.int32)
+    best = np.zeros(v.n_pairs, np.int32)
+    refit = np.zeros(v.n_pairs, np.uint8)
+    native.check(L.ba_ransac_fundamental(C.byref(v), float(thresh_px), int(iters), None,
+                                         inl.ctypes.data, n.ctypes.data, best.ctypes.data,
+                                         refit.ctypes.data))
+    return inl.astype(bool), n, best, refit.astype(bool)
+
+
+def pair_fits(pairs: PairMatches, rot, center, intr, cam_group) -> np.ndarray:
+    """Median Sampson error (pixels) of every pair's matches under the given
+    poses, on the device (sparse.rs:620-645)."""
+    L = native.load()
+    v = pairs.c_view()
+    R, Cc, K = _f64(rot), _f64(center), _f64(intr)
+    cg = np.ascontiguousarray(cam_group, np.uint32)
+    med = np.zeros(v.n_pairs)
+    native.check(L.ba_pair_fits(C.byref(v), R.ctypes.data, Cc.ctypes.data, K.ctypes.data,
+                                cg.ctypes.data, len(cg), len(K.reshape(-1, 5)), None,
+                                med.ctypes.data))
+    return med

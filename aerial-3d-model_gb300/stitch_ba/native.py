@@ -36,6 +36,11 @@ class BaTracks(C.Structure):
                 ("obs_uv", C.c_void_p), ("cam_group", C.c_void_p)]
 
 
+class BaPairMatches(C.Structure):
+    _fields_ = [("n_pairs", C.c_int64), ("n_matches", C.c_int64), ("pair_cam", C.c_void_p),
+                ("match_ptr", C.c_void_p), ("uv", C.c_void_p), ("seed", C.c_void_p)]
+
+
 class BaLog(C.Structure):
     _fields_ = [("cap", C.c_int32), ("new_cost", C.c_void_p), ("lam", C.c_void_p),
                 ("pcg_iters", C.c_void_p), ("accepted", C.c_void_p)]
@@ -73,7 +78,8 @@ EXPORTS = [
     "ba_context_intrinsics_grad", "ba_context_vjp", "ba_context_linearise", "ba_context_cost",
     "ba_context_debug_step", "ba_robust_cost_noalloc", "ba_triangulate",
     "ba_context_upload_tracks", "ba_sparse_summary", "ba_context_sparse_summary",
-    "ba_json_f64", "ba_json_u8", "ba_json_u32", "ba_last_error",
+    "ba_json_f64", "ba_json_u8", "ba_json_u32", "ba_ransac_fundamental", "ba_pair_fits",
+    "ba_last_error",
     "ba_abi_version", "ba_version",
 ]
 
@@ -130,6 +136,10 @@ def load(build_if_missing: bool = True):
                                            C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.ba_sparse_summary.argtypes = [P, S, C.c_int32, C.c_double, C.c_void_p] + [C.c_void_p] * 5
     L.ba_context_sparse_summary.argtypes = [C.c_void_p, C.c_int32, C.c_double] + [C.c_void_p] * 5
+    L.ba_ransac_fundamental.argtypes = [C.POINTER(BaPairMatches), C.c_double, C.c_int32,
+                                        C.c_void_p] + [C.c_void_p] * 4
+    L.ba_pair_fits.argtypes = [C.POINTER(BaPairMatches)] + [C.c_void_p] * 4 + [
+        C.c_int64, C.c_int64, C.c_void_p, C.c_void_p]
     for name in ("ba_json_f64", "ba_json_u8", "ba_json_u32"):
         getattr(L, name).argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_char_p, C.c_int64,
                                      C.POINTER(C.c_int64)]
@@ -140,7 +150,8 @@ def load(build_if_missing: bool = True):
                  "ba_context_vjp", "ba_context_debug_step", "ba_robust_cost_noalloc",
                  "ba_context_linearise", "ba_context_cost", "ba_triangulate",
                  "ba_context_upload_tracks", "ba_sparse_summary", "ba_context_sparse_summary",
-                 "ba_json_f64", "ba_json_u8", "ba_json_u32"):
+                 "ba_json_f64", "ba_json_u8", "ba_json_u32", "ba_ransac_fundamental",
+                 "ba_pair_fits"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -155,3 +155,49 @@ def batched_models(n_models: int = 64, seed: int = 1, cam_range=(20, 800),
         npt = max(50, int(math.ceil(nc * ppc / views_per_point)))
         out.append(generate(replace(base, seed=seed * 1000 + m, n_cams=nc, n_points=npt)))
     return out
+
+
+def pair_matches(p: Problem, min_shared: int = 30, outlier_frac: float = 0.25, seed: int = 0,
+                 max_pairs: int | None = None, width: int = 5472, height: int = 3648):
+    """Putative matches of the photo pairs of a survey (the input of the
+    sparse stage's per-pair RANSAC, sparse.rs:262-300): every pair of cameras
+    (i < j) sharing at least `min_shared` points, with one correspondence
+    per shared point (the two observations, in point order), and a fraction
+    `outlier_frac` of them turned into mismatches by a uniformly random
+    second pixel.  Returns a PairMatches (seeds default to i * 7919 + j)."""
+    from .ba import PairMatches
+    rng = np.random.default_rng(seed)
+    cnt = np.bincount(p.obs_pt, minlength=p.n_points)
+    start = np.concatenate([[0], np.cumsum(cnt)])[:-1]
+    ia, ib = [], []
+    for m in range(2, int(cnt.max(initial=0)) + 1):
+        pts = np.nonzero(cnt == m)[0]
+        if len(pts) == 0:
+            continue
+        r, c = np.triu_indices(m, 1)
+        base = start[pts][:, None]
+        ia.append((base + r[None, :]).reshape(-1))
+        ib.append((base + c[None, :]).reshape(-1))
+    ia = np.concatenate(ia) if ia else np.zeros(0, np.int64)
+    ib = np.concatenate(ib) if ib else np.zeros(0, np.int64)
+    ca, cb = p.obs_cam[ia].astype(np.int64), p.obs_cam[ib].astype(np.int64)
+    swap = ca > cb
+    ia, ib = np.where(swap, ib, ia), np.where(swap, ia, ib)
+    ca, cb = np.minimum(ca, cb), np.maximum(ca, cb)
+    key = ca * p.n_cams + cb
+    order = np.lexsort((p.obs_pt[ia], key))
+    ia, ib, key = ia[order], ib[order], key[order]
+    uk, first, counts = np.unique(key, return_index=True, return_counts=True)
+    keep = counts >= min_shared
+    if max_pairs is not None:
+        keep &= np.cumsum(keep) <= max_pairs
+    sel = np.repeat(keep, counts)
+    ia, ib = ia[sel], ib[sel]
+    counts = counts[keep]
+    pair_cam = np.stack([uk[keep] // p.n_cams, uk[keep] % p.n_cams], 1).astype(np.uint32)
+    uv = np.concatenate([p.obs_uv[ia], p.obs_uv[ib]], 1)
+    bad = rng.random(len(uv)) < outlier_frac
+    uv[bad, 2] = rng.uniform(0, width, bad.sum())
+    uv[bad, 3] = rng.uniform(0, height, bad.sum())
+    match_ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
+    return PairMatches(np.ascontiguousarray(pair_cam), match_ptr, np.ascontiguousarray(uv))

@@ -23,6 +23,18 @@ initial state.
   solve's iteration count.
 
 ``--impl reference`` times that CPU solver alone as the reference arm.
+
+``--stage triangulate|ransac|pair_fits|summary`` measures one of the sparse
+stage's steps around the solve on the same survey instead (one JSON line with
+the GPU call's throughput through its C ABI entry point, host buffers in and
+out, against the oracle on all host cores on a bounded sample, and the
+agreement of the two on that sample):
+  triangulate — one round's triangulation + gating of every track (tracks/s);
+  ransac      — fundamental-matrix RANSAC of every photo pair's putative
+                matches, 600 hypotheses, 1.5 px (pairs/s);
+  pair_fits   — median Sampson error of every pair under the poses (pairs/s);
+  summary     — neighbours, depth ranges and f32 points of the problem
+                (observations/s).
 """
 from __future__ import annotations
 
@@ -477,13 +489,17 @@ def main():
     ap.add_argument("--cpu-sample-iters", type=int, default=2)
     ap.add_argument("--full-iters", type=int, default=int(os.environ.get("BA_FULL_ITERS", "0")) or None)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--stage", default="ba",
+                    choices=["ba", "triangulate", "ransac", "pair_fits", "summary"])
     ap.add_argument("--matrix-free", action="store_true",
                     help="mixed form: matrix-free PCG (S p from per-observation factors)")
     args = ap.parse_args()
     global MIXED_MATRIX_FREE
     MIXED_MATRIX_FREE = args.matrix_free
     ws, rank = dist_env()
-    if args.impl == "reference":
+    if args.stage != "ba":
+        out = stage_arm(args, ws, rank)
+    elif args.impl == "reference":
         if args.full_iters is None:
             args.full_iters = FULL_ITERS.get(args.workload, MAX_ITER)
         out = reference_arm(args, ws, rank)
@@ -491,6 +507,95 @@ def main():
         out = gpu_arm(args, ws, rank)
     if out is not None and rank == 0:
         print(json.dumps(out))
+
+
+def stage_arm(args, ws, rank):
+    """One sparse-stage step on the workload's survey: GPU through the C ABI
+    (host arrays in and out, timed with perf_counter around the call, which
+    returns after its device-to-host copies), and the oracle on all host
+    cores on a bounded sample of the same units."""
+    if rank != 0:
+        return None
+    import stitch_ba
+    from stitch_ba import Tracks, native, survey
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ba_oracle as O
+    O.build()
+    native.load()
+    p, _ = survey.generate(args.workload, seed=args.seed)
+    threads = os.cpu_count() or 1
+    cnt = np.bincount(p.obs_pt, minlength=p.n_points)
+    tp = np.concatenate([[0], np.cumsum(cnt)]).astype(np.uint32)
+    if args.stage == "triangulate":
+        tr = Tracks(tp, p.obs_cam, p.obs_uv, p.cam_group, 1)
+        units, unit = p.n_points, "tracks/s"
+        gpu = lambda: stitch_ba.triangulate(tr, p.rot, p.center, p.intr, 10.0)  # noqa: E731
+        k = min(units, 200000)
+        sub = tp[:k + 1]
+
+        def cpu():
+            return O.triangulate(sub, p.obs_cam[:sub[-1]], p.obs_uv[:sub[-1]], p.rot, p.center,
+                                 p.intr, p.cam_group, 10.0, n_threads=threads)
+
+        def agree(g, c):
+            return {"kept_equal": float((g[0][:k] == c[0]).mean())}
+    elif args.stage in ("ransac", "pair_fits"):
+        pm = survey.pair_matches(p, seed=args.seed)
+        units, unit = len(pm.pair_cam), "pairs/s"
+        npairs = len(pm.pair_cam)
+        seeds = pm.pair_cam[:, 0].astype(np.uint64) * np.uint64(7919) + pm.pair_cam[:, 1]
+        if args.stage == "ransac":
+            gpu = lambda: stitch_ba.ransac_fundamental(pm, 1.5, 600)  # noqa: E731
+            k = min(npairs, 400)
+
+            def cpu():
+                return O.ransac_fundamental(pm.match_ptr[:k + 1], pm.uv, seeds[:k], 1.5, 600,
+                                            n_threads=threads)
+
+            def agree(g, c):
+                return {"best_hypothesis_equal": float((g[2][:k] == c[2]).mean()),
+                        "inlier_flags_equal": float((g[0][:pm.match_ptr[k]] == c[0]).mean())}
+        else:
+            gpu = lambda: stitch_ba.pair_fits(pm, p.rot, p.center, p.intr, p.cam_group)  # noqa: E731
+            k = npairs
+
+            def cpu():
+                return O.pair_fits(pm.pair_cam, pm.match_ptr, pm.uv, p.rot, p.center, p.intr,
+                                   p.cam_group, n_threads=threads)
+
+            def agree(g, c):
+                return {"max_rel_diff": float(np.abs(g - c).max() / np.abs(c).max())}
+    else:
+        units, unit = p.n_obs, "observations/s"
+        gpu = lambda: stitch_ba.sparse_summary(p, 80.0)  # noqa: E731
+        k = units
+
+        def cpu():
+            return O.sparse_summary(p.obs_cam, p.obs_pt, p.rot, p.center, p.points, 80.0)
+
+        def agree(g, c):
+            return {"neighbours_equal": bool(np.array_equal(g.neighbours, c[0])),
+                    "depth_range_equal": bool(np.array_equal(g.depth_range, c[3]))}
+    for _ in range(args.warmup):
+        g = gpu()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        g = gpu()
+        times.append(time.perf_counter() - t0)
+    dt = float(np.median(times))
+    t0 = time.perf_counter()
+    c = cpu()
+    tc = time.perf_counter() - t0
+    return {"metric": f"sparse stage: {args.stage}", "value": units / dt, "unit": unit,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded survey generator, reference camera model)",
+            "config": {"workload": args.workload, "cameras": p.n_cams, "points": p.n_points,
+                       "observations": p.n_obs, "units": units},
+            "cpu_baseline": {"value": k / tc, "unit": unit, "cores": threads, "kind": "port",
+                             "sample": f"{k} of {units} units ({tc:.2f} s)"},
+            "agreement_on_sample": agree(g, c)}
 
 
 # LM iterations the full solve of each workload takes (FP64, measured on the

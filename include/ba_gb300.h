@@ -310,6 +310,49 @@ ba_status ba_context_upload_tracks(ba_context* ctx, const ba_tracks* tracks,
                                    const double* prior, int32_t refine_intrinsics,
                                    double thr_px, int64_t* n_points, int64_t* n_obs);
 
+/* ---- epipolar geometry of photo pairs ------------------------------------ */
+
+/* Putative or verified matches of photo pairs: pair p joins cameras
+ * pair_cam[2p] (i) and pair_cam[2p+1] (j) and owns the correspondences
+ * match_ptr[p] .. match_ptr[p+1] of uv, each (u_i, v_i, u_j, v_j) in
+ * full-resolution pixels (the keypoints the reference indexes with its
+ * (u32, u32) match pairs, gathered).  seed: per-pair RANSAC seeds; NULL
+ * means i * 7919 + j (sparse.rs:290).  Host or device pointers. */
+typedef struct ba_pair_matches {
+  int64_t n_pairs, n_matches;
+  const uint32_t* pair_cam;  /* 2 n_pairs (may be NULL for RANSAC when seed is given) */
+  const uint32_t* match_ptr; /* n_pairs + 1, from 0 to n_matches */
+  const double* uv;          /* 4 n_matches */
+  const uint64_t* seed;      /* n_pairs or NULL */
+} ba_pair_matches;
+
+/* Fundamental-matrix RANSAC of every pair (ransac_fundamental,
+ * geometry.rs:248-300, as sparse.rs:290 calls it per pair: thresh_px 1.5,
+ * iters 600): xorshift64 samples of eight distinct correspondences, the
+ * normalised 8-point F with rank 2 enforced, inliers by squared Sampson
+ * distance < thresh_px^2; the first hypothesis with the most inliers wins and
+ * one refit on its inliers is kept when it has at least as many.  Pairs with
+ * fewer than 12 correspondences get none.  Outputs (host or device, may be
+ * NULL): inlier u8[n_matches], n_inliers i32[n_pairs], best_hypothesis
+ * i32[n_pairs] (-1: none), refit u8[n_pairs].  The sparse stage keeps a
+ * pair's inliers when there are at least 20 (sparse.rs:291-297).
+ * Replaces the per-pair call at sparse.rs:290. */
+ba_status ba_ransac_fundamental(const ba_pair_matches* m, double thresh_px, int32_t iters,
+                                void* stream, uint8_t* inlier, int32_t* n_inliers,
+                                int32_t* best_hypothesis, uint8_t* refit);
+
+/* pair_fits (sparse.rs:620-645) of every pair under the current poses: the
+ * median (element n/2 in total order) of sqrt(Sampson) * f_i of the pair's
+ * matches for E = [t]x R, R = R_j R_i^T, t = R_j (C_i - C_j), on undistorted
+ * normalised coordinates; DBL_MAX for a pair without matches.  Cameras: rot
+ * f64[9 n_cams] (row-major), center f64[3 n_cams], intr f64[5 n_groups],
+ * cam_group u32[n_cams].  Output median_px f64[n_pairs].  The sparse stage
+ * drops pairs whose median is not below 6 px at its working scale
+ * (sparse.rs:362-373).  Replaces the retain closure at sparse.rs:362-373. */
+ba_status ba_pair_fits(const ba_pair_matches* m, const double* rot, const double* center,
+                       const double* intr, const uint32_t* cam_group, int64_t n_cams,
+                       int64_t n_groups, void* stream, double* median_px);
+
 /* ---- sparse-stage outputs ------------------------------------------------- */
 
 /* Per-camera summary of a finished sparse reconstruction, the fields of

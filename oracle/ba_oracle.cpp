@@ -1094,6 +1094,247 @@ int64_t oracle_triangulate(int64_t n_tracks, const uint32_t* track_ptr, const ui
   return nk;
 }
 
+// ---- epipolar geometry: pair pruning and fundamental-matrix RANSAC --------
+
+// Symmetric NxN eigen-decomposition by cyclic Jacobi rotations (as jacobi4;
+// stands in for nalgebra's symmetric_eigen, geometry.rs:209 and :131).
+extern "C++" {
+template <int N>
+static void jacobi_sym(double A[N][N], double V[N][N]) {
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int i = 0; i < N; ++i) {
+      diag += A[i][i] * A[i][i];
+      for (int j = i + 1; j < N; ++j) off += A[i][j] * A[i][j];
+    }
+    if (off <= 1e-34 * diag || off == 0.0) break;
+    for (int p = 0; p < N - 1; ++p)
+      for (int q = p + 1; q < N; ++q) {
+        if (A[p][q] == 0.0) continue;
+        const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) /
+                         (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < N; ++k) {
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - sn * akq;
+          A[k][q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < N; ++k) {
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - sn * aqk;
+          A[q][k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < N; ++k) {
+          const double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - sn * vkq;
+          V[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+}
+}  // extern "C++"
+
+// normalise (geometry.rs:161-183) of one side (side 0: a, 1: b) of the
+// correspondences idx[0..n) of uv (4 values per correspondence: a then b):
+// centroid as a running sum of p/n, mean distance to it, scale sqrt(2)/d.
+static void ep_normalise(const double* uv, const uint32_t* idx, int n, int side,
+                         double* out, double T[9]) {
+  const double nn = (double)n;
+  double mx = 0.0, my = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double* p = uv + 4 * (size_t)idx[i] + 2 * side;
+    mx = mx + p[0] / nn;
+    my = my + p[1] / nn;
+  }
+  double d = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double* p = uv + 4 * (size_t)idx[i] + 2 * side;
+    const double dx = p[0] - mx, dy = p[1] - my;
+    d += std::sqrt(dx * dx + dy * dy);
+  }
+  d /= nn;
+  const double s = d > 1e-12 ? M_SQRT2 / d : 1.0;
+  const double t[9] = {s, 0.0, -s * mx, 0.0, s, -s * my, 0.0, 0.0, 1.0};
+  std::memcpy(T, t, sizeof t);
+  for (int i = 0; i < n; ++i) {
+    const double* p = uv + 4 * (size_t)idx[i] + 2 * side;
+    out[2 * i] = (p[0] - mx) * s;
+    out[2 * i + 1] = (p[1] - my) * s;
+  }
+}
+
+// fundamental (geometry.rs:186-230): normalised 8-point F from the
+// correspondences idx[0..n), smallest eigenvector of the 9x9 normal matrix,
+// rank 2 by removing the smallest singular value (F - (F v) v^T, v the right
+// singular vector of the smallest singular value, from the eigenvectors of
+// F^T F), denormalised T_b^T F T_a and scaled to unit Frobenius norm.
+static bool ep_fundamental(const double* uv, const uint32_t* idx, int n, double F[9]) {
+  if (n < 8) return false;
+  std::vector<double> na(2 * (size_t)n), nb(2 * (size_t)n);
+  double ta[9], tb[9];
+  ep_normalise(uv, idx, n, 0, na.data(), ta);
+  ep_normalise(uv, idx, n, 1, nb.data(), tb);
+  double m[9][9] = {};
+  for (int i = 0; i < n; ++i) {
+    const double p0 = na[2 * i], p1 = na[2 * i + 1], q0 = nb[2 * i], q1 = nb[2 * i + 1];
+    const double row[9] = {q0 * p0, q0 * p1, q0, q1 * p0, q1 * p1, q1, p0, p1, 1.0};
+    for (int r = 0; r < 9; ++r)
+      for (int c = 0; c < 9; ++c) m[r][c] += row[r] * row[c];
+  }
+  double V[9][9];
+  jacobi_sym<9>(m, V);
+  int k = 0;
+  for (int i = 1; i < 9; ++i)
+    if (m[i][i] < m[k][k]) k = i;
+  double fm[9];
+  for (int i = 0; i < 9; ++i) fm[i] = V[i][k];
+  double ftf[3][3], W[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      ftf[r][c] = fm[r] * fm[c] + fm[3 + r] * fm[3 + c] + fm[6 + r] * fm[6 + c];
+  jacobi_sym<3>(ftf, W);
+  int j = 0;
+  for (int i = 1; i < 3; ++i)
+    if (ftf[i][i] < ftf[j][j]) j = i;
+  const double v[3] = {W[0][j], W[1][j], W[2][j]};
+  double f2[9];
+  for (int r = 0; r < 3; ++r) {
+    const double fv = fm[3 * r] * v[0] + fm[3 * r + 1] * v[1] + fm[3 * r + 2] * v[2];
+    for (int c = 0; c < 3; ++c) f2[3 * r + c] = fm[3 * r + c] - fv * v[c];
+  }
+  double tbt[9], tmp[9], full[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) tbt[3 * r + c] = tb[3 * c + r];
+  matmul3(tbt, f2, tmp);
+  matmul3(tmp, ta, full);
+  double nrm = 0.0;
+  for (int i = 0; i < 9; ++i) nrm += full[i] * full[i];
+  nrm = std::sqrt(nrm);
+  if (!(nrm > 1e-15)) return false;
+  for (int i = 0; i < 9; ++i) F[i] = full[i] / nrm;
+  return true;
+}
+
+// sampson (geometry.rs:233-246): squared Sampson distance, f64::MAX when the
+// gradient norm is below 1e-18.
+static double ep_sampson(const double* F, double ax, double ay, double bx, double by) {
+  const double f0 = F[0] * ax + F[1] * ay + F[2];
+  const double f1 = F[3] * ax + F[4] * ay + F[5];
+  const double f2 = F[6] * ax + F[7] * ay + F[8];
+  const double g0 = F[0] * bx + F[3] * by + F[6];
+  const double g1 = F[1] * bx + F[4] * by + F[7];
+  const double e = bx * f0 + by * f1 + f2;
+  const double d = f0 * f0 + f1 * f1 + g0 * g0 + g1 * g1;
+  return d < 1e-18 ? 1.7976931348623157e308 : e * e / d;
+}
+
+// ransac_fundamental (geometry.rs:248-300) per pair: pairs p own the
+// correspondences match_ptr[p]..match_ptr[p+1] of uv (u_a, v_a, u_b, v_b).
+// xorshift64 (13, 7, 17) from seed | 1, index = state % n, eight distinct
+// indices per hypothesis (repeats redrawn); the first hypothesis with the
+// most inliers (Sampson^2 < thresh^2) wins; one refit on its inliers is
+// kept when it has at least as many.  Fewer than 12 correspondences: none.
+// Outputs: inlier u8[n_matches], n_inliers, best hypothesis (-1: none),
+// refit taken (0/1).
+void oracle_ransac_fundamental(int64_t n_pairs, const uint32_t* match_ptr, const double* uv,
+                               const uint64_t* seed, double thresh, int iters, uint8_t* inlier,
+                               int32_t* n_inl, int32_t* best_hyp, uint8_t* refit,
+                               int n_threads) {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads)
+  for (int64_t p = 0; p < n_pairs; ++p) {
+    const uint32_t b = match_ptr[p];
+    const int n = (int)(match_ptr[p + 1] - b);
+    const double* U = uv + 4 * (size_t)b;
+    for (int i = 0; i < n; ++i) inlier[b + i] = 0;
+    n_inl[p] = 0, best_hyp[p] = -1, refit[p] = 0;
+    if (n < 12) continue;
+    const double t2 = thresh * thresh;
+    uint64_t s = seed[p] | 1;
+    auto rnd = [&](uint64_t m) {
+      s ^= s << 13;
+      s ^= s >> 7;
+      s ^= s << 17;
+      return (uint32_t)(s % m);
+    };
+    std::vector<uint32_t> best, cur;
+    uint32_t idx[8];
+    double F[9];
+    for (int it = 0; it < iters; ++it) {
+      int k = 0;
+      while (k < 8) {
+        const uint32_t c = rnd((uint64_t)n);
+        bool dup = false;
+        for (int q = 0; q < k; ++q) dup |= idx[q] == c;
+        if (!dup) idx[k++] = c;
+      }
+      if (!ep_fundamental(U, idx, 8, F)) continue;
+      cur.clear();
+      for (int i = 0; i < n; ++i)
+        if (ep_sampson(F, U[4 * i], U[4 * i + 1], U[4 * i + 2], U[4 * i + 3]) < t2)
+          cur.push_back((uint32_t)i);
+      if (cur.size() > best.size()) best.swap(cur), best_hyp[p] = it;
+    }
+    if (best.size() >= 8 && ep_fundamental(U, best.data(), (int)best.size(), F)) {
+      cur.clear();
+      for (int i = 0; i < n; ++i)
+        if (ep_sampson(F, U[4 * i], U[4 * i + 1], U[4 * i + 2], U[4 * i + 3]) < t2)
+          cur.push_back((uint32_t)i);
+      if (cur.size() >= best.size()) best.swap(cur), refit[p] = 1;
+    }
+    for (uint32_t i : best) inlier[b + i] = 1;
+    n_inl[p] = (int32_t)best.size();
+  }
+}
+
+// pair_fits (sparse.rs:620-645): median Sampson error in pixels (times the
+// first camera's focal length) of a pair's matches under the current poses,
+// E = [t]x R with R = R_b R_a^T, t = R_b (C_a - C_b), on undistorted
+// normalised coordinates; f64::MAX for a pair without matches.
+void oracle_pair_fits(int64_t n_pairs, const uint32_t* pair_cam, const uint32_t* match_ptr,
+                      const double* uv, const double* rot, const double* center,
+                      const double* intr, const uint32_t* cam_group, double* median,
+                      int n_threads) {
+#pragma omp parallel for schedule(dynamic, 4) num_threads(n_threads)
+  for (int64_t p = 0; p < n_pairs; ++p) {
+    const uint32_t ca = pair_cam[2 * p], cb = pair_cam[2 * p + 1];
+    const double* Ra = rot + 9 * (size_t)ca;
+    const double* Rb = rot + 9 * (size_t)cb;
+    const double* Ka = intr + 5 * (size_t)cam_group[ca];
+    const double* Kb = intr + 5 * (size_t)cam_group[cb];
+    double RaT[9], R[9], t[3], S[9], E[9];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) RaT[3 * r + c] = Ra[3 * c + r];
+    matmul3(Rb, RaT, R);
+    const double d[3] = {center[3 * ca] - center[3 * cb], center[3 * ca + 1] - center[3 * cb + 1],
+                         center[3 * ca + 2] - center[3 * cb + 2]};
+    for (int r = 0; r < 3; ++r) t[r] = Rb[3 * r] * d[0] + Rb[3 * r + 1] * d[1] + Rb[3 * r + 2] * d[2];
+    skew(t, S);
+    matmul3(S, R, E);
+    const uint32_t b = match_ptr[p], e = match_ptr[p + 1];
+    if (e == b) {
+      median[p] = 1.7976931348623157e308;
+      continue;
+    }
+    std::vector<double> errs(e - b);
+    for (uint32_t i = b; i < e; ++i) {
+      double x1[2], x2[2];
+      oracle_undistort(Ka, uv + 4 * (size_t)i, x1);
+      oracle_undistort(Kb, uv + 4 * (size_t)i + 2, x2);
+      errs[i - b] = std::sqrt(ep_sampson(E, x1[0], x1[1], x2[0], x2[1])) * Ka[0];
+    }
+    auto key = [](double z) {  // f64::total_cmp
+      uint64_t u;
+      std::memcpy(&u, &z, 8);
+      return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+    };
+    std::sort(errs.begin(), errs.end(), [&](double x, double y) { return key(x) < key(y); });
+    median[p] = errs[errs.size() / 2];
+  }
+}
+
 // Per-camera summary of a finished sparse reconstruction (sparse.rs:470-483,
 // 515-533) and the f32 points of sparse.ply (mod.rs:31-35).  Shared-point
 // counts per ordered pair of distinct cameras of each point and each

@@ -346,3 +346,80 @@ def sparse_summary(obs_cam, obs_pt, rot, center, points, agl: float, max_neighbo
       X.ctypes.data, k, float(agl), nb.ctypes.data, sh.ctypes.data, n_nb.ctypes.data,
       rng.ctypes.data, p32.ctypes.data)
     return nb, sh, n_nb, rng, p32
+
+
+def ransac_fundamental(match_ptr, uv, seed, thresh: float, iters: int = 600, n_threads: int = 0):
+    """geometry.rs:248-300 per pair: (inlier bool[n_matches], n_inliers
+    i32[n_pairs], best hypothesis i32[n_pairs] (-1: none), refit bool)."""
+    L = lib()
+    f = L.oracle_ransac_fundamental
+    f.restype = None
+    f.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    mp = np.ascontiguousarray(match_ptr, np.uint32)
+    U = np.ascontiguousarray(uv, np.float64)
+    sd = np.ascontiguousarray(seed, np.uint64)
+    npairs = len(mp) - 1
+    inl = np.zeros(int(mp[-1]) if npairs >= 0 else 0, np.uint8)
+    n_inl = np.zeros(npairs, np.int32)
+    best = np.zeros(npairs, np.int32)
+    refit = np.zeros(npairs, np.uint8)
+    f(npairs, mp.ctypes.data, U.ctypes.data, sd.ctypes.data, float(thresh), int(iters),
+      inl.ctypes.data, n_inl.ctypes.data, best.ctypes.data, refit.ctypes.data,
+      int(n_threads or L.oracle_max_threads()))
+    return inl.astype(bool), n_inl, best, refit.astype(bool)
+
+
+def pair_fits(pair_cam, match_ptr, uv, rot, center, intr, cam_group, n_threads: int = 0):
+    """sparse.rs:620-645 per pair: median Sampson error in pixels."""
+    L = lib()
+    f = L.oracle_pair_fits
+    f.restype = None
+    f.argtypes = [C.c_int64] + [C.c_void_p] * 8 + [C.c_int]
+    pc = np.ascontiguousarray(pair_cam, np.uint32)
+    mp = np.ascontiguousarray(match_ptr, np.uint32)
+    U = np.ascontiguousarray(uv, np.float64)
+    R = np.ascontiguousarray(rot, np.float64)
+    Cc = np.ascontiguousarray(center, np.float64)
+    K = np.ascontiguousarray(intr, np.float64)
+    cg = np.ascontiguousarray(cam_group, np.uint32)
+    npairs = len(mp) - 1
+    med = np.zeros(npairs)
+    f(npairs, pc.ctypes.data, mp.ctypes.data, U.ctypes.data, R.ctypes.data, Cc.ctypes.data,
+      K.ctypes.data, cg.ctypes.data, med.ctypes.data, int(n_threads or L.oracle_max_threads()))
+    return med
+
+
+def ransac_kat_correspondences():
+    """The correspondences of geometry.rs:355-381 (`fundamental_ransac_
+    separates_inliers`): two cameras over a 60 x 50 x 15 m volume, LCG from
+    seed 7 (s = s * 6364136223846793005 + 1, value (s >> 33) / 2^31 - 0.5),
+    every fourth candidate's second view replaced by a random pixel.
+    Returns (uv [n, 4], true-inlier mask)."""
+    K = np.array([3000.0, 2000.0, 1500.0, -0.02, 0.005])
+    Ra, Ca = from_angles(0.0, -90.0, 0.0), np.array([0.0, 0.0, 80.0])
+    Rb, Cb = from_angles(5.0, -88.0, 0.0), np.array([25.0, 3.0, 81.0])
+    s = [7]
+    M = (1 << 64) - 1
+
+    def r():
+        s[0] = (s[0] * 6364136223846793005 + 1) & M
+        return (s[0] >> 33) / float(1 << 31) - 0.5
+
+    rows, true = [], []
+    for i in range(200):
+        x0 = r() * 60.0 + 12.0
+        x1 = r() * 50.0
+        x2 = r() * 15.0
+        X = np.array([x0, x1, x2])
+        ua, ub = project(Ra, Ca, K, X), project(Rb, Cb, K, X)
+        if ua is None or ub is None:
+            continue
+        if i % 4 == 0:
+            b0 = r() * 4000.0 + 2000.0
+            b1 = r() * 3000.0 + 1500.0
+            rows.append([ua[0], ua[1], b0, b1])
+        else:
+            rows.append([ua[0], ua[1], ub[0], ub[1]])
+        true.append(i % 4 != 0)
+    return np.array(rows), np.array(true)
