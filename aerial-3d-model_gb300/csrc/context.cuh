@@ -58,7 +58,7 @@ struct Context {
   double phase_ms[kPhases] = {0};
   int64_t phase_n[kPhases] = {0};
   int64_t last_nz = 0, last_pairs = 0, last_nl = 0;
-  int32_t last_pcg_kernel = 0, last_pcg_cluster = 0, last_pcg_ctas = 0;
+  int32_t last_pcg_kernel = 0, last_pcg_cluster = 0, last_pcg_ctas = 0, last_coarse_dim = 0;
   PcgTuning tuning[2];  // [0] FP64 form, [1] mixed form
   bool last_graph = false;
   bool last_matrix_free = false;
@@ -108,6 +108,7 @@ struct Opts {
   int32_t graph = 1;       // capture each LM iteration as a CUDA graph
   int32_t autotune = 0;    // tune the PCG configuration before solving
   int32_t stop_patience = 0;  // 0 or 1: the reference's stop rule
+  int32_t coarse = 0;         // mixed cluster PCG: two-level preconditioner
 };
 
 // One solve of the uploaded batch from its initial states, in precision R.

@@ -36,62 +36,28 @@ constexpr int64_t kMaxChunkHyp = int64_t(1) << 22;
 
 // ---- shared device math -------------------------------------------------------
 
-template <int N>
-__device__ void jacobi_sym(double (&A)[N][N], double (&V)[N][N]) {
-  for (int i = 0; i < N; ++i)
-    for (int j = 0; j < N; ++j) V[i][j] = i == j ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 50; ++sweep) {
-    double off = 0.0, diag = 0.0;
-    for (int i = 0; i < N; ++i) {
-      diag += A[i][i] * A[i][i];
-      for (int j = i + 1; j < N; ++j) off += A[i][j] * A[i][j];
-    }
-    if (off <= 1e-34 * diag || off == 0.0) break;
-    for (int p = 0; p < N - 1; ++p)
-      for (int q = p + 1; q < N; ++q) {
-        if (A[p][q] == 0.0) continue;
-        const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
-        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-        for (int k = 0; k < N; ++k) {
-          const double akp = A[k][p], akq = A[k][q];
-          A[k][p] = c * akp - sn * akq;
-          A[k][q] = sn * akp + c * akq;
-        }
-        for (int k = 0; k < N; ++k) {
-          const double apk = A[p][k], aqk = A[q][k];
-          A[p][k] = c * apk - sn * aqk;
-          A[q][k] = sn * apk + c * aqk;
-        }
-        for (int k = 0; k < N; ++k) {
-          const double vkp = V[k][p], vkq = V[k][q];
-          V[k][p] = c * vkp - sn * vkq;
-          V[k][q] = sn * vkp + c * vkq;
-        }
-      }
-  }
-}
-
 // normalise (geometry.rs:161-183) of side `side` (0: first photo, 1: second)
-// of correspondences idx[0..n): centroid as a running sum of p/n, mean
-// distance to it, scale sqrt(2)/d.  Writes the similarity T (row-major) and
-// the centroid/scale (mx, my, s) used to map points on the fly.
-__device__ void ep_normalise(const double* uv, const uint32_t* idx, int n, int side, double* T,
-                             double& mx, double& my, double& s) {
-  const double nn = (double)n;
+// of the eight correspondences idx[0..8): centroid as a running sum of p/8,
+// mean distance to it, scale sqrt(2)/d.  Division by 8 is the exact
+// multiplication by 0.125.  Writes the similarity T (row-major) and the
+// centroid/scale (mx, my, s) used to map points on the fly.
+__device__ void ep_normalise8(const double* uv, const uint32_t* idx, int side, double* T,
+                              double& mx, double& my, double& s) {
   mx = 0.0, my = 0.0;
-  for (int i = 0; i < n; ++i) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
     const double* p = uv + 4 * (size_t)idx[i] + 2 * side;
-    mx = mx + p[0] / nn;
-    my = my + p[1] / nn;
+    mx = mx + p[0] * 0.125;
+    my = my + p[1] * 0.125;
   }
   double d = 0.0;
-  for (int i = 0; i < n; ++i) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
     const double* p = uv + 4 * (size_t)idx[i] + 2 * side;
     const double dx = p[0] - mx, dy = p[1] - my;
     d += sqrt(dx * dx + dy * dy);
   }
-  d /= nn;
+  d *= 0.125;
   s = d > 1e-12 ? 1.4142135623730951 / d : 1.0;
   T[0] = s, T[1] = 0.0, T[2] = -s * mx;
   T[3] = 0.0, T[4] = s, T[5] = -s * my;
@@ -152,13 +118,16 @@ __global__ void ransac_sample_kernel(RansacArgs A) {
   // umulhi(s, M) is floor(s / n) or one less, so one correction is exact.
   const uint64_t M = ~0ull / n;
   for (int it = 0; it < A.iters; ++it) {
-    uint32_t idx[8];
+    // The eight indices stay in registers: every access below has a
+    // compile-time index (fills and duplicate checks are predicated).
+    uint32_t idx[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int k = 0;
     // Bounded: with n >= 12 the xorshift stream yields eight distinct
     // residues within a few dozen draws; the cap only guards the loop.
     for (int draws = 0; k < 8; ++draws) {
       if (draws == (1 << 20)) {
         atomicOr(A.err, ERR_STRUCTURE);
+#pragma unroll
         for (int j = 0; j < 8; ++j) idx[j] = j;
         break;
       }
@@ -169,23 +138,150 @@ __global__ void ransac_sample_kernel(RansacArgs A) {
       if (r >= n) r -= n;
       const uint32_t c = (uint32_t)r;
       bool dup = false;
-      for (int j = 0; j < k; ++j) dup |= idx[j] == c;
-      if (!dup) idx[k++] = c;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) dup |= (j < k) & (idx[j] == c);
+      if (!dup) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (j == k) idx[j] = c;
+        ++k;
+      }
     }
-    for (int j = 0; j < 8; ++j) out[8 * it + j] = idx[j];
+    uint4* o4 = reinterpret_cast<uint4*>(out + 8 * it);
+    o4[0] = make_uint4(idx[0], idx[1], idx[2], idx[3]);
+    o4[1] = make_uint4(idx[4], idx[5], idx[6], idx[7]);
+  }
+}
+
+// Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations (registers).
+__device__ void jacobi3(double (&A)[3][3], double (&V)[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    const double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+    const double diag = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
+    if (off <= 1e-34 * diag || off == 0.0) break;
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+#pragma unroll
+      for (int q = p + 1; q < 3; ++q) {
+        if (A[p][q] == 0.0) continue;
+        const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - sn * akq;
+          A[k][q] = sn * akp + c * akq;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - sn * aqk;
+          A[q][k] = sn * apk + c * aqk;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - sn * vkq;
+          V[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+}
+
+// Eigenvector of the smallest eigenvalue of the symmetric positive
+// semi-definite N x N matrix M (row-major, overwritten) by inverse iteration
+// on its pivoted Cholesky factor, from the start vector x (overwritten with
+// the unit result).  A pivot below 1e-30 trace(M) is raised to that floor, so
+// an exactly singular M yields a null vector.  Single thread.  The reference
+// takes this eigenvector from nalgebra's symmetric_eigen (geometry.rs:209-215)
+// and the rank-2 step's right singular vector from its SVD (:216-221); any
+// accurate method gives it up to sign and rounding when the smallest
+// eigenvalue is simple.
+template <int N>
+__device__ void smallest_eigvec(double* M, double* x) {
+  int perm[N];
+  double tr = 0.0;
+  for (int i = 0; i < N; ++i) perm[i] = i, tr += M[(N + 1) * i];
+  const double floor_d = 1e-30 * tr + 1e-300;
+  double rdiag[N];
+  for (int k = 0; k < N; ++k) {
+    int pk = k;
+    for (int i = k + 1; i < N; ++i)
+      if (M[(N + 1) * i] > M[(N + 1) * pk]) pk = i;
+    if (pk != k) {  // symmetric swap of rows/columns k and pk
+      for (int j = 0; j < N; ++j) {
+        const double t = M[N * k + j];
+        M[N * k + j] = M[N * pk + j], M[N * pk + j] = t;
+      }
+      for (int j = 0; j < N; ++j) {
+        const double t = M[N * j + k];
+        M[N * j + k] = M[N * j + pk], M[N * j + pk] = t;
+      }
+      const int t = perm[k];
+      perm[k] = perm[pk], perm[pk] = t;
+    }
+    const double lkk = sqrt(fmax(M[(N + 1) * k], floor_d));
+    const double rk = 1.0 / lkk;
+    M[(N + 1) * k] = lkk, rdiag[k] = rk;
+    for (int i = k + 1; i < N; ++i) M[N * i + k] *= rk;
+    for (int i = k + 1; i < N; ++i)
+      for (int j = k + 1; j <= i; ++j) {
+        M[N * i + j] -= M[N * i + k] * M[N * j + k];
+        M[N * j + i] = M[N * i + j];
+      }
+  }
+  // L in the lower triangle: P^T M P = L L^T.
+  double nx = 0.0;
+  for (int i = 0; i < N; ++i) nx += x[i] * x[i];
+  if (!(nx > 1e-300) || !(nx < 1e300)) {  // zero or non-finite start: a generic one
+    nx = 0.0;
+    for (int i = 0; i < N; ++i) x[i] = 1.0 - 0.0625 * i, nx += x[i] * x[i];
+  }
+  nx = 1.0 / sqrt(nx);
+  for (int i = 0; i < N; ++i) x[i] *= nx;
+  for (int it = 0; it < 60; ++it) {
+    double y[N];
+    for (int i = 0; i < N; ++i) y[i] = x[perm[i]];
+    for (int i = 0; i < N; ++i) {  // L z = P^T x
+      double a = y[i];
+      for (int j = 0; j < i; ++j) a -= M[N * i + j] * y[j];
+      y[i] = a * rdiag[i];
+    }
+    for (int i = N - 1; i >= 0; --i) {  // L^T w = z
+      double a = y[i];
+      for (int j = i + 1; j < N; ++j) a -= M[N * j + i] * y[j];
+      y[i] = a * rdiag[i];
+    }
+    double z[N], nn = 0.0;
+    for (int i = 0; i < N; ++i) z[perm[i]] = y[i];
+    for (int i = 0; i < N; ++i) nn += z[i] * z[i];
+    nn = 1.0 / sqrt(nn);
+    double dot = 0.0;
+    for (int i = 0; i < N; ++i) z[i] *= nn, dot += z[i] * x[i];
+    const double sg = dot < 0.0 ? -1.0 : 1.0;
+    double diff = 0.0;
+    for (int i = 0; i < N; ++i) diff = fmax(diff, fabs(sg * z[i] - x[i])), x[i] = sg * z[i];
+    if (diff <= 1e-15) break;
   }
 }
 
 // Rank 2, denormalisation and unit norm of the 8-point solution f
 // (geometry.rs:216-229), as ep_fundamental does after its eigenvector.
 __device__ bool ep_finish(const double* fm, const double* ta, const double* tb, double* F) {
+  // Right singular vector of fm's smallest singular value: the eigenvector
+  // of fm^T fm's smallest eigenvalue.
   double ftf[3][3], W[3][3];
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
     for (int c = 0; c < 3; ++c)
       ftf[r][c] = fm[r] * fm[c] + fm[3 + r] * fm[3 + c] + fm[6 + r] * fm[6 + c];
-  jacobi_sym<3>(ftf, W);
+  jacobi3(ftf, W);
   int j = 0;
   if (ftf[1][1] < ftf[j][j]) j = 1;
   if (ftf[2][2] < ftf[j][j]) j = 2;
@@ -228,8 +324,8 @@ __device__ bool ep_finish(const double* fm, const double* ta, const double* tb, 
 __device__ bool ep_fundamental8(const double* uv, const uint32_t* idx, double* As, int stride,
                                 double* F) {
   double ta[9], tb[9], ax, ay, as, bx, by, bs;
-  ep_normalise(uv, idx, 8, 0, ta, ax, ay, as);
-  ep_normalise(uv, idx, 8, 1, tb, bx, by, bs);
+  ep_normalise8(uv, idx, 0, ta, ax, ay, as);
+  ep_normalise8(uv, idx, 1, tb, bx, by, bs);
 #define AS(r, c) As[(9 * (r) + (c)) * stride]
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -245,14 +341,16 @@ __device__ bool ep_fundamental8(const double* uv, const uint32_t* idx, double* A
   for (int c = 0; c < 9; ++c) perm |= (uint64_t)c << (4 * c);
   int rank = 8;
   for (int k = 0; k < 8; ++k) {
+    // Pivot choice on FP32 magnitudes (the choice only steers stability);
+    // a zero pivot is tested exactly.
     int pr = k, pc = k;
-    double best = -1.0;
+    float best = -1.0f;
     for (int r = k; r < 8; ++r)
       for (int c = k; c < 9; ++c) {
-        const double v = fabs(AS(r, c));
+        const float v = fabsf((float)AS(r, c));
         if (v > best) best = v, pr = r, pc = c;
       }
-    if (!(best > 0.0)) {
+    if (AS(pr, pc) == 0.0) {
       rank = k;
       break;
     }
@@ -270,9 +368,9 @@ __device__ bool ep_fundamental8(const double* uv, const uint32_t* idx, double* A
       perm &= ~((uint64_t)15 << (4 * k)) & ~((uint64_t)15 << (4 * pc));
       perm |= (b << (4 * k)) | (a << (4 * pc));
     }
-    const double piv = AS(k, k);
+    const double rpiv = 1.0 / AS(k, k);
     for (int r = k + 1; r < 8; ++r) {
-      const double m = AS(r, k) / piv;
+      const double m = AS(r, k) * rpiv;
       for (int c = k + 1; c < 9; ++c) AS(r, c) -= m * AS(k, c);
     }
   }
@@ -377,12 +475,64 @@ __device__ __forceinline__ int inlier_fp32(const Hyp32& H, float4 c, float t2) {
 
 constexpr int kCountTile = 1024;
 
+// First-tier bounds of one hypothesis over one tile of correspondences, from
+// the tile's largest coordinate magnitudes (ax, ay, bx, by): every |f_k| is
+// at most S_k, so the error bounds of inlier_fp32 become constants de, dd
+// (plus the 8u d term of d's own rounding).
+struct TileBound {
+  float de, dd;
+};
+
+__device__ __forceinline__ TileBound tile_bound(const Hyp32& H, float4 m) {
+  constexpr float u = 5.9604645e-8f;
+  const float* f = H.f;
+  const float S0 = fmaf(fabsf(f[0]), m.x, fmaf(fabsf(f[1]), m.y, fabsf(f[2])));
+  const float S1 = fmaf(fabsf(f[3]), m.x, fmaf(fabsf(f[4]), m.y, fabsf(f[5])));
+  const float S2 = fmaf(fabsf(f[6]), m.x, fmaf(fabsf(f[7]), m.y, fabsf(f[8])));
+  const float T0 = fmaf(fabsf(f[0]), m.z, fmaf(fabsf(f[3]), m.w, fabsf(f[6])));
+  const float T1 = fmaf(fabsf(f[1]), m.z, fmaf(fabsf(f[4]), m.w, fabsf(f[7])));
+  const float d0 = 8.0f * u * S0, d1 = 8.0f * u * S1, d2 = 8.0f * u * S2;
+  const float e0 = 8.0f * u * T0, e1 = 8.0f * u * T1;
+  TileBound B;
+  // |f_hat| <= S + d; bounds rounded up by the 2x in the factors.
+  B.de = 2.0f * (fmaf(m.z, d0, fmaf(m.w, d1, d2)) +
+                 8.0f * u * fmaf(m.z, S0 + d0, fmaf(m.w, S1 + d1, S2 + d2)));
+  B.dd = 2.0f * (d0 * (2.0f * (S0 + d0) + d0) + d1 * (2.0f * (S1 + d1) + d1) +
+                 e0 * (2.0f * (T0 + e0) + e0) + e1 * (2.0f * (T1 + e1) + e1));
+  return B;
+}
+
+// 1 / 0 surely in / out by the tile's constant bounds, -1 undecided.
+__device__ __forceinline__ int inlier_tile(const Hyp32& H, const TileBound& B, float4 c,
+                                           float t2) {
+  constexpr float u = 5.9604645e-8f;
+  const float* f = H.f;
+  const float f0 = fmaf(f[0], c.x, fmaf(f[1], c.y, f[2]));
+  const float f1 = fmaf(f[3], c.x, fmaf(f[4], c.y, f[5]));
+  const float f2 = fmaf(f[6], c.x, fmaf(f[7], c.y, f[8]));
+  const float g0 = fmaf(f[0], c.z, fmaf(f[3], c.w, f[6]));
+  const float g1 = fmaf(f[1], c.z, fmaf(f[4], c.w, f[7]));
+  const float ae = fabsf(fmaf(c.z, f0, fmaf(c.w, f1, f2)));
+  const float d = fmaf(f0, f0, fmaf(f1, f1, fmaf(g0, g0, g1 * g1)));
+  const float dd = fmaf(8.0f * u, d, B.dd);
+  const float lo = d - dd;
+  if (lo > 2e-18f) {
+    const float a = ae + B.de;
+    if (a * a < t2 * lo * (1.0f - 32.0f * u)) return 1;
+    const float o = ae - B.de;
+    if (o > 0.0f && o * o > t2 * (d + dd) * (1.0f + 32.0f * u)) return 0;
+  }
+  return -1;
+}
+
 // CTA per (pair, 32 hypotheses); each warp tests four hypotheses against
 // every correspondence of the pair, the pair's FP32 coordinates staged
-// through shared memory a tile at a time.
+// through shared memory a tile at a time.  Tests are decided by the tile's
+// constant bounds, else by the correspondence's own bounds, else in FP64.
 __global__ void __launch_bounds__(kCountThreads) ransac_count_kernel(RansacArgs A,
                                                                      const float4* uv32) {
   __shared__ float4 tile[kCountTile];
+  __shared__ float4 wmax[kCountThreads / 32];
   const int blocks_per_pair = (A.iters + kHypPerCountCta - 1) / kHypPerCountCta;
   const int64_t q = blockIdx.x / blocks_per_pair;
   const int hb = (int)(blockIdx.x % blocks_per_pair) * kHypPerCountCta;
@@ -411,14 +561,37 @@ __global__ void __launch_bounds__(kCountThreads) ransac_count_kernel(RansacArgs 
   for (uint32_t t0 = 0; t0 < n; t0 += kCountTile) {
     const uint32_t tn = min((uint32_t)kCountTile, n - t0);
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < tn; i += kCountThreads) tile[i] = uv32[b + t0 + i];
+    float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (uint32_t i = threadIdx.x; i < tn; i += kCountThreads) {
+      const float4 c = uv32[b + t0 + i];
+      tile[i] = c;
+      m.x = fmaxf(m.x, fabsf(c.x)), m.y = fmaxf(m.y, fabsf(c.y));
+      m.z = fmaxf(m.z, fabsf(c.z)), m.w = fmaxf(m.w, fabsf(c.w));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      m.x = fmaxf(m.x, __shfl_xor_sync(kFull, m.x, o));
+      m.y = fmaxf(m.y, __shfl_xor_sync(kFull, m.y, o));
+      m.z = fmaxf(m.z, __shfl_xor_sync(kFull, m.z, o));
+      m.w = fmaxf(m.w, __shfl_xor_sync(kFull, m.w, o));
+    }
+    if (lane == 0) wmax[warp] = m;
     __syncthreads();
+#pragma unroll
+    for (int w = 0; w < kCountThreads / 32; ++w) {
+      const float4 v = wmax[w];
+      m.x = fmaxf(m.x, v.x), m.y = fmaxf(m.y, v.y), m.z = fmaxf(m.z, v.z), m.w = fmaxf(m.w, v.w);
+    }
+    TileBound TB[kPerWarp];
+#pragma unroll
+    for (int j = 0; j < kPerWarp; ++j) TB[j] = tile_bound(H[j], m);
     for (uint32_t i = lane; i < tn; i += 32) {
       const float4 c = tile[i];
 #pragma unroll
       for (int j = 0; j < kPerWarp; ++j) {
         if (!ok[j]) continue;
-        int r = inlier_fp32(H[j], c, t2);
+        int r = inlier_tile(H[j], TB[j], c, t2);
+        if (r < 0) r = inlier_fp32(H[j], c, t2);
         if (r < 0) {
           const int64_t h = q * A.iters + hb + warp * kPerWarp + j;
           const double* u64 = A.uv + 4 * ((size_t)b + t0 + i);
@@ -517,74 +690,6 @@ __device__ __forceinline__ double cta_sum_d(double v, double* red) {
   return t;
 }
 
-// Eigenvector of the smallest eigenvalue of the symmetric positive
-// semi-definite 9x9 M (row-major, in shared memory, overwritten) by inverse
-// iteration on its pivoted Cholesky factor; a pivot below 1e-30 trace(M) is
-// raised to that floor, so an exactly singular M yields its null vector.
-// Single thread.  The reference takes this eigenvector from nalgebra's
-// symmetric_eigen (geometry.rs:209-215); any accurate method gives it up to
-// sign and rounding when the smallest eigenvalue is simple.
-__device__ void smallest_eigvec9(double* M, double* v) {
-  int perm[9];
-  double tr = 0.0;
-  for (int i = 0; i < 9; ++i) perm[i] = i, tr += M[10 * i];
-  const double floor_d = 1e-30 * tr + 1e-300;
-  for (int k = 0; k < 9; ++k) {
-    int pk = k;
-    for (int i = k + 1; i < 9; ++i)
-      if (M[10 * i] > M[10 * pk]) pk = i;
-    if (pk != k) {  // symmetric swap of rows/columns k and pk
-      for (int j = 0; j < 9; ++j) {
-        const double t = M[9 * k + j];
-        M[9 * k + j] = M[9 * pk + j], M[9 * pk + j] = t;
-      }
-      for (int j = 0; j < 9; ++j) {
-        const double t = M[9 * j + k];
-        M[9 * j + k] = M[9 * j + pk], M[9 * j + pk] = t;
-      }
-      const int t = perm[k];
-      perm[k] = perm[pk], perm[pk] = t;
-    }
-    const double lkk = sqrt(fmax(M[10 * k], floor_d));
-    M[10 * k] = lkk;
-    const double rk = 1.0 / lkk;
-    for (int i = k + 1; i < 9; ++i) M[9 * i + k] *= rk;
-    for (int i = k + 1; i < 9; ++i)
-      for (int j = k + 1; j <= i; ++j) {
-        M[9 * i + j] -= M[9 * i + k] * M[9 * j + k];
-        M[9 * j + i] = M[9 * i + j];
-      }
-  }
-  // L in the lower triangle; P^T M P = L L^T.
-  double x[9];
-  for (int i = 0; i < 9; ++i) x[i] = 1.0 - 0.0625 * i;
-  for (int it = 0; it < 60; ++it) {
-    double y[9];
-    for (int i = 0; i < 9; ++i) y[i] = x[perm[i]];
-    for (int i = 0; i < 9; ++i) {  // L z = P^T x
-      double a = y[i];
-      for (int j = 0; j < i; ++j) a -= M[9 * i + j] * y[j];
-      y[i] = a / M[10 * i];
-    }
-    for (int i = 8; i >= 0; --i) {  // L^T w = z
-      double a = y[i];
-      for (int j = i + 1; j < 9; ++j) a -= M[9 * j + i] * y[j];
-      y[i] = a / M[10 * i];
-    }
-    double z[9], nn = 0.0;
-    for (int i = 0; i < 9; ++i) z[perm[i]] = y[i];
-    for (int i = 0; i < 9; ++i) nn += z[i] * z[i];
-    nn = 1.0 / sqrt(nn);
-    double dot = 0.0;
-    for (int i = 0; i < 9; ++i) z[i] *= nn, dot += z[i] * x[i];
-    const double sg = dot < 0.0 ? -1.0 : 1.0;
-    double diff = 0.0;
-    for (int i = 0; i < 9; ++i) diff = fmax(diff, fabs(sg * z[i] - x[i])), x[i] = sg * z[i];
-    if (it > 0 && diff <= 1e-15) break;
-  }
-  for (int i = 0; i < 9; ++i) v[i] = x[i];
-}
-
 // CTA per pair: the best hypothesis (the first with the most inliers), its
 // inliers, and one refit on them (geometry.rs:286-298), kept when it has at
 // least as many inliers.  The refit's centroid, mean distance and normal
@@ -672,7 +777,9 @@ __global__ void __launch_bounds__(kRefitThreads) ransac_select_kernel(RansacArgs
   __syncthreads();
   if (threadIdx.x == 0) {
     double fm[9], F[9];
-    smallest_eigvec9(Ms, fm);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) fm[i] = 1.0 - 0.0625 * i;
+    smallest_eigvec<9>(Ms, fm);
     const double ta[9] = {sA, 0.0, -sA * max_, 0.0, sA, -sA * may, 0.0, 0.0, 1.0};
     const double tb[9] = {sB, 0.0, -sB * mbx, 0.0, sB, -sB * mby, 0.0, 0.0, 1.0};
     ok_s = ep_finish(fm, ta, tb, F);

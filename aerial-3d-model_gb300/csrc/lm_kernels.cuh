@@ -297,10 +297,22 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
   du[3] = a01 * iz;
   du[4] = a11 * iz;
   du[5] = a01 * b02 + a11 * b12;
+  w = robust_weight(ev[0] * ev[0] + ev[1] * ev[1], sigma, P.loss);
+  // An observation of a point barely in front of its camera has |J| up to
+  // ~1e19 (w ~ 1e-24), and FP32 J^T J would overflow.  Such a record is
+  // stored whitened, sqrt(w) J and sqrt(w) e with weight 1: every use of the
+  // record is bilinear in (J, e) times w, so the sums are unchanged.  Other
+  // records keep J, e and w as they are.
+  double jmax = 0.0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) jmax = fmax(jmax, fabs(du[i]));
+  jmax *= fmax(1.0, fmax(fabs(xc[0]), fmax(fabs(xc[1]), fabs(xc[2]))));
+  const bool whiten = !(jmax < 1e12);
+  const double sw = whiten ? sqrt(w) : 1.0;
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     const double u0 = du[3 * r], u1 = du[3 * r + 1], u2 = du[3 * r + 2];
-    const float f0 = (float)u0, f1 = (float)u1, f2 = (float)u2;
+    const float f0 = (float)(u0 * sw), f1 = (float)(u1 * sw), f2 = (float)(u2 * sw);
     const float x0 = (float)xc[0], x1 = (float)xc[1], x2 = (float)xc[2];
     out[6 * r + 0] = f2 * x1 - f1 * x2;
     out[6 * r + 1] = f0 * x2 - f2 * x0;
@@ -308,25 +320,24 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       jp[3 * r + j] = u0 * Rm[j] + u1 * Rm[3 + j] + u2 * Rm[6 + j];
-      out[6 * r + 3 + j] = -(float)jp[3 * r + j];
-      out[12 + 3 * r + j] = (float)jp[3 * r + j];
+      out[6 * r + 3 + j] = -(float)(jp[3 * r + j] * sw);
+      out[12 + 3 * r + j] = (float)(jp[3 * r + j] * sw);
     }
   }
   if (refine) {  // ba.rs:87-95
-    out[18] = (float)qx;
-    out[19] = (float)(f * px * r2);
-    out[20] = (float)(f * px * r2 * r2);
-    out[21] = (float)qy;
-    out[22] = (float)(f * py * r2);
-    out[23] = (float)(f * py * r2 * r2);
+    out[18] = (float)(qx * sw);
+    out[19] = (float)(f * px * r2 * sw);
+    out[20] = (float)(f * px * r2 * r2 * sw);
+    out[21] = (float)(qy * sw);
+    out[22] = (float)(f * py * r2 * sw);
+    out[23] = (float)(f * py * r2 * r2 * sw);
   } else {
 #pragma unroll
     for (int i = 18; i < 24; ++i) out[i] = 0.0f;
   }
-  w = robust_weight(ev[0] * ev[0] + ev[1] * ev[1], sigma, P.loss);
-  out[24] = (float)ev[0];
-  out[25] = (float)ev[1];
-  out[26] = (float)w;
+  out[24] = (float)(ev[0] * sw);
+  out[25] = (float)(ev[1] * sw);
+  out[26] = whiten ? 1.0f : (float)w;
   out[27] = 1.0f;
   return true;
 }

@@ -20,6 +20,7 @@
 
 #include <cooperative_groups.h>
 
+#include "coarse.cuh"
 #include "pcg.cuh"
 
 namespace ba {
@@ -57,10 +58,29 @@ struct CgArgs {
   int32_t* iters;
   int32_t max_iter;
   double tol;
+  // Two-level (coarse) form only: see coarse.cuh.
+  const float* W;            // [nb * 42]
+  const float* Einv;         // per model, D x D
+  const int64_t* model_eoff; // [nm]
+  const int32_t* model_g0;   // [nm + 1]
+  const int32_t* grp_row0;   // [groups]
+  const int32_t* grp_row1;   // [groups]
+  const int32_t* job_g0;     // [grid]: this CTA's groups [job_g0, job_g1)
+  const int32_t* job_g1;
+  const uint32_t* grp_loc;   // [groups]: owner rank << 16 | local group slot
+  uint32_t cap_groups;       // group slots per CTA
+  uint32_t cap_dim;          // largest model coarse dimension
 };
 
 inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks) {
   return (size_t)cap_rows * kCgRow * 4 + (size_t)cap_blocks * (36 * 4 + 4);
+}
+
+// Extra shared memory of the two-level form: per row W (42) and W^T r (8);
+// per own group its rows of E^-1 (7 x D), w (7) and c (7); the gathered w of
+// the model (D).
+inline size_t cg_coarse_smem_bytes(uint32_t cap_rows, uint32_t cap_groups, uint32_t cap_dim) {
+  return ((size_t)cap_rows * (42 + 8) + (size_t)cap_groups * (7 * cap_dim + 14) + cap_dim) * 4;
 }
 
 // Sum over lanes 0..7 (lanes >= 8 hold 0); lanes 0..7 receive it.
@@ -130,14 +150,84 @@ __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&
 
 // Scalars of the iteration, computed by thread 0 and read by every thread.
 struct CgScalars {
-  double rz, b2, pq, beta;
+  double rz, b2, pq, beta, rzb;
   float af, bf;
   int stop;
 };
 
+// The coarse step of the two-level form after W^T r is published: gather the
+// model's w from its groups' owners, c = E^-1 w for this CTA's groups, then
+// z = z_B + W c on this CTA's rows; returns this CTA's share of w . c (thread
+// 0; the others return 0).
+__device__ __forceinline__ float cg_coarse_apply(cgx::cluster_group& cl, const CgArgs& A, int m,
+                                                 int32_t g0, int32_t ngr, float* rs, uint32_t nrows,
+                                                 const float* sW, const float* sEi, float* sw,
+                                                 float* swall, float* sc, uint32_t row0) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int32_t gm0 = A.model_g0[m];
+  const int D = kCoarseModes * (A.model_g0[m + 1] - gm0);
+  for (int t = threadIdx.x; t < D; t += kCgThreads) {
+    const uint32_t loc = A.grp_loc[gm0 + t / kCoarseModes];
+    const float* src = cl.map_shared_rank(sw, loc >> 16);
+    swall[t] = src[(loc & 0xffffu) * kCoarseModes + t % kCoarseModes];
+  }
+  __syncthreads();
+  for (int o = warp; o < ngr * kCoarseModes; o += kCgWarps) {
+    const float* er = sEi + (size_t)o * A.cap_dim;
+    float v = 0.0f;
+    for (int t = lane; t < D; t += 32) v += er[t] * swall[t];
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
+    if (lane == 0) sc[o] = v;
+  }
+  __syncthreads();
+  const bool vl = lane < 6;
+  const int ci = vl ? lane : 0;
+  for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
+    const int32_t l = (int32_t)__float_as_int(rs[(size_t)lr * kCgRow + kCgIdx + 3]);
+    if (l < 0 || !vl) continue;
+    const float* w = sW + (size_t)lr * 42 + kCoarseModes * ci;
+    const float* c = sc + kCoarseModes * l;
+    float add = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kCoarseModes; ++j) add += w[j] * c[j];
+    rs[(size_t)lr * kCgRow + kCgZ + ci] += add;
+  }
+  float wc = 0.0f;
+  if (threadIdx.x == 0)
+    for (int o = 0; o < ngr * kCoarseModes; ++o) wc += sw[o] * sc[o];
+  (void)g0;
+  (void)row0;
+  return wc;
+}
+
+// One row's W^T r (7 values) into t[0..6]: lane i < 6 holds r_i.
+__device__ __forceinline__ void cg_row_wtr(const float* w, float ri, float* t) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < kCoarseModes; ++j) {
+    const float v = cg_sum8f(lane < 6 ? w[kCoarseModes * lane + j] * ri : 0.0f);
+    if (lane == 0) t[j] = v;
+  }
+}
+
+// Per own group: w = sum over its rows of W^T r, in row order (thread per
+// group and mode); rows hold their W^T r in sT.
+__device__ __forceinline__ void cg_group_sums(int32_t ngr, const int32_t* grp_row0,
+                                              const int32_t* grp_row1, int32_t g0,
+                                              uint32_t row0, const float* sT, float* sw) {
+  for (int o = threadIdx.x; o < ngr * kCoarseModes; o += kCgThreads) {
+    const int l = o / kCoarseModes, j = o % kCoarseModes;
+    float v = 0.0f;
+    for (int32_t r = grp_row0[g0 + l]; r < grp_row1[g0 + l]; ++r) v += sT[(size_t)(r - row0) * 8 + j];
+    sw[o] = v;
+  }
+}
+
+template <bool kCoarse>
 static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A) {
   __shared__ float wsm[kCgWarps * 4];
-  __shared__ double part[2][4];
+  __shared__ double part[3][4];
   __shared__ double tot[4];
   __shared__ CgScalars sc;
   extern __shared__ __align__(16) unsigned char cg_smem[];
@@ -152,6 +242,16 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   float* rs = reinterpret_cast<float*>(cg_smem);
   float* sS = rs + (size_t)A.cap_rows * kCgRow;
   uint32_t* sL = reinterpret_cast<uint32_t*>(sS + (size_t)A.cap_blocks * 36);
+  // Two-level form: W and W^T r per row, E^-1 rows, w and c per own group,
+  // the gathered w.
+  float* sW = reinterpret_cast<float*>(sL + A.cap_blocks);
+  float* sT = sW + (size_t)A.cap_rows * 42;
+  float* sEi = sT + (size_t)A.cap_rows * 8;
+  float* sw = sEi + (size_t)A.cap_groups * kCoarseModes * A.cap_dim;
+  float* scf = sw + (size_t)A.cap_groups * kCoarseModes;
+  float* swall = scf + (size_t)A.cap_groups * kCoarseModes;
+  const int32_t cg0 = kCoarse ? A.job_g0[blockIdx.x] : 0;
+  const int32_t ngr = kCoarse ? A.job_g1[blockIdx.x] - cg0 : 0;
   const int32_t lens = A.lens_row[J.model];
   const uint32_t lens_loc = lens >= 0 ? A.row_loc[lens] : 0u;
   {
@@ -173,6 +273,23 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       st[kCgIdx] = __int_as_float((int)b0);
       st[kCgIdx + 1] = __int_as_float((int)b1);
       st[kCgIdx + 2] = __int_as_float((int32_t)row == lens ? -1 : A.lens_pos[row]);
+      int32_t lg = -1;  // local group slot (two-level form)
+      if constexpr (kCoarse)
+        for (int32_t l = 0; l < ngr; ++l)
+          if ((int32_t)row >= A.grp_row0[cg0 + l] && (int32_t)row < A.grp_row1[cg0 + l]) lg = l;
+      st[kCgIdx + 3] = __int_as_float(lg);
+    }
+    if constexpr (kCoarse) {
+      for (uint32_t t = threadIdx.x; t < nrows * 42; t += blockDim.x)
+        sW[t] = A.W[42 * (size_t)J.row0 + t];
+      const int32_t gm0 = A.model_g0[J.model];
+      const int D = kCoarseModes * (A.model_g0[J.model + 1] - gm0);
+      const float* Ei = A.Einv + A.model_eoff[J.model];
+      for (int t = threadIdx.x; t < ngr * kCoarseModes * D; t += blockDim.x) {
+        const int o = t / D, col = t % D;
+        sEi[(size_t)o * A.cap_dim + col] =
+            Ei[(size_t)(kCoarseModes * (cg0 - gm0) + o) * D + col];
+      }
     }
   }
   __syncthreads();
@@ -197,16 +314,28 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       drz += ri * zi;
       dbb += ri * ri;
     }
+    if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, ri, sT + (size_t)lr * 8);
+  }
+  if constexpr (kCoarse) {
+    __syncthreads();
+    cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sT, sw);
   }
   const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
   // The first barrier also makes every CTA's shared memory live for DSMEM.
   cg_reduce<2>(cl, w2, wsm, part[1], tot, [&] {
     sc.rz = tot[0];
+    sc.rzb = tot[0];
     sc.b2 = fmax(tot[1], 1e-300);
     sc.beta = 0.0;
     sc.bf = 0.0f;
     sc.stop = 0;
   });
+  if constexpr (kCoarse) {
+    const float wc = cg_coarse_apply(cl, A, J.model, cg0, ngr, rs, nrows, sW, sEi, sw, swall,
+                                     scf, J.row0);
+    const float w1[1] = {threadIdx.x == 0 ? wc : 0.0f};
+    cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] { sc.rz = sc.rzb + tot[0]; });
+  }
   int32_t spmv = 0;
   for (int32_t it = 0; it < A.max_iter; ++it) {
     const int cur = it & 1, prv = cur ^ 1;
@@ -304,15 +433,36 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         drr += ri * ri;
         drz2 += ri * zi;
       }
+      if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, ri, sT + (size_t)lr * 8);
+    }
+    if constexpr (kCoarse) {
+      __syncthreads();
+      cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sT, sw);
     }
     const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};
     cg_reduce<2>(cl, w2b, wsm, part[1], tot, [&] {
       sc.stop = tot[0] < A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
-      sc.beta = tot[1] / sc.rz;                    // ba.rs:189-190
-      sc.bf = (float)sc.beta;
-      sc.rz = tot[1];
+      if constexpr (kCoarse) {
+        sc.rzb = tot[1];  // r . B^-1 r; the coarse share follows
+      } else {
+        sc.beta = tot[1] / sc.rz;                  // ba.rs:189-190
+        sc.bf = (float)sc.beta;
+        sc.rz = tot[1];
+      }
     });
     if (sc.stop) break;
+    if constexpr (kCoarse) {
+      // z = B^-1 r + W E^-1 W^T r; r . z = r . B^-1 r + w . c.
+      const float wc = cg_coarse_apply(cl, A, J.model, cg0, ngr, rs, nrows, sW, sEi, sw, swall,
+                                       scf, J.row0);
+      const float w1[1] = {threadIdx.x == 0 ? wc : 0.0f};
+      cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] {
+        const double rzn = sc.rzb + tot[0];
+        sc.beta = rzn / sc.rz;
+        sc.bf = (float)sc.beta;
+        sc.rz = rzn;
+      });
+    }
   }
   for (uint32_t lr = warp; lr < nrows; lr += kCgWarps)
     if (vl) A.x[6 * (size_t)(J.row0 + lr) + ci] = CGROW(lr)[kCgX + ci];

@@ -162,6 +162,76 @@ inline bool plan_cluster(const Context& ctx, const std::vector<uint32_t>& row_pt
   return true;
 }
 
+// Coarse groups of the two-level preconditioner: each cluster CTA's camera
+// rows (the lens row excluded) split into runs of consecutive rows, about 8
+// rows each and at most kCoarseMaxGroups per model, so a group lives in one
+// CTA.
+struct CoarsePlan {
+  std::vector<int32_t> grp_row0, grp_row1, grp_model, model_g0, row_grp, job_g0, job_g1;
+  std::vector<int64_t> model_eoff;
+  std::vector<uint32_t> grp_loc;
+  uint32_t cap_groups = 0, dmax = 0;
+  int64_t e_total = 0;
+};
+
+inline void plan_coarse(const Context& ctx, const ClusterPlan& cp,
+                        const std::vector<int32_t>& lens_row, int csize, CoarsePlan& pl) {
+  pl = CoarsePlan{};
+  pl.row_grp.assign((size_t)ctx.nb, -1);
+  constexpr int kPerCtaMax = 4;  // group slots per CTA (shared memory)
+  for (int64_t m = 0; m < ctx.nm; ++m) {
+    pl.model_g0.push_back((int32_t)pl.grp_row0.size());
+    // Camera rows per CTA, then groups: about 8 rows each, at most
+    // kCoarseMaxGroups per model shared out in proportion to the rows
+    // (at least one for a CTA with camera rows).
+    std::vector<int64_t> nrow(csize), ng(csize, 0);
+    int64_t total = 0;
+    for (int k = 0; k < csize; ++k) {
+      const CgJob& J = cp.jobs[(size_t)m * csize + k];
+      uint32_t c1 = J.row1;
+      if (lens_row[m] >= 0 && (uint32_t)lens_row[m] >= J.row0 && (uint32_t)lens_row[m] < J.row1)
+        c1 = (uint32_t)lens_row[m];
+      nrow[k] = std::max<int64_t>(0, (int64_t)c1 - (int64_t)J.row0);
+      total += nrow[k];
+    }
+    int64_t want = 0;
+    for (int k = 0; k < csize; ++k) {
+      ng[k] = nrow[k] > 0 ? std::min<int64_t>(kPerCtaMax, (nrow[k] + 7) / 8) : 0;
+      want += ng[k];
+    }
+    while (want > kCoarseMaxGroups) {  // trim the CTA with the smallest groups
+      int best = -1;
+      double best_size = 1e300;
+      for (int k = 0; k < csize; ++k)
+        if (ng[k] > 1 && (double)nrow[k] / ng[k] < best_size)
+          best = k, best_size = (double)nrow[k] / ng[k];
+      if (best < 0) break;
+      --ng[best], --want;
+    }
+    for (int k = 0; k < csize; ++k) {
+      const CgJob& J = cp.jobs[(size_t)m * csize + k];
+      const int64_t n = nrow[k];
+      const int gk = (int)ng[k];
+      pl.job_g0.push_back((int32_t)pl.grp_row0.size());
+      for (int q = 0; q < gk; ++q) {
+        const int32_t a = (int32_t)(J.row0 + n * q / gk), b = (int32_t)(J.row0 + n * (q + 1) / gk);
+        const int32_t g = (int32_t)pl.grp_row0.size();
+        pl.grp_row0.push_back(a), pl.grp_row1.push_back(b), pl.grp_model.push_back((int32_t)m);
+        pl.grp_loc.push_back(((uint32_t)k << 16) | (uint32_t)q);
+        for (int32_t r = a; r < b; ++r) pl.row_grp[r] = g;
+      }
+      pl.job_g1.push_back((int32_t)pl.grp_row0.size());
+      pl.cap_groups = std::max(pl.cap_groups, (uint32_t)gk);
+    }
+    (void)total;
+    const int64_t D = kCoarseModes * ((int64_t)pl.grp_row0.size() - pl.model_g0.back());
+    pl.model_eoff.push_back(pl.e_total);
+    pl.e_total += D * D;
+    pl.dmax = std::max(pl.dmax, (uint32_t)D);
+  }
+  pl.model_g0.push_back((int32_t)pl.grp_row0.size());
+}
+
 template <typename T>
 void h2d(DevBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
   d.alloc(h.size(), s);
@@ -319,6 +389,15 @@ struct LmEngine {
   DevBuf<uint32_t> cg_loc;
   CgArgs ca{};
   size_t cg_smem = 0;
+  // Two-level preconditioner (mixed form, cluster kernel).
+  bool use_coarse = false;
+  DevBuf<float> cW, cE, cEinv;
+  DevBuf<int32_t> c_grp_row0, c_grp_row1, c_grp_model, c_model_g0, c_row_grp, c_job_g0, c_job_g1;
+  DevBuf<int64_t> c_model_eoff;
+  DevBuf<uint32_t> c_grp_loc;
+  CoarseArgs cargs{};
+  int32_t c_ngroups = 0;
+  size_t c_inv_smem = 0;
   PhaseTimer T;
 
   LmEngine(Context& c, const Opts& opts) : ctx(c), o(opts), s(c.stream) {
@@ -445,6 +524,8 @@ struct LmEngine {
   // Matrix-free PCG: one cooperative launch over every SM, one group.
   void setup_implicit() {
     use_cluster = false;
+    use_coarse = false;
+    ctx.last_coarse_dim = 0;
     int occ = 0;
     check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_implicit_kernel<R>, kPcgThreads,
                                                         0),
@@ -462,6 +543,8 @@ struct LmEngine {
   // Grid kernel plan: about rows_target block rows per CTA.
   void plan_grid(int rows_target) {
     use_cluster = false;
+    use_coarse = false;
+    ctx.last_coarse_dim = 0;
     plan = detail::plan_pcg(ctx, SB.h_row_ptr, h_lens, max_ctas, rows_target, (int)smem_rows);
     detail::h2d(jobs, plan.jobs, s);
     detail::h2d(cta_job0, plan.cta_job0, s);
@@ -494,23 +577,33 @@ struct LmEngine {
     int smem_optin = 0;
     check(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx.device),
           "attr");
+    const bool coarse = o.coarse != 0;
+    const auto kfn = coarse ? pcg_cluster_kernel<true> : pcg_cluster_kernel<false>;
     cudaFuncAttributes fa{};
-    check(cudaFuncGetAttributes(&fa, pcg_cluster_kernel), "func attr");
+    check(cudaFuncGetAttributes(&fa, kfn), "func attr");
     const size_t avail = (size_t)smem_optin - fa.sharedSizeBytes;
     const uint32_t rows_cap = (uint32_t)std::min<size_t>(avail / 2 / (kCgRow * 4), 4096);
     detail::ClusterPlan cp;
     if (!detail::plan_cluster(ctx, SB.h_row_ptr, h_lens, csize, rows_cap, cp))
       return unusable("a model has too many block rows for one cluster");
     if (cp.max_blocks == 0 && cp.max_rows == 0) return unusable("empty plan");
+    detail::CoarsePlan gp;
+    size_t coarse_bytes = 0;
+    if (coarse) {
+      detail::plan_coarse(ctx, cp, h_lens, csize, gp);
+      coarse_bytes = cg_coarse_smem_bytes(cp.max_rows, std::max(gp.cap_groups, 1u), std::max(gp.dmax, 1u));
+      if (coarse_invert_smem((int)gp.dmax) > (size_t)smem_optin)
+        return unusable("coarse system too large");
+    }
     const size_t row_bytes = (size_t)cp.max_rows * kCgRow * 4;
-    const uint32_t cap_blocks = (uint32_t)std::min<size_t>(cp.max_blocks, (avail - row_bytes) / (36 * 4 + 4));
-    const size_t smem = cg_smem_bytes(cp.max_rows, cap_blocks);
-    check(cudaFuncSetAttribute(pcg_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem),
+    if (row_bytes + coarse_bytes >= avail) return unusable("row state does not fit");
+    const uint32_t cap_blocks = (uint32_t)std::min<size_t>(
+        cp.max_blocks, (avail - row_bytes - coarse_bytes) / (36 * 4 + 4));
+    const size_t smem = cg_smem_bytes(cp.max_rows, cap_blocks) + coarse_bytes;
+    check(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
           "cluster smem");
     if (csize > 8)
-      check(cudaFuncSetAttribute(pcg_cluster_kernel,
-                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+      check(cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
             "cluster size");
     cudaLaunchConfig_t cfg{};
     cudaLaunchAttribute attr[1];
@@ -525,7 +618,7 @@ struct LmEngine {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    const cudaError_t oe = cudaOccupancyMaxActiveClusters(&nclusters, pcg_cluster_kernel, &cfg);
+    const cudaError_t oe = cudaOccupancyMaxActiveClusters(&nclusters, kfn, &cfg);
     if (oe != cudaSuccess || nclusters < 1) {
       cudaGetLastError();
       return unusable(std::string("no cluster of ") + std::to_string(csize) + " CTAs with " +
@@ -538,10 +631,33 @@ struct LmEngine {
     if (!required && !prefer_cluster && (int64_t)nclusters < ctx.nm) return false;
     detail::h2d(cg_jobs, cp.jobs, s);
     detail::h2d(cg_loc, cp.row_loc, s);
-    check(cudaStreamSynchronize(s), "sync");
     ca = CgArgs{cg_jobs, cg_loc, SB.row_ptr, SB.col_idx, (const float*)S.p, (const float*)pre.p,
                 (const float*)g.p, (float*)x.p, lens_row, lens_pos, SB.diag_pos, cp.max_rows,
                 cap_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol};
+    use_coarse = coarse;
+    ctx.last_coarse_dim = 0;
+    if (coarse) {
+      detail::h2d(c_grp_row0, gp.grp_row0, s), detail::h2d(c_grp_row1, gp.grp_row1, s);
+      detail::h2d(c_grp_model, gp.grp_model, s), detail::h2d(c_model_g0, gp.model_g0, s);
+      detail::h2d(c_row_grp, gp.row_grp, s), detail::h2d(c_job_g0, gp.job_g0, s);
+      detail::h2d(c_job_g1, gp.job_g1, s), detail::h2d(c_model_eoff, gp.model_eoff, s);
+      detail::h2d(c_grp_loc, gp.grp_loc, s);
+      cW.alloc(detail::at_least_1(ctx.nb) * kCoarseW, s);
+      cE.alloc(detail::at_least_1(gp.e_total), s), cEinv.alloc(detail::at_least_1(gp.e_total), s);
+      c_ngroups = (int32_t)gp.grp_row0.size();
+      cargs = CoarseArgs{c_ngroups, c_grp_row0, c_grp_row1, c_grp_model, c_model_g0,
+                         c_model_eoff, c_row_grp, active, cW, cE, cEinv};
+      c_inv_smem = coarse_invert_smem((int)gp.dmax);
+      check(cudaFuncSetAttribute(coarse_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)c_inv_smem),
+            "coarse smem");
+      ca.W = cW, ca.Einv = cEinv, ca.model_eoff = c_model_eoff, ca.model_g0 = c_model_g0;
+      ca.grp_row0 = c_grp_row0, ca.grp_row1 = c_grp_row1, ca.job_g0 = c_job_g0;
+      ca.job_g1 = c_job_g1, ca.grp_loc = c_grp_loc;
+      ca.cap_groups = std::max(gp.cap_groups, 1u), ca.cap_dim = std::max(gp.dmax, 1u);
+      ctx.last_coarse_dim = (int32_t)gp.dmax;
+    }
+    check(cudaStreamSynchronize(s), "sync");
     cg_smem = smem;
     cl_size = csize;
     use_cluster = true;
@@ -668,6 +784,13 @@ struct LmEngine {
                                         dim3(kPcgThreads), args, 0, s),
             "pcg launch");
     } else if (use_cluster) {
+      if (use_coarse && c_ngroups > 0) {
+        BA_LAUNCH(coarse_basis_kernel<<<grid_for(c_ngroups, 64), 64, 0, s>>>(P, ctx.cur(), cargs));
+        BA_LAUNCH(coarse_matrix_kernel<<<(unsigned)c_ngroups, kCoarseMatThreads, 0, s>>>(
+            SV, (const float*)S.p, cargs));
+        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kCoarseInvThreads, c_inv_smem, s>>>(
+            cargs));
+      }
       cudaLaunchConfig_t cfg{};
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -680,7 +803,10 @@ struct LmEngine {
       cfg.stream = s;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      check(cudaLaunchKernelEx(&cfg, pcg_cluster_kernel, ca), "pcg cluster launch");
+      if (use_coarse)
+        check(cudaLaunchKernelEx(&cfg, pcg_cluster_kernel<true>, ca), "pcg cluster launch");
+      else
+        check(cudaLaunchKernelEx(&cfg, pcg_cluster_kernel<false>, ca), "pcg cluster launch");
     } else {
       void* args[] = {&pa};
       check(cudaLaunchCooperativeKernel((void*)pcg_kernel<R>, dim3(plan.ncta), dim3(kPcgThreads),

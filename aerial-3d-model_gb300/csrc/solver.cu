@@ -232,6 +232,7 @@ Opts resolve_options(const ba_options* o) {
     r.graph = o->no_graph ? 0 : 1;
     r.autotune = o->autotune;
     r.stop_patience = o->stop_patience;
+    r.coarse = o->coarse;
   }
   if (r.max_iter < 0) throw BadInput("max_iter must be >= 0");
   if (!(r.sigma > 0.0) || !std::isfinite(r.sigma)) throw BadInput("sigma_px must be finite and > 0");
@@ -240,6 +241,7 @@ Opts resolve_options(const ba_options* o) {
   if (r.matrix_free < 0 || r.matrix_free > 2) throw BadInput("unknown matrix_free mode");
   if (r.pcg_kernel < 0 || r.pcg_kernel > 2) throw BadInput("unknown pcg_kernel");
   if (r.stop_patience < 0) throw BadInput("stop_patience must be >= 0");
+  if (r.coarse != 0 && r.coarse != 1) throw BadInput("coarse must be 0 or 1");
   return r;
 }
 
@@ -345,6 +347,7 @@ void solve(Context& c, const ba_options* opt, ba_stats* stats) {
       st.pcg_cluster = c.last_pcg_cluster;
       st.graph = c.last_graph ? 1 : 0;
       st.pcg_ctas = c.last_pcg_ctas;
+      st.pcg_coarse_dim = c.last_coarse_dim;
       st.pcg_tuned_us = c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].valid
                             ? c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].us_per_iter
                             : 0.0;

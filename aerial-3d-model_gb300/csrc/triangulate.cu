@@ -163,8 +163,11 @@ __global__ void __launch_bounds__(kTriThreads) triangulate_kernel(TriArgs T) {
   }
   bool ok = ng >= 2;
   if (ok) {
-    // max_ray_angle over the kept observations' unit rays.
-    double best_a = 0.0;
+    // max_ray_angle over the kept observations' unit rays (each normalised
+    // once, as the reference does): acos is decreasing, so the largest angle
+    // is acos of the smallest clamped dot product, the same value the
+    // reference's running max of acos keeps.
+    double min_d = 1.0;
     for (uint32_t i = b; i < e; ++i) {
       if (!T.good[i]) continue;
       const double* Ci = T.center + 3 * (size_t)T.obs_cam[i];
@@ -177,12 +180,11 @@ __global__ void __launch_bounds__(kTriThreads) triangulate_kernel(TriArgs T) {
         double rj[3] = {X[0] - Cj[0], X[1] - Cj[1], X[2] - Cj[2]};
         const double lj = sqrt(rj[0] * rj[0] + rj[1] * rj[1] + rj[2] * rj[2]);
         rj[0] /= lj, rj[1] /= lj, rj[2] /= lj;
-        double d = ri[0] * rj[0] + ri[1] * rj[1] + ri[2] * rj[2];
-        d = fmin(1.0, fmax(-1.0, d));
-        best_a = fmax(best_a, acos(d));
+        const double d = ri[0] * rj[0] + ri[1] * rj[1] + ri[2] * rj[2];
+        min_d = fmin(min_d, fmin(1.0, fmax(-1.0, d)));
       }
     }
-    const double deg = best_a * (180.0 / 3.14159265358979323846);
+    const double deg = acos(min_d) * (180.0 / 3.14159265358979323846);
     ok = ng >= 3 ? deg > 2.0 : deg > 6.0;  // sparse.rs:411-415
   }
   if (!ok) {

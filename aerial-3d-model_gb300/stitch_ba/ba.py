@@ -37,6 +37,7 @@ class Options:
     graph: bool = True            # replay a CUDA graph per LM iteration
     autotune: bool = False        # time PCG configurations on the first solve of a form
     stop_patience: int = 0        # consecutive small accepted steps before stopping (0/1: ba.rs rule)
+    coarse: bool = False          # mixed form, cluster PCG: two-level preconditioner
 
 
 @dataclass
@@ -66,6 +67,7 @@ class SolveInfo:
     graph: bool = False           # LM iterations replayed a CUDA graph
     pcg_ctas: int = 0             # CTAs of the PCG launch
     pcg_tuned_us: float = 0.0     # autotuned time per PCG iteration (0: not tuned)
+    coarse_dim: int = 0           # coarse unknowns of the two-level preconditioner
 
     def stats(self) -> BaStats:
         return BaStats(self.iterations, self.initial_rms, self.final_rms)
@@ -92,6 +94,7 @@ def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> n
     c.no_graph = 0 if o.graph else 1
     c.autotune = 1 if o.autotune else 0
     c.stop_patience = int(o.stop_patience)
+    c.coarse = 1 if o.coarse else 0
     c.log = C.cast(C.pointer(log), C.c_void_p) if log is not None else None
     return c
 
@@ -134,6 +137,7 @@ def _info(s: native.BaStatsC) -> SolveInfo:
     info.graph = bool(s.graph)
     info.pcg_ctas = s.pcg_ctas
     info.pcg_tuned_us = s.pcg_tuned_us
+    info.coarse_dim = s.pcg_coarse_dim
     return info
 
 

@@ -52,7 +52,7 @@ class BaOptions(C.Structure):
                 ("matrix_free", C.c_int32), ("memory_cap_bytes", C.c_int64),
                 ("stream", C.c_void_p), ("log", C.c_void_p), ("profile", C.c_int32),
                 ("pcg_kernel", C.c_int32), ("no_graph", C.c_int32), ("autotune", C.c_int32),
-                ("stop_patience", C.c_int32)]
+                ("stop_patience", C.c_int32), ("coarse", C.c_int32)]
 
 
 class BaStatsC(C.Structure):
@@ -66,7 +66,8 @@ class BaStatsC(C.Structure):
                 ("n_blocks", C.c_int64), ("n_nonzero_blocks", C.c_int64),
                 ("n_schur_pairs", C.c_int64), ("n_lens_entries", C.c_int64),
                 ("pcg_kernel", C.c_int32), ("pcg_cluster", C.c_int32), ("graph", C.c_int32),
-                ("pcg_ctas", C.c_int32), ("pcg_tuned_us", C.c_double)]
+                ("pcg_ctas", C.c_int32), ("pcg_tuned_us", C.c_double),
+                ("pcg_coarse_dim", C.c_int32)]
 
 PHASES = ["point", "camera", "schur", "assemble", "pcg", "update", "cost", "control", "setup"]
 

@@ -123,6 +123,11 @@ typedef struct ba_options {
   int32_t stop_patience; /* LM stops after this many consecutive accepted
                            steps with relative decrease < 1e-6; 0 or 1:
                            the reference's rule (ba.rs:372-374)          */
+  int32_t coarse;       /* mixed form, cluster PCG: 1 adds a coarse correction
+                           to the block-Jacobi preconditioner (the seven
+                           similarity motions of each group of consecutive
+                           cameras, up to 32 groups per model); 0: the
+                           reference's block-Jacobi alone                 */
 } ba_options;
 
 /* Kernel phases timed when ba_options.profile is set (ba_stats.ms_phase). */
@@ -164,6 +169,8 @@ typedef struct ba_stats {
   int32_t graph;          /* 1 if the LM iterations replayed a CUDA graph  */
   int32_t pcg_ctas;       /* CTAs of the PCG launch                        */
   double pcg_tuned_us;    /* autotuner's time per PCG iteration (0: none)  */
+  int32_t pcg_coarse_dim; /* coarse unknowns of the two-level preconditioner
+                             (largest model), 0: block-Jacobi alone       */
 } ba_stats;
 
 /* Defaults: max_iter 60, sigma_px 1, Cauchy, FP64, PCG 400 / 1e-20. */

@@ -128,3 +128,45 @@ def test_memory_cap_switches_to_matrix_free():
     _, st2, info2 = solve(p, Options(), sigma=1.0)
     assert info2.pcg_kernel == "grid"
     assert abs(info.final_cost - info2.final_cost) <= 1e-6 * info2.final_cost
+
+
+def test_coarse_preconditioner_reaches_fp64_cost_in_fewer_pcg_iterations():
+    """The mixed form's two-level preconditioner (block Jacobi plus the
+    similarity motions of camera groups) keeps the final cost and needs far
+    fewer PCG iterations per LM step than block Jacobi at the same cap."""
+    p, _ = survey.generate("lawnmower77", seed=3, n_cams=48, n_points=16000)
+    _, _, f64 = solve(p, Options(), sigma=1.0)
+    _, _, bj = solve(p, Options(precision="mixed", pcg_kernel="cluster", pcg_max_iter=40),
+                     sigma=1.0)
+    _, _, two = solve(p, Options(precision="mixed", pcg_kernel="cluster", pcg_max_iter=40,
+                                 coarse=True), sigma=1.0)
+    assert two.coarse_dim > 0 and bj.coarse_dim == 0
+    assert two.final_cost <= f64.final_cost * (1.0 + 1e-6), (two.final_cost, f64.final_cost)
+    # one system: the two-level PCG gets closer to the exact step in 20 iterations
+    ctxs = []
+    for coarse in (False, True):
+        with stitch_ba.Context() as ctx:
+            ctx.upload(p.copy())
+            ctxs.append(ctx.debug_step(1e-4, 1.0, Options(precision="mixed", pcg_kernel="cluster",
+                                                          pcg_max_iter=20, coarse=coarse)))
+    with stitch_ba.Context() as ctx:
+        ctx.upload(p.copy())
+        exact = ctx.debug_step(1e-4, 1.0, Options())
+    xs = np.linalg.solve(exact["S"], exact["g"])
+
+    def err(r):
+        e = r["dx"] - xs
+        return np.sqrt(e @ exact["S"] @ e / (xs @ exact["S"] @ xs))
+
+    assert err(ctxs[1]) < 0.5 * err(ctxs[0]), (err(ctxs[1]), err(ctxs[0]))
+
+
+def test_coarse_option_is_inert_for_fp64_and_graph_replay_matches():
+    p, _ = ref_survey()
+    _, _, a = solve(p, Options(coarse=True))
+    _, _, b = solve(p, Options())
+    assert a.coarse_dim == 0 and a.final_cost == b.final_cost
+    _, _, c = solve(p, Options(precision="mixed", pcg_kernel="cluster", coarse=True, graph=True))
+    _, _, d = solve(p, Options(precision="mixed", pcg_kernel="cluster", coarse=True, graph=False))
+    assert c.coarse_dim > 0 and c.graph and not d.graph
+    assert c.final_cost == d.final_cost and c.iterations == d.iterations
