@@ -83,162 +83,247 @@ static __global__ void coarse_basis_kernel(Prob P, StateView st, CoarseArgs A) {
   }
 }
 
-// E = W^T S W, rows of one group per CTA: the group's rows in order, and
-// within a row every column group's blocks by one warp (no two warps add to
-// the same entries while a row is processed), so the sums are in a fixed
+// E = W^T S W in two passes, both in a fixed order.  (1) A warp per (camera
+// row r, group g of r's model): P[r][g] = W_r^T (sum over r's blocks in g's
+// columns of S_rc W_c), 7 x 7, zero when r has no block there.  (2) A thread
+// per entry of E: the sum of P over the rows of the entry's row group, in row
 // order.  S: FP32 BSR, full symmetric storage.
 constexpr int kCoarseMatThreads = 256;
 
 static __global__ void __launch_bounds__(kCoarseMatThreads)
-    coarse_matrix_kernel(StructView SV, const float* S, CoarseArgs A) {
-  __shared__ float acc[kCoarseModes * kCoarseMaxDim];
+    coarse_rowgroup_kernel(StructView SV, const float* S, CoarseArgs A, int64_t npairs,
+                           const int32_t* pair_row, const int32_t* pair_grp, float* Pbuf) {
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= npairs) return;
+  const int32_t r = pair_row[wid], g = pair_grp[wid];
+  float* P = Pbuf + (size_t)wid * 49;
+  if (!A.active[A.grp_model[g]]) return;
+  // Blocks of row r whose columns lie in rows [c0, c1) of group g.
+  const int32_t c0 = A.grp_row0[g], c1 = A.grp_row1[g];
+  uint32_t lo = SV.row_ptr[r], hi = SV.row_ptr[r + 1];
+  {
+    uint32_t a0 = lo, a1 = hi;
+    while (a0 < a1) {
+      const uint32_t mid = (a0 + a1) >> 1;
+      if ((int32_t)SV.col_idx[mid] < c0) a0 = mid + 1; else a1 = mid;
+    }
+    lo = a0;
+    a1 = hi;
+    while (a0 < a1) {
+      const uint32_t mid = (a0 + a1) >> 1;
+      if ((int32_t)SV.col_idx[mid] < c1) a0 = mid + 1; else a1 = mid;
+    }
+    hi = a0;
+  }
+  // T = sum_k S_k W_col(k) (6 x 7): lane = 7 q + j handles column j of the
+  // blocks lo + q, lo + q + 4, ... (q < 4); the four partials are summed in
+  // order q = 0..3.
+  const int q = lane / 7, j = lane - 7 * (lane / 7);
+  float t[6] = {0, 0, 0, 0, 0, 0};
+  if (q < 4)
+    for (uint32_t k = lo + q; k < hi; k += 4) {
+      const float* blk = S + (size_t)k * 36;
+      const float* Wc = A.W + (size_t)SV.col_idx[k] * kCoarseW;
+      float wc[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) wc[i] = Wc[kCoarseModes * i + j];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        float v = t[i];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v += blk[6 * i + c] * wc[c];
+        t[i] = v;
+      }
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const float v1 = __shfl_down_sync(kFull, t[i], 7), v2 = __shfl_down_sync(kFull, t[i], 14),
+                v3 = __shfl_down_sync(kFull, t[i], 21);
+    t[i] = ((t[i] + v1) + v2) + v3;  // lanes 0..6: column j summed over q
+  }
+  if (lane < kCoarseModes) {
+    const float* Wr = A.W + (size_t)r * kCoarseW;
+#pragma unroll
+    for (int a = 0; a < kCoarseModes; ++a) {
+      float v = 0.0f;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) v += Wr[kCoarseModes * i + a] * t[i];
+      P[a * kCoarseModes + lane] = v;
+    }
+  }
+}
+
+// E entry (7 g1 + a, 7 g2 + b) of model m = sum over rows r of group g1 of
+// P[r][g2][a][b]; pairs are listed row-major by (row, group of the model).
+static __global__ void coarse_sum_kernel(CoarseArgs A, const int64_t* row_pair0,
+                                         const float* Pbuf) {
   const int g1 = blockIdx.x;
   const int m = A.grp_model[g1];
   if (!A.active[m]) return;
   const int gm0 = A.model_g0[m];
-  const int D = kCoarseModes * (A.model_g0[m + 1] - gm0);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int t = threadIdx.x; t < kCoarseModes * D; t += kCoarseMatThreads) acc[t] = 0.0f;
-  __syncthreads();
-  for (int r = A.grp_row0[g1]; r < A.grp_row1[g1]; ++r) {
-    const uint32_t b0 = SV.row_ptr[r], b1 = SV.row_ptr[r + 1];
-    const float* Wr = A.W + (size_t)r * kCoarseW;
-    // Segments of consecutive blocks with the same column group (columns are
-    // sorted and groups are runs of consecutive rows).  Warp w takes the
-    // segments w, w + 8, ...: found by a scan of the row by every warp.
-    int sidx = 0;
-    uint32_t k = b0;
-    while (k < b1) {
-      const int gc = A.row_grp[SV.col_idx[k]];
-      uint32_t e = k + 1;
-      while (e < b1 && A.row_grp[SV.col_idx[e]] == gc) ++e;
-      if (gc >= 0 && (sidx % (kCoarseMatThreads / 32)) == warp) {
-        // T = sum_k S_k W_col(k) (6 x 7): lane j < 7 owns column j.
-        float t[6] = {0, 0, 0, 0, 0, 0};
-        if (lane < kCoarseModes) {
-          for (uint32_t q = k; q < e; ++q) {
-            const float* blk = S + (size_t)q * 36;
-            const float* Wc = A.W + (size_t)SV.col_idx[q] * kCoarseW;
-            float wc[6];
-#pragma unroll
-            for (int i = 0; i < 6; ++i) wc[i] = Wc[kCoarseModes * i + lane];
-#pragma unroll
-            for (int i = 0; i < 6; ++i) {
-              float s = t[i];
-#pragma unroll
-              for (int j = 0; j < 6; ++j) s += blk[6 * i + j] * wc[j];
-              t[i] = s;
-            }
-          }
-          // P[:, lane] = W_r^T T[:, lane]
-          const int col = kCoarseModes * (gc - gm0) + lane;
-#pragma unroll
-          for (int a = 0; a < kCoarseModes; ++a) {
-            float s = 0.0f;
-#pragma unroll
-            for (int i = 0; i < 6; ++i) s += Wr[kCoarseModes * i + a] * t[i];
-            acc[a * D + col] += s;
-          }
-        }
-      }
-      if (gc >= 0) ++sidx;
-      k = e;
-    }
-    __syncthreads();
-  }
+  const int G = A.model_g0[m + 1] - gm0;
+  const int D = kCoarseModes * G;
   float* Em = A.E + A.model_eoff[m];
-  const int row0 = kCoarseModes * (g1 - gm0);
-  for (int t = threadIdx.x; t < kCoarseModes * D; t += kCoarseMatThreads)
-    Em[(size_t)(row0 + t / D) * D + (t % D)] = acc[t];
+  for (int t = threadIdx.x; t < kCoarseModes * D; t += blockDim.x) {
+    const int a = t / D, col = t - (t / D) * D;
+    const int g2 = col / kCoarseModes, bcol = col - kCoarseModes * g2;
+    float v = 0.0f;
+    for (int32_t r = A.grp_row0[g1]; r < A.grp_row1[g1]; ++r)
+      v += Pbuf[(size_t)(row_pair0[r] + g2) * 49 + a * kCoarseModes + bcol];
+    Em[(size_t)(kCoarseModes * (g1 - gm0) + a) * D + col] = v;
+  }
 }
 
-// E^-1 per model (CTA per model): Jacobi scaling, then in-place Gauss-Jordan
-// without pivoting (E is symmetric positive definite).  The 32 x 32 threads
-// each hold a T x T tile of the matrix in registers (T = ceil(D / 32) <= 7);
-// per pivot the owners publish the pivot row and column in shared memory and
-// every thread updates its tile (T <= 6 keeps the tile in registers at
-// 1024 threads).  A coarse unknown whose scaled pivot falls
-// below 1e-6 is dropped (its row and column of the inverse are zero).  The
-// result is unscaled and symmetrised.
-constexpr int kInvTile = (kCoarseMaxDim + 31) / 32;  // 6
+// E^-1 per model (CTA per model): Jacobi scaling, then in-place block
+// Gauss-Jordan without pivoting (E is symmetric positive definite), four
+// pivots per step.  The 16 x 32 threads each hold a TR x TC tile of the
+// matrix in registers (TR = ceil(D / 16) <= 12, TC = ceil(D / 32) <= 6; 512
+// threads leave 128 registers each); per step the owners publish
+// the four pivot rows and columns in shared memory, every thread inverts the
+// 4 x 4 pivot block (a scalar pivot below 1e-6 of the scaled unit diagonal is
+// raised to 1e-6) and updates its tile.  The result is unscaled and
+// symmetrised.
+constexpr int kInvThreads = 512;
+constexpr int kInvTR = (kCoarseMaxDim + 15) / 16;  // 12
+constexpr int kInvTC = (kCoarseMaxDim + 31) / 32;  // 6
+constexpr int kInvB = 4;                           // pivots per step
+constexpr int kInvDimPad = ((kCoarseMaxDim + kInvB - 1) / kInvB) * kInvB;
 
-static __global__ void __launch_bounds__(kCoarseInvThreads, 1) coarse_invert_kernel(CoarseArgs A) {
-  __shared__ float rowk[kCoarseMaxDim], colk[kCoarseMaxDim], dsc[kCoarseMaxDim];
+static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(CoarseArgs A) {
+  __shared__ float rowb[kInvB][kInvDimPad], colb[kInvDimPad][kInvB], dsc[kInvDimPad];
+  __shared__ float rnS[kInvB][kInvDimPad], cnS[kInvDimPad][kInvB];
   const int m = blockIdx.x;
   if (!A.active[m]) return;
   const int D = kCoarseModes * (A.model_g0[m + 1] - A.model_g0[m]);
   if (D == 0) return;
-  const int T = (D + 31) / 32;
-  const int i0 = (threadIdx.x >> 5) * T, j0 = (threadIdx.x & 31) * T;
+  const int TR = (D + 15) / 16, TC = (D + 31) / 32;
+  const int i0 = (threadIdx.x >> 5) * TR, j0 = (threadIdx.x & 31) * TC;
   float* Em = A.E + A.model_eoff[m];
-  for (int i = threadIdx.x; i < D; i += blockDim.x) {
-    const float d = Em[(size_t)i * D + i];
+  for (int i = threadIdx.x; i < kInvDimPad; i += blockDim.x) {
+    const float d = i < D ? Em[(size_t)i * D + i] : 0.0f;
     dsc[i] = d > 0.0f ? rsqrtf(d) : 0.0f;
   }
   __syncthreads();
-  float a[kInvTile][kInvTile];
+  // Padding rows/columns up to a multiple of four are identity.
+  const int Dp = ((D + kInvB - 1) / kInvB) * kInvB;
+  float a[kInvTR][kInvTC];
 #pragma unroll
-  for (int r = 0; r < kInvTile; ++r)
+  for (int r = 0; r < kInvTR; ++r)
 #pragma unroll
-    for (int c = 0; c < kInvTile; ++c) {
+    for (int c = 0; c < kInvTC; ++c) {
       const int i = i0 + r, j = j0 + c;
       float v = 0.0f;
-      if (r < T && c < T && i < D && j < D) {
-        if (dsc[i] == 0.0f || dsc[j] == 0.0f)
+      if (r < TR && c < TC && i < Dp && j < Dp) {
+        if (i >= D || j >= D || dsc[i] == 0.0f || dsc[j] == 0.0f)
           v = i == j ? 1.0f : 0.0f;
         else  // symmetrise the assembled E (FP32 sums in two orders) while scaling
           v = 0.5f * (Em[(size_t)i * D + j] + Em[(size_t)j * D + i]) * dsc[i] * dsc[j];
       }
       a[r][c] = v;
     }
-  for (int k = 0; k < D; ++k) {
-    __syncthreads();  // the previous pivot's row and column have been used
-    const int rk = k - i0, ck = k - j0;
-    // Only the owners of row k and column k publish them (rk, ck < T).
+  for (int k0 = 0; k0 < Dp; k0 += kInvB) {
+    __syncthreads();  // the previous step's rows and columns have been used
 #pragma unroll
-    for (int r = 0; r < kInvTile; ++r)
-      if (r == rk && r < T)
+    for (int r = 0; r < kInvTR; ++r) {
+      const int i = i0 + r, br = i - k0;
+      if (r < TR && br >= 0 && br < kInvB)
 #pragma unroll
-        for (int c = 0; c < kInvTile; ++c)
-          if (c < T && j0 + c < D) rowk[j0 + c] = a[r][c];
+        for (int c = 0; c < kInvTC; ++c)
+          if (c < TC && j0 + c < Dp) rowb[br][j0 + c] = a[r][c];
+    }
 #pragma unroll
-    for (int c = 0; c < kInvTile; ++c)
-      if (c == ck && c < T)
+    for (int c = 0; c < kInvTC; ++c) {
+      const int j = j0 + c, bc = j - k0;
+      if (c < TC && bc >= 0 && bc < kInvB)
 #pragma unroll
-        for (int r = 0; r < kInvTile; ++r)
-          if (r < T && i0 + r < D) colk[i0 + r] = a[r][c];
+        for (int r = 0; r < kInvTR; ++r)
+          if (r < TR && i0 + r < Dp) colb[i0 + r][bc] = a[r][c];
+    }
     __syncthreads();
-    const float piv = rowk[k];
-    const bool drop = !(piv > 1e-6f);
-    const float rp = drop ? 0.0f : 1.0f / piv;
-    float rj[kInvTile];
+    // Inverse of the 4 x 4 pivot block (scalar Gauss-Jordan, registers),
+    // then shared: rn = Pinv * (pivot rows), with Pinv itself in the pivot
+    // columns, and cn = -(pivot columns) * Pinv.
+    {
+      float pb[kInvB][kInvB];
 #pragma unroll
-    for (int c = 0; c < kInvTile; ++c) rj[c] = j0 + c < D ? rowk[j0 + c] * rp : 0.0f;
+      for (int x = 0; x < kInvB; ++x)
 #pragma unroll
-    for (int r = 0; r < kInvTile; ++r) {
-      const int i = i0 + r;
-      const float ci = i < D ? colk[i] : 0.0f;
+        for (int y = 0; y < kInvB; ++y) pb[x][y] = rowb[x][k0 + y];
 #pragma unroll
-      for (int c = 0; c < kInvTile; ++c) {
-        const int j = j0 + c;
-        float v = a[r][c];
-        if (i == k)
-          v = drop ? 0.0f : (j == k ? rp : rj[c]);
-        else if (j == k)
-          v = drop ? 0.0f : -ci * rp;
-        else if (!drop)
-          v -= ci * rj[c];
-        a[r][c] = v;
+      for (int kk = 0; kk < kInvB; ++kk) {
+        const float rp = 1.0f / fmaxf(pb[kk][kk], 1e-6f);
+        float rk[kInvB], ck[kInvB];
+#pragma unroll
+        for (int y = 0; y < kInvB; ++y) rk[y] = y == kk ? rp : pb[kk][y] * rp;
+#pragma unroll
+        for (int x = 0; x < kInvB; ++x) ck[x] = pb[x][kk];
+#pragma unroll
+        for (int x = 0; x < kInvB; ++x)
+#pragma unroll
+          for (int y = 0; y < kInvB; ++y)
+            pb[x][y] = x == kk ? rk[y] : (y == kk ? -ck[x] * rp : pb[x][y] - ck[x] * rk[y]);
+      }
+      for (int j = threadIdx.x; j < Dp; j += blockDim.x) {
+        const int bc = j - k0;
+        const bool pc = bc >= 0 && bc < kInvB;
+#pragma unroll
+        for (int x = 0; x < kInvB; ++x) {
+          float v = 0.0f, w = 0.0f;
+#pragma unroll
+          for (int y = 0; y < kInvB; ++y) {
+            v += pb[x][y] * rowb[y][j];
+            w += colb[j][y] * pb[y][x];
+          }
+          float pv = 0.0f;
+#pragma unroll
+          for (int y = 0; y < kInvB; ++y)
+            if (y == bc) pv = pb[x][y];
+          rnS[x][j] = pc ? pv : v;
+          cnS[j][x] = -w;
+        }
+      }
+    }
+    __syncthreads();
+    float rn[kInvB][kInvTC];
+#pragma unroll
+    for (int x = 0; x < kInvB; ++x)
+#pragma unroll
+      for (int c = 0; c < kInvTC; ++c) rn[x][c] = (c < TC && j0 + c < Dp) ? rnS[x][j0 + c] : 0.0f;
+#pragma unroll
+    for (int r = 0; r < kInvTR; ++r) {
+      const int i = i0 + r, br = i - k0;
+      if (r >= TR || i >= Dp) continue;
+      if (br >= 0 && br < kInvB) {  // a pivot row: Pinv * (pivot rows)
+#pragma unroll
+        for (int c = 0; c < kInvTC; ++c)
+          if (c < TC && j0 + c < Dp) a[r][c] = rnS[br][j0 + c];
+        continue;
+      }
+      float ci[kInvB];
+#pragma unroll
+      for (int y = 0; y < kInvB; ++y) ci[y] = colb[i][y];
+#pragma unroll
+      for (int c = 0; c < kInvTC; ++c) {
+        const int bc = j0 + c - k0;
+        if (bc >= 0 && bc < kInvB) {  // a pivot column: -(pivot columns) * Pinv
+          a[r][c] = cnS[i][bc];
+        } else {
+          float v = a[r][c];
+#pragma unroll
+          for (int y = 0; y < kInvB; ++y) v -= ci[y] * rn[y][c];
+          a[r][c] = v;
+        }
       }
     }
   }
   // Unscale into E (no longer needed), then symmetrise into E^-1.
 #pragma unroll
-  for (int r = 0; r < kInvTile; ++r)
+  for (int r = 0; r < kInvTR; ++r)
 #pragma unroll
-    for (int c = 0; c < kInvTile; ++c) {
+    for (int c = 0; c < kInvTC; ++c) {
       const int i = i0 + r, j = j0 + c;
-      if (r < T && c < T && i < D && j < D) Em[(size_t)i * D + j] = a[r][c] * dsc[i] * dsc[j];
+      if (r < TR && c < TC && i < D && j < D) Em[(size_t)i * D + j] = a[r][c] * dsc[i] * dsc[j];
     }
   __syncthreads();
   float* Im = A.Einv + A.model_eoff[m];

@@ -168,7 +168,8 @@ inline bool plan_cluster(const Context& ctx, const std::vector<uint32_t>& row_pt
 // CTA.
 struct CoarsePlan {
   std::vector<int32_t> grp_row0, grp_row1, grp_model, model_g0, row_grp, job_g0, job_g1;
-  std::vector<int64_t> model_eoff;
+  std::vector<int32_t> pair_row, pair_grp;  // (camera row, group of its model), row-major
+  std::vector<int64_t> model_eoff, row_pair0;
   std::vector<uint32_t> grp_loc;
   uint32_t cap_groups = 0, dmax = 0;
   int64_t e_total = 0;
@@ -178,6 +179,7 @@ inline void plan_coarse(const Context& ctx, const ClusterPlan& cp,
                         const std::vector<int32_t>& lens_row, int csize, CoarsePlan& pl) {
   pl = CoarsePlan{};
   pl.row_grp.assign((size_t)ctx.nb, -1);
+  pl.row_pair0.assign((size_t)ctx.nb, 0);
   constexpr int kPerCtaMax = 4;  // group slots per CTA (shared memory)
   for (int64_t m = 0; m < ctx.nm; ++m) {
     pl.model_g0.push_back((int32_t)pl.grp_row0.size());
@@ -224,6 +226,12 @@ inline void plan_coarse(const Context& ctx, const ClusterPlan& cp,
       pl.cap_groups = std::max(pl.cap_groups, (uint32_t)gk);
     }
     (void)total;
+    const int32_t mg0 = pl.model_g0.back(), mg1 = (int32_t)pl.grp_row0.size();
+    for (int32_t g = mg0; g < mg1; ++g)
+      for (int32_t r = pl.grp_row0[g]; r < pl.grp_row1[g]; ++r) {
+        pl.row_pair0[r] = (int64_t)pl.pair_row.size();
+        for (int32_t h = mg0; h < mg1; ++h) pl.pair_row.push_back(r), pl.pair_grp.push_back(h);
+      }
     const int64_t D = kCoarseModes * ((int64_t)pl.grp_row0.size() - pl.model_g0.back());
     pl.model_eoff.push_back(pl.e_total);
     pl.e_total += D * D;
@@ -393,8 +401,11 @@ struct LmEngine {
   bool use_coarse = false;
   DevBuf<float> cW, cE, cEinv;
   DevBuf<int32_t> c_grp_row0, c_grp_row1, c_grp_model, c_model_g0, c_row_grp, c_job_g0, c_job_g1;
-  DevBuf<int64_t> c_model_eoff;
+  DevBuf<int64_t> c_model_eoff, c_row_pair0;
   DevBuf<uint32_t> c_grp_loc;
+  DevBuf<int32_t> c_pair_row, c_pair_grp;
+  DevBuf<float> c_P;
+  int64_t c_npairs = 0;
   CoarseArgs cargs{};
   int32_t c_ngroups = 0;
   size_t c_inv_smem = 0;
@@ -642,6 +653,10 @@ struct LmEngine {
       detail::h2d(c_row_grp, gp.row_grp, s), detail::h2d(c_job_g0, gp.job_g0, s);
       detail::h2d(c_job_g1, gp.job_g1, s), detail::h2d(c_model_eoff, gp.model_eoff, s);
       detail::h2d(c_grp_loc, gp.grp_loc, s);
+      detail::h2d(c_pair_row, gp.pair_row, s), detail::h2d(c_pair_grp, gp.pair_grp, s);
+      detail::h2d(c_row_pair0, gp.row_pair0, s);
+      c_npairs = (int64_t)gp.pair_row.size();
+      c_P.alloc(detail::at_least_1(c_npairs) * 49, s);
       cW.alloc(detail::at_least_1(ctx.nb) * kCoarseW, s);
       cE.alloc(detail::at_least_1(gp.e_total), s), cEinv.alloc(detail::at_least_1(gp.e_total), s);
       c_ngroups = (int32_t)gp.grp_row0.size();
@@ -786,9 +801,12 @@ struct LmEngine {
     } else if (use_cluster) {
       if (use_coarse && c_ngroups > 0) {
         BA_LAUNCH(coarse_basis_kernel<<<grid_for(c_ngroups, 64), 64, 0, s>>>(P, ctx.cur(), cargs));
-        BA_LAUNCH(coarse_matrix_kernel<<<(unsigned)c_ngroups, kCoarseMatThreads, 0, s>>>(
-            SV, (const float*)S.p, cargs));
-        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kCoarseInvThreads, c_inv_smem, s>>>(
+        if (c_npairs > 0)
+          BA_LAUNCH(coarse_rowgroup_kernel<<<grid_for(c_npairs * 32, kCoarseMatThreads),
+                                             kCoarseMatThreads, 0, s>>>(
+              SV, (const float*)S.p, cargs, c_npairs, c_pair_row, c_pair_grp, c_P));
+        BA_LAUNCH(coarse_sum_kernel<<<(unsigned)c_ngroups, 256, 0, s>>>(cargs, c_row_pair0, c_P));
+        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, c_inv_smem, s>>>(
             cargs));
       }
       cudaLaunchConfig_t cfg{};

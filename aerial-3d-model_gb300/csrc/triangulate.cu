@@ -37,6 +37,9 @@ struct TriArgs {
   double* points;
   uint8_t* good;
   uint32_t* err;
+  uint32_t* obs_track;  // [no] track of each observation
+  double* pn;           // [2 no] undistorted normalised coordinates
+  double* ray;          // [3 no] unit ray from the camera to the point (good obs)
 };
 
 // Symmetric 4x4 eigen-decomposition by cyclic Jacobi rotations: on return A
@@ -98,7 +101,16 @@ __device__ __forceinline__ void undistort(const double* K, const double* u, doub
   p[0] = px, p[1] = py;
 }
 
-__global__ void __launch_bounds__(kTriThreads) triangulate_kernel(TriArgs T) {
+// The round runs in four passes, so that per-observation work is spread
+// over threads of observations rather than serialised per track: (1) track
+// checks and the observation -> track map (thread per track); (2) undistort
+// (thread per observation); (3) A^T A, its smallest eigenvector and the
+// point (thread per track); (4) the reprojection gate and the unit ray of
+// each observation (thread per observation); (5) the ray-angle test and the
+// keep decision (thread per track).  The arithmetic and its order are those
+// of a single pass per track.
+
+__global__ void tri_check_kernel(TriArgs T) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T.nt) return;
   const uint32_t b = T.track_ptr[t], e = T.track_ptr[t + 1];
@@ -108,12 +120,24 @@ __global__ void __launch_bounds__(kTriThreads) triangulate_kernel(TriArgs T) {
     atomicOr(T.err, ERR_BAD_INDEX);
     return;
   }
-  for (uint32_t k = b; k < e; ++k) T.good[k] = 0;
-  for (uint32_t k = b; k < e; ++k)
-    if (T.obs_cam[k] >= (uint64_t)T.nc || T.cam_group[T.obs_cam[k]] >= (uint64_t)T.ng) {
+  for (uint32_t k = b; k < e; ++k) {
+    T.good[k] = 0;
+    T.obs_track[k] = (uint32_t)t;
+    if (T.obs_cam[k] >= (uint64_t)T.nc || T.cam_group[T.obs_cam[k]] >= (uint64_t)T.ng)
       atomicOr(T.err, ERR_BAD_INDEX);
-      return;
-    }
+  }
+}
+
+__global__ void tri_undistort_kernel(TriArgs T) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= T.no || T.obs_track[k] == 0xffffffffu) return;
+  undistort(T.intr + 5 * (size_t)T.cam_group[T.obs_cam[k]], T.obs_uv + 2 * (size_t)k, T.pn + 2 * k);
+}
+
+__global__ void __launch_bounds__(kTriThreads) tri_point_kernel(TriArgs T) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T.nt) return;
+  const uint32_t b = T.track_ptr[t], e = T.track_ptr[t + 1];
   if (e - b < 2) return;
   // A^T A of the linear triangulation (geometry.rs:118-131).
   double ata[4][4] = {};
@@ -121,8 +145,7 @@ __global__ void __launch_bounds__(kTriThreads) triangulate_kernel(TriArgs T) {
     const uint32_t c = T.obs_cam[k];
     const double* R = T.rot + 9 * (size_t)c;
     const double* C = T.center + 3 * (size_t)c;
-    double pn[2];
-    undistort(T.intr + 5 * (size_t)T.cam_group[c], T.obs_uv + 2 * (size_t)k, pn);
+    const double pn[2] = {T.pn[2 * (size_t)k], T.pn[2 * (size_t)k + 1]};
     double tr[3];
 #pragma unroll
     for (int r = 0; r < 3; ++r) tr[r] = -(R[3 * r] * C[0] + R[3 * r + 1] * C[1] + R[3 * r + 2] * C[2]);
@@ -149,50 +172,62 @@ __global__ void __launch_bounds__(kTriThreads) triangulate_kernel(TriArgs T) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) v[i] = best == 0 ? V[i][0] : best == 1 ? V[i][1] : best == 2 ? V[i][2] : V[i][3];
   if (fabs(v[3]) < 1e-12) return;  // geometry.rs:139-141
-  const double X[3] = {v[0] / v[3], v[1] / v[3], v[2] / v[3]};
-  // Reprojection gating (sparse.rs:397-405).
+  T.points[3 * t] = v[0] / v[3], T.points[3 * t + 1] = v[1] / v[3], T.points[3 * t + 2] = v[2] / v[3];
+  T.kept[t] = 2;  // triangulated; decided in tri_keep_kernel
+}
+
+// Reprojection gate (sparse.rs:397-405) and the unit ray of each good
+// observation (geometry.rs:147).
+__global__ void tri_gate_kernel(TriArgs T) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= T.no) return;
+  const uint32_t t = T.obs_track[k];
+  if (t == 0xffffffffu || T.kept[t] != 2) return;
+  const double X[3] = {T.points[3 * (size_t)t], T.points[3 * (size_t)t + 1], T.points[3 * (size_t)t + 2]};
+  const uint32_t c = T.obs_cam[k];
+  const double* C = T.center + 3 * (size_t)c;
+  double u[2];
+  if (!bacam::project(T.rot + 9 * (size_t)c, C, T.intr + 5 * (size_t)T.cam_group[c], X, u)) return;
+  const double dx = u[0] - T.obs_uv[2 * (size_t)k], dy = u[1] - T.obs_uv[2 * (size_t)k + 1];
+  if (!(sqrt(dx * dx + dy * dy) < T.thr)) return;
+  T.good[k] = 1;
+  double r[3] = {X[0] - C[0], X[1] - C[1], X[2] - C[2]};
+  const double l = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  T.ray[3 * k] = r[0] / l, T.ray[3 * k + 1] = r[1] / l, T.ray[3 * k + 2] = r[2] / l;
+}
+
+// Keep the track if two or more observations remain and their rays span
+// more than 2 degrees (three or more views) or 6 degrees (two views):
+// acos is decreasing, so the largest angle is acos of the smallest clamped
+// dot product (the value the reference's running max of acos keeps).
+__global__ void __launch_bounds__(kTriThreads) tri_keep_kernel(TriArgs T) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T.nt || T.kept[t] != 2) return;
+  const uint32_t b = T.track_ptr[t], e = T.track_ptr[t + 1];
   int ng = 0;
-  for (uint32_t k = b; k < e; ++k) {
-    const uint32_t c = T.obs_cam[k];
-    double u[2];
-    if (!bacam::project(T.rot + 9 * (size_t)c, T.center + 3 * (size_t)c,
-                        T.intr + 5 * (size_t)T.cam_group[c], X, u))
-      continue;
-    const double dx = u[0] - T.obs_uv[2 * (size_t)k], dy = u[1] - T.obs_uv[2 * (size_t)k + 1];
-    if (sqrt(dx * dx + dy * dy) < T.thr) T.good[k] = 1, ++ng;
+  double min_d = 1.0;
+  for (uint32_t i = b; i < e; ++i) {
+    if (!T.good[i]) continue;
+    ++ng;
+    const double r0 = T.ray[3 * (size_t)i], r1 = T.ray[3 * (size_t)i + 1], r2 = T.ray[3 * (size_t)i + 2];
+    for (uint32_t j = i + 1; j < e; ++j) {
+      if (!T.good[j]) continue;
+      const double d = r0 * T.ray[3 * (size_t)j] + r1 * T.ray[3 * (size_t)j + 1] + r2 * T.ray[3 * (size_t)j + 2];
+      min_d = fmin(min_d, fmin(1.0, fmax(-1.0, d)));
+    }
   }
   bool ok = ng >= 2;
   if (ok) {
-    // max_ray_angle over the kept observations' unit rays (each normalised
-    // once, as the reference does): acos is decreasing, so the largest angle
-    // is acos of the smallest clamped dot product, the same value the
-    // reference's running max of acos keeps.
-    double min_d = 1.0;
-    for (uint32_t i = b; i < e; ++i) {
-      if (!T.good[i]) continue;
-      const double* Ci = T.center + 3 * (size_t)T.obs_cam[i];
-      double ri[3] = {X[0] - Ci[0], X[1] - Ci[1], X[2] - Ci[2]};
-      const double li = sqrt(ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2]);
-      ri[0] /= li, ri[1] /= li, ri[2] /= li;
-      for (uint32_t j = i + 1; j < e; ++j) {
-        if (!T.good[j]) continue;
-        const double* Cj = T.center + 3 * (size_t)T.obs_cam[j];
-        double rj[3] = {X[0] - Cj[0], X[1] - Cj[1], X[2] - Cj[2]};
-        const double lj = sqrt(rj[0] * rj[0] + rj[1] * rj[1] + rj[2] * rj[2]);
-        rj[0] /= lj, rj[1] /= lj, rj[2] /= lj;
-        const double d = ri[0] * rj[0] + ri[1] * rj[1] + ri[2] * rj[2];
-        min_d = fmin(min_d, fmin(1.0, fmax(-1.0, d)));
-      }
-    }
     const double deg = acos(min_d) * (180.0 / 3.14159265358979323846);
     ok = ng >= 3 ? deg > 2.0 : deg > 6.0;  // sparse.rs:411-415
   }
   if (!ok) {
     for (uint32_t k = b; k < e; ++k) T.good[k] = 0;
+    T.kept[t] = 0;
+    T.points[3 * t] = T.points[3 * t + 1] = T.points[3 * t + 2] = 0.0;
     return;
   }
   T.kept[t] = 1;
-  T.points[3 * t] = X[0], T.points[3 * t + 1] = X[1], T.points[3 * t + 2] = X[2];
 }
 
 // Problem of the kept tracks (sparse.rs:429-440): points in track order,
@@ -237,8 +272,8 @@ void check_tracks(const ba_tracks* tr) {
 // Device copies of the tracks and cameras, the triangulation, and the
 // device outputs (kept, points, good).
 struct TriRun {
-  DevBuf<uint32_t> track_ptr, obs_cam, cam_group, err;
-  DevBuf<double> obs_uv, rot, center, intr, points;
+  DevBuf<uint32_t> track_ptr, obs_cam, cam_group, err, obs_track;
+  DevBuf<double> obs_uv, rot, center, intr, points, pn, ray;
   DevBuf<uint8_t> kept, good;
 
   void run(const ba_tracks* tr, const double* h_rot, const double* h_center, const double* h_intr,
@@ -251,7 +286,7 @@ struct TriRun {
     auto A = [&](auto& d, int64_t n) { d.alloc(std::max<int64_t>(n, 1), s); };
     A(track_ptr, nt + 1), A(obs_cam, no), A(cam_group, nc), A(err, 1);
     A(obs_uv, 2 * no), A(rot, 9 * nc), A(center, 3 * nc), A(intr, 5 * ng), A(points, 3 * nt);
-    A(kept, nt), A(good, no);
+    A(kept, nt), A(good, no), A(obs_track, no), A(pn, 2 * no), A(ray, 3 * no);
     auto up = [&](auto& d, const auto* h, int64_t n) {
       if (n > 0)
         check(cudaMemcpyAsync(d.p, h, n * sizeof(*h), cudaMemcpyDefault, s), "copy in");
@@ -261,9 +296,26 @@ struct TriRun {
     up(rot, h_rot, 9 * nc), up(center, h_center, 3 * nc), up(intr, h_intr, 5 * ng);
     err.zero();
     TriArgs T{nt, no, nc, ng, track_ptr, obs_cam, obs_uv, cam_group, rot, center, intr, thr,
-              kept, points, good, err};
-    if (nt > 0)
-      BA_LAUNCH(triangulate_kernel<<<grid_for(nt, kTriThreads), kTriThreads, 0, s>>>(T));
+              kept, points, good, err, obs_track, pn, ray};
+    // Observations outside every track's range stay unmarked (no track, not good).
+    if (no > 0) {
+      check(cudaMemsetAsync(obs_track.p, 0xff, 4 * no, s), "memset");
+      check(cudaMemsetAsync(good.p, 0, no, s), "memset");
+    }
+    if (nt > 0) BA_LAUNCH(tri_check_kernel<<<grid_for(nt, 256), 256, 0, s>>>(T));
+    {
+      uint32_t e0 = 0;  // indices are checked before any other pass uses them
+      check(cudaMemcpyAsync(&e0, err.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
+      check(cudaStreamSynchronize(s), "triangulate check");
+      if (e0 & ERR_BAD_INDEX)
+        throw BadInput("track_ptr, obs_cam or cam_group out of range (or track_ptr decreasing)");
+    }
+    if (nt > 0 && no > 0) {
+      BA_LAUNCH(tri_undistort_kernel<<<grid_for(no, 256), 256, 0, s>>>(T));
+      BA_LAUNCH(tri_point_kernel<<<grid_for(nt, kTriThreads), kTriThreads, 0, s>>>(T));
+      BA_LAUNCH(tri_gate_kernel<<<grid_for(no, 256), 256, 0, s>>>(T));
+      BA_LAUNCH(tri_keep_kernel<<<grid_for(nt, kTriThreads), kTriThreads, 0, s>>>(T));
+    }
     uint32_t e = 0;
     check(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
     check(cudaStreamSynchronize(s), "triangulate");
