@@ -696,7 +696,12 @@ struct LmEngine {
     } restore{T, timing};
     build_system();
     std::vector<std::pair<int, int>> cand;  // (kernel, rows_target or cluster size)
-    for (int rt : {2, 3, 4, 6, 8, 12, 16}) cand.push_back({1, rt});
+    // With the two-level preconditioner (cluster kernel only) the PCG needs a
+    // fraction of the iterations, so only cluster layouts compete; the grid
+    // layouts remain the fallback when no cluster fits.
+    const bool coarse_only = sizeof(R) == 4 && o.coarse != 0;
+    if (!coarse_only)
+      for (int rt : {2, 3, 4, 6, 8, 12, 16}) cand.push_back({1, rt});
     if constexpr (sizeof(R) == 4)
       for (int cs : {4, 8, 12, 16}) cand.push_back({2, cs});
     cudaEvent_t e0, e1;
@@ -708,6 +713,7 @@ struct LmEngine {
     } ev{e0, e1};
     double best = 1e300;
     std::pair<int, int> best_c{1, 4};
+    bool any = false;
     std::vector<int32_t> hit(ctx.nm);
     for (const auto& c : cand) {
       if (c.first == 1) {
@@ -733,6 +739,23 @@ struct LmEngine {
       for (int32_t v : hit) its = std::max(its, v);
       const double per = (double)tbest / its;
       if (per < best) best = per, best_c = c;
+      any = true;
+    }
+    if (!any) {  // two-level form, but no cluster fits: grid layouts
+      for (int rt : {2, 4, 8}) {
+        plan_grid(rt);
+        const int32_t mi = pa.max_iter;
+        pa.max_iter = kTuneIters;
+        check(cudaEventRecord(e0, s), "event");
+        solve_pcg();
+        check(cudaEventRecord(e1, s), "event");
+        check(cudaEventSynchronize(e1), "tune");
+        pa.max_iter = mi;
+        float ms = 0;
+        check(cudaEventElapsedTime(&ms, e0, e1), "event");
+        const double per = (double)ms / kTuneIters;
+        if (per < best) best = per, best_c = {1, rt};
+      }
     }
     PcgTuning& tu = ctx.tuning[sizeof(R) == 8 ? 0 : 1];
     tu.valid = true;

@@ -55,10 +55,14 @@ METRIC = "BA solve time & kernel HBM GB/s, mixed vs FP64 GPU at equal final cost
 UNIT = "solves/s"
 SIGMA_PX = 1.0
 MAX_ITER = 60
-# The mixed form caps its FP32 PCG at this many iterations per LM step (the
-# FP64 form keeps the reference's 400): FP32 vectors cannot resolve the
-# system's weakest directions any further, and the LM outer loop refines.
-MIXED_PCG_ITERS = 200
+# The mixed form solves each LM step with the two-level preconditioner (block
+# Jacobi plus the similarity motions of camera groups) and caps its FP32 PCG
+# at this many iterations (the FP64 form keeps the reference's block-Jacobi
+# PCG and its 400): 40 up to 1000 cameras per model, 60 above, where the
+# groups (at most 27 per model) get larger and the coarse space weaker.
+MIXED_PCG_ITERS = 40
+MIXED_PCG_ITERS_LARGE = 60
+MIXED_LARGE_CAMS = 1000
 # Per LM iteration, algorithmic bytes of each phase, written as a function of
 # the problem sizes and the storage width s (8 FP64 / 4 FP32): reads and writes
 # each kernel must make at minimum.
@@ -149,6 +153,13 @@ class ClockSampler:
 
 
 MIXED_MATRIX_FREE = False  # --matrix-free: the mixed form applies S without forming it
+MIXED_PCG_CAP = MIXED_PCG_ITERS  # set per workload by set_mixed_cap
+
+
+def set_mixed_cap(ps):
+    global MIXED_PCG_CAP
+    big = max(p.n_cams for p in ps) > MIXED_LARGE_CAMS
+    MIXED_PCG_CAP = MIXED_PCG_ITERS_LARGE if big else MIXED_PCG_ITERS
 
 
 def form_options(prec: str, **kw):
@@ -158,7 +169,8 @@ def form_options(prec: str, **kw):
     kw.setdefault("autotune", True)
     if prec == "mixed":
         mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
-        return Options(precision="mixed", pcg_max_iter=MIXED_PCG_ITERS, matrix_free=mf, **kw)
+        kw.setdefault("coarse", not MIXED_MATRIX_FREE)
+        return Options(precision="mixed", pcg_max_iter=MIXED_PCG_CAP, matrix_free=mf, **kw)
     return Options(precision="fp64", **kw)
 
 
@@ -229,6 +241,7 @@ def gpu_arm(args, ws, rank):
         dist.init_process_group("nccl")
     native.load()
     ps = make_workload(args.workload, rank_seed(args.seed, rank))
+    set_mixed_cap(ps)
     nmod = len(ps)
     tot = totals(ps)
     stream = torch.cuda.current_stream()
@@ -287,6 +300,7 @@ def gpu_arm(args, ws, rank):
             forms[prec]["pcg_autotuned_us_per_iter"] = prof.pcg_tuned_us
             forms[prec]["device_bytes"] = int(prof.device_bytes)
             forms[prec]["pcg_max_iter"] = opts.pcg_max_iter
+            forms[prec]["coarse_dim"] = int(prof.coarse_dim)
             forms[prec]["graph"] = bool(info.graph)
     if "fp64" in forms and "mixed" in forms:
         # Equal final cost: the mixed solve reaches the FP64 solve's final cost
