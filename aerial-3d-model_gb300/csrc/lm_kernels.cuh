@@ -526,8 +526,9 @@ template <typename R>
 __global__ void __launch_bounds__(128)
     point_kernel(Prob P, StateView st, StructView S, IterBufs<R> B, const int32_t* active,
                  const double* lambda, const double* sigma) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.np) return;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= P.np) return;
+  const int64_t p = S.pt_order ? S.pt_order[tid] : tid;
   const uint32_t m = P.pt_model[p];
   if (!active[m]) return;
   const bool refine = P.model_refine[m] != 0;
@@ -1016,8 +1017,9 @@ __global__ void update_cameras_kernel(Prob P, StateView cur, StateView trial, It
 template <typename R>
 __global__ void backsub_kernel(Prob P, StructView S, StateView cur, StateView trial,
                                IterBufs<R> B, const double* sigma, const int32_t* active) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.np) return;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= P.np) return;
+  const int64_t p = S.pt_order ? S.pt_order[tid] : tid;
   const uint32_t m = P.pt_model[p];
   if (!active[m]) return;
   const double* X = cur.points + 3 * p;

@@ -593,7 +593,13 @@ struct LmEngine {
     cudaFuncAttributes fa{};
     check(cudaFuncGetAttributes(&fa, kfn), "func attr");
     const size_t avail = (size_t)smem_optin - fa.sharedSizeBytes;
-    const uint32_t rows_cap = (uint32_t)std::min<size_t>(avail / 2 / (kCgRow * 4), 4096);
+    // Row state takes at most half of the shared memory (the rest caches S
+    // blocks); with the coarse correction, which needs far fewer PCG
+    // iterations, rows may take all of it and S is read from L2.
+    const size_t row_all = (size_t)kCgRow * 4 + (coarse ? (42 + 8) * 4 : 0);
+    const size_t coarse_fixed = coarse ? (size_t)4 * (7 * kCoarseMaxDim + 14) * 4 + kCoarseMaxDim * 4 : 0;
+    const uint32_t rows_cap =
+        (uint32_t)std::min<size_t>(coarse ? (avail - coarse_fixed) / row_all : avail / 2 / (kCgRow * 4), 4096);
     detail::ClusterPlan cp;
     if (!detail::plan_cluster(ctx, SB.h_row_ptr, h_lens, csize, rows_cap, cp))
       return unusable("a model has too many block rows for one cluster");

@@ -53,6 +53,7 @@ struct StateView {
 // Per-call structure (fixed while a call iterates).
 struct StructView {
   const uint32_t* pt_ptr;    // [np+1] observation range of each point
+  const uint32_t* pt_order;  // [np] points by observation count (thread order of per-point kernels)
   const uint32_t* cam_ptr;   // [nc+1]
   const uint32_t* cam_obs;   // [no] observations ordered by camera (stable)
   const uint32_t* grp_ptr;   // [ng+1]

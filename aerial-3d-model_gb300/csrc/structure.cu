@@ -56,6 +56,14 @@ __device__ __forceinline__ bool point_has_lens(const Prob& P, uint32_t p) {
   return P.model_refine[P.pt_model[p]] != 0;
 }
 
+__global__ void order_keys_kernel(int64_t np, const uint32_t* pt_ptr, uint64_t* key,
+                                  uint32_t* idx) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  key[p] = min(pt_ptr[p + 1] - pt_ptr[p], 0xffffu);
+  idx[p] = (uint32_t)p;
+}
+
 __global__ void lens_count_kernel(Prob P, const uint32_t* pt_ptr, uint32_t* cnt) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P.np) return;
@@ -304,6 +312,7 @@ constexpr unsigned T = 256;
 StructView StructBufs::view() const {
   StructView v{};
   v.pt_ptr = pt_ptr;
+  v.pt_order = pt_order;
   v.cam_ptr = cam_ptr;
   v.cam_obs = cam_obs;
   v.grp_ptr = grp_ptr;
@@ -376,6 +385,16 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
   // Point ranges (obs are sorted by point).
   S.pt_ptr.alloc(np + 1, s);
   lower_bounds_u32(P.obs_pt, no, S.pt_ptr, np, s);
+  // Thread order of the per-point kernels: points by observation count
+  // (stable), so that the threads of a warp loop over the same number of
+  // observations.  Results do not depend on it: points are independent.
+  S.pt_order.alloc(std::max<int64_t>(np, 1), s);
+  if (np > 0) {
+    DevBuf<uint64_t> key(np, s), ktmp(np, s);
+    DevBuf<uint32_t> vtmp(np, s);
+    BA_LAUNCH(order_keys_kernel<<<grid_for(np, T), T, 0, s>>>(np, S.pt_ptr, key, S.pt_order));
+    radix_sort_u64_u32(key, S.pt_order, ktmp, vtmp, np, 16, s);
+  }
 
   build_cam_index(P, S, s);
   // Lens entries.

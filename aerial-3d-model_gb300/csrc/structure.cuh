@@ -8,7 +8,7 @@
 namespace ba {
 
 struct StructBufs {
-  DevBuf<uint32_t> pt_ptr, cam_ptr, cam_obs, grp_ptr, grp_cams, lens_ptr, lens_grp, obs_lens;
+  DevBuf<uint32_t> pt_ptr, pt_order, cam_ptr, cam_obs, grp_ptr, grp_cams, lens_ptr, lens_grp, obs_lens;
   DevBuf<uint64_t> pairs;
   DevBuf<uint32_t> slot_ptr, slot_row, slot_col, slot_pos_ab, slot_pos_ba;
   DevBuf<uint32_t> sub_slot, sub_begin, sub_end, slot_sub_ptr;
