@@ -303,11 +303,13 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
   // stored whitened, sqrt(w) J and sqrt(w) e with weight 1: every use of the
   // record is bilinear in (J, e) times w, so the sums are unchanged.  Other
   // records keep J, e and w as they are.
-  double jmax = 0.0;
+  // (the magnitude test runs on FP32 copies: FP64 instructions are the
+  // kernel's bound)
+  float jmax = 0.0f;
 #pragma unroll
-  for (int i = 0; i < 6; ++i) jmax = fmax(jmax, fabs(du[i]));
-  jmax *= fmax(1.0, fmax(fabs(xc[0]), fmax(fabs(xc[1]), fabs(xc[2]))));
-  const bool whiten = !(jmax < 1e12);
+  for (int i = 0; i < 6; ++i) jmax = fmaxf(jmax, fabsf((float)du[i]));
+  jmax *= fmaxf(1.0f, fmaxf(fabsf((float)xc[0]), fmaxf(fabsf((float)xc[1]), fabsf((float)xc[2]))));
+  const bool whiten = !(jmax < 1e12f);
   const double sw = whiten ? sqrt(w) : 1.0;
 #pragma unroll
   for (int r = 0; r < 2; ++r) {

@@ -1,6 +1,9 @@
 // Host driver of the LM loop (ba.rs:198-391) for storage precision R.
 #pragma once
 
+#include <map>
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
@@ -351,6 +354,29 @@ struct IterationGraph {
   }
 };
 
+// Autotuner results shared by the contexts of the process (ba_solve makes a
+// context per call): keyed by form, coarse correction and the shape of the
+// reduced system, so repeated calls on problems of one shape tune once.
+struct TuneKey {
+  int form, coarse;
+  int64_t nm, nb, nz;
+  bool operator<(const TuneKey& o) const {
+    if (form != o.form) return form < o.form;
+    if (coarse != o.coarse) return coarse < o.coarse;
+    if (nm != o.nm) return nm < o.nm;
+    if (nb != o.nb) return nb < o.nb;
+    return nz < o.nz;
+  }
+};
+inline std::mutex& tune_mutex() {
+  static std::mutex m;
+  return m;
+}
+inline std::map<TuneKey, PcgTuning>& tune_cache() {
+  static std::map<TuneKey, PcgTuning> c;
+  return c;
+}
+
 // All device state of one solve: structure, per-iteration buffers, LM
 // control scalars and the PCG plan.
 template <typename R>
@@ -520,7 +546,12 @@ struct LmEngine {
     // Configuration: an earlier tuning of this context for this form, or the
     // defaults (FP64 instructions serialise per SM sub-partition: one row per
     // warp on four warps; FP32 rows are cheap: one per warp on all eight).
-    const PcgTuning& tu = ctx.tuning[sizeof(R) == 8 ? 0 : 1];
+    PcgTuning& tu = ctx.tuning[sizeof(R) == 8 ? 0 : 1];
+    if (!tu.valid && o.autotune && o.pcg_kernel == 0) {
+      std::lock_guard<std::mutex> lk(tune_mutex());
+      auto it = tune_cache().find(tune_key());
+      if (it != tune_cache().end()) tu = it->second;
+    }
     if (tu.valid && o.pcg_kernel == 0) {
       if (tu.kernel != 2 || !try_cluster(tu.cluster, false, true)) plan_grid(tu.rows_target);
     } else if (o.pcg_kernel == 2) {
@@ -769,8 +800,16 @@ struct LmEngine {
     tu.rows_target = best_c.first == 1 ? best_c.second : 4;
     tu.cluster = best_c.first == 2 ? best_c.second : 0;
     tu.us_per_iter = best * 1000.0;
+    {
+      std::lock_guard<std::mutex> lk(tune_mutex());
+      tune_cache()[tune_key()] = tu;
+    }
     if (best_c.first == 2 && try_cluster(best_c.second, false, true)) return;
     plan_grid(tu.rows_target);
+  }
+
+  TuneKey tune_key() const {
+    return TuneKey{sizeof(R) == 8 ? 0 : 1, o.coarse, ctx.nm, ctx.nb, SB.nz};
   }
 
   void set_lambda(double lam) {
