@@ -13,8 +13,12 @@ initial state.
 * ``e2e``    — solves/s through the reference-facing C ABI ``ba_solve`` with
   host (pinned) buffers: H2D of the problem, the solve and D2H of the state
   are inside the timed region.
-* ``forms``  — FP64 plain form and FP32/FP64 mixed form side by side, with the
-  final cost of each and their relative difference.
+* ``forms``  — FP64 plain form (the reference's block-Jacobi PCG, 400
+  iterations) and FP32/FP64 mixed form (two-level PCG: block Jacobi plus the
+  similarity motions of camera groups, 40 iterations; 60 above 1000 cameras
+  per model) side by side, with the final cost of each and their relative
+  difference; the mixed form is the headline when it reaches the FP64 final
+  cost.
 * ``roofline`` — the dominant kernel phase (by device time, from the
   solver's own CUDA-event phase timing) against measured HBM bandwidth.
 * ``cpu_baseline`` — the oracle (a CPU restatement of the reference solver,
