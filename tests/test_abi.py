@@ -54,3 +54,36 @@ def test_header_compiles_as_c():
     p = subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-I", os.path.dirname(HEADER), "-x", "c",
                         "-"], input=src, capture_output=True, text=True)
     assert p.returncode == 0, p.stderr
+
+
+def c_layout(struct, fields):
+    """sizeof and offsetof of a header struct, from a C program built here."""
+    body = "".join(f'printf("%zu ", offsetof({struct}, {f}));' for f in fields)
+    src = ('#include <stdio.h>\n#include <stddef.h>\n#include "ba_gb300.h"\n'
+           f'int main(void){{ printf("%zu ", sizeof({struct})); {body} return 0; }}\n')
+    exe = os.path.join(_build.OUT, "layout_probe")
+    p = subprocess.run(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), "-x", "c", "-", "-o", exe],
+                       input=src, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
+    vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
+    return vals[0], vals[1:]
+
+
+@pytest.mark.parametrize("cname,py", [
+    ("ba_problem", native.BaProblem), ("ba_state", native.BaState), ("ba_log", native.BaLog),
+    ("ba_options", native.BaOptions), ("ba_stats", native.BaStatsC), ("ba_tracks", native.BaTracks),
+    ("ba_pair_matches", native.BaPairMatches)])
+def test_binding_structs_match_the_header_layout(cname, py):
+    names = [f[0] for f in py._fields_]
+    cnames = ["lambda" if n == "lam" else n for n in names]
+    size, offs = c_layout(cname, cnames)
+    assert ctypes.sizeof(py) == size
+    assert [getattr(py, n).offset for n in names] == offs
+
+
+def test_default_options_leave_the_extensions_off():
+    L = native.load()
+    o = native.BaOptions()
+    L.ba_default_options(ctypes.byref(o))
+    assert (o.coarse, o.autotune, o.stop_patience, o.pcg_kernel, o.no_graph, o.matrix_free) == (0,) * 6
+    assert o.precision == 0 and o.loss == 0

@@ -170,3 +170,15 @@ def test_coarse_option_is_inert_for_fp64_and_graph_replay_matches():
     _, _, d = solve(p, Options(precision="mixed", pcg_kernel="cluster", coarse=True, graph=False))
     assert c.coarse_dim > 0 and c.graph and not d.graph
     assert c.final_cost == d.final_cost and c.iterations == d.iterations
+
+
+def test_autotuned_layout_is_kept_across_calls_of_one_shape():
+    """ba_solve builds a context per call; the autotuner's choice for a
+    problem shape is kept for the process, so a second call reuses it."""
+    p, _ = survey.generate("lawnmower77", seed=5, n_cams=30, n_points=9000)
+    o = Options(precision="mixed", autotune=True, coarse=True, pcg_max_iter=40)
+    _, _, a = solve(p, o, sigma=1.0)
+    _, _, b = solve(p, o, sigma=1.0)
+    assert a.pcg_tuned_us > 0 and b.pcg_tuned_us == a.pcg_tuned_us
+    assert (a.pcg_kernel, a.pcg_cluster) == (b.pcg_kernel, b.pcg_cluster)
+    assert a.final_cost == b.final_cost
