@@ -30,7 +30,6 @@ constexpr int kCoarseModes = 7;
 constexpr int kCoarseMaxGroups = 27;                    // per model
 constexpr int kCoarseMaxDim = kCoarseModes * kCoarseMaxGroups;  // 189
 constexpr int kCoarseW = 6 * kCoarseModes;              // W values per row
-constexpr int kCoarseInvThreads = 1024;
 
 struct CoarseArgs {
   int32_t ngroups;           // all models
@@ -46,19 +45,27 @@ struct CoarseArgs {
   float* Einv;               // same layout
 };
 
-// W of every camera row of every group (thread per group).
+// W of every camera row of every group: a warp per group, the centroid as a
+// warp sum in a fixed order, then a lane per row.
 static __global__ void coarse_basis_kernel(Prob P, StateView st, CoarseArgs A) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (g >= A.ngroups || !A.active[A.grp_model[g]]) return;
   const int r0 = A.grp_row0[g], r1 = A.grp_row1[g];
   double c0 = 0.0, c1 = 0.0, c2 = 0.0;
-  for (int r = r0; r < r1; ++r) {
+  for (int r = r0 + lane; r < r1; r += 32) {
     const double* C = st.center + 3 * (size_t)P.blk_id[r];
     c0 += C[0], c1 += C[1], c2 += C[2];
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    c0 += __shfl_xor_sync(kFull, c0, o);
+    c1 += __shfl_xor_sync(kFull, c1, o);
+    c2 += __shfl_xor_sync(kFull, c2, o);
+  }
   const double inv = 1.0 / (double)(r1 - r0);
   c0 *= inv, c1 *= inv, c2 *= inv;
-  for (int r = r0; r < r1; ++r) {
+  for (int r = r0 + lane; r < r1; r += 32) {
     const uint32_t cam = P.blk_id[r];
     const double* R = st.rot + 9 * (size_t)cam;
     const double* C = st.center + 3 * (size_t)cam;
@@ -333,6 +340,5 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
   }
 }
 
-inline size_t coarse_invert_smem(int) { return 0; }
 
 }  // namespace ba

@@ -160,9 +160,9 @@ struct CgScalars {
 // z = z_B + W c on this CTA's rows; returns this CTA's share of w . c (thread
 // 0; the others return 0).
 __device__ __forceinline__ float cg_coarse_apply(cgx::cluster_group& cl, const CgArgs& A, int m,
-                                                 int32_t g0, int32_t ngr, float* rs, uint32_t nrows,
+                                                 int32_t ngr, float* rs, uint32_t nrows,
                                                  const float* sW, const float* sEi, float* sw,
-                                                 float* swall, float* sc, uint32_t row0) {
+                                                 float* swall, float* sc) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int32_t gm0 = A.model_g0[m];
   const int D = kCoarseModes * (A.model_g0[m + 1] - gm0);
@@ -196,8 +196,6 @@ __device__ __forceinline__ float cg_coarse_apply(cgx::cluster_group& cl, const C
   float wc = 0.0f;
   if (threadIdx.x == 0)
     for (int o = 0; o < ngr * kCoarseModes; ++o) wc += sw[o] * sc[o];
-  (void)g0;
-  (void)row0;
   return wc;
 }
 
@@ -331,8 +329,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     sc.stop = 0;
   });
   if constexpr (kCoarse) {
-    const float wc = cg_coarse_apply(cl, A, J.model, cg0, ngr, rs, nrows, sW, sEi, sw, swall,
-                                     scf, J.row0);
+    const float wc = cg_coarse_apply(cl, A, J.model, ngr, rs, nrows, sW, sEi, sw, swall, scf);
     const float w1[1] = {threadIdx.x == 0 ? wc : 0.0f};
     cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] { sc.rz = sc.rzb + tot[0]; });
   }
@@ -453,8 +450,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     if (sc.stop) break;
     if constexpr (kCoarse) {
       // z = B^-1 r + W E^-1 W^T r; r . z = r . B^-1 r + w . c.
-      const float wc = cg_coarse_apply(cl, A, J.model, cg0, ngr, rs, nrows, sW, sEi, sw, swall,
-                                       scf, J.row0);
+      const float wc = cg_coarse_apply(cl, A, J.model, ngr, rs, nrows, sW, sEi, sw, swall, scf);
       const float w1[1] = {threadIdx.x == 0 ? wc : 0.0f};
       cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] {
         const double rzn = sc.rzb + tot[0];

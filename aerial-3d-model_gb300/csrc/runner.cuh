@@ -434,7 +434,6 @@ struct LmEngine {
   int64_t c_npairs = 0;
   CoarseArgs cargs{};
   int32_t c_ngroups = 0;
-  size_t c_inv_smem = 0;
   PhaseTimer T;
 
   LmEngine(Context& c, const Opts& opts) : ctx(c), o(opts), s(c.stream) {
@@ -640,8 +639,6 @@ struct LmEngine {
     if (coarse) {
       detail::plan_coarse(ctx, cp, h_lens, csize, gp);
       coarse_bytes = cg_coarse_smem_bytes(cp.max_rows, std::max(gp.cap_groups, 1u), std::max(gp.dmax, 1u));
-      if (coarse_invert_smem((int)gp.dmax) > (size_t)smem_optin)
-        return unusable("coarse system too large");
     }
     const size_t row_bytes = (size_t)cp.max_rows * kCgRow * 4;
     if (row_bytes + coarse_bytes >= avail) return unusable("row state does not fit");
@@ -699,10 +696,6 @@ struct LmEngine {
       c_ngroups = (int32_t)gp.grp_row0.size();
       cargs = CoarseArgs{c_ngroups, c_grp_row0, c_grp_row1, c_grp_model, c_model_g0,
                          c_model_eoff, c_row_grp, active, cW, cE, cEinv};
-      c_inv_smem = coarse_invert_smem((int)gp.dmax);
-      check(cudaFuncSetAttribute(coarse_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)c_inv_smem),
-            "coarse smem");
       ca.W = cW, ca.Einv = cEinv, ca.model_eoff = c_model_eoff, ca.model_g0 = c_model_g0;
       ca.grp_row0 = c_grp_row0, ca.grp_row1 = c_grp_row1, ca.job_g0 = c_job_g0;
       ca.job_g1 = c_job_g1, ca.grp_loc = c_grp_loc;
@@ -868,13 +861,14 @@ struct LmEngine {
             "pcg launch");
     } else if (use_cluster) {
       if (use_coarse && c_ngroups > 0) {
-        BA_LAUNCH(coarse_basis_kernel<<<grid_for(c_ngroups, 64), 64, 0, s>>>(P, ctx.cur(), cargs));
+        BA_LAUNCH(coarse_basis_kernel<<<grid_for((int64_t)c_ngroups * 32, 128), 128, 0, s>>>(
+            P, ctx.cur(), cargs));
         if (c_npairs > 0)
           BA_LAUNCH(coarse_rowgroup_kernel<<<grid_for(c_npairs * 32, kCoarseMatThreads),
                                              kCoarseMatThreads, 0, s>>>(
               SV, (const float*)S.p, cargs, c_npairs, c_pair_row, c_pair_grp, c_P));
         BA_LAUNCH(coarse_sum_kernel<<<(unsigned)c_ngroups, 256, 0, s>>>(cargs, c_row_pair0, c_P));
-        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, c_inv_smem, s>>>(
+        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, 0, s>>>(
             cargs));
       }
       cudaLaunchConfig_t cfg{};
