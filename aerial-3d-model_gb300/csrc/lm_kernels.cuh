@@ -38,6 +38,7 @@ struct IterBufs {
   R* g;           // [nb][6]
   R* x;           // [nb][6] (dx)
   double* cost_part;  // [ncost][3]
+  float* ptf;         // [np][9] mixed form: L (6) | t = V^-1 v (3) in FP32 for the Z pass
 };
 
 __device__ __forceinline__ double robust_weight(double e2, double sigma, int loss) {
@@ -160,8 +161,8 @@ __device__ __forceinline__ void point_system(const Prob& P, const StateView& st,
       for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = (R)0;
     return;
   }
-  // V, v and the Y / Z products accumulate in the storage precision R (FP32 in
-  // the mixed form); the 3x3 inversion and its Cholesky factor are FP64.
+  // V, v and the Y / Z products accumulate in the storage precision R; the 3x3
+  // inversion and its Cholesky factor are FP64.
   R V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
   for (uint32_t k = s; k < e; ++k) {
     R* o = B.lin + (size_t)k * kLinW;
@@ -263,21 +264,19 @@ __device__ __forceinline__ void point_system(const Prob& P, const StateView& st,
   }
 }
 
-// Mixed form, first pass over an observation: the residual, dudx and Jp in
-// FP64 (the point system V, v and its inverse must be exact: a point whose
-// rays are nearly parallel has a nearly singular V, and FP32 noise in V or v
-// would be amplified by V^-1); the record keeps FP32 Jc, Jp, Jg, e and w.
-__device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& st, int64_t k,
-                                                double sigma, bool refine, float* out,
-                                                double (&jp)[6], double (&ev)[2], double& w) {
+// Mixed form, record of an observation with extreme Jacobians, all in FP64:
+// an observation of a point barely in front of its camera has |J| up to
+// ~1e19 (w ~ 1e-24), and FP32 J^T J would overflow.  Such a record is stored
+// whitened, sqrt(w) J and sqrt(w) e with weight 1: every use of the record is
+// bilinear in (J, e) times w, so the sums are unchanged.  On return `ev` is
+// the (whitened) FP64 residual that goes with the stored record.
+static __device__ __noinline__ void linearise_mixed_extreme(const Prob& P, const StateView& st,
+                                                            int64_t k, double sigma, bool refine,
+                                                            const double (&xc)[3], float* out,
+                                                            double (&ev)[2]) {
   const uint32_t cam = P.obs_cam[k];
   const double* Rm = st.rot + 9 * (size_t)cam;
-  const double* C = st.center + 3 * (size_t)cam;
   const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
-  const double* X = st.points + 3 * (size_t)P.obs_pt[k];
-  double xc[3];
-  bacam::to_cam(Rm, C, X, xc);
-  if (xc[2] <= 1e-6) return false;
   const double f = K[0], k1 = K[3], k2 = K[4];
   const double iz = 1.0 / xc[2];
   const double px = xc[0] * iz, py = xc[1] * iz;
@@ -297,20 +296,8 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
   du[3] = a01 * iz;
   du[4] = a11 * iz;
   du[5] = a01 * b02 + a11 * b12;
-  w = robust_weight(ev[0] * ev[0] + ev[1] * ev[1], sigma, P.loss);
-  // An observation of a point barely in front of its camera has |J| up to
-  // ~1e19 (w ~ 1e-24), and FP32 J^T J would overflow.  Such a record is
-  // stored whitened, sqrt(w) J and sqrt(w) e with weight 1: every use of the
-  // record is bilinear in (J, e) times w, so the sums are unchanged.  Other
-  // records keep J, e and w as they are.
-  // (the magnitude test runs on FP32 copies: FP64 instructions are the
-  // kernel's bound)
-  float jmax = 0.0f;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) jmax = fmaxf(jmax, fabsf((float)du[i]));
-  jmax *= fmaxf(1.0f, fmaxf(fabsf((float)xc[0]), fmaxf(fabsf((float)xc[1]), fabsf((float)xc[2]))));
-  const bool whiten = !(jmax < 1e12f);
-  const double sw = whiten ? sqrt(w) : 1.0;
+  const double w = robust_weight(ev[0] * ev[0] + ev[1] * ev[1], sigma, P.loss);
+  const double sw = sqrt(w);
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     const double u0 = du[3 * r], u1 = du[3 * r + 1], u2 = du[3 * r + 2];
@@ -321,9 +308,9 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
     out[6 * r + 2] = f1 * x0 - f0 * x1;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      jp[3 * r + j] = u0 * Rm[j] + u1 * Rm[3 + j] + u2 * Rm[6 + j];
-      out[6 * r + 3 + j] = -(float)(jp[3 * r + j] * sw);
-      out[12 + 3 * r + j] = (float)(jp[3 * r + j] * sw);
+      const double jp = u0 * Rm[j] + u1 * Rm[3 + j] + u2 * Rm[6 + j];
+      out[6 * r + 3 + j] = -(float)(jp * sw);
+      out[12 + 3 * r + j] = (float)(jp * sw);
     }
   }
   if (refine) {  // ba.rs:87-95
@@ -337,9 +324,108 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
 #pragma unroll
     for (int i = 18; i < 24; ++i) out[i] = 0.0f;
   }
-  out[24] = (float)(ev[0] * sw);
-  out[25] = (float)(ev[1] * sw);
-  out[26] = whiten ? 1.0f : (float)w;
+  ev[0] *= sw;
+  ev[1] *= sw;
+  out[24] = (float)ev[0];
+  out[25] = (float)ev[1];
+  out[26] = 1.0f;
+  out[27] = 1.0f;
+}
+
+// Mixed form, first pass over an observation.  The residual is FP64 (it
+// decides the gradient near convergence); dudx, Jc, Jp, Jg and the robust
+// weight are FP32 and stored as the record.  The point system V, v is summed
+// in FP64 from exactly these stored values (`jp`, `w`; products of FP32
+// numbers are exact in FP64), so V^-1 v is the exact least-squares point
+// step of the stored Jacobians: a point whose rays are nearly parallel has a
+// nearly singular V, and any rounding between V, v and the records would be
+// amplified by V^-1.  On return `ev` is the FP64 residual matching the
+// record (whitened for an extreme record).
+__device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& st, int64_t k,
+                                                double sigma, float sigma_f, float inv_s2,
+                                                bool refine, float* out, float (&jp)[6],
+                                                double (&ev)[2], float& w) {
+  const uint32_t cam = P.obs_cam[k];
+  const double* Rm = st.rot + 9 * (size_t)cam;
+  const double* C = st.center + 3 * (size_t)cam;
+  const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
+  const double* X = st.points + 3 * (size_t)P.obs_pt[k];
+  double xc[3];
+  bacam::to_cam(Rm, C, X, xc);
+  if (xc[2] <= 1e-6) return false;
+  {
+    const double iz = 1.0 / xc[2];
+    const double px = xc[0] * iz, py = xc[1] * iz;
+    const double r2 = px * px + py * py;
+    const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
+    ev[0] = P.obs_uv[2 * k] - (K[0] * (px * d) + K[1]);
+    ev[1] = P.obs_uv[2 * k + 1] - (K[0] * (py * d) + K[2]);
+  }
+  const float x0 = (float)xc[0], x1 = (float)xc[1], x2 = (float)xc[2];
+  const float f = (float)K[0], k1 = (float)K[3], k2 = (float)K[4];
+  const float iz = 1.0f / x2;
+  const float px = x0 * iz, py = x1 * iz;
+  const float r2 = px * px + py * py;
+  const float d = 1.0f + k1 * r2 + k2 * r2 * r2;
+  const float c = 2.0f * (k1 + 2.0f * k2 * r2);
+  const float a00 = (d + c * px * px) * f, a01 = (c * px * py) * f;
+  const float a11 = (d + c * py * py) * f;
+  const float b02 = -x0 * iz * iz, b12 = -x1 * iz * iz;
+  float du[6];
+  du[0] = a00 * iz;
+  du[1] = a01 * iz;
+  du[2] = a00 * b02 + a01 * b12;
+  du[3] = a01 * iz;
+  du[4] = a11 * iz;
+  du[5] = a01 * b02 + a11 * b12;
+  const float e0 = (float)ev[0], e1 = (float)ev[1];
+  const float e2 = e0 * e0 + e1 * e1;
+  float jmax = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) jmax = fmaxf(jmax, fabsf(du[i]));
+  jmax *= fmaxf(1.0f, fmaxf(fabsf(x0), fmaxf(fabsf(x1), fabsf(x2))));
+  // NaN or inf in the FP32 chain fails the test as well.
+  if (!(jmax < 1e12f) || !(e2 < 1e30f)) {
+    linearise_mixed_extreme(P, st, k, sigma, refine, xc, out, ev);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) jp[i] = out[12 + i];
+    w = 1.0f;
+    return true;
+  }
+  if (P.loss == LOSS_HUBER) {
+    const float a = sqrtf(e2);
+    w = a <= sigma_f ? 1.0f : sigma_f / a;
+  } else {
+    w = 1.0f / (1.0f + e2 * inv_s2);  // ba.rs:99
+  }
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const float u0 = du[3 * r], u1 = du[3 * r + 1], u2 = du[3 * r + 2];
+    out[6 * r + 0] = u2 * x1 - u1 * x2;
+    out[6 * r + 1] = u0 * x2 - u2 * x0;
+    out[6 * r + 2] = u1 * x0 - u0 * x1;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float pp = u0 * (float)Rm[j] + u1 * (float)Rm[3 + j] + u2 * (float)Rm[6 + j];
+      jp[3 * r + j] = pp;
+      out[6 * r + 3 + j] = -pp;
+      out[12 + 3 * r + j] = pp;
+    }
+  }
+  if (refine) {  // ba.rs:87-95
+    out[18] = px * d;
+    out[19] = f * px * r2;
+    out[20] = f * px * r2 * r2;
+    out[21] = py * d;
+    out[22] = f * py * r2;
+    out[23] = f * py * r2 * r2;
+  } else {
+#pragma unroll
+    for (int i = 18; i < 24; ++i) out[i] = 0.0f;
+  }
+  out[24] = e0;
+  out[25] = e1;
+  out[26] = w;
   out[27] = 1.0f;
   return true;
 }
@@ -349,40 +435,32 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
 // system needs).  cond(V) <= tr^3 / (4 det) for a 3x3 SPD matrix.
 constexpr double kMixedCondLimit = 1e4;
 
-// Mixed form (R = float): point system in FP64, storage in FP32.  Z and the
-// per-observation reduced gradient r' are formed in FP32 for well-conditioned
-// points and from an FP64 re-linearisation for the rest.
-__device__ __forceinline__ void point_system_mixed(const Prob& P, const StateView& st,
-                                                   const StructView& S, const IterBufs<float>& B,
-                                                   int64_t p, bool refine, double sg, double lam) {
+// Mixed form, a point with cond(V) above kMixedCondLimit: V, v, V^-1 and the
+// second pass all from an FP64 re-linearisation, so that V^-1 v stays the
+// exact point step of the Jacobians the Schur factors are formed from (FP32
+// rounding of the records would be amplified by V^-1).  Z and the gradient
+// shares are rounded to FP32 once.  About 0.4 % of the points of a converging
+// survey take this path.
+static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const StateView& st,
+                                                           const StructView& S,
+                                                           const IterBufs<float>& B, int64_t p,
+                                                           bool refine, double sg, double lam) {
   const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
   double V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
   for (uint32_t k = s; k < e; ++k) {
-    float* o = B.lin + (size_t)k * kLinW;
-    double jp[6], ev[2], w;
-    if (!linearise_mixed(P, st, k, sg, refine, o, jp, ev, w)) {
-      for (int i = 0; i < kLinW; ++i) o[i] = 0.0f;
-      continue;
-    }
-    V[0] += (jp[0] * jp[0] + jp[3] * jp[3]) * w;
-    V[1] += (jp[0] * jp[1] + jp[3] * jp[4]) * w;
-    V[2] += (jp[0] * jp[2] + jp[3] * jp[5]) * w;
-    V[3] += (jp[1] * jp[1] + jp[4] * jp[4]) * w;
-    V[4] += (jp[1] * jp[2] + jp[4] * jp[5]) * w;
-    V[5] += (jp[2] * jp[2] + jp[5] * jp[5]) * w;
-    v[0] += (jp[0] * ev[0] + jp[3] * ev[1]) * w;
-    v[1] += (jp[1] * ev[0] + jp[4] * ev[1]) * w;
-    v[2] += (jp[2] * ev[0] + jp[5] * ev[1]) * w;
-  }
-  if (e - s < 2) {  // ba.rs:238
-    B.kept[p] = 0;
-    for (uint32_t k = s; k < e; ++k) {
-      for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = 0.0f;
-      for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = 0.0f;
-    }
-    for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j)
-      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
-    return;
+    double o[kLinW];
+    if (!linearise<double>(P, st, k, sg, refine, o)) continue;
+    const double w = o[26];
+    const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+    V[0] += (j0 * j0 + j3 * j3) * w;
+    V[1] += (j0 * j1 + j3 * j4) * w;
+    V[2] += (j0 * j2 + j3 * j5) * w;
+    V[3] += (j1 * j1 + j4 * j4) * w;
+    V[4] += (j1 * j2 + j4 * j5) * w;
+    V[5] += (j2 * j2 + j5 * j5) * w;
+    v[0] += (j0 * o[24] + j3 * o[25]) * w;
+    v[1] += (j1 * o[24] + j4 * o[25]) * w;
+    v[2] += (j2 * o[24] + j5 * o[25]) * w;
   }
   double A[9], Ai[9];
   sym3_full(V, A);
@@ -392,11 +470,16 @@ __device__ __forceinline__ void point_system_mixed(const Prob& P, const StateVie
   const bool ok = inv3(A, Ai);  // ba.rs:265
   double L[6] = {0, 0, 0, 0, 0, 0};
   if (ok) chol3(Ai, L);
-  const double tr = A[0] + A[4] + A[8];
-  const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
-                     A[2] * (A[3] * A[7] - A[4] * A[6]);
-  const bool ill = !(det > 0.0) || tr * tr * tr > 4.0 * kMixedCondLimit * det;
-  B.kept[p] = ok ? (ill ? 2 : 1) : 0;
+  B.kept[p] = ok ? 2 : 0;
+  if (!ok) {
+    for (uint32_t k = s; k < e; ++k) {
+      for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = 0.0f;
+      for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = 0.0f;
+    }
+    for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j)
+      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
+    return;
+  }
   const double zv0 = L[0] * v[0] + L[1] * v[1] + L[3] * v[2];
   const double zv1 = L[2] * v[1] + L[4] * v[2];
   const double zv2 = L[5] * v[2];
@@ -406,68 +489,6 @@ __device__ __forceinline__ void point_system_mixed(const Prob& P, const StateVie
   for (int i = 0; i < 6; ++i) pl[i] = L[i];
   B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
   const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
-  if (!ok || !ill) {
-    const float l00 = (float)L[0], l10 = (float)L[1], l11 = (float)L[2], l20 = (float)L[3],
-                l21 = (float)L[4], l22 = (float)L[5];
-    const float tf0 = (float)t0, tf1 = (float)t1, tf2 = (float)t2;
-    for (uint32_t k = s; k < e; ++k) {
-      const float* o = B.lin + (size_t)k * kLinW;
-      float* Z = B.Z + (size_t)k * 18;
-      float* gs = B.gsub + (size_t)k * 9;
-      if (!ok || o[27] == 0.0f) {
-#pragma unroll
-        for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
-        continue;
-      }
-      const float w = o[26];
-      const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
-      // r' = w (e - Jp t)
-      const float r0 = (o[24] - (j0 * tf0 + j1 * tf1 + j2 * tf2)) * w;
-      const float r1 = (o[25] - (j3 * tf0 + j4 * tf1 + j5 * tf2)) * w;
-#pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        const float ca = o[r], cb = o[6 + r];
-        const float y0 = (ca * j0 + cb * j3) * w;
-        const float y1 = (ca * j1 + cb * j4) * w;
-        const float y2 = (ca * j2 + cb * j5) * w;
-        Z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
-        Z[3 * r + 1] = y1 * l11 + y2 * l21;
-        Z[3 * r + 2] = y2 * l22;
-        gs[r] = ca * r0 + cb * r1;
-      }
-#pragma unroll
-      for (int a = 0; a < 3; ++a) gs[6 + a] = o[18 + a] * r0 + o[21 + a] * r1;
-    }
-    for (uint32_t j = l0; j < l1; ++j) {
-      float Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-      for (uint32_t k = s; k < e; ++k) {
-        if (S.obs_lens[k] != j) continue;
-        const float* o = B.lin + (size_t)k * kLinW;
-        if (o[27] == 0.0f) continue;
-        const float w = o[26];
-        const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const float ga = o[18 + a], gb = o[21 + a];
-          Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
-          Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
-          Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
-        }
-      }
-      float* Zl = B.Zl + (size_t)j * 9;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
-        Zl[3 * a + 0] = ok ? y0 * l00 + y1 * l10 + y2 * l20 : 0.0f;
-        Zl[3 * a + 1] = ok ? y1 * l11 + y2 * l21 : 0.0f;
-        Zl[3 * a + 2] = ok ? y2 * l22 : 0.0f;
-      }
-    }
-    return;
-  }
-  // Ill-conditioned point: second pass from an FP64 re-linearisation.
   for (uint32_t k = s; k < e; ++k) {
     float* Z = B.Z + (size_t)k * 18;
     float* gs = B.gsub + (size_t)k * 9;
@@ -524,20 +545,244 @@ __device__ __forceinline__ void point_system_mixed(const Prob& P, const StateVie
   }
 }
 
+// FP64 form: a thread per point (in order of observation count).
 template <typename R>
 __global__ void __launch_bounds__(128)
     point_kernel(Prob P, StateView st, StructView S, IterBufs<R> B, const int32_t* active,
                  const double* lambda, const double* sigma) {
+  static_assert(sizeof(R) == 8, "the mixed form runs obs_record / point_solve_mixed / obs_factor");
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= P.np) return;
   const int64_t p = S.pt_order ? S.pt_order[tid] : tid;
   const uint32_t m = P.pt_model[p];
   if (!active[m]) return;
   const bool refine = P.model_refine[m] != 0;
-  if constexpr (sizeof(R) == 8)
-    point_system<R>(P, st, S, B, p, refine, sigma[m], lambda[m]);
-  else
-    point_system_mixed(P, st, S, B, p, refine, sigma[m], lambda[m]);
+  point_system<R>(P, st, S, B, p, refine, sigma[m], lambda[m]);
+}
+
+// ---- mixed form in three passes: records, point systems, Schur factors -------
+//
+// The point system of the mixed form is split by what each step is indexed by.
+// Observations are sorted by point, so passes over observations read the
+// problem and write the per-observation arrays coalesced (a warp stages its 32
+// records in shared memory and stores them as contiguous runs); only the FP64
+// point-system sums run a thread per point.
+
+constexpr int kObsThreads = 256;
+constexpr int kObsWarps = kObsThreads / 32;
+// Odd pitches: lanes writing the same field of their records hit distinct banks.
+constexpr int kLinPitch = kLinW + 1;
+constexpr int kZPitch = 19;
+constexpr int kGPitch = 9;
+
+// Store a warp's n (<= 32) consecutive records of W floats, staged in shared
+// memory at `pitch`, to dst[0 .. n*W): contiguous 128-byte runs per
+// instruction.  Records whose bit in `mask` is clear are left as they are.
+template <int W>
+__device__ __forceinline__ void warp_store_records(const float* sm, int pitch, float* dst, int n,
+                                                   uint32_t mask, int lane) {
+  for (int i = lane; i < n * W; i += 32) {
+    const int r = i / W;
+    if ((mask >> r) & 1u) dst[i] = sm[r * pitch + (i - r * W)];
+  }
+}
+
+// Pass 1, a thread per observation: the FP32 record (linearise_mixed: FP64
+// residual, FP32 Jacobians and weight).
+static __global__ void __launch_bounds__(kObsThreads, 4)
+    obs_record_kernel(Prob P, StateView st, IterBufs<float> B, const int32_t* active,
+                      const double* sigma) {
+  __shared__ float sm[kObsWarps][32 * kLinPitch];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t k0 = (int64_t)blockIdx.x * kObsThreads + warp * 32;
+  if (k0 >= P.no) return;
+  const int64_t k = k0 + lane;
+  float* rec = &sm[warp][lane * kLinPitch];
+  bool mine = false;
+  if (k < P.no) {
+    const uint32_t m = P.pt_model[P.obs_pt[k]];
+    if (active[m]) {
+      mine = true;
+      const double sg = sigma[m];
+      const float sg_f = (float)sg, inv_s2 = 1.0f / (sg_f * sg_f);
+      float jpf[6], wf;
+      double ev[2];
+      if (!linearise_mixed(P, st, k, sg, sg_f, inv_s2, P.model_refine[m] != 0, rec, jpf, ev, wf)) {
+#pragma unroll
+        for (int i = 0; i < kLinW; ++i) rec[i] = 0.0f;
+      }
+    }
+  }
+  const uint32_t mask = __ballot_sync(0xffffffffu, mine);
+  __syncwarp();
+  const int n = P.no - k0 < 32 ? (int)(P.no - k0) : 32;
+  warp_store_records<kLinW>(sm[warp], kLinPitch, B.lin + k0 * kLinW, n, mask, lane);
+}
+
+// Pass 2, a thread per point (in order of observation count): V and v summed
+// in FP64 from the stored FP32 records (products of FP32 numbers are exact in
+// FP64, so V^-1 v is the exact least-squares step of the stored Jacobians and
+// residuals), the damped inverse, its Cholesky factor, and the point's lens
+// entries.  Points with cond(V) above kMixedCondLimit take the FP64 path of
+// point_system_mixed_ill, which also writes their Z and gradient shares.
+static __global__ void __launch_bounds__(128, 8)
+    point_solve_mixed_kernel(Prob P, StateView st, StructView S, IterBufs<float> B,
+                             const int32_t* active, const double* lambda, const double* sigma) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= P.np) return;
+  const int64_t p = S.pt_order ? S.pt_order[tid] : tid;
+  const uint32_t m = P.pt_model[p];
+  if (!active[m]) return;
+  const bool refine = P.model_refine[m] != 0;
+  const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
+  const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
+  if (e - s < 2) {  // ba.rs:238
+    B.kept[p] = 0;
+    for (uint32_t j = l0; j < l1; ++j)
+      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
+    return;
+  }
+  double V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
+  for (uint32_t k = s; k < e; ++k) {
+    const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
+    const float4 a = o4[3], b = o4[4], c = o4[6];  // jp 12..17, e 24..25, w 26, valid 27
+    if (c.w == 0.0f) continue;
+    const double w = (double)c.z;
+    const double jp[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
+    const double e0 = c.x, e1 = c.y;
+    double q[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) q[i] = jp[i] * w;
+    V[0] = fma(q[3], jp[3], fma(q[0], jp[0], V[0]));
+    V[1] = fma(q[3], jp[4], fma(q[0], jp[1], V[1]));
+    V[2] = fma(q[3], jp[5], fma(q[0], jp[2], V[2]));
+    V[3] = fma(q[4], jp[4], fma(q[1], jp[1], V[3]));
+    V[4] = fma(q[4], jp[5], fma(q[1], jp[2], V[4]));
+    V[5] = fma(q[5], jp[5], fma(q[2], jp[2], V[5]));
+    v[0] = fma(q[3], e1, fma(q[0], e0, v[0]));
+    v[1] = fma(q[4], e1, fma(q[1], e0, v[1]));
+    v[2] = fma(q[5], e1, fma(q[2], e0, v[2]));
+  }
+  const double lam = lambda[m];
+  double A[9], Ai[9];
+  sym3_full(V, A);
+  A[0] = A[0] * (1.0 + lam) + 1e-9;  // ba.rs:262-264
+  A[4] = A[4] * (1.0 + lam) + 1e-9;
+  A[8] = A[8] * (1.0 + lam) + 1e-9;
+  const double tr = A[0] + A[4] + A[8];
+  const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                     A[2] * (A[3] * A[7] - A[4] * A[6]);
+  if (!(det > 0.0) || tr * tr * tr > 4.0 * kMixedCondLimit * det) {
+    point_system_mixed_ill(P, st, S, B, p, refine, sigma[m], lam);
+    return;
+  }
+  const bool ok = inv3(A, Ai);  // ba.rs:265
+  double L[6] = {0, 0, 0, 0, 0, 0};
+  if (ok) chol3(Ai, L);
+  B.kept[p] = ok ? 1 : 0;
+  const double zv0 = L[0] * v[0] + L[1] * v[1] + L[3] * v[2];
+  const double zv1 = L[2] * v[1] + L[4] * v[2];
+  const double zv2 = L[5] * v[2];
+  double* pl = B.ptL + 6 * (size_t)p;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) pl[i] = L[i];
+  B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
+  float* pf = B.ptf + 9 * (size_t)p;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) pf[i] = (float)L[i];
+  pf[6] = (float)(L[0] * zv0);
+  pf[7] = (float)(L[1] * zv0 + L[2] * zv1);
+  pf[8] = (float)(L[3] * zv0 + L[4] * zv1 + L[5] * zv2);
+  const float l00 = (float)L[0], l10 = (float)L[1], l11 = (float)L[2], l20 = (float)L[3],
+              l21 = (float)L[4], l22 = (float)L[5];
+  for (uint32_t j = l0; j < l1; ++j) {  // lens entries (ba.rs:251-259)
+    float Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t k = s; k < e; ++k) {
+      if (S.obs_lens[k] != j) continue;
+      const float* o = B.lin + (size_t)k * kLinW;
+      if (o[27] == 0.0f) continue;
+      const float w = o[26];
+      const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float ga = o[18 + a], gb = o[21 + a];
+        Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
+        Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
+        Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
+      }
+    }
+    float* Zl = B.Zl + (size_t)j * 9;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
+      Zl[3 * a + 0] = ok ? y0 * l00 + y1 * l10 + y2 * l20 : 0.0f;
+      Zl[3 * a + 1] = ok ? y1 * l11 + y2 * l21 : 0.0f;
+      Zl[3 * a + 2] = ok ? y2 * l22 : 0.0f;
+    }
+  }
+}
+
+// Pass 3, a thread per observation: Z = Y L (Y = w Jc^T Jp) and the
+// observation's share of the reduced gradient, Jc^T r' and Jg^T r' with
+// r' = w (e - Jp t), in FP32 from the record and the point's FP32 L and t.
+// Observations of ill-conditioned points were written by pass 2.
+static __global__ void __launch_bounds__(kObsThreads)
+    obs_factor_kernel(Prob P, IterBufs<float> B, const int32_t* active) {
+  __shared__ float smz[kObsWarps][32 * kZPitch];
+  __shared__ float smg[kObsWarps][32 * kGPitch];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t k0 = (int64_t)blockIdx.x * kObsThreads + warp * 32;
+  if (k0 >= P.no) return;
+  const int64_t k = k0 + lane;
+  float* Z = &smz[warp][lane * kZPitch];
+  float* gs = &smg[warp][lane * kGPitch];
+  bool mine = false;
+  if (k < P.no) {
+    const uint32_t p = P.obs_pt[k];
+    const uint8_t kp = B.kept[p];
+    if (active[P.pt_model[p]] && kp != 2) {
+      mine = true;
+      const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
+      float o[kLinW];
+#pragma unroll
+      for (int i = 0; i < kLinW / 4; ++i) {
+        const float4 q = o4[i];
+        o[4 * i] = q.x, o[4 * i + 1] = q.y, o[4 * i + 2] = q.z, o[4 * i + 3] = q.w;
+      }
+      if (kp == 0 || o[27] == 0.0f) {
+#pragma unroll
+        for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
+      } else {
+        const float* pf = B.ptf + 9 * (size_t)p;
+        const float l00 = pf[0], l10 = pf[1], l11 = pf[2], l20 = pf[3], l21 = pf[4], l22 = pf[5];
+        const float t0 = pf[6], t1 = pf[7], t2 = pf[8];
+        const float w = o[26];
+        const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+        const float r0 = (o[24] - (j0 * t0 + j1 * t1 + j2 * t2)) * w;
+        const float r1 = (o[25] - (j3 * t0 + j4 * t1 + j5 * t2)) * w;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          const float ca = o[r], cb = o[6 + r];
+          const float y0 = (ca * j0 + cb * j3) * w;
+          const float y1 = (ca * j1 + cb * j4) * w;
+          const float y2 = (ca * j2 + cb * j5) * w;
+          Z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
+          Z[3 * r + 1] = y1 * l11 + y2 * l21;
+          Z[3 * r + 2] = y2 * l22;
+          gs[r] = ca * r0 + cb * r1;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) gs[6 + a] = o[18 + a] * r0 + o[21 + a] * r1;
+      }
+    }
+  }
+  const uint32_t mask = __ballot_sync(0xffffffffu, mine);
+  __syncwarp();
+  const int n = P.no - k0 < 32 ? (int)(P.no - k0) : 32;
+  warp_store_records<18>(smz[warp], kZPitch, B.Z + k0 * 18, n, mask, lane);
+  warp_store_records<9>(smg[warp], kGPitch, B.gsub + k0 * 9, n, mask, lane);
 }
 
 // ---- per camera: U, g, lens terms (ba.rs:273-292) ----------------------------
@@ -686,24 +931,52 @@ static __global__ void __launch_bounds__(kCostThreads)
   const uint32_t m = S.cost_chunk_model[ch];
   if (active && !active[m]) return;
   const double sg = sigma[m];
-  const double behind = sg * sg * 10.0;  // ba.rs:116
+  const double s2 = sg * sg, inv_s2 = 1.0 / s2;
+  const double behind = s2 * 10.0;  // ba.rs:116
+  const bool cauchy = P.loss == LOSS_CAUCHY;
+  // Cauchy: sum_k s^2 ln(1 + e_k^2/s^2) = s^2 ln(prod_k (1 + e_k^2/s^2)).  The
+  // factors (each >= 1) are multiplied into `prod`, kept in [1, 2) by moving
+  // its binary exponent into `expo` after every product, and one logarithm
+  // per thread closes the sum: FP64 throughout, one rounding per product
+  // instead of one logarithm per observation.
+  double prod = 1.0;
+  int64_t expo = 0;
   double acc[3] = {0.0, 0.0, 0.0};
   for (uint32_t k = S.cost_chunk_begin[ch] + threadIdx.x; k < S.cost_chunk_end[ch];
        k += blockDim.x) {
     const uint32_t cam = P.obs_cam[k];
-    double u[2];
-    if (bacam::project(st.rot + 9 * (size_t)cam, st.center + 3 * (size_t)cam,
-                       st.intr + 5 * (size_t)P.cam_group[cam],
-                       st.points + 3 * (size_t)P.obs_pt[k], u)) {
-      const double ex = P.obs_uv[2 * (size_t)k] - u[0], ey = P.obs_uv[2 * (size_t)k + 1] - u[1];
+    const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
+    double xc[3];
+    bacam::to_cam(st.rot + 9 * (size_t)cam, st.center + 3 * (size_t)cam,
+                  st.points + 3 * (size_t)P.obs_pt[k], xc);
+    if (xc[2] > 1e-6) {  // Pose::project (geometry.rs:28-32, 66-72)
+      const double iz = 1.0 / xc[2];
+      const double px = xc[0] * iz, py = xc[1] * iz;
+      const double r2 = px * px + py * py;
+      const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
+      const double ex = P.obs_uv[2 * (size_t)k] - (K[0] * d * px + K[1]);
+      const double ey = P.obs_uv[2 * (size_t)k + 1] - (K[0] * d * py + K[2]);
       const double e2 = ex * ex + ey * ey;
-      acc[0] += robust_rho(e2, sg, P.loss);
+      if (cauchy) {
+        const double q = 1.0 + e2 * inv_s2;  // ba.rs:114
+        if (q < 1.0e300) {
+          prod *= q;
+          const int hi = __double2hiint(prod);
+          expo += (hi >> 20) - 1023;
+          prod = __hiloint2double((hi & 0x800FFFFF) | (1023 << 20), __double2loint(prod));
+        } else {
+          acc[0] += s2 * log(q);
+        }
+      } else {
+        acc[0] += robust_rho(e2, sg, P.loss);
+      }
       acc[1] += e2;
       acc[2] += 1.0;
     } else {
       acc[0] += behind;
     }
   }
+  if (cauchy) acc[0] += s2 * (log(prod) + (double)expo * 0.69314718055994530942);
   block_sum<3>(acc, scratch);
   if (threadIdx.x == 0) {
     part[3 * ch] = acc[0];

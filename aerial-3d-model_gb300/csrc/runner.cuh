@@ -390,6 +390,7 @@ struct LmEngine {
   DevBuf<R> lin, gsub, Z, Zl, S, pre, g, x, z, p;
   DevBuf<double> ptL, ptzv, part;
   DevBuf<uint8_t> kept;
+  DevBuf<float> ptf;  // mixed form only
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
@@ -483,8 +484,9 @@ struct LmEngine {
     // Camera sums are read for every camera, including ones without observations.
     camU.zero(), camgj.zero(), camgs.zero(), camX.zero(), caml.zero(), grpU.zero(), grpg.zero();
     x.zero();
+    if (sizeof(R) == 4) ptf.alloc(at_least_1(np) * 9, s);
     B = IterBufs<R>{lin, gsub, Z, Zl, ptL, ptzv, kept, camU, camgj, camgs, camX, caml,
-                    grpU, grpg, part, S, pre, g, x, cost_part};
+                    grpU, grpg, part, S, pre, g, x, cost_part, ptf.p};
     lambda.alloc(nm, s), cost.alloc(nm, s), new_cost.alloc(nm, s), rms.alloc(nm, s);
     sq.alloc(nm, s), sigma.alloc(nm, s), n_front.alloc(nm, s), pcg_total.alloc(nm, s);
     active.alloc(nm, s), accepted.alloc(nm, s), iters.alloc(nm, s), pcg_iters.alloc(nm, s);
@@ -823,8 +825,19 @@ struct LmEngine {
   void build_system() {
     const StateView cur = ctx.cur();
     T.mark(-1);
-    BA_LAUNCH(point_kernel<R><<<grid_for(ctx.np, 128), 128, 0, s>>>(P, cur, SV, B, active, lambda,
-                                                                   sigma));
+    if constexpr (sizeof(R) == 4) {
+      if (ctx.no > 0)
+        BA_LAUNCH(obs_record_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
+            P, cur, B, active, sigma));
+      BA_LAUNCH(point_solve_mixed_kernel<<<grid_for(ctx.np, 128), 128, 0, s>>>(
+          P, cur, SV, B, active, lambda, sigma));
+      if (ctx.no > 0)
+        BA_LAUNCH(obs_factor_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
+            P, B, active));
+    } else {
+      BA_LAUNCH(point_kernel<R><<<grid_for(ctx.np, 128), 128, 0, s>>>(P, cur, SV, B, active,
+                                                                     lambda, sigma));
+    }
     T.mark(BA_PHASE_POINT);
     if (ctx.nc > 0)
       BA_LAUNCH(camera_kernel<R><<<(unsigned)ctx.nc, kCamThreads, 0, s>>>(P, SV, B, active));

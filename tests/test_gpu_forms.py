@@ -69,9 +69,12 @@ def test_cluster_and_grid_kernels_agree_on_one_system():
         a = ctx.debug_step(1e-4, 1.0, Options(precision="mixed", pcg_kernel="grid"), dense=False)
         b = ctx.debug_step(1e-4, 1.0, Options(precision="mixed", pcg_kernel="cluster"),
                            dense=False)
-    # both stop on the same |r|^2 < 1e-20 |b|^2 test, which FP32 rounding can
-    # move by an iteration or two
-    assert abs(a["pcg_iters"] - b["pcg_iters"]) <= 3
+    # both stop on the same |r|^2 < 1e-20 |b|^2 test; after a few hundred
+    # iterations the FP32 residual sits at its rounding floor, where the two
+    # kernels' different summation orders move the stopping iteration by a
+    # few (up to 2 % of the count)
+    ia, ib = a["pcg_iters"], b["pcg_iters"]
+    assert abs(ia - ib) <= max(3, 0.02 * max(ia, ib)), (ia, ib)
     rel = np.linalg.norm(a["dx"] - b["dx"]) / np.linalg.norm(a["dx"])
     assert rel < 1e-3, rel
 
