@@ -94,17 +94,21 @@ static __global__ void coarse_basis_kernel(Prob P, StateView st, CoarseArgs A) {
 // row r, group g of r's model): P[r][g] = W_r^T (sum over r's blocks in g's
 // columns of S_rc W_c), 7 x 7, zero when r has no block there.  (2) A thread
 // per entry of E: the sum of P over the rows of the entry's row group, in row
-// order.  S: FP32 BSR, full symmetric storage.
+// order.  S: the FP64 values of the reduced matrix before its rounding to
+// FP32 (full symmetric BSR); the sums are FP64 and E is rounded to FP32 once.
+// The group motions nearly annihilate S (its weakest directions are the
+// similarity motions held only by the GPS priors), so W^T S W is a small
+// difference of large terms: from FP32 S it would be rounding noise.
 constexpr int kCoarseMatThreads = 256;
 
 static __global__ void __launch_bounds__(kCoarseMatThreads)
-    coarse_rowgroup_kernel(StructView SV, const float* S, CoarseArgs A, int64_t npairs,
-                           const int32_t* pair_row, const int32_t* pair_grp, float* Pbuf) {
+    coarse_rowgroup_kernel(StructView SV, const double* S, CoarseArgs A, int64_t npairs,
+                           const int32_t* pair_row, const int32_t* pair_grp, double* Pbuf) {
   const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (wid >= npairs) return;
   const int32_t r = pair_row[wid], g = pair_grp[wid];
-  float* P = Pbuf + (size_t)wid * 49;
+  double* P = Pbuf + (size_t)wid * 49;
   if (!A.active[A.grp_model[g]]) return;
   // Blocks of row r whose columns lie in rows [c0, c1) of group g.
   const int32_t c0 = A.grp_row0[g], c1 = A.grp_row1[g];
@@ -127,17 +131,17 @@ static __global__ void __launch_bounds__(kCoarseMatThreads)
   // blocks lo + q, lo + q + 4, ... (q < 4); the four partials are summed in
   // order q = 0..3.
   const int q = lane / 7, j = lane - 7 * (lane / 7);
-  float t[6] = {0, 0, 0, 0, 0, 0};
+  double t[6] = {0, 0, 0, 0, 0, 0};
   if (q < 4)
     for (uint32_t k = lo + q; k < hi; k += 4) {
-      const float* blk = S + (size_t)k * 36;
+      const double* blk = S + (size_t)k * 36;
       const float* Wc = A.W + (size_t)SV.col_idx[k] * kCoarseW;
-      float wc[6];
+      double wc[6];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) wc[i] = Wc[kCoarseModes * i + j];
+      for (int i = 0; i < 6; ++i) wc[i] = (double)Wc[kCoarseModes * i + j];
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        float v = t[i];
+        double v = t[i];
 #pragma unroll
         for (int c = 0; c < 6; ++c) v += blk[6 * i + c] * wc[c];
         t[i] = v;
@@ -145,17 +149,17 @@ static __global__ void __launch_bounds__(kCoarseMatThreads)
     }
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    const float v1 = __shfl_down_sync(kFull, t[i], 7), v2 = __shfl_down_sync(kFull, t[i], 14),
-                v3 = __shfl_down_sync(kFull, t[i], 21);
+    const double v1 = __shfl_down_sync(kFull, t[i], 7), v2 = __shfl_down_sync(kFull, t[i], 14),
+                 v3 = __shfl_down_sync(kFull, t[i], 21);
     t[i] = ((t[i] + v1) + v2) + v3;  // lanes 0..6: column j summed over q
   }
   if (lane < kCoarseModes) {
     const float* Wr = A.W + (size_t)r * kCoarseW;
 #pragma unroll
     for (int a = 0; a < kCoarseModes; ++a) {
-      float v = 0.0f;
+      double v = 0.0;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) v += Wr[kCoarseModes * i + a] * t[i];
+      for (int i = 0; i < 6; ++i) v += (double)Wr[kCoarseModes * i + a] * t[i];
       P[a * kCoarseModes + lane] = v;
     }
   }
@@ -164,7 +168,7 @@ static __global__ void __launch_bounds__(kCoarseMatThreads)
 // E entry (7 g1 + a, 7 g2 + b) of model m = sum over rows r of group g1 of
 // P[r][g2][a][b]; pairs are listed row-major by (row, group of the model).
 static __global__ void coarse_sum_kernel(CoarseArgs A, const int64_t* row_pair0,
-                                         const float* Pbuf) {
+                                         const double* Pbuf) {
   const int g1 = blockIdx.x;
   const int m = A.grp_model[g1];
   if (!A.active[m]) return;
@@ -175,10 +179,10 @@ static __global__ void coarse_sum_kernel(CoarseArgs A, const int64_t* row_pair0,
   for (int t = threadIdx.x; t < kCoarseModes * D; t += blockDim.x) {
     const int a = t / D, col = t - (t / D) * D;
     const int g2 = col / kCoarseModes, bcol = col - kCoarseModes * g2;
-    float v = 0.0f;
+    double v = 0.0;
     for (int32_t r = A.grp_row0[g1]; r < A.grp_row1[g1]; ++r)
       v += Pbuf[(size_t)(row_pair0[r] + g2) * 49 + a * kCoarseModes + bcol];
-    Em[(size_t)(kCoarseModes * (g1 - gm0) + a) * D + col] = v;
+    Em[(size_t)(kCoarseModes * (g1 - gm0) + a) * D + col] = (float)v;
   }
 }
 

@@ -893,6 +893,130 @@ __global__ void __launch_bounds__(kCamThreads)
   }
 }
 
+// Exact float -> double in integer instructions (the FP64 pipe, which also
+// executes the hardware conversion, is the bound of the FP64 sums here).
+// Zero, subnormal, infinite and NaN inputs take the hardware conversion.
+__device__ __forceinline__ double f2d_exact(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) return (double)x;
+  const uint32_t hi = (u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// Mixed form, per camera (ba.rs:273-292): U = sum w Jc^T Jc (21), X = sum w
+// Jc^T Jg (18), the lens block (6), and the sums of the observations' reduced-
+// gradient shares.  Products are FP32; every lane sums runs of kCamRun
+// observations in FP32, the warp adds its lanes' runs by a fixed butterfly and
+// folds the result into FP64 sums spread over its lanes (lane l holds entries
+// l and l + 32); the gradient shares are summed in FP64 per observation.  The
+// warps' FP64 sums are added in warp order: the result does not depend on
+// timing.  A camera sees thousands of observations: plain FP32 accumulation
+// would bury the weak, prior-only directions of the reduced system.
+constexpr int kCamMixThreads = 256;
+constexpr int kCamMixWarps = kCamMixThreads / 32;
+constexpr int kCamRun = 8;
+
+static __global__ void __launch_bounds__(kCamMixThreads)
+    camera_mixed_kernel(Prob P, StructView S, IterBufs<float> B, const int32_t* active) {
+  __shared__ double part[kCamMixWarps][kCamN + 9];
+  const int64_t c = blockIdx.x;
+  if (c >= P.nc) return;
+  const uint32_t m = P.cam_model[c];
+  if (!active[m]) return;
+  const bool refine = P.model_refine[m] != 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float acc[kCamN];
+#pragma unroll
+  for (int i = 0; i < kCamN; ++i) acc[i] = 0.0f;
+  double lo = 0.0, hi = 0.0;  // this lane's FP64 sums of entries lane, lane + 32
+  double gacc[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) gacc[i] = 0.0;
+  const uint32_t b = S.cam_ptr[c], e = S.cam_ptr[c + 1];
+  for (uint32_t base = b; base < e; base += kCamMixThreads * kCamRun) {
+    // The next observation's index is loaded one step ahead, and a record is
+    // read whole before its validity is tested: two dependent loads per step.
+    uint32_t i = base + threadIdx.x;
+    uint32_t k = i < e ? S.cam_obs[i] : 0u;
+#pragma unroll 1
+    for (int j = 0; j < kCamRun; ++j) {
+      if (i >= e) break;
+      const uint32_t in = i + kCamMixThreads;
+      const uint32_t kn = (j + 1 < kCamRun && in < e) ? S.cam_obs[in] : 0u;
+      const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
+      const float4 q6 = o4[6];  // e 24..25, w 26, valid 27
+      const float4 q0 = o4[0], q1 = o4[1], q2 = o4[2];
+      const uint32_t pt = P.obs_pt[k];
+      const float* gs = B.gsub + (size_t)k * 9;
+      float gv[6];
+#pragma unroll
+      for (int a = 0; a < 6; ++a) gv[a] = gs[a];
+      i = in, k = kn;
+      if (q6.w == 0.0f || !B.kept[pt]) continue;  // ba.rs:274-277
+      const float jc[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+      const float w = q6.z;
+      int u = 0;
+#pragma unroll
+      for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int bb = a; bb < 6; ++bb) acc[u++] += (jc[a] * jc[bb] + jc[6 + a] * jc[6 + bb]) * w;
+#pragma unroll
+      for (int a = 0; a < 6; ++a) gacc[a] += f2d_exact(gv[a]);
+      if (refine) {
+        const float4 q4 = o4[4], q5 = o4[5];
+        const float jg[6] = {q4.z, q4.w, q5.x, q5.y, q5.z, q5.w};
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb)
+            acc[21 + 3 * a + bb] += (jc[a] * jg[bb] + jc[6 + a] * jg[3 + bb]) * w;
+        int v = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int bb = a; bb < 3; ++bb)
+            acc[39 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) gacc[6 + a] += f2d_exact(gs[6 + a]);
+      }
+    }
+    // Warp-uniform: fold this round's FP32 runs into the lanes' FP64 sums.
+    float mlo = 0.0f, mhi = 0.0f;
+#pragma unroll
+    for (int t = 0; t < kCamN; ++t) {
+      const float sum = warp_sum(acc[t]);
+      acc[t] = 0.0f;
+      if (t < 32) mlo = lane == t ? sum : mlo;
+      else mhi = lane == t - 32 ? sum : mhi;
+    }
+    lo += f2d_exact(mlo);
+    hi += f2d_exact(mhi);
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) gacc[i] = warp_sum(gacc[i]);
+  part[warp][lane] = lo;
+  if (lane + 32 < kCamN) part[warp][lane + 32] = hi;
+  if (lane < 9) {
+    double g = gacc[0];
+#pragma unroll
+    for (int i = 1; i < 9; ++i) g = lane == i ? gacc[i] : g;
+    part[warp][kCamN + lane] = g;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < kCamN + 9) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kCamMixWarps; ++w) v += part[w][t];
+    if (t < 21) B.camU[21 * c + t] = v;
+    else if (t < 39) B.camX[18 * c + (t - 21)] = v;
+    else if (t < kCamN) B.caml[12 * c + (t - 39)] = v;
+    else if (t < kCamN + 6) B.camgj[6 * c + (t - kCamN)] = v, B.camgs[6 * c + (t - kCamN)] = 0.0;
+    else B.caml[12 * c + 6 + (t - kCamN - 6)] = v, B.caml[12 * c + 9 + (t - kCamN - 6)] = 0.0;
+  }
+}
+
 // ---- per lens group: sum of its cameras' lens terms, in camera order ---------
 
 static __global__ void __launch_bounds__(128)
@@ -1086,13 +1210,21 @@ __device__ __forceinline__ void load_Z18(const double* s, double* z) {
     z[2 * i] = t.x, z[2 * i + 1] = t.y;
   }
 }
+// An FP32 record of 72 bytes starts on an 8-byte boundary: read the 80 bytes
+// from the 16-byte boundary at or below it as five 16-byte loads (Z is
+// allocated with 16 bytes of padding after its last record).
 __device__ __forceinline__ void load_Z18(const float* s, float* z) {
-  const float2* v = reinterpret_cast<const float2*>(s);
+  const uintptr_t a = reinterpret_cast<uintptr_t>(s);
+  const float4* v = reinterpret_cast<const float4*>(a & ~(uintptr_t)15);
+  const bool off = (a & 15) != 0;
+  float f[20];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) {
-    const float2 t = __ldg(v + i);
-    z[2 * i] = t.x, z[2 * i + 1] = t.y;
+  for (int i = 0; i < 5; ++i) {
+    const float4 t = __ldg(v + i);
+    f[4 * i] = t.x, f[4 * i + 1] = t.y, f[4 * i + 2] = t.z, f[4 * i + 3] = t.w;
   }
+#pragma unroll
+  for (int i = 0; i < 18; ++i) z[i] = off ? f[i + 2] : f[i];
 }
 
 template <typename R>
@@ -1173,7 +1305,7 @@ __global__ void __launch_bounds__(256)
 
 template <typename R>
 __global__ void assemble_kernel(Prob P, StateView st, StructView S, IterBufs<R> B,
-                                const int32_t* active, const double* lambda) {
+                                const int32_t* active, const double* lambda, double* S64) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.ns * 36) return;
   const int64_t s = t / 36;
@@ -1217,6 +1349,13 @@ __global__ void assemble_kernel(Prob P, StateView st, StructView S, IterBufs<R> 
   const uint32_t pab = S.slot_pos_ab[s], pba = S.slot_pos_ba[s];
   if (pab < S.nz) B.S[(size_t)pab * 36 + 6 * r + c] = (R)val;
   if (a != bcol && pba < S.nz) B.S[(size_t)pba * 36 + 6 * c + r] = (R)val;
+  // Mixed form with the two-level PCG: S before its rounding to FP32, for the
+  // coarse matrix W^T S W (the gauge motions nearly annihilate S, and FP32
+  // rounding of S is as large as what is left).
+  if (S64) {
+    if (pab < S.nz) S64[(size_t)pab * 36 + 6 * r + c] = val;
+    if (a != bcol && pba < S.nz) S64[(size_t)pba * 36 + 6 * c + r] = val;
+  }
 }
 
 template <typename R>

@@ -431,7 +431,7 @@ struct LmEngine {
   DevBuf<int64_t> c_model_eoff, c_row_pair0;
   DevBuf<uint32_t> c_grp_loc;
   DevBuf<int32_t> c_pair_row, c_pair_grp;
-  DevBuf<float> c_P;
+  DevBuf<double> c_P, c_S64;
   int64_t c_npairs = 0;
   CoarseArgs cargs{};
   int32_t c_ngroups = 0;
@@ -464,7 +464,9 @@ struct LmEngine {
     SV = SB.view();
     ctx.last_nz = SB.nz, ctx.last_pairs = SB.npairs - nb, ctx.last_nl = SB.nl;
     lin.alloc(at_least_1(no) * kLinW, s), gsub.alloc(at_least_1(no) * 9, s);
-    Z.alloc(at_least_1(no) * 18, s), Zl.alloc(at_least_1(SB.nl) * 9, s);
+    // 16 bytes of padding: FP32 records are read as 16-byte vectors from the
+    // 16-byte boundary at or below each 72-byte record.
+    Z.alloc(at_least_1(no) * 18 + 4, s), Zl.alloc(at_least_1(SB.nl) * 9, s);
     ptL.alloc(at_least_1(np) * 6, s), ptzv.alloc(at_least_1(np) * 3, s);
     kept.alloc(at_least_1(np), s);
     camU.alloc(at_least_1(nc) * 21, s), camgj.alloc(at_least_1(nc) * 6, s);
@@ -485,6 +487,9 @@ struct LmEngine {
     camU.zero(), camgj.zero(), camgs.zero(), camX.zero(), caml.zero(), grpU.zero(), grpg.zero();
     x.zero();
     if (sizeof(R) == 4) ptf.alloc(at_least_1(np) * 9, s);
+    // Two-level PCG (mixed form): the FP64 values of S for the coarse matrix,
+    // written by every assembly (the autotuner assembles before it plans).
+    if (sizeof(R) == 4 && o.coarse && !implicit) c_S64.alloc(at_least_1(SB.nz) * 36, s);
     B = IterBufs<R>{lin, gsub, Z, Zl, ptL, ptzv, kept, camU, camgj, camgs, camX, caml,
                     grpU, grpg, part, S, pre, g, x, cost_part, ptf.p};
     lambda.alloc(nm, s), cost.alloc(nm, s), new_cost.alloc(nm, s), rms.alloc(nm, s);
@@ -839,8 +844,13 @@ struct LmEngine {
                                                                      lambda, sigma));
     }
     T.mark(BA_PHASE_POINT);
-    if (ctx.nc > 0)
-      BA_LAUNCH(camera_kernel<R><<<(unsigned)ctx.nc, kCamThreads, 0, s>>>(P, SV, B, active));
+    if (ctx.nc > 0) {
+      if constexpr (sizeof(R) == 4)
+        BA_LAUNCH(camera_mixed_kernel<<<(unsigned)ctx.nc, kCamMixThreads, 0, s>>>(P, SV, B,
+                                                                                 active));
+      else
+        BA_LAUNCH(camera_kernel<R><<<(unsigned)ctx.nc, kCamThreads, 0, s>>>(P, SV, B, active));
+    }
     BA_LAUNCH(group_kernel<<<grid_for(ctx.ng * 32, 128), 128, 0, s>>>(P, SV, caml, grpU, grpg,
                                                                      active));
     T.mark(BA_PHASE_CAMERA);
@@ -858,8 +868,8 @@ struct LmEngine {
       BA_LAUNCH(schur_kernel<R><<<grid_for(SB.nsub * 32, 256), 256, 0, s>>>(P, SV, B, active));
     T.mark(BA_PHASE_SCHUR);
     if (SB.ns > 0)
-      BA_LAUNCH(assemble_kernel<R><<<grid_for(SB.ns * 36, 256), 256, 0, s>>>(P, cur, SV, B, active,
-                                                                            lambda));
+      BA_LAUNCH(assemble_kernel<R><<<grid_for(SB.ns * 36, 256), 256, 0, s>>>(
+          P, cur, SV, B, active, lambda, c_S64.p));
     BA_LAUNCH(rhs_kernel<R><<<grid_for(ctx.nb * 6, 256), 256, 0, s>>>(P, cur, B, active));
     BA_LAUNCH(precond_kernel<R><<<grid_for(ctx.nb, 128), 128, 0, s>>>(P, SV, B, active));
     T.mark(BA_PHASE_ASSEMBLE);
@@ -879,7 +889,7 @@ struct LmEngine {
         if (c_npairs > 0)
           BA_LAUNCH(coarse_rowgroup_kernel<<<grid_for(c_npairs * 32, kCoarseMatThreads),
                                              kCoarseMatThreads, 0, s>>>(
-              SV, (const float*)S.p, cargs, c_npairs, c_pair_row, c_pair_grp, c_P));
+              SV, c_S64.p, cargs, c_npairs, c_pair_row, c_pair_grp, c_P));
         BA_LAUNCH(coarse_sum_kernel<<<(unsigned)c_ngroups, 256, 0, s>>>(cargs, c_row_pair0, c_P));
         BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, 0, s>>>(
             cargs));

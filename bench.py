@@ -321,6 +321,14 @@ def gpu_arm(args, ws, rank):
             if log.accepted[i] and log.new_cost[i] <= f64 * (1.0 + 1e-6):
                 hit = i
                 break
+        # Per LM iteration of the profiled solve: trial cost relative to the
+        # FP64 final cost, accepted (1/0), PCG iterations.
+        for prec in ("fp64", "mixed"):
+            lg = profile_info[prec]
+            if nmod == 1 and lg.new_cost is not None:
+                forms[prec]["lm_trace"] = [
+                    [float("%.3g" % (lg.new_cost[i] / f64 - 1.0)), int(lg.accepted[i]),
+                     int(lg.pcg_iters[i])] for i in range(int(lg.iterations))]
         if hit is not None:
             forms["mixed"]["iteration_reaching_fp64_cost"] = hit + 1
             forms["mixed"]["ms_to_fp64_cost_est"] = forms["mixed"]["ms_per_solve"] * (hit + 1) / max(
