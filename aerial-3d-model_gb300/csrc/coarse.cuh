@@ -41,6 +41,7 @@ struct CoarseArgs {
   const int32_t* row_grp;    // [nb] group of each block row (-1: lens row)
   const int32_t* active;
   float* W;                  // [nb * 42] row-major 6 x 7
+  double* W64;               // the same values in FP64 (for the coarse matrix)
   float* E;                  // per model D x D, D = 7 * groups of the model
   float* Einv;               // same layout
 };
@@ -83,10 +84,14 @@ static __global__ void coarse_basis_kernel(Prob P, StateView st, CoarseArgs A) {
     w[3][5] = -d1, w[4][5] = d0;
     w[3][6] = d0, w[4][6] = d1, w[5][6] = d2;  // scale
     float* out = A.W + (size_t)r * kCoarseW;
+    double* out64 = A.W64 + (size_t)r * kCoarseW;
 #pragma unroll
     for (int i = 0; i < 6; ++i)
 #pragma unroll
-      for (int j = 0; j < kCoarseModes; ++j) out[kCoarseModes * i + j] = w[i][j];
+      for (int j = 0; j < kCoarseModes; ++j) {
+        out[kCoarseModes * i + j] = w[i][j];
+        out64[kCoarseModes * i + j] = (double)w[i][j];
+      }
   }
 }
 
@@ -135,10 +140,10 @@ static __global__ void __launch_bounds__(kCoarseMatThreads)
   if (q < 4)
     for (uint32_t k = lo + q; k < hi; k += 4) {
       const double* blk = S + (size_t)k * 36;
-      const float* Wc = A.W + (size_t)SV.col_idx[k] * kCoarseW;
+      const double* Wc = A.W64 + (size_t)SV.col_idx[k] * kCoarseW;
       double wc[6];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) wc[i] = (double)Wc[kCoarseModes * i + j];
+      for (int i = 0; i < 6; ++i) wc[i] = Wc[kCoarseModes * i + j];
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
         double v = t[i];
@@ -153,15 +158,19 @@ static __global__ void __launch_bounds__(kCoarseMatThreads)
                  v3 = __shfl_down_sync(kFull, t[i], 21);
     t[i] = ((t[i] + v1) + v2) + v3;  // lanes 0..6: column j summed over q
   }
-  if (lane < kCoarseModes) {
-    const float* Wr = A.W + (size_t)r * kCoarseW;
+  // P = W_r^T T: the 49 entries over the 32 lanes in two rounds (an FP64
+  // warp instruction costs the same for one active lane as for 32); lane b
+  // holds column b of T.
+  const double* Wr = A.W64 + (size_t)r * kCoarseW;
 #pragma unroll
-    for (int a = 0; a < kCoarseModes; ++a) {
-      double v = 0.0;
+  for (int rd = 0; rd < 2; ++rd) {
+    const int o = lane + 32 * rd;
+    const int oo = o < kCoarseModes * kCoarseModes ? o : 0;
+    const int a = oo / kCoarseModes, b = oo - kCoarseModes * (oo / kCoarseModes);
+    double v = 0.0;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) v += (double)Wr[kCoarseModes * i + a] * t[i];
-      P[a * kCoarseModes + lane] = v;
-    }
+    for (int i = 0; i < 6; ++i) v += Wr[kCoarseModes * i + a] * __shfl_sync(kFull, t[i], b);
+    if (o < kCoarseModes * kCoarseModes) P[o] = v;
   }
 }
 
@@ -254,8 +263,9 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
     __syncthreads();
     // Inverse of the 4 x 4 pivot block (scalar Gauss-Jordan, registers),
     // then shared: rn = Pinv * (pivot rows), with Pinv itself in the pivot
-    // columns, and cn = -(pivot columns) * Pinv.
-    {
+    // columns, and cn = -(pivot columns) * Pinv.  A thread per column j < Dp
+    // (Dp <= 192 < 512 threads).
+    if ((int)threadIdx.x < Dp) {
       float pb[kInvB][kInvB];
 #pragma unroll
       for (int x = 0; x < kInvB; ++x)
@@ -338,6 +348,7 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
     }
   __syncthreads();
   float* Im = A.Einv + A.model_eoff[m];
+#pragma unroll 4
   for (int t = threadIdx.x; t < D * D; t += blockDim.x) {
     const int i = t / D, j = t - (t / D) * D;
     Im[t] = 0.5f * (Em[t] + Em[(size_t)j * D + i]);

@@ -1313,9 +1313,21 @@ __global__ void assemble_kernel(Prob P, StateView st, StructView S, IterBufs<R> 
   const uint32_t a = S.slot_row[s], bcol = S.slot_col[s];
   const uint32_t m = P.blk_model[a];
   if (!active[m]) return;
-  double sum = 0.0;  // sub-segment sums in FP64 in both forms
-  for (uint32_t u = S.slot_sub_ptr[s]; u < S.slot_sub_ptr[s + 1]; ++u)
-    sum += B.part[(size_t)u * 36 + el];
+  // Sub-segment sums in FP64 in both forms, in sub-segment order.  A block
+  // with many sub-segments (the lens block of a model: one per 512 points)
+  // is one long dependent chain: its loads are issued eight at a time.
+  double sum = 0.0;
+  const uint32_t u1 = S.slot_sub_ptr[s + 1];
+  const double* pp = B.part + el;
+  uint32_t u = S.slot_sub_ptr[s];
+  for (; u + 8 <= u1; u += 8) {
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = pp[(size_t)(u + q) * 36];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sum += v[q];
+  }
+  for (; u < u1; ++u) sum += pp[(size_t)u * 36];
   double val;
   const bool lens_a = P.blk_is_lens[a] != 0;
   if (a == bcol) {

@@ -427,6 +427,7 @@ struct LmEngine {
   // Two-level preconditioner (mixed form, cluster kernel).
   bool use_coarse = false;
   DevBuf<float> cW, cE, cEinv;
+  DevBuf<double> cW64;
   DevBuf<int32_t> c_grp_row0, c_grp_row1, c_grp_model, c_model_g0, c_row_grp, c_job_g0, c_job_g1;
   DevBuf<int64_t> c_model_eoff, c_row_pair0;
   DevBuf<uint32_t> c_grp_loc;
@@ -699,10 +700,11 @@ struct LmEngine {
       c_npairs = (int64_t)gp.pair_row.size();
       c_P.alloc(detail::at_least_1(c_npairs) * 49, s);
       cW.alloc(detail::at_least_1(ctx.nb) * kCoarseW, s);
+      cW64.alloc(detail::at_least_1(ctx.nb) * kCoarseW, s);
       cE.alloc(detail::at_least_1(gp.e_total), s), cEinv.alloc(detail::at_least_1(gp.e_total), s);
       c_ngroups = (int32_t)gp.grp_row0.size();
       cargs = CoarseArgs{c_ngroups, c_grp_row0, c_grp_row1, c_grp_model, c_model_g0,
-                         c_model_eoff, c_row_grp, active, cW, cE, cEinv};
+                         c_model_eoff, c_row_grp, active, cW, cW64, cE, cEinv};
       ca.W = cW, ca.Einv = cEinv, ca.model_eoff = c_model_eoff, ca.model_g0 = c_model_g0;
       ca.grp_row0 = c_grp_row0, ca.grp_row1 = c_grp_row1, ca.job_g0 = c_job_g0;
       ca.job_g1 = c_job_g1, ca.grp_loc = c_grp_loc;
