@@ -264,6 +264,42 @@ __device__ __forceinline__ void point_system(const Prob& P, const StateView& st,
   }
 }
 
+// Exact float -> double in integer instructions (the FP64 pipe, which also
+// executes the hardware conversion, is the bound of the FP64 sums here).
+// Zero, subnormal, infinite and NaN inputs take the hardware conversion.
+__device__ __forceinline__ double f2d_exact(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) return (double)x;
+  const uint32_t hi = (u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// Mixed form, FP32 copy of each camera's rotation (row-major), focal length
+// and radial terms k1, k2: the per-observation pass reads them instead of
+// converting FP64 state per observation.
+constexpr int kCamF = 12;
+
+static __global__ void cam_f32_kernel(Prob P, StateView st, float* camf, const int32_t* active) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= P.nc || !active[P.cam_model[c]]) return;
+  const double* R = st.rot + 9 * (size_t)c;
+  const double* K = st.intr + 5 * (size_t)P.cam_group[c];
+  float* o = camf + kCamF * (size_t)c;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) o[i] = (float)R[i];
+  o[9] = (float)K[0], o[10] = (float)K[3], o[11] = (float)K[4];
+}
+
+// 1/x for x > 0 to about 1e-14 relative: an FP32 reciprocal refined by one
+// FP64 Newton step (two FP64 instructions and two conversions instead of an
+// IEEE division).  The mixed form's residual needs this accuracy only far
+// below the FP32 rounding of the stored residual.
+__device__ __forceinline__ double rcp_newton(double x) {
+  const double r = (double)(1.0f / (float)x);
+  return fma(r, fma(-x, r, 1.0), r);
+}
+
 // Mixed form, record of an observation with extreme Jacobians, all in FP64:
 // an observation of a point barely in front of its camera has |J| up to
 // ~1e19 (w ~ 1e-24), and FP32 J^T J would overflow.  Such a record is stored
@@ -341,10 +377,11 @@ static __device__ __noinline__ void linearise_mixed_extreme(const Prob& P, const
 // nearly singular V, and any rounding between V, v and the records would be
 // amplified by V^-1.  On return `ev` is the FP64 residual matching the
 // record (whitened for an extreme record).
-__device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& st, int64_t k,
-                                                double sigma, float sigma_f, float inv_s2,
-                                                bool refine, float* out, float (&jp)[6],
-                                                double (&ev)[2], float& w) {
+__device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& st,
+                                                const float* camf, int64_t k, double sigma,
+                                                float sigma_f, float inv_s2, bool refine,
+                                                float* out, float (&jp)[6], double (&ev)[2],
+                                                float& w) {
   const uint32_t cam = P.obs_cam[k];
   const double* Rm = st.rot + 9 * (size_t)cam;
   const double* C = st.center + 3 * (size_t)cam;
@@ -354,15 +391,16 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
   bacam::to_cam(Rm, C, X, xc);
   if (xc[2] <= 1e-6) return false;
   {
-    const double iz = 1.0 / xc[2];
+    const double iz = rcp_newton(xc[2]);
     const double px = xc[0] * iz, py = xc[1] * iz;
     const double r2 = px * px + py * py;
     const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
     ev[0] = P.obs_uv[2 * k] - (K[0] * (px * d) + K[1]);
     ev[1] = P.obs_uv[2 * k + 1] - (K[0] * (py * d) + K[2]);
   }
+  const float* cf = camf + kCamF * (size_t)cam;
   const float x0 = (float)xc[0], x1 = (float)xc[1], x2 = (float)xc[2];
-  const float f = (float)K[0], k1 = (float)K[3], k2 = (float)K[4];
+  const float f = cf[9], k1 = cf[10], k2 = cf[11];
   const float iz = 1.0f / x2;
   const float px = x0 * iz, py = x1 * iz;
   const float r2 = px * px + py * py;
@@ -406,7 +444,7 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
     out[6 * r + 2] = u1 * x0 - u0 * x1;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const float pp = u0 * (float)Rm[j] + u1 * (float)Rm[3 + j] + u2 * (float)Rm[6 + j];
+      const float pp = u0 * cf[j] + u1 * cf[3 + j] + u2 * cf[6 + j];
       jp[3 * r + j] = pp;
       out[6 * r + 3 + j] = -pp;
       out[12 + 3 * r + j] = pp;
@@ -590,8 +628,8 @@ __device__ __forceinline__ void warp_store_records(const float* sm, int pitch, f
 // Pass 1, a thread per observation: the FP32 record (linearise_mixed: FP64
 // residual, FP32 Jacobians and weight).
 static __global__ void __launch_bounds__(kObsThreads, 4)
-    obs_record_kernel(Prob P, StateView st, IterBufs<float> B, const int32_t* active,
-                      const double* sigma) {
+    obs_record_kernel(Prob P, StateView st, IterBufs<float> B, const float* camf,
+                      const int32_t* active, const double* sigma) {
   __shared__ float sm[kObsWarps][32 * kLinPitch];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t k0 = (int64_t)blockIdx.x * kObsThreads + warp * 32;
@@ -607,7 +645,8 @@ static __global__ void __launch_bounds__(kObsThreads, 4)
       const float sg_f = (float)sg, inv_s2 = 1.0f / (sg_f * sg_f);
       float jpf[6], wf;
       double ev[2];
-      if (!linearise_mixed(P, st, k, sg, sg_f, inv_s2, P.model_refine[m] != 0, rec, jpf, ev, wf)) {
+      if (!linearise_mixed(P, st, camf, k, sg, sg_f, inv_s2, P.model_refine[m] != 0, rec, jpf,
+                           ev, wf)) {
 #pragma unroll
         for (int i = 0; i < kLinW; ++i) rec[i] = 0.0f;
       }
@@ -647,9 +686,10 @@ static __global__ void __launch_bounds__(128, 8)
     const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
     const float4 a = o4[3], b = o4[4], c = o4[6];  // jp 12..17, e 24..25, w 26, valid 27
     if (c.w == 0.0f) continue;
-    const double w = (double)c.z;
-    const double jp[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
-    const double e0 = c.x, e1 = c.y;
+    const double w = f2d_exact(c.z);
+    const double jp[6] = {f2d_exact(a.x), f2d_exact(a.y), f2d_exact(a.z),
+                          f2d_exact(a.w), f2d_exact(b.x), f2d_exact(b.y)};
+    const double e0 = f2d_exact(c.x), e1 = f2d_exact(c.y);
     double q[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) q[i] = jp[i] * w;
@@ -891,17 +931,6 @@ __global__ void __launch_bounds__(kCamThreads)
     for (int i = 0; i < 6; ++i) B.caml[12 * c + i] = accd[39 + i];
     for (int i = 0; i < 6; ++i) B.caml[12 * c + 6 + i] = gacc[12 + i];
   }
-}
-
-// Exact float -> double in integer instructions (the FP64 pipe, which also
-// executes the hardware conversion, is the bound of the FP64 sums here).
-// Zero, subnormal, infinite and NaN inputs take the hardware conversion.
-__device__ __forceinline__ double f2d_exact(float x) {
-  const uint32_t u = __float_as_uint(x);
-  const uint32_t ex = (u >> 23) & 0xffu;
-  if (ex == 0u || ex == 0xffu) return (double)x;
-  const uint32_t hi = (u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + (896u << 20));
-  return __hiloint2double((int)hi, (int)(u << 29));
 }
 
 // Mixed form, per camera (ba.rs:273-292): U = sum w Jc^T Jc (21), X = sum w

@@ -390,7 +390,7 @@ struct LmEngine {
   DevBuf<R> lin, gsub, Z, Zl, S, pre, g, x, z, p;
   DevBuf<double> ptL, ptzv, part;
   DevBuf<uint8_t> kept;
-  DevBuf<float> ptf;  // mixed form only
+  DevBuf<float> ptf, camf;  // mixed form only
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
@@ -487,7 +487,7 @@ struct LmEngine {
     // Camera sums are read for every camera, including ones without observations.
     camU.zero(), camgj.zero(), camgs.zero(), camX.zero(), caml.zero(), grpU.zero(), grpg.zero();
     x.zero();
-    if (sizeof(R) == 4) ptf.alloc(at_least_1(np) * 9, s);
+    if (sizeof(R) == 4) ptf.alloc(at_least_1(np) * 9, s), camf.alloc(at_least_1(nc) * kCamF, s);
     // Two-level PCG (mixed form): the FP64 values of S for the coarse matrix,
     // written by every assembly (the autotuner assembles before it plans).
     if (sizeof(R) == 4 && o.coarse && !implicit) c_S64.alloc(at_least_1(SB.nz) * 36, s);
@@ -833,9 +833,11 @@ struct LmEngine {
     const StateView cur = ctx.cur();
     T.mark(-1);
     if constexpr (sizeof(R) == 4) {
+      if (ctx.nc > 0)
+        BA_LAUNCH(cam_f32_kernel<<<grid_for(ctx.nc, 128), 128, 0, s>>>(P, cur, camf, active));
       if (ctx.no > 0)
         BA_LAUNCH(obs_record_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
-            P, cur, B, active, sigma));
+            P, cur, B, camf, active, sigma));
       BA_LAUNCH(point_solve_mixed_kernel<<<grid_for(ctx.np, 128), 128, 0, s>>>(
           P, cur, SV, B, active, lambda, sigma));
       if (ctx.no > 0)
