@@ -185,7 +185,9 @@ static __global__ void coarse_sum_kernel(CoarseArgs A, const int64_t* row_pair0,
   const int G = A.model_g0[m + 1] - gm0;
   const int D = kCoarseModes * G;
   float* Em = A.E + A.model_eoff[m];
-  for (int t = threadIdx.x; t < kCoarseModes * D; t += blockDim.x) {
+  // blockIdx.y splits the group's 7 x D entries over gridDim.y CTAs.
+  for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < kCoarseModes * D;
+       t += gridDim.y * blockDim.x) {
     const int a = t / D, col = t - (t / D) * D;
     const int g2 = col / kCoarseModes, bcol = col - kCoarseModes * g2;
     double v = 0.0;

@@ -658,6 +658,42 @@ static __global__ void __launch_bounds__(kObsThreads, 4)
   warp_store_records<kLinW>(sm[warp], kLinPitch, B.lin + k0 * kLinW, n, mask, lane);
 }
 
+// Double-float accumulation: hi + lo += w a b for FP32 w, a, b, where
+// (p, q) = w a exactly (p = w a rounded, q = fma(w, a, -p)).  The products are
+// split exactly with FMAs and added by Knuth's two-sum, so hi + lo carries
+// about 48 bits — close to FP64 — from FP32 instructions, which on this GPU
+// run 64 times faster than FP64 ones.
+__device__ __forceinline__ void df_add_prod(float& hi, float& lo, float p, float q, float b) {
+  const float a = p * b;
+  const float c = fmaf(p, b, -a) + q * b;  // the rest of (p + q) b
+  const float s = hi + a;
+  const float bb = s - hi;
+  lo += ((hi - (s - bb)) + (a - bb)) + c;
+  hi = s;
+}
+
+// Double-float accumulation hi + lo += x (Knuth's two-sum).
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bb = s - hi;
+  lo += (hi - (s - bb)) + (x - bb);
+  hi = s;
+}
+
+// Lower Cholesky factor of a symmetric positive definite 3x3 (row-major) by
+// reciprocal square roots (mixed form); a non-positive pivot gives zeros.
+__device__ __forceinline__ void chol3_rsqrt(const double* A, double* L) {
+  const double a00 = A[0], a10 = A[3], a11 = A[4], a20 = A[6], a21 = A[7], a22 = A[8];
+  const double r0 = a00 > 0.0 ? rsqrt(a00) : 0.0;
+  const double l00 = a00 * r0, l10 = a10 * r0, l20 = a20 * r0;
+  const double t11 = a11 - l10 * l10;
+  const double r1 = t11 > 0.0 ? rsqrt(t11) : 0.0;
+  const double l11 = t11 * r1, l21 = (a21 - l20 * l10) * r1;
+  const double t22 = a22 - l20 * l20 - l21 * l21;
+  const double l22 = t22 > 0.0 ? t22 * rsqrt(t22) : 0.0;
+  L[0] = l00, L[1] = l10, L[2] = l11, L[3] = l20, L[4] = l21, L[5] = l22;
+}
+
 // Pass 2, a thread per point (in order of observation count): V and v summed
 // in FP64 from the stored FP32 records (products of FP32 numbers are exact in
 // FP64, so V^-1 v is the exact least-squares step of the stored Jacobians and
@@ -681,45 +717,71 @@ static __global__ void __launch_bounds__(128, 8)
       for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
     return;
   }
-  double V[6] = {0, 0, 0, 0, 0, 0}, v[3] = {0, 0, 0};
+  // V and v as double-float sums of the stored FP32 values (about 48 bits:
+  // V^-1 v stays the exact point step of the stored records to ~1e-10
+  // relative for the well-conditioned points that use it), then FP64.
+  float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};
+  float vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0};
   for (uint32_t k = s; k < e; ++k) {
     const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
     const float4 a = o4[3], b = o4[4], c = o4[6];  // jp 12..17, e 24..25, w 26, valid 27
     if (c.w == 0.0f) continue;
-    const double w = f2d_exact(c.z);
-    const double jp[6] = {f2d_exact(a.x), f2d_exact(a.y), f2d_exact(a.z),
-                          f2d_exact(a.w), f2d_exact(b.x), f2d_exact(b.y)};
-    const double e0 = f2d_exact(c.x), e1 = f2d_exact(c.y);
-    double q[6];
+    const float w = c.z;
+    const float jp[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
+    float ph[6], pq[6];  // w jp = ph + pq exactly
 #pragma unroll
-    for (int i = 0; i < 6; ++i) q[i] = jp[i] * w;
-    V[0] = fma(q[3], jp[3], fma(q[0], jp[0], V[0]));
-    V[1] = fma(q[3], jp[4], fma(q[0], jp[1], V[1]));
-    V[2] = fma(q[3], jp[5], fma(q[0], jp[2], V[2]));
-    V[3] = fma(q[4], jp[4], fma(q[1], jp[1], V[3]));
-    V[4] = fma(q[4], jp[5], fma(q[1], jp[2], V[4]));
-    V[5] = fma(q[5], jp[5], fma(q[2], jp[2], V[5]));
-    v[0] = fma(q[3], e1, fma(q[0], e0, v[0]));
-    v[1] = fma(q[4], e1, fma(q[1], e0, v[1]));
-    v[2] = fma(q[5], e1, fma(q[2], e0, v[2]));
+    for (int i = 0; i < 6; ++i) ph[i] = w * jp[i], pq[i] = fmaf(w, jp[i], -ph[i]);
+    // V (upper triangle 00 01 02 11 12 22) += w (jp_i jp_j + jp_{3+i} jp_{3+j})
+    constexpr int VI[6] = {0, 0, 0, 1, 1, 2}, VJ[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      df_add_prod(Vh[t], Vl[t], ph[VI[t]], pq[VI[t]], jp[VJ[t]]);
+      df_add_prod(Vh[t], Vl[t], ph[3 + VI[t]], pq[3 + VI[t]], jp[3 + VJ[t]]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      df_add_prod(vh[i], vl[i], ph[i], pq[i], c.x);
+      df_add_prod(vh[i], vl[i], ph[3 + i], pq[3 + i], c.y);
+    }
   }
+  double V[6], v[3];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) V[t] = f2d_exact(Vh[t]) + f2d_exact(Vl[t]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) v[i] = f2d_exact(vh[i]) + f2d_exact(vl[i]);
   const double lam = lambda[m];
-  double A[9], Ai[9];
+  double A[9];
   sym3_full(V, A);
   A[0] = A[0] * (1.0 + lam) + 1e-9;  // ba.rs:262-264
   A[4] = A[4] * (1.0 + lam) + 1e-9;
   A[8] = A[8] * (1.0 + lam) + 1e-9;
+  // Cofactors of the first row: the determinant serves the conditioning
+  // test and the inverse (ba.rs:265; exactly-singular V is skipped).
+  const double c00 = A[4] * A[8] - A[5] * A[7];
+  const double c01 = A[5] * A[6] - A[3] * A[8];
+  const double c02 = A[3] * A[7] - A[4] * A[6];
+  const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
   const double tr = A[0] + A[4] + A[8];
-  const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
-                     A[2] * (A[3] * A[7] - A[4] * A[6]);
   if (!(det > 0.0) || tr * tr * tr > 4.0 * kMixedCondLimit * det) {
     point_system_mixed_ill(P, st, S, B, p, refine, sigma[m], lam);
     return;
   }
-  const bool ok = inv3(A, Ai);  // ba.rs:265
-  double L[6] = {0, 0, 0, 0, 0, 0};
-  if (ok) chol3(Ai, L);
-  B.kept[p] = ok ? 1 : 0;
+  double Ai[9];
+  {
+    const double id = 1.0 / det;
+    Ai[0] = c00 * id;
+    Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+    Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+    Ai[3] = c01 * id;
+    Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+    Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+    Ai[6] = c02 * id;
+    Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+    Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+  }
+  double L[6];
+  chol3_rsqrt(Ai, L);
+  B.kept[p] = 1;
   const double zv0 = L[0] * v[0] + L[1] * v[1] + L[3] * v[2];
   const double zv1 = L[2] * v[1] + L[4] * v[2];
   const double zv2 = L[5] * v[2];
@@ -755,9 +817,9 @@ static __global__ void __launch_bounds__(128, 8)
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       const float y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
-      Zl[3 * a + 0] = ok ? y0 * l00 + y1 * l10 + y2 * l20 : 0.0f;
-      Zl[3 * a + 1] = ok ? y1 * l11 + y2 * l21 : 0.0f;
-      Zl[3 * a + 2] = ok ? y2 * l22 : 0.0f;
+      Zl[3 * a + 0] = y0 * l00 + y1 * l10 + y2 * l20;
+      Zl[3 * a + 1] = y1 * l11 + y2 * l21;
+      Zl[3 * a + 2] = y2 * l22;
     }
   }
 }
@@ -938,7 +1000,8 @@ __global__ void __launch_bounds__(kCamThreads)
 // gradient shares.  Products are FP32; every lane sums runs of kCamRun
 // observations in FP32, the warp adds its lanes' runs by a fixed butterfly and
 // folds the result into FP64 sums spread over its lanes (lane l holds entries
-// l and l + 32); the gradient shares are summed in FP64 per observation.  The
+// l and l + 32); the gradient shares are summed per lane as double-float
+// pairs (about 48 bits) and then in FP64.  The
 // warps' FP64 sums are added in warp order: the result does not depend on
 // timing.  A camera sees thousands of observations: plain FP32 accumulation
 // would bury the weak, prior-only directions of the reduced system.
@@ -959,9 +1022,9 @@ static __global__ void __launch_bounds__(kCamMixThreads)
 #pragma unroll
   for (int i = 0; i < kCamN; ++i) acc[i] = 0.0f;
   double lo = 0.0, hi = 0.0;  // this lane's FP64 sums of entries lane, lane + 32
-  double gacc[9];
+  float gh[9], gl[9];         // gradient shares, double-float
 #pragma unroll
-  for (int i = 0; i < 9; ++i) gacc[i] = 0.0;
+  for (int i = 0; i < 9; ++i) gh[i] = 0.0f, gl[i] = 0.0f;
   const uint32_t b = S.cam_ptr[c], e = S.cam_ptr[c + 1];
   for (uint32_t base = b; base < e; base += kCamMixThreads * kCamRun) {
     // The next observation's index is loaded one step ahead, and a record is
@@ -991,7 +1054,7 @@ static __global__ void __launch_bounds__(kCamMixThreads)
 #pragma unroll
         for (int bb = a; bb < 6; ++bb) acc[u++] += (jc[a] * jc[bb] + jc[6 + a] * jc[6 + bb]) * w;
 #pragma unroll
-      for (int a = 0; a < 6; ++a) gacc[a] += f2d_exact(gv[a]);
+      for (int a = 0; a < 6; ++a) df_add(gh[a], gl[a], gv[a]);
       if (refine) {
         const float4 q4 = o4[4], q5 = o4[5];
         const float jg[6] = {q4.z, q4.w, q5.x, q5.y, q5.z, q5.w};
@@ -1007,7 +1070,7 @@ static __global__ void __launch_bounds__(kCamMixThreads)
           for (int bb = a; bb < 3; ++bb)
             acc[39 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) gacc[6 + a] += f2d_exact(gs[6 + a]);
+        for (int a = 0; a < 3; ++a) df_add(gh[6 + a], gl[6 + a], gs[6 + a]);
       }
     }
     // Warp-uniform: fold this round's FP32 runs into the lanes' FP64 sums.
@@ -1022,8 +1085,9 @@ static __global__ void __launch_bounds__(kCamMixThreads)
     lo += f2d_exact(mlo);
     hi += f2d_exact(mhi);
   }
+  double gacc[9];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) gacc[i] = warp_sum(gacc[i]);
+  for (int i = 0; i < 9; ++i) gacc[i] = warp_sum(f2d_exact(gh[i]) + f2d_exact(gl[i]));
   part[warp][lane] = lo;
   if (lane + 32 < kCamN) part[warp][lane + 32] = hi;
   if (lane < 9) {
@@ -1270,7 +1334,9 @@ __device__ __forceinline__ void load_Z(const IterBufs<R>& B, int64_t no, uint32_
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256)
+// FP32 form: 3 CTAs per SM (80 registers; the kernel is bound by the latency
+// of its gathers, and the extra resident warps hide more of it).
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1)
     schur_kernel(Prob P, StructView S, IterBufs<R> B, const int32_t* active) {
   const int64_t sub = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;

@@ -894,7 +894,8 @@ struct LmEngine {
           BA_LAUNCH(coarse_rowgroup_kernel<<<grid_for(c_npairs * 32, kCoarseMatThreads),
                                              kCoarseMatThreads, 0, s>>>(
               SV, c_S64.p, cargs, c_npairs, c_pair_row, c_pair_grp, c_P));
-        BA_LAUNCH(coarse_sum_kernel<<<(unsigned)c_ngroups, 256, 0, s>>>(cargs, c_row_pair0, c_P));
+        BA_LAUNCH(coarse_sum_kernel<<<dim3((unsigned)c_ngroups, 6), 224, 0, s>>>(cargs, c_row_pair0,
+                                                                            c_P));
         BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, 0, s>>>(
             cargs));
       }
