@@ -24,6 +24,8 @@
 #include "ba_common.cuh"
 #include "lm_kernels.cuh"
 
+#include <cooperative_groups.h>
+
 namespace ba {
 
 constexpr int kCoarseModes = 7;
@@ -197,164 +199,180 @@ static __global__ void coarse_sum_kernel(CoarseArgs A, const int64_t* row_pair0,
   }
 }
 
-// E^-1 per model (CTA per model): Jacobi scaling, then in-place block
-// Gauss-Jordan without pivoting (E is symmetric positive definite), four
-// pivots per step.  The 16 x 32 threads each hold a TR x TC tile of the
-// matrix in registers (TR = ceil(D / 16) <= 12, TC = ceil(D / 32) <= 6; 512
-// threads leave 128 registers each); per step the owners publish
-// the four pivot rows and columns in shared memory, every thread inverts the
-// 4 x 4 pivot block (a scalar pivot below 1e-6 of the scaled unit diagonal is
-// raised to 1e-6) and updates its tile.  The result is unscaled and
-// symmetrised.
-constexpr int kInvThreads = 512;
-constexpr int kInvTR = (kCoarseMaxDim + 15) / 16;  // 12
-constexpr int kInvTC = (kCoarseMaxDim + 31) / 32;  // 6
-constexpr int kInvB = 4;                           // pivots per step
-constexpr int kInvDimPad = ((kCoarseMaxDim + kInvB - 1) / kInvB) * kInvB;
+// E^-1 per model, one thread-block cluster of kInvCl CTAs per model: Jacobi
+// scaling, then in-place block Gauss-Jordan without pivoting (E is symmetric
+// positive definite), four pivots per step.  The matrix, padded with identity
+// to Dq = a multiple of 32 (<= 192), is split into kInvCl column slabs of
+// W = Dq / kInvCl columns, one per CTA, held in registers (a thread holds 3
+// rows x 3 columns).  Per step the CTA owning the four pivot columns
+// publishes them and the inverse of the 4 x 4 pivot block (a scalar pivot
+// below 1e-6 of the scaled unit diagonal is raised to 1e-6) in double-
+// buffered shared memory; after one cluster barrier every CTA copies them
+// through distributed shared memory and updates its slab:
+//   pivot rows        <- Pinv * (pivot rows)   (Pinv itself in the pivot columns)
+//   pivot columns     <- -(pivot columns) * Pinv
+//   everything else  -= (pivot columns) * Pinv * (pivot rows).
+// The result is unscaled and symmetrised.
+constexpr int kInvCl = 8;
+constexpr int kInvClThreads = 512;
+constexpr int kInvMaxPad = 192;  // kCoarseMaxDim rounded up to a multiple of 32
+static_assert(kInvMaxPad >= kCoarseMaxDim && kInvMaxPad % 32 == 0, "slab layout");
+static_assert(kInvMaxPad / kInvCl <= 24 && kInvClThreads == 64 * 8, "3 x 3 elements a thread");
 
-static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(CoarseArgs A) {
-  __shared__ float rowb[kInvB][kInvDimPad], colb[kInvDimPad][kInvB], dsc[kInvDimPad];
-  __shared__ float rnS[kInvB][kInvDimPad], cnS[kInvDimPad][kInvB];
-  const int m = blockIdx.x;
+static __global__ void __cluster_dims__(kInvCl, 1, 1) __launch_bounds__(kInvClThreads, 1)
+    coarse_invert_kernel(CoarseArgs A) {
+  namespace cgi = cooperative_groups;
+  cgi::cluster_group cl = cgi::this_cluster();
+  __shared__ float dsc[kInvMaxPad];
+  __shared__ __align__(16) float colP[2][kInvMaxPad][4];  // published pivot columns
+  __shared__ float pinvP[2][4][4];                        // published pivot-block inverse
+  __shared__ __align__(16) float colL[kInvMaxPad][4];     // this step's copies
+  __shared__ float pinvL[4][4];
+  __shared__ float rowL[4][kInvMaxPad / kInvCl];          // this slab's part of the pivot rows
+  const int q = (int)cl.block_rank();
+  const int m = blockIdx.x / kInvCl;  // uniform over the cluster
   if (!A.active[m]) return;
   const int D = kCoarseModes * (A.model_g0[m + 1] - A.model_g0[m]);
   if (D == 0) return;
-  const int TR = (D + 15) / 16, TC = (D + 31) / 32;
-  const int i0 = (threadIdx.x >> 5) * TR, j0 = (threadIdx.x & 31) * TC;
+  const int Dq = ((D + 31) / 32) * 32, W = Dq / kInvCl;
+  const int t = threadIdx.x, r0 = (t >> 3) * 3, c0 = (t & 7) * 3;
   float* Em = A.E + A.model_eoff[m];
-  for (int i = threadIdx.x; i < kInvDimPad; i += blockDim.x) {
+  for (int i = t; i < kInvMaxPad; i += kInvClThreads) {
     const float d = i < D ? Em[(size_t)i * D + i] : 0.0f;
     dsc[i] = d > 0.0f ? rsqrtf(d) : 0.0f;
   }
   __syncthreads();
-  // Padding rows/columns up to a multiple of four are identity.
-  const int Dp = ((D + kInvB - 1) / kInvB) * kInvB;
-  float a[kInvTR][kInvTC];
+  float a[3][3];
 #pragma unroll
-  for (int r = 0; r < kInvTR; ++r)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < kInvTC; ++c) {
-      const int i = i0 + r, j = j0 + c;
+    for (int c = 0; c < 3; ++c) {
+      const int i = r0 + r, jl = c0 + c, j = q * W + jl;
       float v = 0.0f;
-      if (r < TR && c < TC && i < Dp && j < Dp) {
+      if (i < Dq && jl < W) {
         if (i >= D || j >= D || dsc[i] == 0.0f || dsc[j] == 0.0f)
           v = i == j ? 1.0f : 0.0f;
-        else  // symmetrise the assembled E (FP32 sums in two orders) while scaling
+        else  // symmetrise the assembled E while scaling
           v = 0.5f * (Em[(size_t)i * D + j] + Em[(size_t)j * D + i]) * dsc[i] * dsc[j];
       }
       a[r][c] = v;
     }
-  for (int k0 = 0; k0 < Dp; k0 += kInvB) {
-    __syncthreads();  // the previous step's rows and columns have been used
+  for (int k0 = 0, step = 0; k0 < Dq; k0 += 4, ++step) {
+    const int buf = step & 1;
+    const int owner = k0 / W, kl = k0 - owner * W;  // W is a multiple of 4
+    __syncthreads();  // the previous step's reads of rowL, colL and pinvL are done
 #pragma unroll
-    for (int r = 0; r < kInvTR; ++r) {
-      const int i = i0 + r, br = i - k0;
-      if (r < TR && br >= 0 && br < kInvB)
+    for (int r = 0; r < 3; ++r) {
+      const int y = r0 + r - k0;
+      if (y >= 0 && y < 4)
 #pragma unroll
-        for (int c = 0; c < kInvTC; ++c)
-          if (c < TC && j0 + c < Dp) rowb[br][j0 + c] = a[r][c];
+        for (int c = 0; c < 3; ++c)
+          if (c0 + c < W) rowL[y][c0 + c] = a[r][c];
     }
+    if (q == owner) {
 #pragma unroll
-    for (int c = 0; c < kInvTC; ++c) {
-      const int j = j0 + c, bc = j - k0;
-      if (c < TC && bc >= 0 && bc < kInvB)
+      for (int c = 0; c < 3; ++c) {
+        const int x = c0 + c - kl;
+        if (x >= 0 && x < 4)
 #pragma unroll
-        for (int r = 0; r < kInvTR; ++r)
-          if (r < TR && i0 + r < Dp) colb[i0 + r][bc] = a[r][c];
-    }
-    __syncthreads();
-    // Inverse of the 4 x 4 pivot block (scalar Gauss-Jordan, registers),
-    // then shared: rn = Pinv * (pivot rows), with Pinv itself in the pivot
-    // columns, and cn = -(pivot columns) * Pinv.  A thread per column j < Dp
-    // (Dp <= 192 < 512 threads).
-    if ((int)threadIdx.x < Dp) {
-      float pb[kInvB][kInvB];
-#pragma unroll
-      for (int x = 0; x < kInvB; ++x)
-#pragma unroll
-        for (int y = 0; y < kInvB; ++y) pb[x][y] = rowb[x][k0 + y];
-#pragma unroll
-      for (int kk = 0; kk < kInvB; ++kk) {
-        const float rp = 1.0f / fmaxf(pb[kk][kk], 1e-6f);
-        float rk[kInvB], ck[kInvB];
-#pragma unroll
-        for (int y = 0; y < kInvB; ++y) rk[y] = y == kk ? rp : pb[kk][y] * rp;
-#pragma unroll
-        for (int x = 0; x < kInvB; ++x) ck[x] = pb[x][kk];
-#pragma unroll
-        for (int x = 0; x < kInvB; ++x)
-#pragma unroll
-          for (int y = 0; y < kInvB; ++y)
-            pb[x][y] = x == kk ? rk[y] : (y == kk ? -ck[x] * rp : pb[x][y] - ck[x] * rk[y]);
+          for (int r = 0; r < 3; ++r)
+            if (r0 + r < Dq) colP[buf][r0 + r][x] = a[r][c];
       }
-      for (int j = threadIdx.x; j < Dp; j += blockDim.x) {
-        const int bc = j - k0;
-        const bool pc = bc >= 0 && bc < kInvB;
+      __syncthreads();
+      if (t == 0) {  // inverse of the 4 x 4 pivot block (scalar Gauss-Jordan)
+        float pb[4][4];
 #pragma unroll
-        for (int x = 0; x < kInvB; ++x) {
-          float v = 0.0f, w = 0.0f;
+        for (int x = 0; x < 4; ++x)
 #pragma unroll
-          for (int y = 0; y < kInvB; ++y) {
-            v += pb[x][y] * rowb[y][j];
-            w += colb[j][y] * pb[y][x];
-          }
-          float pv = 0.0f;
+          for (int y = 0; y < 4; ++y) pb[x][y] = colP[buf][k0 + x][y];
 #pragma unroll
-          for (int y = 0; y < kInvB; ++y)
-            if (y == bc) pv = pb[x][y];
-          rnS[x][j] = pc ? pv : v;
-          cnS[j][x] = -w;
+        for (int kk = 0; kk < 4; ++kk) {
+          const float rp = 1.0f / fmaxf(pb[kk][kk], 1e-6f);
+          float rk[4], ck[4];
+#pragma unroll
+          for (int y = 0; y < 4; ++y) rk[y] = y == kk ? rp : pb[kk][y] * rp;
+#pragma unroll
+          for (int x = 0; x < 4; ++x) ck[x] = pb[x][kk];
+#pragma unroll
+          for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int y = 0; y < 4; ++y)
+              pb[x][y] = x == kk ? rk[y] : (y == kk ? -ck[x] * rp : pb[x][y] - ck[x] * rk[y]);
         }
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) pinvP[buf][x][y] = pb[x][y];
       }
     }
+    cl.sync();  // the owner's pivot columns and Pinv, and every slab's pivot rows
+    {
+      const float* srcC = cl.map_shared_rank(&colP[buf][0][0], (unsigned)owner);
+      const float* srcP = cl.map_shared_rank(&pinvP[buf][0][0], (unsigned)owner);
+      for (int u = t; u < Dq * 4; u += kInvClThreads) (&colL[0][0])[u] = srcC[u];
+      if (t < 16) (&pinvL[0][0])[t] = srcP[t];
+    }
     __syncthreads();
-    float rn[kInvB][kInvTC];
+    float rn[4][3];  // Pinv * (pivot rows) for this thread's columns
 #pragma unroll
-    for (int x = 0; x < kInvB; ++x)
+    for (int x = 0; x < 4; ++x)
 #pragma unroll
-      for (int c = 0; c < kInvTC; ++c) rn[x][c] = (c < TC && j0 + c < Dp) ? rnS[x][j0 + c] : 0.0f;
+      for (int c = 0; c < 3; ++c) {
+        const int jl = c0 + c < W ? c0 + c : 0;
+        float v = 0.0f;
 #pragma unroll
-    for (int r = 0; r < kInvTR; ++r) {
-      const int i = i0 + r, br = i - k0;
-      if (r >= TR || i >= Dp) continue;
-      if (br >= 0 && br < kInvB) {  // a pivot row: Pinv * (pivot rows)
-#pragma unroll
-        for (int c = 0; c < kInvTC; ++c)
-          if (c < TC && j0 + c < Dp) a[r][c] = rnS[br][j0 + c];
-        continue;
+        for (int y = 0; y < 4; ++y) v += pinvL[x][y] * rowL[y][jl];
+        rn[x][c] = v;
       }
-      float ci[kInvB];
 #pragma unroll
-      for (int y = 0; y < kInvB; ++y) ci[y] = colb[i][y];
+    for (int r = 0; r < 3; ++r) {
+      const int i = r0 + r, y = i - k0;
+      const float4 cv = *reinterpret_cast<const float4*>(&colL[i < Dq ? i : 0][0]);
+      const bool prow = y >= 0 && y < 4;
 #pragma unroll
-      for (int c = 0; c < kInvTC; ++c) {
-        const int bc = j0 + c - k0;
-        if (bc >= 0 && bc < kInvB) {  // a pivot column: -(pivot columns) * Pinv
-          a[r][c] = cnS[i][bc];
+      for (int c = 0; c < 3; ++c) {
+        const int x = c0 + c - kl;
+        const bool pcol = q == owner && x >= 0 && x < 4;
+        if (prow) {
+          a[r][c] = pcol ? pinvL[y][x] : rn[y][c];
+        } else if (pcol) {
+          float w = 0.0f;
+          w += cv.x * pinvL[0][x];
+          w += cv.y * pinvL[1][x];
+          w += cv.z * pinvL[2][x];
+          w += cv.w * pinvL[3][x];
+          a[r][c] = -w;
         } else {
           float v = a[r][c];
-#pragma unroll
-          for (int y = 0; y < kInvB; ++y) v -= ci[y] * rn[y][c];
+          v -= cv.x * rn[0][c];
+          v -= cv.y * rn[1][c];
+          v -= cv.z * rn[2][c];
+          v -= cv.w * rn[3][c];
           a[r][c] = v;
         }
       }
     }
   }
-  // Unscale into E (no longer needed), then symmetrise into E^-1.
+  // Unscale into E (no longer needed), then symmetrise into E^-1 once every
+  // slab is written.
 #pragma unroll
-  for (int r = 0; r < kInvTR; ++r)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < kInvTC; ++c) {
-      const int i = i0 + r, j = j0 + c;
-      if (r < TR && c < TC && i < D && j < D) Em[(size_t)i * D + j] = a[r][c] * dsc[i] * dsc[j];
+    for (int c = 0; c < 3; ++c) {
+      const int i = r0 + r, jl = c0 + c, j = q * W + jl;
+      if (i < D && jl < W && j < D) Em[(size_t)i * D + j] = a[r][c] * dsc[i] * dsc[j];
     }
-  __syncthreads();
+  __threadfence();
+  cl.sync();
   float* Im = A.Einv + A.model_eoff[m];
-#pragma unroll 4
-  for (int t = threadIdx.x; t < D * D; t += blockDim.x) {
-    const int i = t / D, j = t - (t / D) * D;
-    Im[t] = 0.5f * (Em[t] + Em[(size_t)j * D + i]);
-  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int i = r0 + r, jl = c0 + c, j = q * W + jl;
+      if (i < D && jl < W && j < D)
+        Im[(size_t)i * D + j] = 0.5f * (Em[(size_t)i * D + j] + Em[(size_t)j * D + i]);
+    }
 }
 
 
