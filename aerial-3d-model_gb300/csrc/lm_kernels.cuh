@@ -1535,9 +1535,34 @@ __global__ void update_cameras_kernel(Prob P, StateView cur, StateView trial, It
   }
 }
 
+// Mixed form, first pass of the back-substitution: a thread per observation
+// of a kept, well-conditioned point forms u_k = Z_k^T dx of its camera (FP32,
+// coalesced; the per-point pass then sums the point's u_k in order).
+static __global__ void __launch_bounds__(256)
+    obs_backsub_kernel(Prob P, IterBufs<float> B, float* obs_u, const int32_t* active) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= P.no) return;
+  const uint32_t p = P.obs_pt[k];
+  if (!active[P.pt_model[p]] || B.kept[p] != 1) return;
+  float z[18];
+  load_Z18(B.Z + (size_t)k * 18, z);
+  const float* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
+  float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f;
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    const float dr = d[r];
+    u0 += z[3 * r] * dr;
+    u1 += z[3 * r + 1] * dr;
+    u2 += z[3 * r + 2] * dr;
+  }
+  float* u = obs_u + 3 * (size_t)k;
+  u[0] = u0, u[1] = u1, u[2] = u2;
+}
+
 template <typename R>
 __global__ void backsub_kernel(Prob P, StructView S, StateView cur, StateView trial,
-                               IterBufs<R> B, const double* sigma, const int32_t* active) {
+                               IterBufs<R> B, const double* sigma, const int32_t* active,
+                               const float* obs_u) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= P.np) return;
   const int64_t p = S.pt_order ? S.pt_order[tid] : tid;
@@ -1580,15 +1605,24 @@ __global__ void backsub_kernel(Prob P, StructView S, StateView cur, StateView tr
     a2 = B.ptzv[3 * p + 2] - L[5] * u2;
   } else {
     R b0 = (R)B.ptzv[3 * p], b1 = (R)B.ptzv[3 * p + 1], b2 = (R)B.ptzv[3 * p + 2];
-    for (uint32_t k = s; k < e; ++k) {
-      const R* Z = B.Z + (size_t)k * 18;
-      const R* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
+    if constexpr (sizeof(R) == 4) {  // u_k from obs_backsub_kernel
+      for (uint32_t k = s; k < e; ++k) {
+        const float* u = obs_u + 3 * (size_t)k;
+        b0 -= u[0];
+        b1 -= u[1];
+        b2 -= u[2];
+      }
+    } else {
+      for (uint32_t k = s; k < e; ++k) {
+        const R* Z = B.Z + (size_t)k * 18;
+        const R* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
 #pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        const R dr = d[r];
-        b0 -= Z[3 * r] * dr;
-        b1 -= Z[3 * r + 1] * dr;
-        b2 -= Z[3 * r + 2] * dr;
+        for (int r = 0; r < 6; ++r) {
+          const R dr = d[r];
+          b0 -= Z[3 * r] * dr;
+          b1 -= Z[3 * r + 1] * dr;
+          b2 -= Z[3 * r + 2] * dr;
+        }
       }
     }
     for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j) {

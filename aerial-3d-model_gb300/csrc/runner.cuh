@@ -390,7 +390,7 @@ struct LmEngine {
   DevBuf<R> lin, gsub, Z, Zl, S, pre, g, x, z, p;
   DevBuf<double> ptL, ptzv, part;
   DevBuf<uint8_t> kept;
-  DevBuf<float> ptf, camf;  // mixed form only
+  DevBuf<float> ptf, camf, obs_u;  // mixed form only
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
@@ -487,7 +487,10 @@ struct LmEngine {
     // Camera sums are read for every camera, including ones without observations.
     camU.zero(), camgj.zero(), camgs.zero(), camX.zero(), caml.zero(), grpU.zero(), grpg.zero();
     x.zero();
-    if (sizeof(R) == 4) ptf.alloc(at_least_1(np) * 9, s), camf.alloc(at_least_1(nc) * kCamF, s);
+    if (sizeof(R) == 4) {
+      ptf.alloc(at_least_1(np) * 9, s), camf.alloc(at_least_1(nc) * kCamF, s);
+      obs_u.alloc(at_least_1(no) * 3, s);
+    }
     // Two-level PCG (mixed form): the FP64 values of S for the coarse matrix,
     // written by every assembly (the autotuner assembles before it plans).
     if (sizeof(R) == 4 && o.coarse && !implicit) c_S64.alloc(at_least_1(SB.nz) * 36, s);
@@ -930,8 +933,12 @@ struct LmEngine {
     const StateView cur = ctx.cur(), tri = ctx.trial();
     BA_LAUNCH(update_cameras_kernel<R><<<grid_for(std::max(ctx.nc, ctx.ng), 256), 256, 0, s>>>(
         P, cur, tri, B, active));
+    if constexpr (sizeof(R) == 4) {
+      if (ctx.no > 0)
+        BA_LAUNCH(obs_backsub_kernel<<<grid_for(ctx.no, 256), 256, 0, s>>>(P, B, obs_u.p, active));
+    }
     BA_LAUNCH(backsub_kernel<R><<<grid_for(ctx.np, 256), 256, 0, s>>>(P, SV, cur, tri, B, sigma,
-                                                                     active));
+                                                                     active, obs_u.p));
     T.mark(BA_PHASE_UPDATE);
   }
 
