@@ -893,16 +893,13 @@ constexpr int kCamThreads = 128;
 constexpr int kCamN = 45;  // 21 U | 18 X | 6 lens U     (storage precision)
 constexpr int kCamG = 18;  // 6 gj | 6 gs | 3 lg | 3 ls  (FP64)
 
+// FP64 form, per camera (ba.rs:273-292): every sum in FP64; a CTA per camera,
+// its observations gathered through the camera ordering.  (The mixed form
+// runs camera_mixed_kernel.)
 template <typename R>
 __global__ void __launch_bounds__(kCamThreads)
     camera_kernel(Prob P, StructView S, IterBufs<R> B, const int32_t* active) {
-  // FP64 form: every sum in FP64.  Mixed form: products in FP32, summed in
-  // FP32 over runs of kCamChunk observations and then folded into FP64 (a
-  // camera sees thousands of observations: plain FP32 accumulation would
-  // bury the weak, prior-only directions of the reduced system); the
-  // gradient is the FP64 sum of the observations' reduced-gradient shares.
-  constexpr int kCamChunk = 8;
-  constexpr bool kMixed = sizeof(R) == 4;
+  static_assert(sizeof(R) == 8, "the mixed form runs camera_mixed_kernel");
   __shared__ double scratch[kCamN * 32];
   __shared__ double gscratch[kCamG * 32];
   const int64_t c = blockIdx.x;
@@ -910,78 +907,51 @@ __global__ void __launch_bounds__(kCamThreads)
   const uint32_t m = P.cam_model[c];
   if (!active[m]) return;
   const bool refine = P.model_refine[m] != 0;
-  R acc[kCamN];
   double accd[kCamN];
   double gacc[kCamG];
 #pragma unroll
-  for (int i = 0; i < kCamN; ++i) acc[i] = (R)0, accd[i] = 0.0;
+  for (int i = 0; i < kCamN; ++i) accd[i] = 0.0;
 #pragma unroll
   for (int i = 0; i < kCamG; ++i) gacc[i] = 0.0;
-  int run = 0;
   const uint32_t b = S.cam_ptr[c], e = S.cam_ptr[c + 1];
   for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     const uint32_t k = S.cam_obs[i];
-    const R* o = B.lin + (size_t)k * kLinW;
-    if (o[27] == (R)0 || !B.kept[P.obs_pt[k]]) continue;  // ba.rs:274-277
-    const R w = o[26];
-    R jc[12];
+    const double* o = B.lin + (size_t)k * kLinW;
+    if (o[27] == 0.0 || !B.kept[P.obs_pt[k]]) continue;  // ba.rs:274-277
+    const double w = o[26];
+    double jc[12];
 #pragma unroll
     for (int t = 0; t < 12; ++t) jc[t] = o[t];
     int u = 0;
 #pragma unroll
     for (int a = 0; a < 6; ++a)
 #pragma unroll
-      for (int bb = a; bb < 6; ++bb) acc[u++] += (jc[a] * jc[bb] + jc[6 + a] * jc[6 + bb]) * w;
-    const R* gs = B.gsub + (size_t)k * 9;
-    if constexpr (kMixed) {
+      for (int bb = a; bb < 6; ++bb) accd[u++] += (jc[a] * jc[bb] + jc[6 + a] * jc[6 + bb]) * w;
+    const double* gs = B.gsub + (size_t)k * 9;
+    const double e0 = o[24], e1 = o[25];
 #pragma unroll
-      for (int a = 0; a < 6; ++a) gacc[a] += (double)gs[a];
-    } else {
-      const double e0 = (double)o[24], e1 = (double)o[25], wd = (double)w;
-#pragma unroll
-      for (int a = 0; a < 6; ++a) {
-        gacc[a] += ((double)jc[a] * e0 + (double)jc[6 + a] * e1) * wd;
-        gacc[6 + a] += (double)gs[a];
-      }
+    for (int a = 0; a < 6; ++a) {
+      gacc[a] += (jc[a] * e0 + jc[6 + a] * e1) * w;
+      gacc[6 + a] += gs[a];
     }
     if (refine) {
-      const R jg[6] = {o[18], o[19], o[20], o[21], o[22], o[23]};
+      const double jg[6] = {o[18], o[19], o[20], o[21], o[22], o[23]};
 #pragma unroll
       for (int a = 0; a < 6; ++a)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb)
-          acc[21 + 3 * a + bb] += (jc[a] * jg[bb] + jc[6 + a] * jg[3 + bb]) * w;
+          accd[21 + 3 * a + bb] += (jc[a] * jg[bb] + jc[6 + a] * jg[3 + bb]) * w;
       int v = 0;
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int bb = a; bb < 3; ++bb) acc[39 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
-      if constexpr (kMixed) {
+        for (int bb = a; bb < 3; ++bb) accd[39 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) gacc[12 + a] += (double)gs[6 + a];
-      } else {
-        const double e0 = (double)o[24], e1 = (double)o[25], wd = (double)w;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          gacc[12 + a] += ((double)jg[a] * e0 + (double)jg[3 + a] * e1) * wd;
-          gacc[15 + a] += (double)gs[6 + a];
-        }
+      for (int a = 0; a < 3; ++a) {
+        gacc[12 + a] += (jg[a] * e0 + jg[3 + a] * e1) * w;
+        gacc[15 + a] += gs[6 + a];
       }
     }
-    if constexpr (kMixed) {
-      if (++run == kCamChunk) {
-        run = 0;
-#pragma unroll
-        for (int t = 0; t < kCamN; ++t) accd[t] += (double)acc[t], acc[t] = (R)0;
-      }
-    }
-  }
-  if constexpr (kMixed) {
-#pragma unroll
-    for (int t = 0; t < kCamN; ++t) accd[t] += (double)acc[t];
-  } else {
-#pragma unroll
-    for (int t = 0; t < kCamN; ++t) accd[t] = acc[t];
   }
   block_sum<kCamN>(accd, scratch);
   block_sum<kCamG>(gacc, gscratch);
@@ -1073,7 +1043,7 @@ static __global__ void __launch_bounds__(kCamMixThreads)
         for (int a = 0; a < 3; ++a) df_add(gh[6 + a], gl[6 + a], gs[6 + a]);
       }
     }
-    // Warp-uniform: fold this round's FP32 runs into the lanes' FP64 sums.
+    // Warp-uniform: fold these runs' FP32 sums into the lanes' FP64 sums.
     float mlo = 0.0f, mhi = 0.0f;
 #pragma unroll
     for (int t = 0; t < kCamN; ++t) {
