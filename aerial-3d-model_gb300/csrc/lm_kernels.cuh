@@ -722,12 +722,26 @@ static __global__ void __launch_bounds__(128, 8)
   // relative for the well-conditioned points that use it), then FP64.
   float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};
   float vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0};
+  // The point's first lens entry (usually its only one) sums Y = w Jg^T Jp in
+  // the same pass (ba.rs:251-259); further entries take a second pass below.
+  float Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (uint32_t k = s; k < e; ++k) {
     const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
     const float4 a = o4[3], b = o4[4], c = o4[6];  // jp 12..17, e 24..25, w 26, valid 27
     if (c.w == 0.0f) continue;
     const float w = c.z;
     const float jp[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
+    if (l1 > l0 && S.obs_lens[k] == l0) {
+      const float4 g2 = o4[5];  // jg 20..23
+      const float jg[6] = {b.z, b.w, g2.x, g2.y, g2.z, g2.w};
+#pragma unroll
+      for (int t = 0; t < 3; ++t) {
+        const float ga = jg[t], gb = jg[3 + t];
+        Y[3 * t + 0] += (ga * jp[0] + gb * jp[3]) * w;
+        Y[3 * t + 1] += (ga * jp[1] + gb * jp[4]) * w;
+        Y[3 * t + 2] += (ga * jp[2] + gb * jp[5]) * w;
+      }
+    }
     float ph[6], pq[6];  // w jp = ph + pq exactly
 #pragma unroll
     for (int i = 0; i < 6; ++i) ph[i] = w * jp[i], pq[i] = fmaf(w, jp[i], -ph[i]);
@@ -798,8 +812,11 @@ static __global__ void __launch_bounds__(128, 8)
   const float l00 = (float)L[0], l10 = (float)L[1], l11 = (float)L[2], l20 = (float)L[3],
               l21 = (float)L[4], l22 = (float)L[5];
   for (uint32_t j = l0; j < l1; ++j) {  // lens entries (ba.rs:251-259)
-    float Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (uint32_t k = s; k < e; ++k) {
+    if (j > l0) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) Y[i] = 0.0f;
+    }
+    for (uint32_t k = s; k < e && j > l0; ++k) {
       if (S.obs_lens[k] != j) continue;
       const float* o = B.lin + (size_t)k * kLinW;
       if (o[27] == 0.0f) continue;
