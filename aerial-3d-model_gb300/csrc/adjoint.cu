@@ -184,7 +184,7 @@ void context_cost(Context& c, const ba_options* opt, double* cost, double* rms, 
   check(cudaMemcpyAsync(sg.p, h_sg.data(), 8 * c.nm, cudaMemcpyHostToDevice, s), "h2d");
   BA_LAUNCH(cost_chunk_kernel<<<(unsigned)std::max<int64_t>(pl.n, 1), kCostThreads, 0, s>>>(
       P, c.cur(), SV, part, nullptr, sg));
-  BA_LAUNCH(cost_final_kernel<<<grid_for(c.nm * 32, 128), 128, 0, s>>>(P, c.cur(), SV, part,
+  BA_LAUNCH(cost_final_kernel<<<(unsigned)c.nm, kCostFinalThreads, 0, s>>>(P, c.cur(), SV, part,
                                                                       nullptr, dc, dsq, dn));
   std::vector<double> hc(c.nm), hsq(c.nm);
   std::vector<int64_t> hn(c.nm);

@@ -1189,32 +1189,34 @@ static __global__ void __launch_bounds__(kCostThreads)
   }
 }
 
-// Warp per model: chunk partials in order, plus the GPS prior term.
-static __global__ void cost_final_kernel(Prob P, StateView st, StructView S, const double* part,
-                                  const int32_t* active, double* cost, double* sq,
-                                  int64_t* n_front) {
-  const int64_t m = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+// CTA per model: the chunk partials and the GPS prior term over the model's
+// cameras (ba.rs:103-128), summed in a fixed order (strided per thread, then
+// the block's fixed tree).
+constexpr int kCostFinalThreads = 256;
+
+static __global__ void __launch_bounds__(kCostFinalThreads)
+    cost_final_kernel(Prob P, StateView st, StructView S, const double* part,
+                      const int32_t* active, double* cost, double* sq, int64_t* n_front) {
+  __shared__ double scratch[4 * 32];
+  const int64_t m = blockIdx.x;
   if (m >= P.nm) return;
   if (active && !active[m]) return;
-  double a[3] = {0.0, 0.0, 0.0};
-  for (uint32_t c = S.model_chunk0[m] + lane; c < S.model_chunk0[m + 1]; c += 32)
+  double a[4] = {0.0, 0.0, 0.0, 0.0};  // robust cost, squared residuals, count, prior
+  for (uint32_t c = S.model_chunk0[m] + threadIdx.x; c < S.model_chunk0[m + 1]; c += blockDim.x)
     for (int i = 0; i < 3; ++i) a[i] += part[3 * (size_t)c + i];
-  double pr = 0.0;
   if (P.prior_mask) {
-    for (uint32_t c = P.model_cam0[m] + lane; c < P.model_cam0[m + 1]; c += 32) {
+    for (uint32_t c = P.model_cam0[m] + threadIdx.x; c < P.model_cam0[m + 1]; c += blockDim.x) {
       if (!P.prior_mask[c]) continue;
       const double* q = P.prior + 6 * (size_t)c;
       const double dx = st.center[3 * (size_t)c] - q[0];
       const double dy = st.center[3 * (size_t)c + 1] - q[1];
       const double dz = st.center[3 * (size_t)c + 2] - q[2];
-      pr += (dx / q[3]) * (dx / q[3]) + (dy / q[4]) * (dy / q[4]) + (dz / q[5]) * (dz / q[5]);
+      a[3] += (dx / q[3]) * (dx / q[3]) + (dy / q[4]) * (dy / q[4]) + (dz / q[5]) * (dz / q[5]);
     }
   }
-  for (int i = 0; i < 3; ++i) a[i] = warp_sum(a[i]);
-  pr = warp_sum(pr);
-  if (lane == 0) {
-    cost[m] = a[0] + pr;
+  block_sum<4>(a, scratch);
+  if (threadIdx.x == 0) {
+    cost[m] = a[0] + a[3];
     sq[m] = a[1];
     n_front[m] = (int64_t)a[2];
   }

@@ -827,7 +827,7 @@ struct LmEngine {
                  int64_t* out_n) {
     BA_LAUNCH(cost_chunk_kernel<<<(unsigned)detail::at_least_1(SB.ncost), kCostThreads, 0, s>>>(
         P, st, SV, cost_part, act, sigma));
-    BA_LAUNCH(cost_final_kernel<<<grid_for(ctx.nm * 32, 128), 128, 0, s>>>(
+    BA_LAUNCH(cost_final_kernel<<<(unsigned)ctx.nm, kCostFinalThreads, 0, s>>>(
         P, st, SV, cost_part, act, out_cost, out_sq, out_n));
   }
 
