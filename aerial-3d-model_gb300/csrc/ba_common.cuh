@@ -17,9 +17,11 @@ enum : uint32_t {
   ERR_UNSORTED = 4u,         // observations not sorted by point
   ERR_MODEL_MIX = 8u,        // observation links a camera and a point of different models
   ERR_STRUCTURE = 16u,       // internal index check failed (write skipped)
+  ERR_NONFINITE = 32u,       // NaN / Inf in a measurement, prior or initial state; sigma <= 0
 };
 
-// Spin limit of every device-side wait: ~2 s at the maximum SM clock.
+// Default spin limit of every device-side wait: ~2 s at the maximum SM clock
+// (ba_options.wait_limit_cycles overrides it).
 constexpr long long kSpinCycles = 4000000000LL;
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -56,53 +58,6 @@ __device__ __forceinline__ void block_sum(T (&v)[N], T* scratch) {
     }
   }
   __syncthreads();
-}
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-// Barrier over the `n` CTAs of one group.  bar[0] counts arrivals, bar[1] is
-// the generation.  Bounded: after kSpinCycles the waiter sets
-// ERR_BARRIER_TIMEOUT and every CTA of every group leaves at its next wait.
-// Returns false on timeout (the caller must return).
-__device__ __forceinline__ bool group_sync(unsigned* bar, unsigned n,
-                                           unsigned* err) {
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    if (n > 1) {
-      const unsigned gen = ld_acquire(bar + 1);
-      __threadfence();
-      const unsigned arrived = atomicAdd(bar, 1u);
-      if (arrived == n - 1) {
-        atomicExch(bar, 0u);
-        __threadfence();
-        atomicAdd(bar + 1, 1u);
-      } else {
-        const long long t0 = clock64();
-        while (ld_acquire(bar + 1) == gen) {
-          __nanosleep(20);
-          if ((*(volatile unsigned*)err) & ERR_BARRIER_TIMEOUT) {
-            ok = 0;
-            break;
-          }
-          if (clock64() - t0 > kSpinCycles) {
-            atomicOr(err, ERR_BARRIER_TIMEOUT);
-            ok = 0;
-            break;
-          }
-        }
-        __threadfence();
-      }
-    }
-    ok_s = ok;
-  }
-  __syncthreads();
-  return ok_s != 0;
 }
 
 // Symmetric 3x3 stored as 6 upper entries: 00 01 02 11 12 22.

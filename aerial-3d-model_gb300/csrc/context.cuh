@@ -109,6 +109,9 @@ struct Opts {
   int32_t autotune = 0;    // tune the PCG configuration before solving
   int32_t stop_patience = 0;  // 0 or 1: the reference's stop rule
   int32_t coarse = 0;         // mixed cluster PCG: two-level preconditioner
+  int32_t hold_cta = 0;       // fault injection: grid PCG CTA hold_cta-1 skips its exchanges
+  long long wait_limit = kSpinCycles;  // spin limit of device-side waits (cycles)
+  int64_t workspace_limit = 0;         // device bytes the call may hold (0: no limit)
 };
 
 // One solve of the uploaded batch from its initial states, in precision R.

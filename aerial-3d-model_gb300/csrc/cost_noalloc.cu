@@ -14,6 +14,11 @@
 // contents.  Each call writes every partial it later reads, so nothing needs
 // clearing; but calls whose kernels overlap on the GPU (different streams, or
 // different host threads on one stream without ordering) race on it.
+//
+// Indices are checked in the kernel: an observation whose camera, point or
+// lens group is out of range is skipped and counted, and the call returns
+// BA_BAD_INPUT (the solver's own upload check, ERR_BAD_INDEX, rejects the
+// same inputs).
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -31,9 +36,11 @@ constexpr int64_t kNoAllocChunkObs = 4096;
 constexpr int64_t kNoAllocChunks = 8192;  // 8192 x 4096 = 33,554,432 observations
 constexpr int kMaxDevices = 64;
 
-// Scratch of ba_robust_cost_noalloc: [kNoAllocChunks][3] partials (cost, sum
-// of squares, count), then 3 doubles of result.  196,632 bytes per device.
-__device__ __align__(256) double g_noalloc_scratch[kNoAllocChunks * 3 + 3];
+// Scratch of ba_robust_cost_noalloc: [kNoAllocChunks][4] partials (cost, sum
+// of squares, count, observations with an index out of range), then 4
+// doubles of result.  262,176 bytes per device.
+constexpr int kNoAllocParts = 4;
+__device__ __align__(256) double g_noalloc_scratch[kNoAllocChunks * kNoAllocParts + kNoAllocParts];
 
 __device__ __forceinline__ double rho(double e2, double sigma, int loss) {
   if (loss == BA_LOSS_HUBER) {
@@ -46,18 +53,27 @@ __device__ __forceinline__ double rho(double e2, double sigma, int loss) {
 
 __global__ void __launch_bounds__(kNoAllocThreads)
     noalloc_chunk_kernel(ba_problem P, ba_state st, double sigma, int loss, double* scratch) {
-  __shared__ double red[3 * 32];
+  __shared__ double red[kNoAllocParts * 32];
   const int64_t ch = blockIdx.x;
   const int64_t b = ch * kNoAllocChunkObs;
   const int64_t e = min(P.n_obs, b + kNoAllocChunkObs);
   const double behind = sigma * sigma * 10.0;  // ba.rs:116
-  double acc[3] = {0.0, 0.0, 0.0};
+  double acc[kNoAllocParts] = {0.0, 0.0, 0.0, 0.0};
   for (int64_t k = b + threadIdx.x; k < e; k += blockDim.x) {
-    const uint32_t cam = P.obs_cam[k];
+    const uint32_t cam = P.obs_cam[k], pt = P.obs_pt[k];
+    // Every index is checked before it addresses memory.
+    if ((int64_t)cam >= P.n_cams || (int64_t)pt >= P.n_points) {
+      acc[3] += 1.0;
+      continue;
+    }
+    const uint32_t grp = P.cam_group[cam];
+    if ((int64_t)grp >= P.n_groups) {
+      acc[3] += 1.0;
+      continue;
+    }
     double u[2];
     if (bacam::project(st.rot + 9 * (size_t)cam, st.center + 3 * (size_t)cam,
-                       st.intr + 5 * (size_t)P.cam_group[cam],
-                       st.points + 3 * (size_t)P.obs_pt[k], u)) {
+                       st.intr + 5 * (size_t)grp, st.points + 3 * (size_t)pt, u)) {
       const double ex = P.obs_uv[2 * k] - u[0], ey = P.obs_uv[2 * k + 1] - u[1];
       const double e2 = ex * ex + ey * ey;
       acc[0] += rho(e2, sigma, loss);
@@ -67,17 +83,17 @@ __global__ void __launch_bounds__(kNoAllocThreads)
       acc[0] += behind;
     }
   }
-  block_sum<3>(acc, red);
+  block_sum<kNoAllocParts>(acc, red);
   if (threadIdx.x == 0)
-    for (int i = 0; i < 3; ++i) scratch[3 * ch + i] = acc[i];
+    for (int i = 0; i < kNoAllocParts; ++i) scratch[kNoAllocParts * ch + i] = acc[i];
 }
 
 __global__ void noalloc_final_kernel(ba_problem P, ba_state st, int64_t nchunks,
                                      double* scratch) {
   const int lane = threadIdx.x;
-  double a[3] = {0.0, 0.0, 0.0};
+  double a[kNoAllocParts] = {0.0, 0.0, 0.0, 0.0};
   for (int64_t c = lane; c < nchunks; c += 32)
-    for (int i = 0; i < 3; ++i) a[i] += scratch[3 * c + i];
+    for (int i = 0; i < kNoAllocParts; ++i) a[i] += scratch[kNoAllocParts * c + i];
   double pr = 0.0;  // ba.rs:120-126
   if (P.prior_mask) {
     for (int64_t c = lane; c < P.n_cams; c += 32) {
@@ -88,13 +104,14 @@ __global__ void noalloc_final_kernel(ba_problem P, ba_state st, int64_t nchunks,
       pr += (dx / q[3]) * (dx / q[3]) + (dy / q[4]) * (dy / q[4]) + (dz / q[5]) * (dz / q[5]);
     }
   }
-  for (int i = 0; i < 3; ++i) a[i] = warp_sum(a[i]);
+  for (int i = 0; i < kNoAllocParts; ++i) a[i] = warp_sum(a[i]);
   pr = warp_sum(pr);
   if (lane == 0) {
-    double* out = scratch + 3 * kNoAllocChunks;
+    double* out = scratch + kNoAllocParts * kNoAllocChunks;
     out[0] = a[0] + pr;
     out[1] = a[1];
     out[2] = a[2];
+    out[3] = a[3];
   }
 }
 
@@ -148,11 +165,14 @@ extern "C" ba_status ba_robust_cost_noalloc(const ba_problem* problem, const ba_
       BA_LAUNCH(noalloc_chunk_kernel<<<(unsigned)nchunks, kNoAllocThreads, 0, s>>>(
           P, S, sigma_px, loss, scratch));
     BA_LAUNCH(noalloc_final_kernel<<<1, 32, 0, s>>>(P, S, nchunks, scratch));
-    double out[3];
-    check(cudaMemcpyAsync(out, scratch + 3 * kNoAllocChunks, sizeof out, cudaMemcpyDeviceToHost,
-                          s),
+    double out[kNoAllocParts];
+    check(cudaMemcpyAsync(out, scratch + kNoAllocParts * kNoAllocChunks, sizeof out,
+                          cudaMemcpyDeviceToHost, s),
           "d2h");
     check(cudaStreamSynchronize(s), "cost");
+    if (out[3] > 0.0)
+      throw BadInput(std::to_string((int64_t)out[3]) +
+                     " observations have a camera, point or lens group index out of range");
     if (cost) *cost = out[0];
     if (rms) *rms = std::sqrt(out[1] / std::max(out[2], 1.0));
     if (n_in_front) *n_in_front = (int64_t)out[2];

@@ -67,6 +67,8 @@ struct PcgArgs {
   int32_t max_iter;
   double tol;
   unsigned* err;
+  long long spin;    // spin limit of a group wait, in SM clock cycles
+  int32_t hold_cta;  // fault injection: CTA hold_cta - 1 leaves before its first exchange (0: off)
 };
 
 // Partial-sum slots.  Grid kernel: 0,1 init (rz, bb) | 2..5 (pq, lens q
@@ -148,9 +150,9 @@ __device__ __forceinline__ double sum8(double v) {
 // (release) after publishing its partials, and waits (acquire) until the
 // counter reaches `target`, which grows by the group size per exchange from
 // the launch's base value.  Only warp 0 of a CTA takes part; the partials are
-// then read with all loads in flight at once.  Bounded: after kSpinCycles the
-// waiter sets ERR_BARRIER_TIMEOUT; every CTA leaves at its next exchange.
-// Args: any type with part, ncta, bar and err as in PcgArgs.
+// then read with all loads in flight at once.  Bounded: after A.spin cycles
+// the waiter sets ERR_BARRIER_TIMEOUT; every CTA leaves at its next exchange.
+// Args: any type with part, ncta, bar, err and spin as in PcgArgs.
 template <int N, typename Args, typename Post>
 __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm, double* tot,
                                              const Args& A, const PcgJob& J, int slot,
@@ -189,7 +191,7 @@ __device__ __forceinline__ bool group_reduce(const double (&wv)[N], double* wsm,
             ok = 0;
             break;
           }
-          if (clock64() - t0 > kSpinCycles) {
+          if (clock64() - t0 > A.spin) {
             atomicOr(A.err, ERR_BARRIER_TIMEOUT);
             ok = 0;
             break;
@@ -482,6 +484,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel(PcgArgs<R> A) {
   __shared__ PcgScalars<R> sc;
   extern __shared__ __align__(16) unsigned char pcg_smem[];
   R* rs = reinterpret_cast<R*>(pcg_smem);
+  // Fault injection (tests of the timeout path): this CTA never arrives, so
+  // the other members of its group give up after A.spin cycles.
+  if (A.hold_cta > 0 && (int32_t)blockIdx.x == A.hold_cta - 1) return;
   for (int jb = A.cta_job0[blockIdx.x]; jb < A.cta_job0[blockIdx.x + 1]; ++jb) {
     const PcgJob J = A.jobs[jb];
     if (!A.active[J.model]) continue;

@@ -53,6 +53,7 @@ struct ImpArgs {
   int32_t* iters;
   int32_t max_iter;
   double tol;
+  long long spin;  // spin limit of a group wait, in SM clock cycles
 };
 
 // Implicit-product scalars, computed once per CTA by thread 0.

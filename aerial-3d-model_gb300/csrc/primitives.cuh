@@ -40,6 +40,34 @@ inline size_t& dev_bytes_peak() {
   return v;
 }
 
+// Device-memory budget of the current call on this thread: DevBuf
+// allocations that would take the bytes held since the call began above
+// `limit` fail with cudaErrorMemoryAllocation (BA_OOM) before cudaMallocAsync
+// is called.  limit 0: no budget.
+struct DevBudget {
+  int64_t limit = 0, base = 0;
+};
+inline DevBudget& dev_budget() {
+  static thread_local DevBudget b;
+  return b;
+}
+// Sets the budget for its scope; an enclosing budget (ba_solve around its
+// upload and solve) stays in force.
+struct DevBudgetScope {
+  bool set = false;
+  explicit DevBudgetScope(int64_t limit) {
+    if (limit > 0 && dev_budget().limit == 0) {
+      dev_budget() = DevBudget{limit, (int64_t)dev_bytes_live()};
+      set = true;
+    }
+  }
+  ~DevBudgetScope() {
+    if (set) dev_budget() = DevBudget{};
+  }
+  DevBudgetScope(const DevBudgetScope&) = delete;
+  DevBudgetScope& operator=(const DevBudgetScope&) = delete;
+};
+
 // Stream-ordered device buffer (cudaMallocAsync from the device's default
 // pool, whose release threshold the context raises so freed blocks are
 // reused by the next solve instead of being returned to the driver).
@@ -67,6 +95,15 @@ struct DevBuf {
     s = st;
     n = count;
     if (count) {
+      const DevBudget& bud = dev_budget();
+      if (bud.limit > 0 &&
+          (int64_t)dev_bytes_live() - bud.base + (int64_t)(count * sizeof(T)) > bud.limit) {
+        n = 0;
+        throw CudaError(cudaErrorMemoryAllocation,
+                        "device allocation of " + std::to_string(count * sizeof(T)) +
+                            " bytes beyond the call's workspace limit of " +
+                            std::to_string(bud.limit) + " bytes");
+      }
       cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), st);
       if (e != cudaSuccess) {
         p = nullptr;

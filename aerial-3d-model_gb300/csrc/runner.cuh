@@ -588,7 +588,7 @@ struct LmEngine {
     pcg_part.alloc(kParts * (size_t)imp_ncta, s);
     ia = ImpArgs<R>{bar, bar_base, pcg_part, imp_ncta, ctx.err, P, SV, Z, Zl, kept, own, camX,
                     pre, g, x, rbuf, z, p, qbuf, tbuf, h_lens[0], (int32_t)ctx.nb, pcg_iters,
-                    o.pcg_max_iter, o.pcg_tol};
+                    o.pcg_max_iter, o.pcg_tol, o.wait_limit};
     ctx.last_pcg_kernel = 3, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = imp_ncta;
   }
 
@@ -606,7 +606,8 @@ struct LmEngine {
     check(cudaStreamSynchronize(s), "sync");  // host plan vectors
     pa = PcgArgs<R>{jobs, cta_job0, bar, bar_base, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx,
                     S, pre, g, x, z, p, ctx.nb, lens_row, lens_pos, SB.diag_pos, smem_rows,
-                    smem_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol, ctx.err};
+                    smem_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol, ctx.err,
+                    o.wait_limit, o.hold_cta};
     grid_rows_target = rows_target;
     ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = plan.ncta;
   }
@@ -972,8 +973,10 @@ struct LmEngine {
     check(cudaMemcpyAsync(h_cost0.data(), cost.p, 8 * nm, cudaMemcpyDeviceToHost, s), "d2h");
     check(cudaMemcpyAsync(h_sq0.data(), sq.p, 8 * nm, cudaMemcpyDeviceToHost, s), "d2h");
     check(cudaMemcpyAsync(h_n0.data(), n_front.p, 8 * nm, cudaMemcpyDeviceToHost, s), "d2h");
+    // Pinned words read after every LM iteration: [0] any model active,
+    // [1] the device error bits (a wait that gave up ends the solve).
     int32_t* h_any = nullptr;
-    check(cudaMallocHost((void**)&h_any, sizeof(int32_t)), "pinned");
+    check(cudaMallocHost((void**)&h_any, 2 * sizeof(int32_t)), "pinned");
     struct PinnedFree {
       int32_t* p;
       ~PinnedFree() { cudaFreeHost(p); }
@@ -991,9 +994,10 @@ struct LmEngine {
         iteration();
       }
       check(cudaMemcpyAsync(h_any, any.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
+      check(cudaMemcpyAsync(h_any + 1, ctx.err.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
       check(cudaStreamSynchronize(s), "lm iteration");
       T.flush(ctx.phase_ms, ctx.phase_n);
-      if (!*h_any) break;
+      if (!h_any[0] || h_any[1]) break;
     }
     ctx.last_graph = graph.exec != nullptr;
     eval_cost(ctx.cur(), nullptr, cost, sq, n_front);  // ba.rs:385

@@ -169,9 +169,10 @@ void upload(Context& c, const ba_problem* P, const ba_state* S, int32_t n) {
   check(cudaStreamSynchronize(s), "upload");
   c.last_h2d_ms = now_ms() - t0;
   c.last_h2d_bytes = bytes;
-  // Validate indices and ordering once (device).
+  // Validate indices, ordering and finiteness once (device).
   c.err.zero();
-  validate_problem(c.prob(0), c.grp_model, c.err, s);
+  validate_problem(c.prob(0), StateView{c.init_rot, c.init_center, c.init_intr, c.init_points},
+                   c.grp_model, c.err, s);
   uint32_t e = 0;
   check(cudaMemcpyAsync(&e, c.err.p, 4, cudaMemcpyDeviceToHost, s), "d2h");
   check(cudaStreamSynchronize(s), "validate");
@@ -184,6 +185,8 @@ void upload(Context& c, const ba_problem* P, const ba_state* S, int32_t n) {
     if (e & ERR_BAD_INDEX) msg += " camera/point/group index out of range;";
     if (e & ERR_UNSORTED) msg += " observations are not sorted by point;";
     if (e & ERR_MODEL_MIX) msg += " an observation links different models;";
+    if (e & ERR_NONFINITE)
+      msg += " a measurement, prior or initial state value is not finite (or a prior sigma <= 0);";
     throw BadInput(msg);
   }
 }
@@ -233,6 +236,9 @@ Opts resolve_options(const ba_options* o) {
     r.autotune = o->autotune;
     r.stop_patience = o->stop_patience;
     r.coarse = o->coarse;
+    r.hold_cta = o->fault_hold_pcg_cta;
+    if (o->wait_limit_cycles > 0) r.wait_limit = o->wait_limit_cycles;
+    r.workspace_limit = o->workspace_limit_bytes > 0 ? o->workspace_limit_bytes : 0;
   }
   if (r.max_iter < 0) throw BadInput("max_iter must be >= 0");
   if (!(r.sigma > 0.0) || !std::isfinite(r.sigma)) throw BadInput("sigma_px must be finite and > 0");
@@ -242,6 +248,7 @@ Opts resolve_options(const ba_options* o) {
   if (r.pcg_kernel < 0 || r.pcg_kernel > 2) throw BadInput("unknown pcg_kernel");
   if (r.stop_patience < 0) throw BadInput("stop_patience must be >= 0");
   if (r.coarse != 0 && r.coarse != 1) throw BadInput("coarse must be 0 or 1");
+  if (r.hold_cta < 0) throw BadInput("fault_hold_pcg_cta must be >= 0");
   return r;
 }
 
@@ -312,6 +319,7 @@ void solve(Context& c, const ba_options* opt, ba_stats* stats) {
   if (!c.uploaded) throw BadInput("no problem uploaded");
   const Opts o = resolve_options(opt);
   check(cudaSetDevice(c.device), "cudaSetDevice");
+  DevBudgetScope budget(o.workspace_limit);
   const int64_t l0 = g_launches;
   dev_bytes_peak() = dev_bytes_live();
   const double t0 = now_ms();
@@ -325,6 +333,8 @@ void solve(Context& c, const ba_options* opt, ba_stats* stats) {
   check(cudaStreamSynchronize(c.stream), "solve");
   if (e & ERR_BARRIER_TIMEOUT)
     throw CudaError(cudaErrorLaunchTimeout, "a device-side barrier gave up waiting");
+  if (e)
+    throw CudaError(cudaErrorAssert, "device check failed (error bits " + std::to_string(e) + ")");
   const double t1 = now_ms();
   if (stats) {
     for (int64_t m = 0; m < c.nm; ++m) {
@@ -431,6 +441,8 @@ ba_status ba_solve_batch(const ba_problem* problems, ba_state* states, int32_t n
   // call must not race another thread's call.
   ba_context* c = nullptr;
   const double t0 = now_ms();
+  // The workspace limit covers the whole call: problem copies and solve.
+  DevBudgetScope budget(opt ? opt->workspace_limit_bytes : 0);
   ba_status st = ba_context_create(-1, opt ? opt->stream : nullptr, &c);
   if (st != BA_OK) return st;
   st = ba_context_upload(c, problems, states, n);

@@ -21,26 +21,41 @@
 namespace ba {
 namespace {
 
-__global__ void validate_kernel(Prob P, const uint32_t* grp_model, uint32_t* err) {
+__device__ __forceinline__ bool all_finite(const double* v, int n) {
+  bool ok = true;
+  for (int i = 0; i < n; ++i) ok = ok && isfinite(v[i]);
+  return ok;
+}
+
+__global__ void validate_kernel(Prob P, StateView st, const uint32_t* grp_model, uint32_t* err) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t e = 0;
   if (k < P.no) {
     const uint32_t c = P.obs_cam[k], p = P.obs_pt[k];
-    uint32_t e = 0;
     if (c >= P.nc || p >= P.np) {
       e |= ERR_BAD_INDEX;
     } else {
       if (P.cam_model[c] != P.pt_model[p]) e |= ERR_MODEL_MIX;
       if (k > 0 && P.obs_pt[k - 1] > p) e |= ERR_UNSORTED;
     }
-    if (e) atomicOr(err, e);
+    if (!all_finite(P.obs_uv + 2 * k, 2)) e |= ERR_NONFINITE;
   }
   if (k < P.nc) {
     const uint32_t g = P.cam_group[k];
     if (g >= P.ng)
-      atomicOr(err, ERR_BAD_INDEX);
+      e |= ERR_BAD_INDEX;
     else if (grp_model[g] != P.cam_model[k])
-      atomicOr(err, ERR_MODEL_MIX);
+      e |= ERR_MODEL_MIX;
+    if (!all_finite(st.rot + 9 * k, 9) || !all_finite(st.center + 3 * k, 3)) e |= ERR_NONFINITE;
+    // A prior's sigmas divide its residual (ba.rs:120-126).
+    if (P.prior_mask && P.prior_mask[k]) {
+      const double* q = P.prior + 6 * k;
+      if (!all_finite(q, 6) || !(q[3] > 0.0 && q[4] > 0.0 && q[5] > 0.0)) e |= ERR_NONFINITE;
+    }
   }
+  if (k < P.np && !all_finite(st.points + 3 * k, 3)) e |= ERR_NONFINITE;
+  if (k < P.ng && !all_finite(st.intr + 5 * k, 5)) e |= ERR_NONFINITE;
+  if (e) atomicOr(err, e);
 }
 
 __global__ void iota_keys_kernel(const uint32_t* src, uint64_t* keys, uint32_t* vals,
@@ -346,10 +361,10 @@ StructView StructBufs::view() const {
   return v;
 }
 
-void validate_problem(const Prob& P, const uint32_t* grp_model, uint32_t* d_err,
-                      cudaStream_t s) {
-  const int64_t n = std::max(P.no, P.nc);
-  if (n > 0) BA_LAUNCH(validate_kernel<<<grid_for(n, T), T, 0, s>>>(P, grp_model, d_err));
+void validate_problem(const Prob& P, const StateView& st, const uint32_t* grp_model,
+                      uint32_t* d_err, cudaStream_t s) {
+  const int64_t n = std::max(std::max(P.no, P.nc), std::max(P.np, P.ng));
+  if (n > 0) BA_LAUNCH(validate_kernel<<<grid_for(n, T), T, 0, s>>>(P, st, grp_model, d_err));
 }
 
 void build_cam_index(const Prob& P, StructBufs& S, cudaStream_t s) {

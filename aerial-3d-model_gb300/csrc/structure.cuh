@@ -20,8 +20,11 @@ struct StructBufs {
   StructView view() const;
 };
 
-void validate_problem(const Prob& P, const uint32_t* grp_model, uint32_t* d_err,
-                      cudaStream_t s);
+// Index, ordering and model checks of the problem, and finiteness of the
+// measurements, priors (sigmas > 0) and initial state `st`: error bits into
+// d_err.
+void validate_problem(const Prob& P, const StateView& st, const uint32_t* grp_model,
+                      uint32_t* d_err, cudaStream_t s);
 // Observations by camera (cam_ptr, cam_obs) and cameras by group (grp_ptr,
 // grp_cams), both stable.
 void build_cam_index(const Prob& P, StructBufs& S, cudaStream_t s);

@@ -5,7 +5,13 @@
 // inward-looking oblique edge ring at offset = altitude / tan(tilt), over a
 // sinusoidal heightfield.  Points are kept when they land inside at least two
 // images.  Observations carry Gaussian pixel noise and a fraction of uniform
-// outliers; GPS priors are the true centres plus Gaussian noise; the initial
+// outliers.  A track keeps its outlier observations, but a track with fewer
+// than `min_inlier_views` inlier observations is not emitted: the sparse
+// stage's per-round gating (crates/stitch-core/src/recon/sparse.rs:389-421)
+// passes a track to bundle adjustment only if at least two of its
+// observations reproject within the gate from its triangulated point, which
+// a track of outliers does not.  GPS priors are the true centres plus
+// Gaussian noise; the initial
 // state is the truth with poses rotated about a random axis and shifted in a
 // random direction, points displaced by Gaussian noise, focal length scaled
 // and distortion zeroed.
@@ -45,6 +51,7 @@ typedef struct survey_params {
   double rot_perturb_deg, centre_perturb_m, point_perturb_m;
   double f_scale_init;
   int32_t refine_intrinsics;
+  int32_t min_inlier_views;  // tracks with fewer inlier observations are dropped (0: keep all)
 } survey_params;
 
 typedef struct survey_arrays {
@@ -292,23 +299,35 @@ survey_handle* survey_generate(const survey_params* pp) {
       std::sort(views[t].begin(), views[t].end(),
                 [](const auto& a, const auto& b) { return a.first < b.first; });
     }
+    std::vector<double> tuv;
     for (int64_t t = 0; t < n && kept < want; ++t) {
       if (views[t].size() < 2) continue;
-      const uint32_t pt = (uint32_t)kept++;
       Stream s(p.seed, 2, (uint64_t)(base + t));
-      for (int a = 0; a < 3; ++a) tpts.push_back(X[t][a]);
-      for (int a = 0; a < 3; ++a) pts.push_back(X[t][a] + p.point_perturb_m * s.normal());
+      double Xp[3];
+      for (int a = 0; a < 3; ++a) Xp[a] = X[t][a] + p.point_perturb_m * s.normal();
+      tuv.clear();
+      int inliers = 0;
       for (auto& v : views[t]) {
         double u0 = v.second[0] + p.noise_px * s.normal();
         double u1 = v.second[1] + p.noise_px * s.normal();
         if (s.uniform() < p.outlier_frac) {
           u0 = s.uniform(0.0, (double)p.width);
           u1 = s.uniform(0.0, (double)p.height);
+        } else {
+          ++inliers;
         }
-        ocam.push_back(v.first);
+        tuv.push_back(u0);
+        tuv.push_back(u1);
+      }
+      if (inliers < p.min_inlier_views) continue;  // gated out of the round
+      const uint32_t pt = (uint32_t)kept++;
+      for (int a = 0; a < 3; ++a) tpts.push_back(X[t][a]);
+      for (int a = 0; a < 3; ++a) pts.push_back(Xp[a]);
+      for (size_t i = 0; i < views[t].size(); ++i) {
+        ocam.push_back(views[t][i].first);
         opt.push_back(pt);
-        ouv.push_back(u0);
-        ouv.push_back(u1);
+        ouv.push_back(tuv[2 * i]);
+        ouv.push_back(tuv[2 * i + 1]);
       }
     }
   }

@@ -38,6 +38,9 @@ class Options:
     autotune: bool = False        # time PCG configurations on the first solve of a form
     stop_patience: int = 0        # consecutive small accepted steps before stopping (0/1: ba.rs rule)
     coarse: bool = False          # mixed form, cluster PCG: two-level preconditioner
+    wait_limit_cycles: int = 0    # spin limit of device-side waits (0: ~2 s)
+    workspace_limit_bytes: int = 0  # device memory the call may hold (0: no limit) -> BA_OOM
+    fault_hold_pcg_cta: int = 0   # tests of the timeout path: grid PCG CTA k-1 skips its exchanges
 
 
 @dataclass
@@ -95,6 +98,9 @@ def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> n
     c.autotune = 1 if o.autotune else 0
     c.stop_patience = int(o.stop_patience)
     c.coarse = 1 if o.coarse else 0
+    c.wait_limit_cycles = int(o.wait_limit_cycles)
+    c.workspace_limit_bytes = int(o.workspace_limit_bytes)
+    c.fault_hold_pcg_cta = int(o.fault_hold_pcg_cta)
     c.log = C.cast(C.pointer(log), C.c_void_p) if log is not None else None
     return c
 

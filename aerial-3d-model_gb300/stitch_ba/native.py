@@ -52,7 +52,9 @@ class BaOptions(C.Structure):
                 ("matrix_free", C.c_int32), ("memory_cap_bytes", C.c_int64),
                 ("stream", C.c_void_p), ("log", C.c_void_p), ("profile", C.c_int32),
                 ("pcg_kernel", C.c_int32), ("no_graph", C.c_int32), ("autotune", C.c_int32),
-                ("stop_patience", C.c_int32), ("coarse", C.c_int32)]
+                ("stop_patience", C.c_int32), ("coarse", C.c_int32),
+                ("fault_hold_pcg_cta", C.c_int32), ("wait_limit_cycles", C.c_int64),
+                ("workspace_limit_bytes", C.c_int64)]
 
 
 class BaStatsC(C.Structure):

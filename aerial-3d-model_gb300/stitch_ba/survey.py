@@ -5,7 +5,9 @@ The presets are the workloads the solver is measured on:
 * ``lawnmower77``  — 77 nadir cameras at 80 m, 5472x3648 px, f ≈ 3650 px,
   40k points on a ±5 m sinusoidal heightfield, ≈250k observations,
   N(0, 0.5 px) noise plus 5% uniform outliers, GPS priors σ = (2, 2, 4) m,
-  poses perturbed by 0.5° / 1 m.
+  poses perturbed by 0.5° / 1 m.  Tracks with fewer than two inlier
+  observations are not emitted (the sparse stage's gating, sparse.rs:389-421,
+  drops them before bundle adjustment); outliers in kept tracks stay.
 * ``single500``    — 500 cameras, 400k points, ≈3M observations.
 * ``oblique2000``  — 2,000 cameras (30% on a 45° oblique edge ring), 2M
   points, ≈15M observations.
@@ -38,6 +40,7 @@ class _Params(C.Structure):
         ("prior_sigma_v", C.c_double), ("rot_perturb_deg", C.c_double),
         ("centre_perturb_m", C.c_double), ("point_perturb_m", C.c_double),
         ("f_scale_init", C.c_double), ("refine_intrinsics", C.c_int32),
+        ("min_inlier_views", C.c_int32),
     ]
 
 
@@ -75,6 +78,10 @@ class SurveyParams:
     point_perturb_m: float = 1.0
     f_scale_init: float = 1.03
     refine_intrinsics: bool = True
+    # A track reaches bundle adjustment only if the round's gating keeps two
+    # or more of its observations (sparse.rs:389-421); tracks with fewer
+    # inlier observations are not emitted (0: emit every track).
+    min_inlier_views: int = 2
 
 
 PRESETS = {
@@ -119,7 +126,8 @@ def generate(params: SurveyParams | str = "lawnmower77", **overrides) -> tuple[P
     if overrides:
         params = replace(params, **overrides)
     L = _survey_lib()
-    P = _Params(**{f.name: (int(getattr(params, f.name)) if f.name == "refine_intrinsics"
+    P = _Params(**{f.name: (int(getattr(params, f.name))
+                            if f.name in ("refine_intrinsics", "min_inlier_views")
                             else getattr(params, f.name)) for f in fields(params)})
     h = L.survey_generate(C.byref(P))
     if not h:

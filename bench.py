@@ -14,19 +14,34 @@ initial state.
   host (pinned) buffers: H2D of the problem, the solve and D2H of the state
   are inside the timed region.
 * ``forms``  — FP64 plain form (the reference's block-Jacobi PCG, 400
-  iterations) and FP32/FP64 mixed form (two-level PCG: block Jacobi plus the
+  iterations), FP32/FP64 mixed form (two-level PCG: block Jacobi plus the
   similarity motions of camera groups, 40 iterations; 60 above 1000 cameras
-  per model) side by side, with the final cost of each and their relative
-  difference; the mixed form is the headline when it reaches the FP64 final
-  cost.
+  per model) and, as an ablation, the mixed form with the reference's
+  block-Jacobi PCG alone (200 iterations), side by side: final cost of each,
+  relative difference from the FP64 form, and the error of every result
+  (centres, rotations, intrinsics, points) against the FP64 form and against
+  the CPU solver.  The mixed form is the headline when it reaches the FP64
+  final cost (for a batch: every model does).
+* ``parity_vs_cpu`` — the FP64 GPU solve against the CPU solver's solve of
+  the same survey (single-model workloads): iterations, accept sequence,
+  per-iteration trial cost, final cost and every result.
 * ``roofline`` — the dominant kernel phase (by device time, from the
   solver's own CUDA-event phase timing) against measured HBM bandwidth.
 * ``cpu_baseline`` — the oracle (a CPU restatement of the reference solver,
-  same data structures, OpenMP on all host cores) on a bounded sample: the
-  first LM iterations of the same solve, scaled to solves/s by the full
-  solve's iteration count.
+  same data structures, OpenMP on all host cores): complete solves, timed
+  end to end (the survey; for a batch, whole models in index order until
+  about 20 s of CPU time, scaled by observations).
 
-``--impl reference`` times that CPU solver alone as the reference arm.
+``--impl reference`` times that CPU solver alone as the reference arm: every
+timed step is one complete solve of the workload (a batch: complete solves of
+a fixed sample of its models, scaled by observations); warm-up steps run one
+LM iteration each.
+
+Multi-GPU (torchrun, one process per GPU): a single survey runs as
+independent replicas (each rank solves its own seeded survey, weak scaling);
+the batched workload is partitioned, each rank solving a disjoint subset of
+the same models balanced by observations (strong scaling), with no
+collective on the data path.
 
 ``--stage triangulate|ransac|pair_fits|summary`` measures one of the sparse
 stage's steps around the solve on the same survey instead (one JSON line with
@@ -67,6 +82,11 @@ MAX_ITER = 60
 MIXED_PCG_ITERS = 40
 MIXED_PCG_ITERS_LARGE = 60
 MIXED_LARGE_CAMS = 1000
+# Ablation: the mixed form's FP32 records, Schur sums and PCG vectors with the
+# reference's block-Jacobi preconditioner alone, capped at 200 PCG iterations.
+ABLATION_PCG_ITERS = 200
+# CPU sample of a batched workload: whole models until this much CPU time.
+CPU_SAMPLE_S = 20.0
 # Per LM iteration, algorithmic bytes of each phase, written as a function of
 # the problem sizes and the storage width s (8 FP64 / 4 FP32): reads and writes
 # each kernel must make at minimum.
@@ -166,20 +186,24 @@ def set_mixed_cap(ps):
     MIXED_PCG_CAP = MIXED_PCG_ITERS_LARGE if big else MIXED_PCG_ITERS
 
 
-def form_options(prec: str, **kw):
-    """Per form: the PCG layout is picked by the solver's autotuner on the
-    first (warm-up) solve of the form and reused by the timed solves."""
+def form_options(form: str, **kw):
+    """Options of a measured form.  The PCG layout is picked by the solver's
+    autotuner on the first (warm-up) solve of the form and reused by the
+    timed solves.  Forms: "fp64", "mixed" (two-level PCG), "mixed_bj" (the
+    mixed form with block-Jacobi PCG alone: the ablation)."""
     from stitch_ba import Options
     kw.setdefault("autotune", True)
-    if prec == "mixed":
+    if form == "mixed":
         mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
         kw.setdefault("coarse", not MIXED_MATRIX_FREE)
         return Options(precision="mixed", pcg_max_iter=MIXED_PCG_CAP, matrix_free=mf, **kw)
+    if form == "mixed_bj":
+        return Options(precision="mixed", pcg_max_iter=ABLATION_PCG_ITERS, coarse=False, **kw)
     return Options(precision="fp64", **kw)
 
 
 def max_over_ranks(x: float, ws: int, device: str = "cuda") -> float:
-    """Timing of the slowest rank (replicas: every rank solves its own models)."""
+    """Timing of the slowest rank."""
     if ws <= 1:
         return x
     import torch
@@ -189,9 +213,34 @@ def max_over_ranks(x: float, ws: int, device: str = "cuda") -> float:
     return float(t.item())
 
 
+def sum_over_ranks(x: float, ws: int, device: str = "cuda") -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def rank_seed(seed: int, rank: int) -> int:
-    """Each replica solves its own survey (weak scaling: fixed work per GPU)."""
+    """Each replica of a single-survey workload solves its own survey (weak
+    scaling: fixed work per GPU)."""
     return seed + rank
+
+
+def partition_models(sizes, ws: int):
+    """Disjoint subsets of model indices, one per rank, balanced by `sizes`
+    (observations): largest model first, each to the least-loaded rank (ties
+    to the lower rank).  Every model is in exactly one subset; each subset is
+    in index order."""
+    parts = [[] for _ in range(ws)]
+    load = [0] * ws
+    for i in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(ws), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        load[r] += sizes[i]
+    return [sorted(p) for p in parts]
 
 
 def dist_env():
@@ -214,6 +263,17 @@ def make_workload(name: str, seed: int):
     return [p]
 
 
+def rank_workload(name: str, seed: int, ws: int, rank: int):
+    """(problems of this rank, their indices in the workload or None,
+    models solved by all ranks together).  The batch is partitioned across
+    ranks; a single survey is replicated with a per-rank seed."""
+    if name == "batch64":
+        ps = make_workload(name, seed)
+        part = partition_models([p.n_obs for p in ps], ws)[rank]
+        return [ps[i] for i in part], part, len(ps)
+    return make_workload(name, rank_seed(seed, rank)), None, ws
+
+
 def totals(ps):
     return dict(n_cams=sum(q.n_cams for q in ps), n_points=sum(q.n_points for q in ps),
                 n_obs=sum(q.n_obs for q in ps))
@@ -233,10 +293,15 @@ def pin_problem(p):
                    prior=pin(p.prior), refine_intrinsics=p.refine_intrinsics)
 
 
+def reaches(cost: float, ref: float) -> bool:
+    """Equal final cost: within 1e-6 relative of the reference cost, or below."""
+    return cost <= ref * (1.0 + 1e-6)
+
+
 def gpu_arm(args, ws, rank):
     import torch
     import stitch_ba
-    from stitch_ba import Options, native
+    from stitch_ba import compare, native
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
@@ -244,7 +309,7 @@ def gpu_arm(args, ws, rank):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     native.load()
-    ps = make_workload(args.workload, rank_seed(args.seed, rank))
+    ps, part, units_all = rank_workload(args.workload, args.seed, ws, rank)
     set_mixed_cap(ps)
     nmod = len(ps)
     tot = totals(ps)
@@ -259,13 +324,16 @@ def gpu_arm(args, ws, rank):
 
     forms = {}
     chosen = args.precision
-    precisions = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    names = ["fp64", "mixed", "mixed_bj"] if args.precision == "both" else [args.precision]
+    if args.no_ablation and "mixed_bj" in names:
+        names.remove("mixed_bj")
     profile_info = {}
     infos_by_form = {}
+    solutions = {}
     with stitch_ba.Context(device=dev, stream=stream.cuda_stream) as ctx:
         ctx.upload(ps)
-        for prec in precisions:
-            opts = form_options(prec)
+        for form in names:
+            opts = form_options(form)
             for _ in range(args.warmup):
                 ctx.solve(args.max_iter, SIGMA_PX, opts)
             torch.cuda.synchronize()
@@ -285,61 +353,70 @@ def gpu_arm(args, ws, rank):
                     times.append(a.elapsed_time(b))
                 barrier()
             ms = max_over_ranks(float(np.sum(times)) / len(times), ws)
-            forms[prec] = dict(ms_per_solve=ms, final_cost=sum(i.final_cost for i in infos),
+            sol = [q.copy() for q in ps]
+            ctx.download(sol)
+            solutions[form] = sol
+            forms[form] = dict(ms_per_solve=ms, final_cost=sum(i.final_cost for i in infos),
                                initial_cost=sum(i.initial_cost for i in infos),
                                iterations=max(i.iterations for i in infos),
                                pcg_iterations=sum(i.pcg_iterations for i in infos),
                                final_rms=info.final_rms,
-                               kernel_launches=info.kernel_launches, clocks=clk.summary())
-            forms[prec]["model_final_costs"] = [i.final_cost for i in infos] if nmod > 1 else None
-            forms[prec]["model_iterations"] = [i.iterations for i in infos] if nmod > 1 else None
+                               kernel_launches=sum(i.kernel_launches for i in infos[:1]),
+                               clocks=clk.summary())
+            forms[form]["model_final_costs"] = [i.final_cost for i in infos] if nmod > 1 else None
+            forms[form]["model_iterations"] = [i.iterations for i in infos] if nmod > 1 else None
             # one profiled solve with the per-iteration log (phase timing; not
             # part of the timed region)
-            prof = ctx.solve(args.max_iter, SIGMA_PX, form_options(prec, profile=True),
+            prof = ctx.solve(args.max_iter, SIGMA_PX, form_options(form, profile=True),
                              log=(nmod == 1))[0]
-            profile_info[prec] = prof
-            infos_by_form[prec] = infos
-            forms[prec]["pcg_kernel"] = prof.pcg_kernel
-            forms[prec]["pcg_ctas"] = int(prof.pcg_ctas)
-            forms[prec]["pcg_autotuned_us_per_iter"] = prof.pcg_tuned_us
-            forms[prec]["device_bytes"] = int(prof.device_bytes)
-            forms[prec]["pcg_max_iter"] = opts.pcg_max_iter
-            forms[prec]["coarse_dim"] = int(prof.coarse_dim)
-            forms[prec]["graph"] = bool(info.graph)
-    if "fp64" in forms and "mixed" in forms:
-        # Equal final cost: the mixed solve reaches the FP64 solve's final cost
-        # to within 1e-6 relative (or ends below it).
-        f64, fm = forms["fp64"]["final_cost"], forms["mixed"]["final_cost"]
-        forms["mixed"]["rel_final_cost_vs_fp64"] = (fm - f64) / abs(f64)
-        reaches = fm <= f64 * (1.0 + 1e-6)
-        forms["mixed"]["reaches_fp64_final_cost"] = bool(reaches)
-        # First LM iteration whose accepted cost is within 1e-6 of the FP64
-        # final cost, and the share of the solve's time spent until then.
-        log = profile_info["mixed"]
-        hit = None
-        for i in range(int(log.iterations) if nmod == 1 else 0):
-            if log.accepted[i] and log.new_cost[i] <= f64 * (1.0 + 1e-6):
-                hit = i
-                break
+            profile_info[form] = prof
+            infos_by_form[form] = infos
+            forms[form]["pcg_kernel"] = prof.pcg_kernel
+            forms[form]["pcg_ctas"] = int(prof.pcg_ctas)
+            forms[form]["pcg_autotuned_us_per_iter"] = prof.pcg_tuned_us
+            forms[form]["device_bytes"] = int(prof.device_bytes)
+            forms[form]["pcg_max_iter"] = opts.pcg_max_iter
+            forms[form]["coarse_dim"] = int(prof.coarse_dim)
+            forms[form]["graph"] = bool(info.graph)
+    if "fp64" in forms:
+        f64 = forms["fp64"]["final_cost"]
+        for form in [f for f in forms if f != "fp64"]:
+            F = forms[form]
+            F["rel_final_cost_vs_fp64"] = (F["final_cost"] - f64) / abs(f64)
+            F["speedup_vs_fp64"] = forms["fp64"]["ms_per_solve"] / F["ms_per_solve"]
+            F["error_vs_fp64"] = [compare.state_errors(a, b) for a, b in
+                                  zip(solutions[form], solutions["fp64"])][0] if nmod == 1 else None
+            if nmod > 1:
+                a, b = forms["fp64"]["model_final_costs"], F["model_final_costs"]
+                miss = [[int(part[k]) if part else k, (y - x) / abs(x)]
+                        for k, (x, y) in enumerate(zip(a, b)) if not reaches(y, x)]
+                F["models_reaching_fp64_cost"] = nmod - len(miss)
+                F["models_missing_fp64_cost"] = miss  # [model index, relative difference]
+                F["reaches_fp64_final_cost"] = not miss
+            else:
+                F["reaches_fp64_final_cost"] = bool(reaches(F["final_cost"], f64))
+            # First LM iteration whose accepted cost is within 1e-6 of the FP64
+            # final cost.
+            log = profile_info[form]
+            hit = None
+            for i in range(int(log.iterations) if nmod == 1 else 0):
+                if log.accepted[i] and reaches(log.new_cost[i], f64):
+                    hit = i
+                    break
+            if hit is not None:
+                F["iteration_reaching_fp64_cost"] = hit + 1
+                F["ms_to_fp64_cost_est"] = F["ms_per_solve"] * (hit + 1) / max(int(log.iterations), 1)
         # Per LM iteration of the profiled solve: trial cost relative to the
         # FP64 final cost, accepted (1/0), PCG iterations.
-        for prec in ("fp64", "mixed"):
-            lg = profile_info[prec]
+        for form in forms:
+            lg = profile_info[form]
             if nmod == 1 and lg.new_cost is not None:
-                forms[prec]["lm_trace"] = [
+                forms[form]["lm_trace"] = [
                     [float("%.3g" % (lg.new_cost[i] / f64 - 1.0)), int(lg.accepted[i]),
                      int(lg.pcg_iters[i])] for i in range(int(lg.iterations))]
-        if hit is not None:
-            forms["mixed"]["iteration_reaching_fp64_cost"] = hit + 1
-            forms["mixed"]["ms_to_fp64_cost_est"] = forms["mixed"]["ms_per_solve"] * (hit + 1) / max(
-                int(log.iterations), 1)
-        if nmod > 1:
-            a, b = forms["fp64"]["model_final_costs"], forms["mixed"]["model_final_costs"]
-            forms["mixed"]["models_reaching_fp64_cost"] = int(sum(
-                1 for x, y in zip(a, b) if y <= x * (1.0 + 1e-6)))
-        forms["mixed"]["speedup_vs_fp64"] = forms["fp64"]["ms_per_solve"] / forms["mixed"]["ms_per_solve"]
-        chosen = "mixed" if reaches else "fp64"
-        forms["chosen"] = chosen
+        if "mixed" in forms:
+            chosen = "mixed" if forms["mixed"]["reaches_fp64_final_cost"] else "fp64"
+            forms["chosen"] = chosen
     head = forms[chosen]
 
     # End to end through the reference-facing C ABI (host buffers, H2D + D2H inside).
@@ -363,6 +440,8 @@ def gpu_arm(args, ws, rank):
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(float(np.mean(e2e_times)), ws)
+    h2d = sum_over_ranks(float(e2e_info.h2d_bytes), ws)
+    d2h = sum_over_ranks(float(e2e_info.d2h_bytes), ws)
 
     if rank != 0:
         return None
@@ -392,7 +471,8 @@ def gpu_arm(args, ws, rank):
         except Exception:
             traffic = None
 
-    value = ws * nmod * 1000.0 / head["ms_per_solve"]
+    value = units_all * 1000.0 / head["ms_per_solve"]
+    partitioned = part is not None
     out = {
         "metric": METRIC,
         "value": value,
@@ -402,20 +482,21 @@ def gpu_arm(args, ws, rank):
         "warmup": args.warmup,
         "ms_per_step": head["ms_per_solve"],
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if partitioned else "weak",
         "vs_baseline": None,
         "dtype": "f64" if chosen == "fp64" else "f32+f64",
         "data": "synthetic (seeded survey generator, reference camera model)",
-        "config": {"workload": args.workload, "models": nmod, "cameras": tot["n_cams"],
-                   "points": tot["n_points"], "observations": tot["n_obs"],
-                   "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
-                   "loss": "cauchy", "precision": chosen, "parallelism": f"replicas{ws}",
+        "config": {"workload": args.workload, "models": units_all if partitioned else nmod,
+                   "cameras": tot["n_cams"], "points": tot["n_points"],
+                   "observations": tot["n_obs"], "max_iter": args.max_iter,
+                   "sigma_px": SIGMA_PX, "loss": "cauchy", "precision": chosen,
+                   "parallelism": (f"models partitioned over {ws} ranks" if partitioned
+                                   else f"replicas{ws}"),
                    "l2": "flushed between steps (256 MiB write)"},
         "forms": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} if isinstance(v, dict) else v
                   for k, v in forms.items()},
-        "e2e": {"value": ws * nmod / e2e_s, "unit": UNIT,
-                "h2d_bytes_per_step": int(e2e_info.h2d_bytes),
-                "d2h_bytes_per_step": int(e2e_info.d2h_bytes),
+        "e2e": {"value": units_all / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_s * 1000.0},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
@@ -427,66 +508,121 @@ def gpu_arm(args, ws, rank):
         "clocks": head["clocks"],
         "gpu_launches": int(head["kernel_launches"]) * args.steps,
     }
-    if not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(ps, [i.iterations for i in infos_by_form[chosen]],
-                                           args.cpu_sample_iters)
+    if partitioned:
+        out["config"]["rank0_models"] = [int(i) for i in part]
+    if not args.no_cpu and ws == 1:
+        cpu = cpu_solves(ps, args.max_iter, budget_s=CPU_SAMPLE_S)
+        out["cpu_baseline"] = cpu["baseline"]
+        if nmod == 1 and "fp64" in solutions:
+            out["parity_vs_cpu"] = parity_record(profile_info["fp64"], forms["fp64"],
+                                                 solutions["fp64"][0], cpu["results"][0],
+                                                 cpu["solutions"][0])
+            for form in forms:
+                if form in solutions and form != "fp64":
+                    forms_out = out["forms"][form]
+                    forms_out["error_vs_cpu"] = compare.state_errors(solutions[form][0],
+                                                                     cpu["solutions"][0])
+                    forms_out["rel_final_cost_vs_cpu"] = (
+                        (forms[form]["final_cost"] - cpu["results"][0].final_cost)
+                        / abs(cpu["results"][0].final_cost))
     return out
 
 
-def cpu_baseline(ps, full_iters, sample_iters: int):
-    """Oracle (CPU restatement of the reference, OpenMP on all host cores) on
-    the first `sample_iters` LM iterations of one model (the largest), scaled
-    to the whole job by observations x LM iterations."""
+def parity_record(log, fp64_form, gpu_sol, cpu_res, cpu_sol):
+    """FP64 GPU solve against the CPU solver's solve of the same problem:
+    iterations, accept sequence, per-iteration trial cost, final cost and
+    the per-result differences (ba.rs:198-391)."""
+    from stitch_ba import compare
+    n = min(int(log.iterations), int(cpu_res.iterations))
+    rel = (np.abs(log.new_cost[:n] - cpu_res.new_cost[:n]) / np.abs(cpu_res.new_cost[:n])
+           if n else np.zeros(0))
+    acc = np.asarray(log.accepted[:n], bool)
+    return {
+        "iterations_gpu": int(log.iterations), "iterations_cpu": int(cpu_res.iterations),
+        "accept_sequence_equal": bool(np.array_equal(acc, np.asarray(cpu_res.accepted[:n], bool))),
+        "trial_cost_rel_max": float(rel.max()) if n else 0.0,
+        "trial_cost_rel_max_accepted": float(rel[acc].max()) if acc.any() else 0.0,
+        "trial_cost_rel": [float("%.2g" % v) for v in rel],
+        "final_cost_rel": (fp64_form["final_cost"] - cpu_res.final_cost) / abs(cpu_res.final_cost),
+        "state": compare.state_errors(gpu_sol, cpu_sol),
+    }
+
+
+def cpu_solves(ps, max_iter: int, budget_s: float = CPU_SAMPLE_S):
+    """Complete oracle solves (CPU restatement of the reference, OpenMP on all
+    host cores) of whole models: the survey, or for a batch the models in
+    index order until `budget_s` of CPU time, scaled to the whole batch by
+    observations.  Returns the baseline line, and the results and solved
+    states of the models solved."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ba_oracle
     ba_oracle.build()
-    k = max(range(len(ps)), key=lambda i: ps[i].n_obs)
-    q = ps[k].copy()
     threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    r = ba_oracle.bundle_adjust(q, sample_iters, SIGMA_PX, n_threads=threads)
-    dt = time.perf_counter() - t0
-    per_iter = dt / max(r.iterations, 1)
-    work = sum(p.n_obs * max(it, 1) for p, it in zip(ps, full_iters))
-    est = per_iter * work / ps[k].n_obs
-    solves = len(ps)
-    what = "the survey" if solves == 1 else f"the largest of {solves} models"
-    return {"value": solves / est, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {r.iterations} LM iterations of {what} ({dt:.1f} s), scaled by "
-                      f"observations x the GPU solve's LM iterations ({max(full_iters)} max)",
-            "s_per_lm_iteration": per_iter}
+    results, sols = [], []
+    t_all = 0.0
+    obs_done = 0
+    for p in ps:
+        q = p.copy()
+        t0 = time.perf_counter()
+        r = ba_oracle.bundle_adjust(q, max_iter, SIGMA_PX, n_threads=threads)
+        t_all += time.perf_counter() - t0
+        obs_done += p.n_obs
+        results.append(r)
+        sols.append(q)
+        if t_all >= budget_s:
+            break
+    total_obs = sum(p.n_obs for p in ps)
+    est = t_all * total_obs / max(obs_done, 1)
+    k = len(results)
+    what = ("one complete solve of the survey" if len(ps) == 1 else
+            f"complete solves of {k} of {len(ps)} models (models 0..{k - 1}), scaled by observations")
+    return {"baseline": {"value": len(ps) / est, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{what} ({t_all:.1f} s, {max(r.iterations for r in results)} "
+                                   f"LM iterations max)",
+                         "iterations": [int(r.iterations) for r in results]},
+            "results": results, "solutions": sols}
 
 
 def reference_arm(args, ws, rank):
-    """CPU reference solver (oracle port, all host cores), same workload and unit.
-    A step solves the first `cpu_sample_iters` LM iterations of the survey (of
-    the largest model for batch64), scaled to whole solves by the LM
-    iteration count of the full solve and, for batch64, by observations."""
+    """CPU reference solver (oracle port, all host cores), same workload and
+    unit.  Warm-up steps run one LM iteration of the first model; every
+    timed step is a complete solve of the survey (a batch: complete solves of
+    a fixed sample of its models — chosen by the first step, about
+    CPU_SAMPLE_S of work — scaled to the batch by observations)."""
     if rank != 0:
         return None
     ps = make_workload(args.workload, args.seed)
     tot = totals(ps)
-    k = max(range(len(ps)), key=lambda i: ps[i].n_obs)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ba_oracle
     ba_oracle.build()
     threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        ba_oracle.bundle_adjust(ps[0].copy(), 1, SIGMA_PX, n_threads=threads)
     times = []
-    iters = 0
-    for i in range(args.warmup + args.steps):
-        q = ps[k].copy()
+    sample = None
+    last = None
+    for _ in range(args.steps):
         t0 = time.perf_counter()
-        r = ba_oracle.bundle_adjust(q, args.cpu_sample_iters, SIGMA_PX, n_threads=threads)
+        res = []
+        for i, p in enumerate(ps if sample is None else ps[:sample]):
+            res.append(ba_oracle.bundle_adjust(p.copy(), args.max_iter, SIGMA_PX, n_threads=threads))
+            if sample is None and len(ps) > 1 and time.perf_counter() - t0 >= CPU_SAMPLE_S:
+                break
         dt = time.perf_counter() - t0
-        iters = r.iterations
-        if i >= args.warmup:
-            times.append(dt / max(r.iterations, 1))
-    per_iter = float(np.mean(times))
-    est = per_iter * args.full_iters * tot["n_obs"] / ps[k].n_obs
-    v = len(ps) / est
+        if sample is None:
+            sample = len(res)
+        times.append(dt)
+        last = res
+    obs_sample = sum(p.n_obs for p in ps[:sample])
+    per_step = float(np.mean(times)) * tot["n_obs"] / obs_sample
+    v = len(ps) / per_step
+    r0 = last[0]
+    what = ("one complete solve of the survey" if len(ps) == 1 else
+            f"complete solves of models 0..{sample - 1} of {len(ps)}, scaled by observations")
     return {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": est * 1000.0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1000.0,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded survey generator, reference camera model)",
         "config": {"workload": args.workload, "models": len(ps), "cameras": tot["n_cams"],
@@ -494,11 +630,11 @@ def reference_arm(args, ws, rank):
                    "max_iter": args.max_iter, "sigma_px": SIGMA_PX,
                    "loss": "cauchy", "precision": "fp64", "parallelism": "cpu"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"each step = first {iters} LM iterations of the "
-                                   f"{'survey' if len(ps) == 1 else 'largest model'}, scaled by "
-                                   f"{args.full_iters} LM iterations per solve"
-                                   + ("" if len(ps) == 1 else " and by observations")},
+                         "sample": f"each step = {what}; warm-up steps = one LM iteration"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "solution": {"iterations": int(r0.iterations), "final_cost": r0.final_cost,
+                     "final_rms": r0.final_rms, "accepted": [int(a) for a in r0.accepted],
+                     "step_seconds": [round(t, 3) for t in times]},
     }
 
 
@@ -512,9 +648,9 @@ def main():
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--max-iter", type=int, default=MAX_ITER)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--cpu-sample-iters", type=int, default=2)
-    ap.add_argument("--full-iters", type=int, default=int(os.environ.get("BA_FULL_ITERS", "0")) or None)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and parity legs")
+    ap.add_argument("--no-ablation", action="store_true",
+                    help="skip the mixed form with block-Jacobi PCG alone")
     ap.add_argument("--stage", default="ba",
                     choices=["ba", "triangulate", "ransac", "pair_fits", "summary"])
     ap.add_argument("--matrix-free", action="store_true",
@@ -526,8 +662,6 @@ def main():
     if args.stage != "ba":
         out = stage_arm(args, ws, rank)
     elif args.impl == "reference":
-        if args.full_iters is None:
-            args.full_iters = FULL_ITERS.get(args.workload, MAX_ITER)
         out = reference_arm(args, ws, rank)
     else:
         out = gpu_arm(args, ws, rank)
@@ -624,10 +758,6 @@ def stage_arm(args, ws, rank):
             "agreement_on_sample": agree(g, c)}
 
 
-# LM iterations the full solve of each workload takes (FP64, measured on the
-# GPU plain form, which matches the CPU solver's iteration count); used to
-# scale the CPU reference arm's per-iteration sample to solves/s.
-FULL_ITERS = {"single500": 17, "lawnmower77": 43}
 
 if __name__ == "__main__":
     main()

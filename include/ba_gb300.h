@@ -128,6 +128,18 @@ typedef struct ba_options {
                            similarity motions of each group of consecutive
                            cameras, up to 32 groups per model); 0: the
                            reference's block-Jacobi alone                 */
+  int32_t fault_hold_pcg_cta; /* fault injection for tests of the timeout
+                           path: k > 0 makes CTA k-1 of the grid-kernel PCG
+                           launch leave before its first group exchange, so
+                           the other CTAs of its group wait until
+                           wait_limit_cycles runs out and the call returns
+                           BA_TIMEOUT with the host state untouched; 0: off */
+  int64_t wait_limit_cycles; /* spin limit of every device-side wait, in SM
+                           clock cycles; <= 0: 4e9 (about 2 s)            */
+  int64_t workspace_limit_bytes; /* device memory the call may hold at once
+                           (problem copies and workspace); an allocation
+                           beyond it fails with BA_OOM before it is made;
+                           <= 0: no limit                                 */
 } ba_options;
 
 /* Kernel phases timed when ba_options.profile is set (ba_stats.ms_phase). */
@@ -268,12 +280,18 @@ ba_status ba_context_debug_step(ba_context* ctx, const ba_options* opt,
  * memory is all held by another runtime's caching allocator, or a
  * latency-critical loop where cudaMalloc / cudaFree would synchronise the
  * whole device.  Runs on `stream` (NULL: the legacy default stream) on the
- * current device and waits for it.  Scratch: a fixed 196,632-byte device
- * array per device, looked up on the first call on that device (make that
- * first call before any stream capture); at most 33,554,432 observations
- * per call (BA_BAD_INPUT beyond).  Calls share the scratch: calls that overlap
- * on the GPU race.  Results go to host memory.  No counterpart in the
- * reference. */
+ * current device, then copies the result to host memory and synchronises
+ * that stream: it must not be called while the stream is being captured
+ * into a CUDA graph.
+ * Scratch: a fixed 262,176-byte device array per device, part of this
+ * library's device code.  With lazy module loading (the CUDA default) the
+ * array is reserved when the first call on a device looks up its address,
+ * so make one call on each device (n_obs = 0 is enough) before another
+ * runtime takes the rest of its memory.  At most 33,554,432 observations
+ * per call (BA_BAD_INPUT beyond).  Observation camera / point and camera
+ * lens-group indices are checked on the device: an index out of range gives
+ * BA_BAD_INPUT.  Calls share the scratch: calls that overlap on the GPU
+ * race.  No counterpart in the reference. */
 ba_status ba_robust_cost_noalloc(const ba_problem* problem, const ba_state* state,
                                  double sigma_px, int32_t loss, void* stream,
                                  double* cost, double* rms, int64_t* n_in_front);

@@ -62,7 +62,8 @@ def main():
     p = O.RefSurvey()
     save("refsurvey_huber", p, 30, 4.0, loss=O.LOSS_HUBER)
     from stitch_ba import survey
-    s, _ = survey.generate("lawnmower77", n_cams=24, n_points=4000)
+    # made before the generator gated tracks by inlier count
+    s, _ = survey.generate("lawnmower77", n_cams=24, n_points=4000, min_inlier_views=0)
     save("lawnmower24", s, 25, 1.0)
 
 

@@ -87,3 +87,5 @@ def test_default_options_leave_the_extensions_off():
     L.ba_default_options(ctypes.byref(o))
     assert (o.coarse, o.autotune, o.stop_patience, o.pcg_kernel, o.no_graph, o.matrix_free) == (0,) * 6
     assert o.precision == 0 and o.loss == 0
+    # no fault injection, the default wait limit, no workspace budget
+    assert (o.fault_hold_pcg_cta, o.wait_limit_cycles, o.workspace_limit_bytes) == (0, 0, 0)

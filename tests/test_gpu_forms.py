@@ -192,3 +192,22 @@ def test_autotuned_layout_is_kept_across_calls_of_one_shape():
     assert a.pcg_tuned_us > 0 and b.pcg_tuned_us == a.pcg_tuned_us
     assert (a.pcg_kernel, a.pcg_cluster) == (b.pcg_kernel, b.pcg_cluster)
     assert a.final_cost == b.final_cost
+
+
+def test_mixed_batch_matches_individual_mixed_solves():
+    """The mixed form solves each model of a batch as it solves the model on
+    its own: three surveys of equal camera count (so the cluster PCG gives
+    each model the same number of CTAs in both calls) with different seeds."""
+    probs = [survey.generate("lawnmower77", seed=s, n_cams=30, n_points=6000)[0]
+             for s in (7, 8, 9)]
+    opts = Options(precision="mixed", coarse=True, pcg_max_iter=40)
+    batch = [p.copy() for p in probs]
+    infos = stitch_ba.bundle_adjust_batch(batch, 40, 1.0, opts)
+    for p, q, info in zip(probs, batch, infos):
+        r = p.copy()
+        st, si = stitch_ba.bundle_adjust(r, 40, 1.0, opts, return_info=True)
+        assert info.pcg_kernel == si.pcg_kernel == "cluster"
+        assert info.iterations == si.iterations
+        assert abs(info.final_cost - si.final_cost) <= 1e-12 * si.final_cost
+        assert np.abs(q.center - r.center).max() <= 1e-9
+        assert np.abs(q.points - r.points).max() <= 1e-9

@@ -6,10 +6,15 @@ Tolerances (FP64 plain form vs the CPU restatement of ba.rs):
     cond ~1e10 (nadir-only: focal length and flying height trade off) and PCG
     either stops at 400 products or on a tolerance crossing that moves with
     rounding alone; the oracle with its hash-map summation order permuted
-    moves by ~1e-9 .. 5e-9 (reference_spread);
-  * final camera centres 1e-6 m, rotations 1e-8 rad; points 1e-3 m (not in
-    the contract; the reference's own run-to-run spread on the 400-product
-    `lawnmower24` solve is 1e-4 .. 3e-4 m for points, 2e-7 m for centres).
+    (the reference's own source of run-to-run differences, ba.rs:147) moves
+    by ~1e-9 .. 5e-9 on the fixtures and by up to ~1e-7 on the 77-camera
+    survey (reference_spread);
+  * final camera centres 1e-6 m and rotations 1e-8 rad, or 5x the
+    reference's own spread where that is larger (77 cameras: centres move by
+    up to ~4e-4 m between the reference's own runs, along the weak
+    directions the GPS priors alone hold); points 1e-3 m on the fixtures.
+Every test records the deviation it measured (the `parity_record` fixture),
+so the distance to the contract's 1e-9 / 1e-6 m / 1e-8 rad is visible.
 """
 import os
 
@@ -18,7 +23,7 @@ import pytest
 
 import ba_oracle as O
 import stitch_ba
-from stitch_ba import Options, Problem
+from stitch_ba import Options, Problem, compare, survey
 
 pytestmark = pytest.mark.gpu
 
@@ -62,29 +67,34 @@ def load_fixture(name):
     return p, f
 
 
-def rot_angle(Ra, Rb):
-    """Angle of Ra Rb^T from its skew part (accurate for small angles)."""
-    D = np.einsum("nij,nkj->nik", Ra, Rb)
-    v = np.stack([D[:, 2, 1] - D[:, 1, 2], D[:, 0, 2] - D[:, 2, 0], D[:, 1, 0] - D[:, 0, 1]], 1)
-    return np.arcsin(np.clip(np.linalg.norm(v, axis=1) / 2, 0, 1))
+rot_angle = compare.rot_angle
 
 
 def check_against(p, info, ref_new_cost, ref_accepted, ref_state, tol):
+    """Per-iteration trial cost within `tol`, the same accept sequence and the
+    final state within 1e-6 m / 1e-8 rad (points 1e-3 m); returns the
+    deviations measured."""
     n = min(len(info.new_cost), len(ref_new_cost))
     assert n > 0
     rel = np.abs(info.new_cost[:n] - ref_new_cost[:n]) / np.abs(ref_new_cost[:n])
+    rot, center, intr, points = ref_state
+    dev = {"trial_cost_rel_max": float(rel.max()), "tolerance": tol,
+           "centre_m_max": float(np.abs(p.center - center).max()),
+           "rotation_rad_max": float(rot_angle(p.rot, rot).max()),
+           "points_m_max": float(np.abs(p.points - points).max()),
+           "intr_rel_max": float(np.abs(p.intr - intr).max() / np.abs(intr).max())}
     assert rel.max() < tol, (rel.max(), rel)
     assert np.array_equal(info.accepted[:n], np.asarray(ref_accepted[:n], bool))
-    rot, center, intr, points = ref_state
-    assert np.abs(p.center - center).max() < 1e-6
-    assert rot_angle(p.rot, rot).max() < 1e-8
-    assert np.abs(p.points - points).max() < 1e-3
-    assert np.abs(p.intr - intr).max() <= 1e-6 * np.abs(intr).max()
+    assert dev["centre_m_max"] < 1e-6
+    assert dev["rotation_rad_max"] < 1e-8
+    assert dev["points_m_max"] < 1e-3
+    assert dev["intr_rel_max"] <= 1e-6
+    return dev
 
 
 @pytest.mark.parametrize("name", ["refsurvey", "refsurvey_fixed_intr", "refsurvey_huber",
                                   "lawnmower24"])
-def test_fp64_matches_golden(name):
+def test_fp64_matches_golden(name, parity_record):
     p, f = load_fixture(name)
     loss = "huber" if int(f["loss"]) == 1 else "cauchy"
     st, info = stitch_ba.bundle_adjust(p, int(f["max_iter"]), float(f["sigma"]),
@@ -92,10 +102,92 @@ def test_fp64_matches_golden(name):
     assert st.iterations == int(f["iterations"])
     assert abs(st.initial_rms - float(f["initial_rms"])) <= 1e-12 * float(f["initial_rms"])
     tol = cost_tol(name)
-    assert abs(info.final_cost - float(f["final_cost"])) <= tol * float(f["final_cost"])
-    check_against(p, info, f["new_cost"], f["accepted"],
-                  (f["out_rot"], f["out_center"], f["out_intr"], f["out_points"]), tol)
+    final_rel = abs(info.final_cost - float(f["final_cost"])) / float(f["final_cost"])
+    dev = check_against(p, info, f["new_cost"], f["accepted"],
+                        (f["out_rot"], f["out_center"], f["out_intr"], f["out_points"]), tol)
+    dev.update(final_cost_rel=final_rel, reference_spread=reference_spread(name),
+               iterations=int(st.iterations))
+    parity_record["fp64_vs_oracle:" + name] = dev
+    assert final_rel <= tol
     assert info.kernel_launches > 0
+
+
+def _oracle_runs(p, max_iter, sigma, seeds):
+    """The oracle's solve of `p` (fixed hash-map order) and its solves with
+    the SpMV block order permuted by each seed (the reference's own
+    run-to-run variation, ba.rs:147), on all host cores."""
+    threads = os.cpu_count() or 1
+    base = p.copy()
+    r0 = O.bundle_adjust(base, max_iter, sigma, n_threads=threads)
+    runs = []
+    try:
+        for seed in seeds:
+            O.set_spmv_shuffle(seed)
+            q = p.copy()
+            runs.append((O.bundle_adjust(q, max_iter, sigma, n_threads=threads), q))
+    finally:
+        O.set_spmv_shuffle(0)
+    return (r0, base), runs
+
+
+def test_fp64_matches_cpu_solver_on_lawnmower77(parity_record):
+    """The 77-camera lawnmower survey (77 cameras, 40k points, ~246k
+    observations, 5% outliers, GPS priors): FP64 GPU solve against the
+    oracle's solve (ba.rs:198-391), iteration by iteration.
+
+    The same iterations and accept sequence; per-iteration trial cost, final
+    cost, centres and rotations within the contract's 1e-9 / 1e-6 m /
+    1e-8 rad, or within 5x the spread of the reference's own runs where
+    that is larger (measured here: two permuted-order runs of the oracle)."""
+    p, _ = survey.generate("lawnmower77", seed=1)
+    (r0, base), runs = _oracle_runs(p, 60, 1.0, (11, 12))
+    sp_cost = sp_final = sp_c = sp_r = 0.0
+    for r, q in runs:
+        assert r.iterations == r0.iterations
+        n = r.iterations
+        sp_cost = max(sp_cost, float(np.max(np.abs(r.new_cost[:n] - r0.new_cost[:n]) /
+                                            r0.new_cost[:n])))
+        sp_final = max(sp_final, abs(r.final_cost - r0.final_cost) / r0.final_cost)
+        sp_c = max(sp_c, float(np.abs(q.center - base.center).max()))
+        sp_r = max(sp_r, float(rot_angle(q.rot, base.rot).max()))
+    q = p.copy()
+    st, info = stitch_ba.bundle_adjust(q, 60, 1.0, return_info=True)
+    n = r0.iterations
+    rel = np.abs(info.new_cost[:n] - r0.new_cost[:n]) / r0.new_cost[:n]
+    dev = {"iterations": int(info.iterations), "oracle_iterations": int(n),
+           "trial_cost_rel_max": float(rel.max()),
+           "final_cost_rel": abs(info.final_cost - r0.final_cost) / r0.final_cost,
+           "centre_m_max": float(np.abs(q.center - base.center).max()),
+           "rotation_rad_max": float(rot_angle(q.rot, base.rot).max()),
+           "points_m_max": float(np.abs(q.points - base.points).max()),
+           "reference_spread": {"trial_cost_rel": sp_cost, "final_cost_rel": sp_final,
+                                "centre_m": sp_c, "rotation_rad": sp_r}}
+    parity_record["fp64_vs_oracle:lawnmower77"] = dev
+    assert info.iterations == r0.iterations
+    assert np.array_equal(info.accepted, np.asarray(r0.accepted, bool))
+    assert dev["trial_cost_rel_max"] <= max(1e-9, 5 * sp_cost), dev
+    assert dev["final_cost_rel"] <= max(1e-9, 5 * sp_final), dev
+    assert dev["centre_m_max"] <= max(1e-6, 5 * sp_c), dev
+    assert dev["rotation_rad_max"] <= max(1e-8, 5 * sp_r), dev
+
+
+def test_mixed_form_error_per_result_on_lawnmower77(parity_record):
+    """The mixed FP32/FP64 form against the FP64 form on the 77-camera
+    survey, every result the solve updates (ba.rs:338-366): final cost,
+    centres, rotations, intrinsics and points, with stated bounds."""
+    p, _ = survey.generate("lawnmower77", seed=1)
+    a, b = p.copy(), p.copy()
+    _, f64 = stitch_ba.bundle_adjust(a, 60, 1.0, return_info=True)
+    _, mix = stitch_ba.bundle_adjust(b, 60, 1.0, Options(precision="mixed", coarse=True,
+                                                          pcg_max_iter=40), return_info=True)
+    err = compare.state_errors(b, a)
+    err["final_cost_rel"] = (mix.final_cost - f64.final_cost) / f64.final_cost
+    parity_record["mixed_vs_fp64:lawnmower77"] = err
+    assert err["final_cost_rel"] <= 1e-6
+    assert err["centre_m"]["max"] < 2e-2, err
+    assert err["rotation_rad"]["max"] < 2e-4, err
+    assert err["intrinsics_rel"]["f"] < 1e-4, err
+    assert err["points_m"]["p99"] < 5e-2 and err["points_m"]["max"] < 0.5, err
 
 
 def test_reference_known_answer_on_gpu():
@@ -132,7 +224,6 @@ def test_reduced_system_matches_oracle(name):
         d = ctx.debug_step(1e-4, sigma)
     assert np.abs(d["S"] - r["S"]).max() <= 1e-12 * np.abs(r["S"]).max()
     assert np.abs(d["g"] - r["g"]).max() <= 1e-12 * np.abs(r["g"]).max()
-    assert np.array_equal(np.abs(d["S"]) > 0, np.abs(r["S"]) > 0) or True
     # PCG solution and trial cost: PCG stops on an ill-conditioned system.
     assert np.abs(d["dx"] - r["dx"]).max() <= 1e-5 * np.abs(r["dx"]).max()
     assert abs(d["trial_cost"] - r["trial_cost"]) <= 1e-8 * r["trial_cost"]
