@@ -694,29 +694,39 @@ __device__ __forceinline__ void chol3_rsqrt(const double* A, double* L) {
   L[0] = l00, L[1] = l10, L[2] = l11, L[3] = l20, L[4] = l21, L[5] = l22;
 }
 
-// Pass 2, a thread per point (in order of observation count): V and v summed
-// in FP64 from the stored FP32 records (products of FP32 numbers are exact in
-// FP64, so V^-1 v is the exact least-squares step of the stored Jacobians and
-// residuals), the damped inverse, its Cholesky factor, and the point's lens
-// entries.  Points with cond(V) above kMixedCondLimit take the FP64 path of
+// Pass 2, a thread per point: V and v summed in FP64 from the stored FP32
+// records (products of FP32 numbers are exact in FP64, so V^-1 v is the
+// exact least-squares step of the stored Jacobians and residuals), the
+// damped inverse, its Cholesky factor, and the point's lens entries.  Points
+// with cond(V) above kMixedCondLimit take the FP64 path of
 // point_system_mixed_ill, which also writes their Z and gradient shares.
-static __global__ void __launch_bounds__(128, 8)
+//
+// A CTA takes kPtSolveThreads consecutive points, whose records are one
+// contiguous range (observations are sorted by point).  The CTA stages the
+// part of each record the sums read (Jp, Jg, e, w, valid: floats 12..27, one
+// 16-byte-aligned 64-byte run) and its lens entry in shared memory, in rounds
+// of kPtStageRecs records read with coalesced 16-byte loads; each thread then
+// adds its own point's records in observation order, as a thread reading
+// them from global memory would.
+constexpr int kPtSolveThreads = 128;
+constexpr int kPtStageRecs = 512;
+constexpr int kPtStagePitch = 17;  // staged floats per record: lin[12..27], lens entry
+
+static __global__ void __launch_bounds__(kPtSolveThreads, 6)
     point_solve_mixed_kernel(Prob P, StateView st, StructView S, IterBufs<float> B,
                              const int32_t* active, const double* lambda, const double* sigma) {
-  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= P.np) return;
-  const int64_t p = S.pt_order ? S.pt_order[tid] : tid;
-  const uint32_t m = P.pt_model[p];
-  if (!active[m]) return;
-  const bool refine = P.model_refine[m] != 0;
-  const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
-  const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
-  if (e - s < 2) {  // ba.rs:238
-    B.kept[p] = 0;
-    for (uint32_t j = l0; j < l1; ++j)
-      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
-    return;
-  }
+  __shared__ float srec[kPtStageRecs * kPtStagePitch];
+  const int64_t pb = (int64_t)blockIdx.x * kPtSolveThreads;
+  if (pb >= P.np) return;  // uniform over the CTA
+  const int64_t pe = pb + kPtSolveThreads < P.np ? pb + kPtSolveThreads : P.np;
+  const int64_t p = pb + threadIdx.x;
+  const bool in = p < pe;
+  const uint32_t m = in ? P.pt_model[p] : 0u;
+  const bool act = in && active[m] != 0;
+  if (!__syncthreads_or(act)) return;  // every point of the CTA in a finished model
+  const uint32_t s = in ? S.pt_ptr[p] : 0u, e = in ? S.pt_ptr[p + 1] : 0u;
+  const uint32_t l0 = in ? S.lens_ptr[p] : 0u, l1 = in ? S.lens_ptr[p + 1] : 0u;
+  const bool sum = act && e - s >= 2;  // ba.rs:238
   // V and v as double-float sums of the stored FP32 values (about 48 bits:
   // V^-1 v stays the exact point step of the stored records to ~1e-10
   // relative for the well-conditioned points that use it), then FP64.
@@ -725,38 +735,60 @@ static __global__ void __launch_bounds__(128, 8)
   // The point's first lens entry (usually its only one) sums Y = w Jg^T Jp in
   // the same pass (ba.rs:251-259); further entries take a second pass below.
   float Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (uint32_t k = s; k < e; ++k) {
-    const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
-    const float4 a = o4[3], b = o4[4], c = o4[6];  // jp 12..17, e 24..25, w 26, valid 27
-    if (c.w == 0.0f) continue;
-    const float w = c.z;
-    const float jp[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
-    if (l1 > l0 && S.obs_lens[k] == l0) {
-      const float4 g2 = o4[5];  // jg 20..23
-      const float jg[6] = {b.z, b.w, g2.x, g2.y, g2.z, g2.w};
+  const uint32_t rb = S.pt_ptr[pb], re = S.pt_ptr[pe];
+  for (uint32_t c0 = rb; c0 < re; c0 += kPtStageRecs) {
+    const uint32_t c1 = re - c0 < (uint32_t)kPtStageRecs ? re : c0 + kPtStageRecs;
+    const uint32_t n = c1 - c0;
+    for (uint32_t t = threadIdx.x; t < 4 * n; t += kPtSolveThreads) {
+      const uint32_t r = t >> 2, q = t & 3;
+      const float4 v = reinterpret_cast<const float4*>(B.lin + (size_t)(c0 + r) * kLinW + 12)[q];
+      float* d = srec + r * kPtStagePitch + 4 * q;
+      d[0] = v.x, d[1] = v.y, d[2] = v.z, d[3] = v.w;
+    }
+    for (uint32_t r = threadIdx.x; r < n; r += kPtSolveThreads)
+      srec[r * kPtStagePitch + 16] = __uint_as_float(S.obs_lens[c0 + r]);
+    __syncthreads();
+    const uint32_t k0 = s > c0 ? s : c0, k1 = e < c1 ? e : c1;
+    for (uint32_t k = sum ? k0 : k1; k < k1; ++k) {
+      const float* o = srec + (k - c0) * kPtStagePitch;  // o[i] = lin[12 + i]
+      if (o[15] == 0.0f) continue;                       // valid
+      const float w = o[14];
+      const float jp[6] = {o[0], o[1], o[2], o[3], o[4], o[5]};
+      if (l1 > l0 && __float_as_uint(o[16]) == l0) {
+        const float jg[6] = {o[6], o[7], o[8], o[9], o[10], o[11]};
 #pragma unroll
-      for (int t = 0; t < 3; ++t) {
-        const float ga = jg[t], gb = jg[3 + t];
-        Y[3 * t + 0] += (ga * jp[0] + gb * jp[3]) * w;
-        Y[3 * t + 1] += (ga * jp[1] + gb * jp[4]) * w;
-        Y[3 * t + 2] += (ga * jp[2] + gb * jp[5]) * w;
+        for (int t = 0; t < 3; ++t) {
+          const float ga = jg[t], gb = jg[3 + t];
+          Y[3 * t + 0] += (ga * jp[0] + gb * jp[3]) * w;
+          Y[3 * t + 1] += (ga * jp[1] + gb * jp[4]) * w;
+          Y[3 * t + 2] += (ga * jp[2] + gb * jp[5]) * w;
+        }
+      }
+      float ph[6], pq[6];  // w jp = ph + pq exactly
+#pragma unroll
+      for (int i = 0; i < 6; ++i) ph[i] = w * jp[i], pq[i] = fmaf(w, jp[i], -ph[i]);
+      // V (upper triangle 00 01 02 11 12 22) += w (jp_i jp_j + jp_{3+i} jp_{3+j})
+      constexpr int VI[6] = {0, 0, 0, 1, 1, 2}, VJ[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        df_add_prod(Vh[t], Vl[t], ph[VI[t]], pq[VI[t]], jp[VJ[t]]);
+        df_add_prod(Vh[t], Vl[t], ph[3 + VI[t]], pq[3 + VI[t]], jp[3 + VJ[t]]);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        df_add_prod(vh[i], vl[i], ph[i], pq[i], o[12]);
+        df_add_prod(vh[i], vl[i], ph[3 + i], pq[3 + i], o[13]);
       }
     }
-    float ph[6], pq[6];  // w jp = ph + pq exactly
-#pragma unroll
-    for (int i = 0; i < 6; ++i) ph[i] = w * jp[i], pq[i] = fmaf(w, jp[i], -ph[i]);
-    // V (upper triangle 00 01 02 11 12 22) += w (jp_i jp_j + jp_{3+i} jp_{3+j})
-    constexpr int VI[6] = {0, 0, 0, 1, 1, 2}, VJ[6] = {0, 1, 2, 1, 2, 2};
-#pragma unroll
-    for (int t = 0; t < 6; ++t) {
-      df_add_prod(Vh[t], Vl[t], ph[VI[t]], pq[VI[t]], jp[VJ[t]]);
-      df_add_prod(Vh[t], Vl[t], ph[3 + VI[t]], pq[3 + VI[t]], jp[3 + VJ[t]]);
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      df_add_prod(vh[i], vl[i], ph[i], pq[i], c.x);
-      df_add_prod(vh[i], vl[i], ph[3 + i], pq[3 + i], c.y);
-    }
+    __syncthreads();
+  }
+  if (!act) return;
+  const bool refine = P.model_refine[m] != 0;
+  if (!sum) {  // fewer than two observations (ba.rs:238)
+    B.kept[p] = 0;
+    for (uint32_t j = l0; j < l1; ++j)
+      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
+    return;
   }
   double V[6], v[3];
 #pragma unroll

@@ -12,6 +12,13 @@
 // no software spin inside the iteration.  The iteration is the reference's,
 // with p_j = z_j + β p_j(prev) formed on the fly as in the grid kernel.
 //
+// Two-level form (coarse correction z = B^-1 r + W E^-1 W^T r): the coarse
+// vector of the next residual, w = W^T r_{k+1}, is formed as W^T r_k −
+// α W^T q_k from group sums every CTA publishes before the iteration's first
+// barrier (α is known right after it), so an iteration still needs only two
+// cluster reductions: p·q (then α, the coarse gather and c = E^-1 w), and
+// r·r with r·z (then β).
+//
 // Every CTA of a cluster executes the same sequence of cluster barriers:
 // loop exits depend only on reduced scalars, which every CTA computes from
 // the same partials in the same order (bit-identical), and the kernel has no
@@ -76,11 +83,18 @@ inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks) {
   return (size_t)cap_rows * kCgRow * 4 + (size_t)cap_blocks * (36 * 4 + 4);
 }
 
-// Extra shared memory of the two-level form: per row W (42) and W^T r (8);
-// per own group its rows of E^-1 (7 x D), w (7) and c (7); the gathered w of
-// the model (D).
+// Extra shared memory of the two-level form, in floats: per row W (42),
+// W^T r (8) and W^T q (8); per own group its rows of E^-1 (7 x D), the group
+// sums of W^T r (two buffers by iteration parity: a CTA writes the next one
+// while others still read the current one) and of W^T q (7 each), and c (7);
+// the gathered w of the model (D).
+constexpr int kCgCoarseRowF = 42 + 8 + 8;
+__host__ __device__ constexpr size_t cg_coarse_group_floats(uint32_t cap_dim) {
+  return (size_t)kCoarseModes * cap_dim + 4 * kCoarseModes;
+}
 inline size_t cg_coarse_smem_bytes(uint32_t cap_rows, uint32_t cap_groups, uint32_t cap_dim) {
-  return ((size_t)cap_rows * (42 + 8) + (size_t)cap_groups * (7 * cap_dim + 14) + cap_dim) * 4;
+  return ((size_t)cap_rows * kCgCoarseRowF + (size_t)cap_groups * cg_coarse_group_floats(cap_dim) +
+          cap_dim) * 4;
 }
 
 // Sum over lanes 0..7 (lanes >= 8 hold 0); lanes 0..7 receive it.
@@ -150,26 +164,27 @@ __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&
 
 // Scalars of the iteration, computed by thread 0 and read by every thread.
 struct CgScalars {
-  double rz, b2, pq, beta, rzb;
+  double rz, b2, pq, beta;
   float af, bf;
   int stop;
 };
 
-// The coarse step of the two-level form after W^T r is published: gather the
-// model's w from its groups' owners, c = E^-1 w for this CTA's groups, then
-// z = z_B + W c on this CTA's rows; returns this CTA's share of w . c (thread
-// 0; the others return 0).
-__device__ __forceinline__ float cg_coarse_apply(cgx::cluster_group& cl, const CgArgs& A, int m,
-                                                 int32_t ngr, float* rs, uint32_t nrows,
-                                                 const float* sW, const float* sEi, float* sw,
-                                                 float* swall, float* sc) {
+// The coarse step of the two-level form, once the group sums are published:
+// gather the model's w = W^T r − α W^T q from the groups' owners (α = 0 and
+// no W^T q at the start: w = W^T b), then c = E^-1 w for this CTA's groups
+// (into sc, 7 per group).  Ends with a CTA barrier.
+__device__ __forceinline__ void cg_coarse_solve(cgx::cluster_group& cl, const CgArgs& A, int m,
+                                                int32_t ngr, const float* sEi, const float* swr,
+                                                const float* swq, float alpha, float* swall,
+                                                float* sc) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int32_t gm0 = A.model_g0[m];
   const int D = kCoarseModes * (A.model_g0[m + 1] - gm0);
   for (int t = threadIdx.x; t < D; t += kCgThreads) {
     const uint32_t loc = A.grp_loc[gm0 + t / kCoarseModes];
-    const float* src = cl.map_shared_rank(sw, loc >> 16);
-    swall[t] = src[(loc & 0xffffu) * kCoarseModes + t % kCoarseModes];
+    const int o = (int)(loc & 0xffffu) * kCoarseModes + t % kCoarseModes;
+    const float wr = cl.map_shared_rank(swr, loc >> 16)[o];
+    swall[t] = swq ? wr - alpha * cl.map_shared_rank(swq, loc >> 16)[o] : wr;
   }
   __syncthreads();
   for (int o = warp; o < ngr * kCoarseModes; o += kCgWarps) {
@@ -181,22 +196,19 @@ __device__ __forceinline__ float cg_coarse_apply(cgx::cluster_group& cl, const C
     if (lane == 0) sc[o] = v;
   }
   __syncthreads();
-  const bool vl = lane < 6;
-  const int ci = vl ? lane : 0;
-  for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
-    const int32_t l = (int32_t)__float_as_int(rs[(size_t)lr * kCgRow + kCgIdx + 3]);
-    if (l < 0 || !vl) continue;
-    const float* w = sW + (size_t)lr * 42 + kCoarseModes * ci;
-    const float* c = sc + kCoarseModes * l;
-    float add = 0.0f;
+}
+
+// A row's coarse share of z, (W c)_i for lane i < 6 (rows outside every
+// group, such as the lens row, add nothing).
+__device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const float* sc,
+                                           int ci) {
+  if (lg < 0) return 0.0f;
+  const float* w = sWrow + kCoarseModes * ci;
+  const float* c = sc + kCoarseModes * lg;
+  float add = 0.0f;
 #pragma unroll
-    for (int j = 0; j < kCoarseModes; ++j) add += w[j] * c[j];
-    rs[(size_t)lr * kCgRow + kCgZ + ci] += add;
-  }
-  float wc = 0.0f;
-  if (threadIdx.x == 0)
-    for (int o = 0; o < ngr * kCoarseModes; ++o) wc += sw[o] * sc[o];
-  return wc;
+  for (int j = 0; j < kCoarseModes; ++j) add += w[j] * c[j];
+  return add;
 }
 
 // One row's W^T r (7 values) into t[0..6]: lane i < 6 holds r_i.
@@ -240,14 +252,17 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   float* rs = reinterpret_cast<float*>(cg_smem);
   float* sS = rs + (size_t)A.cap_rows * kCgRow;
   uint32_t* sL = reinterpret_cast<uint32_t*>(sS + (size_t)A.cap_blocks * 36);
-  // Two-level form: W and W^T r per row, E^-1 rows, w and c per own group,
-  // the gathered w.
+  // Two-level form: W, W^T r and W^T q per row, E^-1 rows, the group sums
+  // of W^T r (two buffers) and W^T q and c per own group, the gathered w.
   float* sW = reinterpret_cast<float*>(sL + A.cap_blocks);
   float* sT = sW + (size_t)A.cap_rows * 42;
-  float* sEi = sT + (size_t)A.cap_rows * 8;
-  float* sw = sEi + (size_t)A.cap_groups * kCoarseModes * A.cap_dim;
-  float* scf = sw + (size_t)A.cap_groups * kCoarseModes;
-  float* swall = scf + (size_t)A.cap_groups * kCoarseModes;
+  float* sTq = sT + (size_t)A.cap_rows * 8;
+  float* sEi = sTq + (size_t)A.cap_rows * 8;
+  const size_t gsz = (size_t)A.cap_groups * kCoarseModes;
+  float* sw = sEi + gsz * A.cap_dim;  // [2][groups][7]
+  float* swq = sw + 2 * gsz;
+  float* scf = swq + gsz;
+  float* swall = scf + gsz;
   const int32_t cg0 = kCoarse ? A.job_g0[blockIdx.x] : 0;
   const int32_t ngr = kCoarse ? A.job_g1[blockIdx.x] - cg0 : 0;
   const int32_t lens = A.lens_row[J.model];
@@ -322,16 +337,27 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   // The first barrier also makes every CTA's shared memory live for DSMEM.
   cg_reduce<2>(cl, w2, wsm, part[1], tot, [&] {
     sc.rz = tot[0];
-    sc.rzb = tot[0];
     sc.b2 = fmax(tot[1], 1e-300);
     sc.beta = 0.0;
     sc.bf = 0.0f;
     sc.stop = 0;
   });
   if constexpr (kCoarse) {
-    const float wc = cg_coarse_apply(cl, A, J.model, ngr, rs, nrows, sW, sEi, sw, swall, scf);
-    const float w1[1] = {threadIdx.x == 0 ? wc : 0.0f};
-    cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] { sc.rz = sc.rzb + tot[0]; });
+    // z = B^-1 b + W E^-1 W^T b, and r . z with it.
+    cg_coarse_solve(cl, A, J.model, ngr, sEi, sw, nullptr, 0.0f, swall, scf);
+    float drz0 = 0.0f;
+    for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
+      float* st = CGROW(lr);
+      const int32_t lg = __float_as_int(st[kCgIdx + 3]);
+      const float add = cg_row_wc(sW + (size_t)lr * 42, lg, scf, ci);
+      if (vl) {
+        const float zi = st[kCgZ + ci] + add;
+        st[kCgZ + ci] = zi;
+        drz0 += st[kCgR + ci] * zi;
+      }
+    }
+    const float w1[1] = {cg_sum8f(drz0)};
+    cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] { sc.rz = tot[0]; });
   }
   int32_t spmv = 0;
   for (int32_t it = 0; it < A.max_iter; ++it) {
@@ -372,6 +398,9 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         st[kCgP + 8 * cur + ci] = pi;
       }
       if (vl) dpq += pi * qi;
+      // W^T q of the row for the next coarse vector (the lens row, in no
+      // group, has W = 0; its transposed terms arrive after the reduction).
+      if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, qi, sTq + (size_t)lr * 8);
       const int32_t lp = __float_as_int(st[kCgIdx + 2]);
       if (lp >= 0) {  // S_cg^T p_c for the lens column
         const int t = lane / 3, j = lane - 3 * (lane / 3);
@@ -390,6 +419,10 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     }
     const float w4[4] = {cg_sum8f(dpq), __shfl_sync(kFull, dlens, 0), __shfl_sync(kFull, dlens, 1),
                          __shfl_sync(kFull, dlens, 2)};
+    if constexpr (kCoarse) {
+      __syncthreads();
+      cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sTq, swq);
+    }
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
     cg_reduce<4>(cl, w4, wsm, part[0], tot, [&] {
       double pq = tot[0];
@@ -413,6 +446,10 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     ++spmv;
     if (sc.stop) break;
     const float af = sc.af;
+    // Two-level form: c = E^-1 w for this CTA's groups, with the next
+    // residual's coarse vector w = W^T r − α W^T q from every group's owner.
+    if constexpr (kCoarse)
+      cg_coarse_solve(cl, A, J.model, ngr, sEi, sw + (size_t)cur * gsz, swq, af, swall, scf);
     float drr = 0.0f, drz2 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
@@ -425,40 +462,29 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       float zi = 0.0f;
 #pragma unroll
       for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
+      if constexpr (kCoarse) {
+        // z = B^-1 r + W c, and W^T r of the row for the next iteration
+        zi += cg_row_wc(sW + (size_t)lr * 42, __float_as_int(st[kCgIdx + 3]), scf, ci);
+        cg_row_wtr(sW + (size_t)lr * 42, ri, sT + (size_t)lr * 8);
+      }
       if (vl) {
         st[kCgZ + ci] = zi;
         drr += ri * ri;
         drz2 += ri * zi;
       }
-      if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, ri, sT + (size_t)lr * 8);
     }
     if constexpr (kCoarse) {
       __syncthreads();
-      cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sT, sw);
+      cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sT, sw + (size_t)prv * gsz);
     }
     const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};
     cg_reduce<2>(cl, w2b, wsm, part[1], tot, [&] {
       sc.stop = tot[0] < A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
-      if constexpr (kCoarse) {
-        sc.rzb = tot[1];  // r . B^-1 r; the coarse share follows
-      } else {
-        sc.beta = tot[1] / sc.rz;                  // ba.rs:189-190
-        sc.bf = (float)sc.beta;
-        sc.rz = tot[1];
-      }
+      sc.beta = tot[1] / sc.rz;                  // ba.rs:189-190
+      sc.bf = (float)sc.beta;
+      sc.rz = tot[1];
     });
     if (sc.stop) break;
-    if constexpr (kCoarse) {
-      // z = B^-1 r + W E^-1 W^T r; r . z = r . B^-1 r + w . c.
-      const float wc = cg_coarse_apply(cl, A, J.model, ngr, rs, nrows, sW, sEi, sw, swall, scf);
-      const float w1[1] = {threadIdx.x == 0 ? wc : 0.0f};
-      cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] {
-        const double rzn = sc.rzb + tot[0];
-        sc.beta = rzn / sc.rz;
-        sc.bf = (float)sc.beta;
-        sc.rz = rzn;
-      });
-    }
   }
   for (uint32_t lr = warp; lr < nrows; lr += kCgWarps)
     if (vl) A.x[6 * (size_t)(J.row0 + lr) + ci] = CGROW(lr)[kCgX + ci];

@@ -638,8 +638,9 @@ struct LmEngine {
     // Row state takes at most half of the shared memory (the rest caches S
     // blocks); with the coarse correction, which needs far fewer PCG
     // iterations, rows may take all of it and S is read from L2.
-    const size_t row_all = (size_t)kCgRow * 4 + (coarse ? (42 + 8) * 4 : 0);
-    const size_t coarse_fixed = coarse ? (size_t)4 * (7 * kCoarseMaxDim + 14) * 4 + kCoarseMaxDim * 4 : 0;
+    const size_t row_all = (size_t)kCgRow * 4 + (coarse ? (size_t)kCgCoarseRowF * 4 : 0);
+    const size_t coarse_fixed =
+        coarse ? (size_t)4 * cg_coarse_group_floats(kCoarseMaxDim) * 4 + kCoarseMaxDim * 4 : 0;
     const uint32_t rows_cap =
         (uint32_t)std::min<size_t>(coarse ? (avail - coarse_fixed) / row_all : avail / 2 / (kCgRow * 4), 4096);
     detail::ClusterPlan cp;
@@ -842,7 +843,7 @@ struct LmEngine {
       if (ctx.no > 0)
         BA_LAUNCH(obs_record_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
             P, cur, B, camf, active, sigma));
-      BA_LAUNCH(point_solve_mixed_kernel<<<grid_for(ctx.np, 128), 128, 0, s>>>(
+      BA_LAUNCH(point_solve_mixed_kernel<<<grid_for(ctx.np, kPtSolveThreads), kPtSolveThreads, 0, s>>>(
           P, cur, SV, B, active, lambda, sigma));
       if (ctx.no > 0)
         BA_LAUNCH(obs_factor_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(

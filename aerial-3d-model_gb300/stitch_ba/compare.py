@@ -30,16 +30,36 @@ def _stats(v: np.ndarray, p99: bool = False) -> dict:
     return out
 
 
+def similarity_fit(src: np.ndarray, dst: np.ndarray):
+    """Least-squares similarity (s, R, t) with dst ≈ s R src + t (Umeyama's
+    closed form: SVD of the cross-covariance of the centred point sets)."""
+    ms, md = src.mean(0), dst.mean(0)
+    xs, xd = src - ms, dst - md
+    U, S, Vt = np.linalg.svd(xd.T @ xs / len(src))
+    d = np.sign(np.linalg.det(U @ Vt))
+    D = np.diag([1.0, 1.0, d])
+    R = U @ D @ Vt
+    var = (xs ** 2).sum() / len(src)
+    s = float(np.trace(np.diag(S) @ D) / var) if var > 0 else 1.0
+    return s, R, md - s * R @ ms
+
+
 def state_errors(a, b, far_m: float = 1.0) -> dict:
     """Per-result differences of solution `a` from solution `b` (objects with
     rot, center, intr, points).  Points: max / median / 99th percentile of
-    the distance, and how many points differ by more than `far_m` metres."""
+    the distance, and how many points differ by more than `far_m` metres.
+
+    `aligned`: the same centre, rotation and point differences after `a` is
+    mapped onto `b` by the similarity that best fits its camera centres —
+    the part of the difference that is not a motion of the whole block
+    (translation, rotation, scale: the directions that only the GPS priors
+    hold, which the reference's stop rule leaves least converged)."""
     dc = np.linalg.norm(a.center - b.center, axis=1)
     dr = rot_angle(a.rot, b.rot)
     dp = np.linalg.norm(a.points - b.points, axis=1)
     di = np.abs(np.asarray(a.intr) - np.asarray(b.intr)).reshape(-1, 5)
     scale = np.maximum(np.abs(np.asarray(b.intr)).reshape(-1, 5), 1e-300)
-    return {
+    out = {
         "centre_m": _stats(dc),
         "rotation_rad": _stats(dr),
         "points_m": dict(_stats(dp, p99=True), n_above=int((dp > far_m).sum()), above_m=far_m),
@@ -47,3 +67,19 @@ def state_errors(a, b, far_m: float = 1.0) -> dict:
         "intrinsics_rel": {n: float((di[:, i] / scale[:, i]).max())
                            for i, n in enumerate(INTR_NAMES)},
     }
+    if len(a.center) >= 3:
+        s, R, t = similarity_fit(a.center, b.center)
+        ca = s * a.center @ R.T + t
+        pa = s * a.points @ R.T + t
+        ra = np.einsum("nij,kj->nik", a.rot.reshape(-1, 3, 3), R)  # world change: R_cam R^T
+        out["aligned"] = {
+            "similarity": {"scale_minus_1": s - 1.0,
+                           "rotation_rad": float(np.arcsin(min(1.0, np.linalg.norm(
+                               [R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]) / 2))),
+                           "translation_m": float(np.linalg.norm(t + (s * R - np.eye(3)) @
+                                                                 a.center.mean(0)))},
+            "centre_m": _stats(np.linalg.norm(ca - b.center, axis=1)),
+            "rotation_rad": _stats(rot_angle(ra, b.rot)),
+            "points_m": _stats(np.linalg.norm(pa - b.points, axis=1), p99=True),
+        }
+    return out

@@ -96,8 +96,12 @@ def test_autotuner_picks_a_configuration_and_keeps_the_result(precision):
     assert tuned.pcg_tuned_us > 0.0
     assert again.pcg_kernel == tuned.pcg_kernel and again.pcg_ctas == tuned.pcg_ctas
     assert again.final_cost == tuned.final_cost
-    # a different PCG layout only reorders FP64 sums
-    assert abs(tuned.final_cost - base.final_cost) <= 1e-6 * base.final_cost
+    # a different PCG layout only reorders sums: FP64 sums in the FP64 form;
+    # FP32 sums in the mixed form, whose end game then takes other small
+    # steps (the stop rule fires on the first small decrease), within a few
+    # 1e-6 on this survey
+    tol = 1e-6 if precision == "fp64" else 2e-5
+    assert abs(tuned.final_cost - base.final_cost) <= tol * base.final_cost
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
