@@ -215,3 +215,173 @@ def test_mixed_form_error_per_result_on_lawnmower77(parity_record):
     parity_record["mixed_vs_fp64:lawnmower77:pcg100"] = {
         "final_cost_rel": err100["final_cost_rel"], "iterations": err100["iterations"]}
     assert err100["final_cost_rel"] <= 1e-6, err100
+
+
+def test_reference_known_answer_on_gpu():
+    """ba.rs:482-492 assertions, on the GPU."""
+    p, f = load_fixture("refsurvey")
+    st = stitch_ba.bundle_adjust(p, 60, 4.0)
+    assert st.initial_rms > 20.0 and st.final_rms < 0.8, st
+    assert abs(p.intr[0, 0] / 3000.0 - 1.0) < 0.025
+
+
+def test_linearise_and_cost_match_oracle():
+    p, _ = load_fixture("lawnmower24")
+    with stitch_ba.Context() as ctx:
+        ctx.upload(p)
+        lin = ctx.linearise(1.0)
+        c, r, n = ctx.cost(1.0)
+    lo = O.linearise(p, 1.0)
+    assert np.array_equal(lin["valid"], lo["valid"])
+    for k in ("e", "jc", "jg", "jp", "w"):
+        scale = np.abs(lo[k]).max()
+        assert np.abs(lin[k] - lo[k]).max() <= 1e-12 * scale, k
+    co, ro, no = O.robust_cost(p, 1.0)
+    assert abs(c[0] - co) <= 1e-12 * co and abs(r[0] - ro) <= 1e-12 * ro and n[0] == no
+
+
+@pytest.mark.parametrize("name", ["refsurvey", "lawnmower24"])
+def test_reduced_system_matches_oracle(name):
+    """One LM system element-wise (ba.rs:221-331): S and g to rounding."""
+    p, f = load_fixture(name)
+    sigma = float(f["sigma"])
+    r = O.lm_step(p, 1e-4, sigma)
+    with stitch_ba.Context() as ctx:
+        ctx.upload(p)
+        d = ctx.debug_step(1e-4, sigma)
+    assert np.abs(d["S"] - r["S"]).max() <= 1e-12 * np.abs(r["S"]).max()
+    assert np.abs(d["g"] - r["g"]).max() <= 1e-12 * np.abs(r["g"]).max()
+    # PCG solution and trial cost: PCG stops on an ill-conditioned system.
+    assert np.abs(d["dx"] - r["dx"]).max() <= 1e-5 * np.abs(r["dx"]).max()
+    assert abs(d["trial_cost"] - r["trial_cost"]) <= 1e-8 * r["trial_cost"]
+
+
+def test_solver_is_deterministic():
+    p, f = load_fixture("lawnmower24")
+    q = p.copy()
+    a = stitch_ba.bundle_adjust(p, 10, 1.0, return_info=True)[1]
+    b = stitch_ba.bundle_adjust(q, 10, 1.0, return_info=True)[1]
+    assert np.array_equal(a.new_cost, b.new_cost)
+    assert np.array_equal(p.points, q.points) and np.array_equal(p.rot, q.rot)
+
+
+def test_batch_matches_individual_solves():
+    names = ["refsurvey", "lawnmower24", "refsurvey_fixed_intr"]
+    probs = [load_fixture(n)[0] for n in names]
+    singles = [p.copy() for p in probs]
+    infos = stitch_ba.bundle_adjust_batch(probs, 25, 4.0)
+    for p, q, info in zip(probs, singles, infos):
+        st, si = stitch_ba.bundle_adjust(q, 25, 4.0, return_info=True)
+        assert info.iterations == si.iterations
+        assert abs(info.final_cost - si.final_cost) <= 1e-8 * si.final_cost
+        assert np.abs(p.center - q.center).max() < 1e-6
+
+
+def test_intrinsics_gradient_matches_finite_differences():
+    """Adjoint d cost / d (f, cx, cy, k1, k2) against FP64 central differences
+    of the oracle's cost (h = 1e-6 relative)."""
+    p, f = load_fixture("refsurvey")
+    sigma = 4.0
+    with stitch_ba.Context() as ctx:
+        ctx.upload(p)
+        g = ctx.intrinsics_grad(sigma)[0]
+    for i in range(5):
+        q = p.copy()
+        h = 1e-6 * max(abs(q.intr[0, i]), 1e-2)  # relative step, floored for k1 = k2 = 0
+        q.intr[0, i] += h
+        cp = O.robust_cost(q, sigma)[0]
+        q.intr[0, i] -= 2 * h
+        cm = O.robust_cost(q, sigma)[0]
+        fd = (cp - cm) / (2 * h)
+        assert abs(g[i] - fd) <= 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max()), (i, g[i], fd)
+
+
+def test_vjp_matches_oracle_jacobians():
+    p, f = load_fixture("lawnmower24")
+    rng = np.random.default_rng(3)
+    lam = rng.standard_normal((p.n_obs, 2))
+    mu = rng.standard_normal((p.n_cams, 3))
+    with stitch_ba.Context() as ctx:
+        ctx.upload(p)
+        gc, gp, gi = ctx.vjp(1.0, lam, mu)
+    lo = O.linearise(p, 1.0)
+    v = lo["valid"]
+    ref_c = np.zeros((p.n_cams, 6))
+    ref_p = np.zeros((p.n_points, 3))
+    np.add.at(ref_c, p.obs_cam[v], -np.einsum("kij,ki->kj", lo["jc"][v], lam[v]))
+    np.add.at(ref_p, p.obs_pt[v], -np.einsum("kij,ki->kj", lo["jp"][v], lam[v]))
+    ref_c[:, 3:] += mu / p.prior[:, 3:]
+    assert np.abs(gc - ref_c).max() <= 1e-10 * np.abs(ref_c).max()
+    assert np.abs(gp - ref_p).max() <= 1e-10 * np.abs(ref_p).max()
+    ref_g = -np.einsum("kij,ki->j", lo["jg"][v], lam[v])
+    assert np.abs(gi[0, [0, 3, 4]] - ref_g).max() <= 1e-10 * np.abs(ref_g).max()
+    assert abs(gi[0, 1] + lam[v, 0].sum()) <= 1e-9 * np.abs(lam).sum()
+    assert abs(gi[0, 2] + lam[v, 1].sum()) <= 1e-9 * np.abs(lam).sum()
+
+
+def _tiny(n_obs_per_point=3):
+    p, f = load_fixture("refsurvey")
+    keep = p.obs_pt < 40
+    return Problem(intr=p.intr, rot=p.rot, center=p.center, cam_group=p.cam_group,
+                   points=p.points[:40], obs_cam=p.obs_cam[keep], obs_pt=p.obs_pt[keep],
+                   obs_uv=p.obs_uv[keep], prior_mask=p.prior_mask, prior=p.prior)
+
+
+def test_edge_cases_match_oracle():
+    # no observations at all: priors only
+    p = _tiny()
+    e = Problem(intr=p.intr, rot=p.rot, center=p.center, cam_group=p.cam_group,
+                points=p.points, obs_cam=np.zeros(0, np.uint32), obs_pt=np.zeros(0, np.uint32),
+                obs_uv=np.zeros((0, 2)), prior_mask=p.prior_mask, prior=p.prior)
+    for q in (e, _tiny()):
+        ref = q.copy()
+        st = stitch_ba.bundle_adjust(q, 20, 4.0)
+        r = O.bundle_adjust(ref, 20, 4.0)
+        assert st.iterations == r.iterations
+        assert abs(st.final_rms - r.final_rms) <= 1e-9 * max(r.final_rms, 1.0)
+        assert np.abs(q.center - ref.center).max() < 1e-6
+    # points with a single observation, a point behind its camera, no priors
+    q = _tiny()
+    ptr = np.searchsorted(q.obs_pt, np.arange(q.n_points + 1))
+    drop = np.zeros(q.n_obs, bool)
+    drop[ptr[3] + 1:ptr[4]] = True  # point 3 keeps one observation
+    q = Problem(intr=q.intr, rot=q.rot, center=q.center, cam_group=q.cam_group,
+                points=q.points.copy(), obs_cam=q.obs_cam[~drop], obs_pt=q.obs_pt[~drop],
+                obs_uv=q.obs_uv[~drop], prior_mask=None, prior=None)
+    q.points[5, 2] = 200.0  # above the cameras: behind every camera
+    ref = q.copy()
+    st = stitch_ba.bundle_adjust(q, 15, 4.0)
+    r = O.bundle_adjust(ref, 15, 4.0)
+    assert st.iterations == r.iterations
+    assert np.abs(q.points - ref.points).max() < 1e-5
+    # max_iter = 0: only the cost
+    q = _tiny()
+    ref = q.copy()
+    st = stitch_ba.bundle_adjust(q, 0, 4.0)
+    assert st.iterations == 0 and np.array_equal(q.points, ref.points)
+
+
+def test_bad_input_is_rejected():
+    p = _tiny()
+    bad = p.copy()
+    bad.obs_pt = bad.obs_pt[::-1].copy()
+    with pytest.raises(stitch_ba.BaError) as e:
+        stitch_ba.bundle_adjust(bad, 5, 4.0)
+    assert e.value.status == 1 and "sorted" in str(e.value)
+    bad = p.copy()
+    bad.obs_cam[0] = 99
+    with pytest.raises(stitch_ba.BaError):
+        stitch_ba.bundle_adjust(bad, 5, 4.0)
+    with pytest.raises(stitch_ba.BaError):
+        stitch_ba.bundle_adjust(p.copy(), 5, 0.0)
+    bad = p.copy()
+    bad.cam_group[0] = 3
+    with pytest.raises(stitch_ba.BaError):
+        stitch_ba.bundle_adjust(bad, 5, 4.0)
+    # the state is untouched after a rejected call
+    q = p.copy()
+    q.obs_pt = q.obs_pt[::-1].copy()
+    before = q.points.copy()
+    with pytest.raises(stitch_ba.BaError):
+        stitch_ba.bundle_adjust(q, 5, 4.0)
+    assert np.array_equal(before, q.points)
