@@ -1,7 +1,7 @@
 // Block-Jacobi PCG of the reduced camera system (ba.rs:155-196) with one
 // thread-block cluster per model and the whole solve in the cluster's
-// distributed shared memory: mixed form only (FP32 matrix and vectors, FP64
-// inner products).
+// distributed shared memory: mixed form only (FP32 matrix and vectors,
+// double-float inner products).
 //
 // A model's block rows are split over the CTAs of its cluster (balanced by
 // blocks); each CTA keeps its rows' state (x, r, z, two buffers of p, q and
@@ -105,67 +105,101 @@ __device__ __forceinline__ float cg_sum8f(float v) {
   return v;
 }
 
+// Double-float numbers: hi + lo with |lo| <= ulp(hi) / 2, about 48 bits from
+// FP32 instructions (on this GPU an FP64 warp instruction occupies its SM
+// sub-partition for ~64 cycles).
+struct DFloat {
+  float hi, lo;
+};
+// Sum of two double-floats (Knuth's two-sum of the high parts, the low parts
+// added to the error, renormalised).
+__device__ __forceinline__ DFloat df_sum(DFloat a, DFloat b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo);
+  const float hi = s + e;
+  return DFloat{hi, e - (hi - s)};
+}
+// x y for FP32 x and a double-float y: the exact product x y.hi (split by an
+// FMA) plus x y.lo.
+__device__ __forceinline__ DFloat df_scale(float x, DFloat y) {
+  const float p = x * y.hi;
+  const float e = fmaf(x, y.hi, -p) + x * y.lo;
+  const float hi = p + e;
+  return DFloat{hi, e - (hi - p)};
+}
+__device__ __forceinline__ DFloat df_shfl_xor(DFloat v, int o) {
+  return DFloat{__shfl_xor_sync(kFull, v.hi, o), __shfl_xor_sync(kFull, v.lo, o)};
+}
+
 // Inner products: a warp sums its rows' products in FP32 (a few rows of six
-// components); the warps' partials are summed in FP64 over the CTA and then
-// over the cluster's CTAs, in a fixed order, by warp 0 alone (an FP64 warp
-// instruction occupies its SM sub-partition for ~64 cycles on this GPU, so
-// FP64 work stays off the other warps).  wv: N (<= 4) values held by lane 0
-// of every warp; all threads receive the totals in tot (shared memory).
+// components); the warps' partials are summed as double-floats over the CTA
+// and then over the cluster's CTAs, in a fixed order, by warp 0.  wv: N
+// (<= 4) values held by lane 0 of every warp; all threads receive the totals
+// in tot (shared memory).  Every CTA sums the same partials in the same
+// order, so every CTA sees bit-identical totals.
+//
+// Exchange by push: before the cluster barrier, lane r of warp 0 stores the
+// CTA's partials into CTA r's inbox (inbox[source rank][value]); after it,
+// every CTA reads its own inbox.  A warp that loads from many CTAs waits on
+// each remote round trip (measured: ~4.5k cycles for one load per CTA of a
+// 16-CTA cluster), while remote stores complete behind the barrier's
+// release.  Consecutive reductions use different inboxes: a CTA can only
+// write inbox n + 2 after the barrier of reduction n + 1, which every reader
+// of inbox n has passed.
 template <int N, typename Post>
 __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&wv)[N],
-                                          float* wsm, double* part, double* tot, Post&& post) {
+                                          float* wsm, DFloat (*inbox)[4], DFloat* tot,
+                                          Post&& post) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
     for (int i = 0; i < 4; ++i) wsm[warp * 4 + i] = i < N ? wv[i < N ? i : 0] : 0.0f;
   __syncthreads();
+  const int csize = (int)cl.num_blocks();
   if (warp == 0) {
-    double c = 0.0;  // lane = 4 w + i (mod 32): warps w, w + 8, ... in order
+    // lane = 4 w + i: warps w and w + 8 (value i), then over w in a fixed tree
+    static_assert(kCgWarps * 4 == 64, "two warp partials per lane");
+    DFloat c = df_sum(DFloat{wsm[lane], 0.0f}, DFloat{wsm[32 + lane], 0.0f});
+    c = df_sum(c, df_shfl_xor(c, 4));
+    c = df_sum(c, df_shfl_xor(c, 8));
+    c = df_sum(c, df_shfl_xor(c, 16));
+    DFloat v[N];
 #pragma unroll
-    for (int o = 0; o < kCgWarps * 4; o += 32) c += (double)wsm[o + lane];
-    c += __shfl_xor_sync(kFull, c, 4);
-    c += __shfl_xor_sync(kFull, c, 8);
-    c += __shfl_xor_sync(kFull, c, 16);
-    if (lane < 4) part[lane] = c;
+    for (int i = 0; i < N; ++i)
+      v[i] = DFloat{__shfl_sync(kFull, c.hi, i), __shfl_sync(kFull, c.lo, i)};
+    if (lane < csize) {
+      DFloat* dst = cl.map_shared_rank(&inbox[0][0], (unsigned)lane) + 4 * cl.block_rank();
+#pragma unroll
+      for (int i = 0; i < N; ++i) dst[i] = v[i];
+    }
   }
   cl.sync();
   if (warp == 0) {
-    // lane r < cluster size holds CTA r's values; recursive halving leaves
-    // the sum of value i in lanes 4i..4i+3.
-    const int csize = (int)cl.num_blocks();
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
-    if (lane < csize) {
-      const double* rp = cl.map_shared_rank(part, (unsigned)lane);
+    // lane r < cluster size (<= 16) holds CTA r's values; lanes 16..31 hold
+    // zeros and the butterfly stays within each half-warp.
+    DFloat v[N];
 #pragma unroll
-      for (int i = 0; i < N; ++i) v[i] = rp[i];
+    for (int i = 0; i < N; ++i) v[i] = lane < csize ? inbox[lane][i] : DFloat{0.0f, 0.0f};
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1)
+#pragma unroll
+      for (int i = 0; i < N; ++i) v[i] = df_sum(v[i], df_shfl_xor(v[i], o));
+    if (lane == 0) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) tot[i] = v[i];
+      post();  // the iteration's scalars, once per CTA
     }
-    {
-      const bool up = lane & 8;
-      const double s0 = up ? v[0] : v[2], s1 = up ? v[1] : v[3];
-      const double r0 = __shfl_xor_sync(kFull, s0, 8), r1 = __shfl_xor_sync(kFull, s1, 8);
-      v[0] = (up ? v[2] : v[0]) + r0;
-      v[1] = (up ? v[3] : v[1]) + r1;
-    }
-    {
-      const bool up = lane & 4;
-      const double s0 = up ? v[0] : v[1];
-      const double r0 = __shfl_xor_sync(kFull, s0, 4);
-      v[0] = (up ? v[1] : v[0]) + r0;
-    }
-    v[0] += __shfl_xor_sync(kFull, v[0], 2);
-    v[0] += __shfl_xor_sync(kFull, v[0], 1);
-    v[0] += __shfl_xor_sync(kFull, v[0], 16);  // lanes >= 16 hold zeros
-    if ((lane & 3) == 0 && lane < 16) tot[lane >> 2] = v[0];
-    __syncwarp();
-    if (lane == 0) post();  // the iteration's scalars, once per CTA
   }
   __syncthreads();
 }
 
-// Scalars of the iteration, computed by thread 0 and read by every thread.
+// Scalars of the iteration, computed by thread 0 and read by every thread:
+// r.z as a double-float, b.b, α and β in FP32 (the precision of the vectors
+// they scale).
 struct CgScalars {
-  double rz, b2, pq, beta;
-  float af, bf;
+  DFloat rz;
+  float b2, af, bf;
   int stop;
 };
 
@@ -211,14 +245,15 @@ __device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const
   return add;
 }
 
-// One row's W^T r (7 values) into t[0..6]: lane i < 6 holds r_i.
-__device__ __forceinline__ void cg_row_wtr(const float* w, float ri, float* t) {
+// One row's W^T x (7 values) into t[0..6]: lane i < 6 holds x_i; lane j < 7
+// forms mode j from the six broadcast components.
+__device__ __forceinline__ void cg_row_wtr(const float* w, float xi, float* t) {
   const int lane = threadIdx.x & 31;
+  const int j = lane < kCoarseModes ? lane : 0;
+  float v = 0.0f;
 #pragma unroll
-  for (int j = 0; j < kCoarseModes; ++j) {
-    const float v = cg_sum8f(lane < 6 ? w[kCoarseModes * lane + j] * ri : 0.0f);
-    if (lane == 0) t[j] = v;
-  }
+  for (int i = 0; i < 6; ++i) v += w[kCoarseModes * i + j] * __shfl_sync(kFull, xi, i);
+  if (lane < kCoarseModes) t[j] = v;
 }
 
 // Per own group: w = sum over its rows of W^T r, in row order (thread per
@@ -237,8 +272,9 @@ __device__ __forceinline__ void cg_group_sums(int32_t ngr, const int32_t* grp_ro
 template <bool kCoarse>
 static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A) {
   __shared__ float wsm[kCgWarps * 4];
-  __shared__ double part[3][4];
-  __shared__ double tot[4];
+  __shared__ DFloat inbox[3][kCgMaxCluster][4];  // reduction inboxes (push)
+  __shared__ DFloat tot[4];
+  __shared__ float lens_p[4];  // the lens row's p, pushed by its owner
   __shared__ CgScalars sc;
   extern __shared__ __align__(16) unsigned char cg_smem[];
   cgx::cluster_group cl = cgx::this_cluster();
@@ -266,7 +302,6 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   const int32_t cg0 = kCoarse ? A.job_g0[blockIdx.x] : 0;
   const int32_t ngr = kCoarse ? A.job_g1[blockIdx.x] - cg0 : 0;
   const int32_t lens = A.lens_row[J.model];
-  const uint32_t lens_loc = lens >= 0 ? A.row_loc[lens] : 0u;
   {
     const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
     float4* dst = reinterpret_cast<float4*>(sS);
@@ -335,10 +370,9 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   }
   const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
   // The first barrier also makes every CTA's shared memory live for DSMEM.
-  cg_reduce<2>(cl, w2, wsm, part[1], tot, [&] {
+  cg_reduce<2>(cl, w2, wsm, inbox[1], tot, [&] {
     sc.rz = tot[0];
-    sc.b2 = fmax(tot[1], 1e-300);
-    sc.beta = 0.0;
+    sc.b2 = tot[1].hi;
     sc.bf = 0.0f;
     sc.stop = 0;
   });
@@ -357,7 +391,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       }
     }
     const float w1[1] = {cg_sum8f(drz0)};
-    cg_reduce<1>(cl, w1, wsm, part[2], tot, [&] { sc.rz = tot[0]; });
+    cg_reduce<1>(cl, w1, wsm, inbox[2], tot, [&] { sc.rz = tot[0]; });
   }
   int32_t spmv = 0;
   for (int32_t it = 0; it < A.max_iter; ++it) {
@@ -398,6 +432,15 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         st[kCgP + 8 * cur + ci] = pi;
       }
       if (vl) dpq += pi * qi;
+      if ((int32_t)(J.row0 + lr) == lens) {
+        // every CTA's post needs the lens row's p (its share of p.q): push it
+        const float p0 = __shfl_sync(kFull, pi, 0), p1 = __shfl_sync(kFull, pi, 1),
+                    p2 = __shfl_sync(kFull, pi, 2);
+        if (lane < (int)cl.num_blocks()) {
+          float* dst = cl.map_shared_rank(lens_p, (unsigned)lane);
+          dst[0] = p0, dst[1] = p1, dst[2] = p2;
+        }
+      }
       // W^T q of the row for the next coarse vector (the lens row, in no
       // group, has W = 0; its transposed terms arrive after the reduction).
       if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, qi, sTq + (size_t)lr * 8);
@@ -424,24 +467,22 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sTq, swq);
     }
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
-    cg_reduce<4>(cl, w4, wsm, part[0], tot, [&] {
-      double pq = tot[0];
+    cg_reduce<4>(cl, w4, wsm, inbox[0], tot, [&] {
+      DFloat pq = tot[0];
       if (lens >= 0) {
         // The lens row's q gets the transposed camera terms; its share of
-        // p.q is p_g . (sum S_cg^T p_c), with p_g stored by its owner before
+        // p.q is p_g . (sum S_cg^T p_c), with p_g pushed by its owner before
         // the barrier.
-        const float* lrow =
-            cl.map_shared_rank(rs, lens_loc >> 16) + (size_t)(lens_loc & 0xffffu) * kCgRow;
-        pq += (double)lrow[kCgP + 8 * cur + 0] * tot[1] + (double)lrow[kCgP + 8 * cur + 1] * tot[2] +
-              (double)lrow[kCgP + 8 * cur + 2] * tot[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) pq = df_sum(pq, df_scale(lens_p[c], tot[1 + c]));
         if (lens_here) {
           float* q = CGROW((uint32_t)lens - J.row0) + kCgQ;
-          for (int c = 0; c < 3; ++c) q[c] = (float)((double)q[c] + tot[1 + c]);
+          for (int c = 0; c < 3; ++c) q[c] = df_sum(DFloat{q[c], 0.0f}, tot[1 + c]).hi;
         }
       }
-      sc.pq = pq;
-      sc.stop = fabs(pq) < 1e-300 ? 1 : 0;  // ba.rs:174
-      sc.af = sc.stop ? 0.0f : (float)(sc.rz / pq);
+      // ba.rs:174 breaks on a vanishing p.q; an FP32 quotient needs it normal
+      sc.stop = fabsf(pq.hi) < 1.17549435e-38f ? 1 : 0;
+      sc.af = sc.stop ? 0.0f : sc.rz.hi / pq.hi;
     });
     ++spmv;
     if (sc.stop) break;
@@ -478,10 +519,9 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sT, sw + (size_t)prv * gsz);
     }
     const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};
-    cg_reduce<2>(cl, w2b, wsm, part[1], tot, [&] {
-      sc.stop = tot[0] < A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
-      sc.beta = tot[1] / sc.rz;                  // ba.rs:189-190
-      sc.bf = (float)sc.beta;
+    cg_reduce<2>(cl, w2b, wsm, inbox[1], tot, [&] {
+      sc.stop = tot[0].hi < (float)A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
+      sc.bf = tot[1].hi / sc.rz.hi;                        // ba.rs:189-190
       sc.rz = tot[1];
     });
     if (sc.stop) break;

