@@ -6,8 +6,13 @@
 // A model's block rows are split over the CTAs of its cluster (balanced by
 // blocks); each CTA keeps its rows' state (x, r, z, two buffers of p, q and
 // the block-Jacobi inverse) and its rows' S blocks in shared memory for the
-// whole solve.  A row's neighbour values z_j and p_j(prev) are read straight
-// from the owning CTA's shared memory (DSMEM), and the two reductions of an
+// whole solve.  Every value another CTA needs is pushed to it: a CTA keeps a
+// cache of the neighbour rows its blocks multiply (z_j and both buffers of
+// p_j), and each row's owner stores the row's new z and p into the caches of
+// the CTAs that read it (a host-built subscriber list) before the cluster
+// barrier after which they are read.  Remote loads would be round trips a
+// warp waits on (~4.5k cycles when its lanes read from 16 CTAs); remote
+// stores complete behind the barrier's release.  The two reductions of an
 // iteration meet at hardware cluster barriers: no global memory traffic and
 // no software spin inside the iteration.  The iteration is the reference's,
 // with p_j = z_j + β p_j(prev) formed on the fly as in the grid kernel.
@@ -38,9 +43,12 @@ constexpr int kCgThreads = 512;
 constexpr int kCgWarps = kCgThreads / 32;
 constexpr int kCgMaxCluster = 16;
 // Row state in floats: x r z p0 p1 q (8 each, 6 used) | M (36) | the row's
-// first and end block and its lens block (int bits) | pad.
+// first and end block, its lens block, its coarse group slot and its
+// subscriber range (int bits) | pad.
 constexpr int kCgX = 0, kCgR = 8, kCgZ = 16, kCgP = 24, kCgQ = 40, kCgM = 48, kCgIdx = 84;
-constexpr int kCgRow = 88;
+constexpr int kCgRow = 92;
+// Neighbour cache slot in floats: z (8, 6 used) | p buffer 0 (8) | p buffer 1.
+constexpr int kCgCache = 24;
 
 struct CgJob {
   int32_t model;
@@ -77,24 +85,32 @@ struct CgArgs {
   const uint32_t* grp_loc;   // [groups]: owner rank << 16 | local group slot
   uint32_t cap_groups;       // group slots per CTA
   uint32_t cap_dim;          // largest model coarse dimension
+  // Neighbour caches: the cache slot of every block's column in its row's
+  // CTA, and per row the (CTA rank << 16 | slot) entries of the caches that
+  // hold it.
+  const uint32_t* blk_slot;  // [nz]
+  const uint32_t* sub_ptr;   // [nb + 1]
+  const uint32_t* sub_ent;
+  uint32_t cap_cache;        // cache slots per CTA
 };
 
-inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks) {
-  return (size_t)cap_rows * kCgRow * 4 + (size_t)cap_blocks * (36 * 4 + 4);
+inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks, uint32_t cap_cache) {
+  return (size_t)cap_rows * kCgRow * 4 + (size_t)cap_blocks * (36 * 4 + 4) +
+         (size_t)cap_cache * kCgCache * 4;
 }
 
 // Extra shared memory of the two-level form, in floats: per row W (42),
-// W^T r (8) and W^T q (8); per own group its rows of E^-1 (7 x D), the group
-// sums of W^T r (two buffers by iteration parity: a CTA writes the next one
-// while others still read the current one) and of W^T q (7 each), and c (7);
-// the gathered w of the model (D).
+// W^T r (8) and W^T q (8); per own group its rows of E^-1 (7 x D) and c (7);
+// the model's group sums of W^T r (two buffers by iteration parity: owners
+// push the next one while the current one is read) and of W^T q (D each),
+// pushed by every group's owner.
 constexpr int kCgCoarseRowF = 42 + 8 + 8;
-__host__ __device__ constexpr size_t cg_coarse_group_floats(uint32_t cap_dim) {
-  return (size_t)kCoarseModes * cap_dim + 4 * kCoarseModes;
+__host__ __device__ constexpr size_t cg_coarse_fixed_floats(uint32_t cap_groups,
+                                                            uint32_t cap_dim) {
+  return (size_t)cap_groups * (kCoarseModes * cap_dim + kCoarseModes) + 3 * (size_t)cap_dim;
 }
 inline size_t cg_coarse_smem_bytes(uint32_t cap_rows, uint32_t cap_groups, uint32_t cap_dim) {
-  return ((size_t)cap_rows * kCgCoarseRowF + (size_t)cap_groups * cg_coarse_group_floats(cap_dim) +
-          cap_dim) * 4;
+  return ((size_t)cap_rows * kCgCoarseRowF + cg_coarse_fixed_floats(cap_groups, cap_dim)) * 4;
 }
 
 // Sum over lanes 0..7 (lanes >= 8 hold 0); lanes 0..7 receive it.
@@ -203,28 +219,22 @@ struct CgScalars {
   int stop;
 };
 
-// The coarse step of the two-level form, once the group sums are published:
-// gather the model's w = W^T r − α W^T q from the groups' owners (α = 0 and
-// no W^T q at the start: w = W^T b), then c = E^-1 w for this CTA's groups
-// (into sc, 7 per group).  Ends with a CTA barrier.
-__device__ __forceinline__ void cg_coarse_solve(cgx::cluster_group& cl, const CgArgs& A, int m,
-                                                int32_t ngr, const float* sEi, const float* swr,
-                                                const float* swq, float alpha, float* swall,
-                                                float* sc) {
+// The coarse step of the two-level form, once every group's sums have been
+// pushed: c = E^-1 w for this CTA's groups (into sc, 7 per group), with the
+// model's w = W^T r − α W^T q (α = 0 and no W^T q at the start: w = W^T b).
+// Ends with a CTA barrier.
+__device__ __forceinline__ void cg_coarse_solve(const CgArgs& A, int m, int32_t ngr,
+                                                const float* sEi, const float* wr,
+                                                const float* wq, float alpha, float* sc) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int32_t gm0 = A.model_g0[m];
-  const int D = kCoarseModes * (A.model_g0[m + 1] - gm0);
-  for (int t = threadIdx.x; t < D; t += kCgThreads) {
-    const uint32_t loc = A.grp_loc[gm0 + t / kCoarseModes];
-    const int o = (int)(loc & 0xffffu) * kCoarseModes + t % kCoarseModes;
-    const float wr = cl.map_shared_rank(swr, loc >> 16)[o];
-    swall[t] = swq ? wr - alpha * cl.map_shared_rank(swq, loc >> 16)[o] : wr;
-  }
-  __syncthreads();
+  const int D = kCoarseModes * (A.model_g0[m + 1] - A.model_g0[m]);
   for (int o = warp; o < ngr * kCoarseModes; o += kCgWarps) {
     const float* er = sEi + (size_t)o * A.cap_dim;
     float v = 0.0f;
-    for (int t = lane; t < D; t += 32) v += er[t] * swall[t];
+    if (wq)
+      for (int t = lane; t < D; t += 32) v += er[t] * (wr[t] - alpha * wq[t]);
+    else
+      for (int t = lane; t < D; t += 32) v += er[t] * wr[t];
 #pragma unroll
     for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
     if (lane == 0) sc[o] = v;
@@ -256,16 +266,37 @@ __device__ __forceinline__ void cg_row_wtr(const float* w, float xi, float* t) {
   if (lane < kCoarseModes) t[j] = v;
 }
 
-// Per own group: w = sum over its rows of W^T r, in row order (thread per
-// group and mode); rows hold their W^T r in sT.
-__device__ __forceinline__ void cg_group_sums(int32_t ngr, const int32_t* grp_row0,
-                                              const int32_t* grp_row1, int32_t g0,
-                                              uint32_t row0, const float* sT, float* sw) {
+// Per own group: the sum over its rows of W^T x, in row order (thread per
+// group and mode; rows hold their W^T x in sT), pushed into the model-wide
+// array `dst` (D floats, at this CTA's groups' offset) of every CTA.
+__device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int32_t ngr,
+                                                   const int32_t* grp_row0,
+                                                   const int32_t* grp_row1, int32_t g0,
+                                                   int32_t goff, uint32_t row0, const float* sT,
+                                                   float* dst) {
+  const int csize = (int)cl.num_blocks();
   for (int o = threadIdx.x; o < ngr * kCoarseModes; o += kCgThreads) {
     const int l = o / kCoarseModes, j = o % kCoarseModes;
     float v = 0.0f;
     for (int32_t r = grp_row0[g0 + l]; r < grp_row1[g0 + l]; ++r) v += sT[(size_t)(r - row0) * 8 + j];
-    sw[o] = v;
+    for (int k = 0; k < csize; ++k) cl.map_shared_rank(dst, (unsigned)k)[goff + o] = v;
+  }
+}
+
+// Push a row's six values (lane i < 6 holds x_i) into the neighbour cache of
+// every CTA that reads the row, at float offset `off` of its slot there.
+__device__ __forceinline__ void cg_push_row(cgx::cluster_group& cl, float* cache,
+                                            const uint32_t* sub_ent, uint32_t s0, uint32_t s1,
+                                            float xi, int off) {
+  const int lane = threadIdx.x & 31;
+  float x[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) x[i] = __shfl_sync(kFull, xi, i);
+  for (uint32_t t = s0 + lane; t < s1; t += 32) {
+    const uint32_t e = __ldg(sub_ent + t);
+    float* dst = cl.map_shared_rank(cache, e >> 16) + (size_t)(e & 0xffffu) * kCgCache + off;
+    *reinterpret_cast<float4*>(dst) = make_float4(x[0], x[1], x[2], x[3]);
+    *reinterpret_cast<float2*>(dst + 4) = make_float2(x[4], x[5]);
   }
 }
 
@@ -285,29 +316,34 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   const uint32_t B0 = A.row_ptr[J.row0];
   const uint32_t nblk = A.row_ptr[J.row1] - B0;
   const uint32_t ncached = nblk < A.cap_blocks ? nblk : A.cap_blocks;
+  // Shared memory: row state | cached S blocks | neighbour cache | cached
+  // blocks' cache slots | two-level form: W, W^T r and W^T q per row, E^-1
+  // rows and c per own group, the model's group sums of W^T r (two buffers)
+  // and W^T q.
   float* rs = reinterpret_cast<float*>(cg_smem);
   float* sS = rs + (size_t)A.cap_rows * kCgRow;
-  uint32_t* sL = reinterpret_cast<uint32_t*>(sS + (size_t)A.cap_blocks * 36);
-  // Two-level form: W, W^T r and W^T q per row, E^-1 rows, the group sums
-  // of W^T r (two buffers) and W^T q and c per own group, the gathered w.
+  float* cache = sS + (size_t)A.cap_blocks * 36;
+  uint32_t* sL = reinterpret_cast<uint32_t*>(cache + (size_t)A.cap_cache * kCgCache);
   float* sW = reinterpret_cast<float*>(sL + A.cap_blocks);
   float* sT = sW + (size_t)A.cap_rows * 42;
   float* sTq = sT + (size_t)A.cap_rows * 8;
   float* sEi = sTq + (size_t)A.cap_rows * 8;
   const size_t gsz = (size_t)A.cap_groups * kCoarseModes;
-  float* sw = sEi + gsz * A.cap_dim;  // [2][groups][7]
-  float* swq = sw + 2 * gsz;
-  float* scf = swq + gsz;
-  float* swall = scf + gsz;
+  float* scf = sEi + gsz * A.cap_dim;
+  float* wall_r = scf + gsz;                  // [2][D]
+  float* wall_q = wall_r + 2 * (size_t)A.cap_dim;  // [D]
   const int32_t cg0 = kCoarse ? A.job_g0[blockIdx.x] : 0;
   const int32_t ngr = kCoarse ? A.job_g1[blockIdx.x] - cg0 : 0;
+  const int32_t goff = kCoarse ? kCoarseModes * (cg0 - A.model_g0[J.model]) : 0;
   const int32_t lens = A.lens_row[J.model];
   {
     const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
     float4* dst = reinterpret_cast<float4*>(sS);
     for (uint32_t c = threadIdx.x; c < ncached * 9; c += blockDim.x) dst[c] = src[c];
-    for (uint32_t t = threadIdx.x; t < ncached; t += blockDim.x)
-      sL[t] = A.row_loc[A.col_idx[B0 + t]];
+    for (uint32_t t = threadIdx.x; t < ncached; t += blockDim.x) sL[t] = A.blk_slot[B0 + t];
+    // p(prev) of iteration 0 is 0 in every cached row; the z values arrive
+    // by push after the first cluster barrier.
+    for (uint32_t t = threadIdx.x; t < A.cap_cache * kCgCache; t += blockDim.x) cache[t] = 0.0f;
     for (uint32_t t = threadIdx.x; t < nrows * 36; t += blockDim.x)
       rs[(size_t)(t / 36) * kCgRow + kCgM + (t % 36)] = A.pre[36 * (size_t)J.row0 + t];
     // Per row: its block range (the lens row: its diagonal block only; its
@@ -326,6 +362,8 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         for (int32_t l = 0; l < ngr; ++l)
           if ((int32_t)row >= A.grp_row0[cg0 + l] && (int32_t)row < A.grp_row1[cg0 + l]) lg = l;
       st[kCgIdx + 3] = __int_as_float(lg);
+      st[kCgIdx + 4] = __int_as_float((int)A.sub_ptr[row]);
+      st[kCgIdx + 5] = __int_as_float((int)A.sub_ptr[row + 1]);
     }
     if constexpr (kCoarse) {
       for (uint32_t t = threadIdx.x; t < nrows * 42; t += blockDim.x)
@@ -364,12 +402,9 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     }
     if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, ri, sT + (size_t)lr * 8);
   }
-  if constexpr (kCoarse) {
-    __syncthreads();
-    cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sT, sw);
-  }
   const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
-  // The first barrier also makes every CTA's shared memory live for DSMEM.
+  // The first barrier also makes every CTA's shared memory live for DSMEM:
+  // nothing is pushed before it.
   cg_reduce<2>(cl, w2, wsm, inbox[1], tot, [&] {
     sc.rz = tot[0];
     sc.b2 = tot[1].hi;
@@ -378,20 +413,32 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   });
   if constexpr (kCoarse) {
     // z = B^-1 b + W E^-1 W^T b, and r . z with it.
-    cg_coarse_solve(cl, A, J.model, ngr, sEi, sw, nullptr, 0.0f, swall, scf);
+    cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sT, wall_r);
+    cl.sync();
+    cg_coarse_solve(A, J.model, ngr, sEi, wall_r, nullptr, 0.0f, scf);
     float drz0 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
       const int32_t lg = __float_as_int(st[kCgIdx + 3]);
       const float add = cg_row_wc(sW + (size_t)lr * 42, lg, scf, ci);
+      float zi = 0.0f;
       if (vl) {
-        const float zi = st[kCgZ + ci] + add;
+        zi = st[kCgZ + ci] + add;
         st[kCgZ + ci] = zi;
         drz0 += st[kCgR + ci] * zi;
       }
+      cg_push_row(cl, cache, A.sub_ent, (uint32_t)__float_as_int(st[kCgIdx + 4]),
+                  (uint32_t)__float_as_int(st[kCgIdx + 5]), zi, 0);
     }
     const float w1[1] = {cg_sum8f(drz0)};
     cg_reduce<1>(cl, w1, wsm, inbox[2], tot, [&] { sc.rz = tot[0]; });
+  } else {
+    for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
+      const float* st = CGROW(lr);
+      cg_push_row(cl, cache, A.sub_ent, (uint32_t)__float_as_int(st[kCgIdx + 4]),
+                  (uint32_t)__float_as_int(st[kCgIdx + 5]), vl ? st[kCgZ + ci] : 0.0f, 0);
+    }
+    cl.sync();  // z of iteration 0 in every cache
   }
   int32_t spmv = 0;
   for (int32_t it = 0; it < A.max_iter; ++it) {
@@ -405,12 +452,12 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       for (uint32_t k = b0 + lane; k < b1; k += 32) {
         const uint32_t kk = k - B0;
-        const uint32_t loc = kk < ncached ? sL[kk] : A.row_loc[A.col_idx[k]];
-        const float* rrow = cl.map_shared_rank(rs, loc >> 16) + (size_t)(loc & 0xffffu) * kCgRow;
-        const float4 z0 = *reinterpret_cast<const float4*>(rrow + kCgZ);
-        const float4 z1 = *reinterpret_cast<const float4*>(rrow + kCgZ + 4);
-        const float4 q0 = *reinterpret_cast<const float4*>(rrow + kCgP + 8 * prv);
-        const float4 q1 = *reinterpret_cast<const float4*>(rrow + kCgP + 8 * prv + 4);
+        const uint32_t slot = kk < ncached ? sL[kk] : __ldg(A.blk_slot + k);
+        const float* crow = cache + (size_t)slot * kCgCache;
+        const float4 z0 = *reinterpret_cast<const float4*>(crow);
+        const float4 z1 = *reinterpret_cast<const float4*>(crow + 4);
+        const float4 q0 = *reinterpret_cast<const float4*>(crow + 8 + 8 * prv);
+        const float4 q1 = *reinterpret_cast<const float4*>(crow + 8 + 8 * prv + 4);
         const float pp[6] = {z0.x + q0.x * bf, z0.y + q0.y * bf, z0.z + q0.z * bf,
                              z0.w + q0.w * bf, z1.x + q1.x * bf, z1.y + q1.y * bf};
         float m[36];
@@ -432,6 +479,8 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         st[kCgP + 8 * cur + ci] = pi;
       }
       if (vl) dpq += pi * qi;
+      cg_push_row(cl, cache, A.sub_ent, (uint32_t)__float_as_int(st[kCgIdx + 4]),
+                  (uint32_t)__float_as_int(st[kCgIdx + 5]), pi, 8 + 8 * cur);
       if ((int32_t)(J.row0 + lr) == lens) {
         // every CTA's post needs the lens row's p (its share of p.q): push it
         const float p0 = __shfl_sync(kFull, pi, 0), p1 = __shfl_sync(kFull, pi, 1),
@@ -464,7 +513,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
                          __shfl_sync(kFull, dlens, 2)};
     if constexpr (kCoarse) {
       __syncthreads();
-      cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sTq, swq);
+      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sTq, wall_q);
     }
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
     cg_reduce<4>(cl, w4, wsm, inbox[0], tot, [&] {
@@ -490,7 +539,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     // Two-level form: c = E^-1 w for this CTA's groups, with the next
     // residual's coarse vector w = W^T r − α W^T q from every group's owner.
     if constexpr (kCoarse)
-      cg_coarse_solve(cl, A, J.model, ngr, sEi, sw + (size_t)cur * gsz, swq, af, swall, scf);
+      cg_coarse_solve(A, J.model, ngr, sEi, wall_r + (size_t)cur * A.cap_dim, wall_q, af, scf);
     float drr = 0.0f, drz2 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
@@ -513,10 +562,13 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
         drr += ri * ri;
         drz2 += ri * zi;
       }
+      cg_push_row(cl, cache, A.sub_ent, (uint32_t)__float_as_int(st[kCgIdx + 4]),
+                  (uint32_t)__float_as_int(st[kCgIdx + 5]), zi, 0);
     }
     if constexpr (kCoarse) {
       __syncthreads();
-      cg_group_sums(ngr, A.grp_row0, A.grp_row1, cg0, J.row0, sT, sw + (size_t)prv * gsz);
+      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sT,
+                         wall_r + (size_t)prv * A.cap_dim);
     }
     const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};
     cg_reduce<2>(cl, w2b, wsm, inbox[1], tot, [&] {

@@ -165,6 +165,53 @@ inline bool plan_cluster(const Context& ctx, const std::vector<uint32_t>& row_pt
   return true;
 }
 
+// Neighbour caches of the cluster PCG: for each CTA the distinct columns its
+// rows' blocks multiply (the lens row: its diagonal block only), in order of
+// first use; blk_slot[k] = the cache slot of block k's column in its row's
+// CTA; per row the (CTA rank << 16 | slot) entries of the caches that hold
+// it, which its owner pushes the row's z and p into.
+struct CachePlan {
+  std::vector<uint32_t> blk_slot, sub_ptr, sub_ent;
+  uint32_t cap = 0;
+};
+
+inline bool plan_cache(const ClusterPlan& cp, int csize, const std::vector<uint32_t>& row_ptr,
+                       const std::vector<uint32_t>& col_idx, const std::vector<uint32_t>& diag_pos,
+                       const std::vector<int32_t>& lens_row, int64_t nb, CachePlan& pl) {
+  pl = CachePlan{};
+  pl.blk_slot.assign(std::max<size_t>(col_idx.size(), 1), 0);
+  std::vector<std::vector<uint32_t>> subs((size_t)nb);
+  std::vector<int64_t> stamp((size_t)nb, -1);
+  std::vector<uint32_t> slot_of((size_t)nb, 0);
+  for (size_t g = 0; g < cp.jobs.size(); ++g) {
+    const CgJob& J = cp.jobs[g];
+    const uint32_t rank = (uint32_t)(g % (size_t)csize);
+    const int32_t lens = lens_row[J.model];
+    uint32_t n = 0;
+    for (uint32_t r = J.row0; r < J.row1; ++r) {
+      uint32_t b0 = row_ptr[r], b1 = row_ptr[r + 1];
+      if ((int32_t)r == lens) b0 = diag_pos[r], b1 = b0 + 1;
+      for (uint32_t k = b0; k < b1; ++k) {
+        const uint32_t c = col_idx[k];
+        if (stamp[c] != (int64_t)g) {
+          stamp[c] = (int64_t)g;
+          slot_of[c] = n++;
+          subs[c].push_back((rank << 16) | slot_of[c]);
+        }
+        pl.blk_slot[k] = slot_of[c];
+      }
+    }
+    if (n > 0xffffu) return false;
+    pl.cap = std::max(pl.cap, n);
+  }
+  pl.sub_ptr.assign((size_t)nb + 1, 0);
+  for (int64_t r = 0; r < nb; ++r) pl.sub_ptr[r + 1] = pl.sub_ptr[r] + (uint32_t)subs[r].size();
+  pl.sub_ent.reserve(std::max<size_t>(pl.sub_ptr[nb], 1));
+  for (int64_t r = 0; r < nb; ++r) pl.sub_ent.insert(pl.sub_ent.end(), subs[r].begin(), subs[r].end());
+  if (pl.sub_ent.empty()) pl.sub_ent.push_back(0);
+  return true;
+}
+
 // Coarse groups of the two-level preconditioner: each cluster CTA's camera
 // rows (the lens row excluded) split into runs of consecutive rows, about 8
 // rows each and at most kCoarseMaxGroups per model, so a group lives in one
@@ -421,7 +468,8 @@ struct LmEngine {
   bool use_cluster = false;
   int cl_size = 0;
   DevBuf<CgJob> cg_jobs;
-  DevBuf<uint32_t> cg_loc;
+  DevBuf<uint32_t> cg_loc, cg_slot, cg_subp, cg_sube;
+  std::vector<uint32_t> h_col_idx, h_diag_pos;  // host copies for the cache plan
   CgArgs ca{};
   size_t cg_smem = 0;
   // Two-level preconditioner (mixed form, cluster kernel).
@@ -639,8 +687,7 @@ struct LmEngine {
     // blocks); with the coarse correction, which needs far fewer PCG
     // iterations, rows may take all of it and S is read from L2.
     const size_t row_all = (size_t)kCgRow * 4 + (coarse ? (size_t)kCgCoarseRowF * 4 : 0);
-    const size_t coarse_fixed =
-        coarse ? (size_t)4 * cg_coarse_group_floats(kCoarseMaxDim) * 4 + kCoarseMaxDim * 4 : 0;
+    const size_t coarse_fixed = coarse ? cg_coarse_fixed_floats(4, kCoarseMaxDim) * 4 : 0;
     const uint32_t rows_cap =
         (uint32_t)std::min<size_t>(coarse ? (avail - coarse_fixed) / row_all : avail / 2 / (kCgRow * 4), 4096);
     detail::ClusterPlan cp;
@@ -653,11 +700,25 @@ struct LmEngine {
       detail::plan_coarse(ctx, cp, h_lens, csize, gp);
       coarse_bytes = cg_coarse_smem_bytes(cp.max_rows, std::max(gp.cap_groups, 1u), std::max(gp.dmax, 1u));
     }
+    if (h_col_idx.empty() && SB.nz > 0) {
+      h_col_idx.resize((size_t)SB.nz);
+      h_diag_pos.resize((size_t)ctx.nb);
+      check(cudaMemcpyAsync(h_col_idx.data(), SB.col_idx.p, 4 * (size_t)SB.nz,
+                            cudaMemcpyDeviceToHost, s), "d2h");
+      check(cudaMemcpyAsync(h_diag_pos.data(), SB.diag_pos.p, 4 * (size_t)ctx.nb,
+                            cudaMemcpyDeviceToHost, s), "d2h");
+      check(cudaStreamSynchronize(s), "sync");
+    }
+    detail::CachePlan kp;
+    if (!detail::plan_cache(cp, csize, SB.h_row_ptr, h_col_idx, h_diag_pos, h_lens, ctx.nb, kp))
+      return unusable("a CTA's neighbour cache exceeds 65,535 rows");
     const size_t row_bytes = (size_t)cp.max_rows * kCgRow * 4;
-    if (row_bytes + coarse_bytes >= avail) return unusable("row state does not fit");
+    const size_t cache_bytes = (size_t)kp.cap * kCgCache * 4;
+    if (row_bytes + coarse_bytes + cache_bytes >= avail)
+      return unusable("row state and neighbour cache do not fit");
     const uint32_t cap_blocks = (uint32_t)std::min<size_t>(
-        cp.max_blocks, (avail - row_bytes - coarse_bytes) / (36 * 4 + 4));
-    const size_t smem = cg_smem_bytes(cp.max_rows, cap_blocks) + coarse_bytes;
+        cp.max_blocks, (avail - row_bytes - coarse_bytes - cache_bytes) / (36 * 4 + 4));
+    const size_t smem = cg_smem_bytes(cp.max_rows, cap_blocks, kp.cap) + coarse_bytes;
     check(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
           "cluster smem");
     if (csize > 8)
@@ -689,9 +750,13 @@ struct LmEngine {
     if (!required && !prefer_cluster && (int64_t)nclusters < ctx.nm) return false;
     detail::h2d(cg_jobs, cp.jobs, s);
     detail::h2d(cg_loc, cp.row_loc, s);
+    detail::h2d(cg_slot, kp.blk_slot, s);
+    detail::h2d(cg_subp, kp.sub_ptr, s);
+    detail::h2d(cg_sube, kp.sub_ent, s);
     ca = CgArgs{cg_jobs, cg_loc, SB.row_ptr, SB.col_idx, (const float*)S.p, (const float*)pre.p,
                 (const float*)g.p, (float*)x.p, lens_row, lens_pos, SB.diag_pos, cp.max_rows,
                 cap_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol};
+    ca.blk_slot = cg_slot, ca.sub_ptr = cg_subp, ca.sub_ent = cg_sube, ca.cap_cache = kp.cap;
     use_coarse = coarse;
     ctx.last_coarse_dim = 0;
     if (coarse) {
