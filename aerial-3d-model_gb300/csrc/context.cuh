@@ -26,6 +26,8 @@ struct PcgTuning {
   int rows_target = 4;  // grid kernel: block rows per CTA
   int cluster = 0;      // cluster kernel: CTAs per cluster
   double us_per_iter = 0.0;
+  int sub_len = 0;      // Schur pairs per warp sub-segment (0: the default)
+  double schur_us = 0.0;
 };
 
 struct Context {
@@ -59,6 +61,7 @@ struct Context {
   int64_t phase_n[kPhases] = {0};
   int64_t last_nz = 0, last_pairs = 0, last_nl = 0;
   int32_t last_pcg_kernel = 0, last_pcg_cluster = 0, last_pcg_ctas = 0, last_coarse_dim = 0;
+  int32_t last_sub_len = 0;
   PcgTuning tuning[2];  // [0] FP64 form, [1] mixed form
   bool last_graph = false;
   bool last_matrix_free = false;

@@ -454,6 +454,7 @@ struct LmEngine {
   DevBuf<double> pcg_part;
   DevBuf<int32_t> lens_row, lens_pos;
   uint32_t smem_rows = 0, smem_blocks = 0;
+  uint32_t sub_len = kSubLen;  // Schur pairs per warp sub-segment
   size_t smem_bytes = 0;
   int pcg_rows_target = 0, grid_rows_target = 0, max_ctas = 0;
   std::vector<int32_t> h_lens;
@@ -510,6 +511,8 @@ struct LmEngine {
     build_structure(P, ctx.h_obs0, SB, ctx.err, s, cap);
     implicit = SB.implicit;
     ctx.last_matrix_free = implicit;
+    sub_len = kSubLen;
+    ctx.last_sub_len = implicit ? 0 : (int32_t)sub_len;
     SV = SB.view();
     ctx.last_nz = SB.nz, ctx.last_pairs = SB.npairs - nb, ctx.last_nl = SB.nl;
     lin.alloc(at_least_1(no) * kLinW, s), gsub.alloc(at_least_1(no) * 9, s);
@@ -610,6 +613,7 @@ struct LmEngine {
       auto it = tune_cache().find(tune_key());
       if (it != tune_cache().end()) tu = it->second;
     }
+    if (tu.valid && tu.sub_len > 0) set_sub_len((uint32_t)tu.sub_len);
     if (tu.valid && o.pcg_kernel == 0) {
       if (tu.kernel != 2 || !try_cluster(tu.cluster, false, true)) plan_grid(tu.rows_target);
     } else if (o.pcg_kernel == 2) {
@@ -619,6 +623,18 @@ struct LmEngine {
     } else {
       plan_grid(pcg_rows_target > 0 ? pcg_rows_target : (sizeof(R) == 8 ? 4 : 8));
     }
+  }
+
+  // Schur sub-segments of at most L pairs (a warp each): rebuilt from the
+  // pair list, with the partial-sum buffer they write.
+  void set_sub_len(uint32_t L) {
+    if (implicit || SB.ns == 0 || L == sub_len) return;
+    build_subsegments(SB, L, s);
+    part.alloc(detail::at_least_1(SB.nsub) * 36, s);
+    SV = SB.view();
+    B.part = part;
+    sub_len = L;
+    ctx.last_sub_len = (int32_t)L;
   }
 
   // Matrix-free PCG: one cooperative launch over every SM, one group.
@@ -804,6 +820,33 @@ struct LmEngine {
       ~Restore() { t.on = v; }
     } restore{T, timing};
     build_system();
+    // Schur sub-segment length: pairs per warp (more warps in flight to hide
+    // the factor gathers, against more partial sums to add).
+    double schur_us = 0.0;
+    if (SB.ns > 0) {
+      cudaEvent_t a, b;
+      check(cudaEventCreate(&a), "event");
+      check(cudaEventCreate(&b), "event");
+      float best_ms = 1e30f;
+      uint32_t best_L = sub_len;
+      for (uint32_t L : {256u, 512u, 1024u, 2048u}) {
+        set_sub_len(L);
+        for (int rep = 0; rep < 3; ++rep) {
+          check(cudaEventRecord(a, s), "event");
+          BA_LAUNCH(schur_kernel<R><<<grid_for(SB.nsub * 32, 256), 256, 0, s>>>(P, SV, B, active));
+          check(cudaEventRecord(b, s), "event");
+          check(cudaEventSynchronize(b), "tune");
+          float ms = 0;
+          check(cudaEventElapsedTime(&ms, a, b), "event");
+          if (ms < best_ms) best_ms = ms, best_L = L;
+        }
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      set_sub_len(best_L);
+      schur_us = best_ms * 1000.0;
+      build_system();  // the system with the kept sub-segments
+    }
     std::vector<std::pair<int, int>> cand;  // (kernel, rows_target or cluster size)
     // With the two-level preconditioner (cluster kernel only) the PCG needs a
     // fraction of the iterations, so only cluster layouts compete; the grid
@@ -872,6 +915,8 @@ struct LmEngine {
     tu.rows_target = best_c.first == 1 ? best_c.second : 4;
     tu.cluster = best_c.first == 2 ? best_c.second : 0;
     tu.us_per_iter = best * 1000.0;
+    tu.sub_len = (int)sub_len;
+    tu.schur_us = schur_us;
     {
       std::lock_guard<std::mutex> lk(tune_mutex());
       tune_cache()[tune_key()] = tu;

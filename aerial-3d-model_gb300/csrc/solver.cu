@@ -358,6 +358,10 @@ void solve(Context& c, const ba_options* opt, ba_stats* stats) {
       st.graph = c.last_graph ? 1 : 0;
       st.pcg_ctas = c.last_pcg_ctas;
       st.pcg_coarse_dim = c.last_coarse_dim;
+      st.schur_sub_len = c.last_sub_len;
+      st.schur_tuned_us = c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].valid
+                              ? c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].schur_us
+                              : 0.0;
       st.pcg_tuned_us = c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].valid
                             ? c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].us_per_iter
                             : 0.0;

@@ -293,15 +293,17 @@ __global__ void place_lower_kernel(const uint64_t* tkeys, const uint32_t* tvals,
   pos_ba[tvals[i]] = pos;
 }
 
-__global__ void sub_count_kernel(const uint32_t* slot_ptr, int64_t ns, uint32_t* cnt) {
+__global__ void sub_count_kernel(const uint32_t* slot_ptr, int64_t ns, uint32_t sub_len,
+                                 uint32_t* cnt) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= ns) return;
   const uint32_t len = slot_ptr[s + 1] - slot_ptr[s];
-  cnt[s] = len == 0 ? 1u : (len + kSubLen - 1) / kSubLen;
+  cnt[s] = len == 0 ? 1u : (len + sub_len - 1) / sub_len;
 }
 
 __global__ void sub_fill_kernel(const uint32_t* slot_ptr, const uint32_t* sub_ptr, int64_t ns,
-                                uint32_t* sub_slot, uint32_t* sub_begin, uint32_t* sub_end) {
+                                uint32_t sub_len, uint32_t* sub_slot, uint32_t* sub_begin,
+                                uint32_t* sub_end) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= ns) return;
   const uint32_t b = slot_ptr[s], e = slot_ptr[s + 1];
@@ -309,8 +311,8 @@ __global__ void sub_fill_kernel(const uint32_t* slot_ptr, const uint32_t* sub_pt
   for (uint32_t t = 0; t < n; ++t) {
     const uint32_t o = sub_ptr[s] + t;
     sub_slot[o] = (uint32_t)s;
-    sub_begin[o] = b + t * kSubLen;
-    sub_end[o] = min(e, b + (t + 1) * kSubLen);
+    sub_begin[o] = b + t * sub_len;
+    sub_end[o] = min(e, b + (t + 1) * sub_len);
   }
 }
 
@@ -391,6 +393,21 @@ void build_cam_index(const Prob& P, StructBufs& S, cudaStream_t s) {
     S.grp_ptr.alloc(ng + 1, s);
     lower_bounds_u64(k, nc, S.grp_ptr, ng, 1, s);
   }
+}
+
+void build_subsegments(StructBufs& S, uint32_t sub_len, cudaStream_t s) {
+  const int64_t ns = S.ns;
+  if (ns <= 0) return;
+  DevBuf<uint32_t> cnt(ns + 1, s);
+  BA_LAUNCH(sub_count_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, ns, sub_len, cnt));
+  check(cudaMemsetAsync(cnt.p + ns, 0, 4, s), "memset");
+  S.slot_sub_ptr.alloc(ns + 1, s);
+  S.nsub = (int64_t)exclusive_scan_u32(cnt, S.slot_sub_ptr, ns + 1, s);
+  S.sub_slot.alloc(S.nsub, s);
+  S.sub_begin.alloc(S.nsub, s);
+  S.sub_end.alloc(S.nsub, s);
+  BA_LAUNCH(sub_fill_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, S.slot_sub_ptr, ns, sub_len,
+                                                        S.sub_slot, S.sub_begin, S.sub_end));
 }
 
 void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, StructBufs& S,
@@ -507,19 +524,7 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
                                                                  S.slot_pos_ba, ns, S.nz, err));
     }
     slot_key.release();
-    // Warp sub-segments of the Schur sums.
-    {
-      DevBuf<uint32_t> cnt(ns + 1, s);
-      BA_LAUNCH(sub_count_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, ns, cnt));
-      check(cudaMemsetAsync(cnt.p + ns, 0, 4, s), "memset");
-      S.slot_sub_ptr.alloc(ns + 1, s);
-      S.nsub = (int64_t)exclusive_scan_u32(cnt, S.slot_sub_ptr, ns + 1, s);
-      S.sub_slot.alloc(S.nsub, s);
-      S.sub_begin.alloc(S.nsub, s);
-      S.sub_end.alloc(S.nsub, s);
-      BA_LAUNCH(sub_fill_kernel<<<grid_for(ns, T), T, 0, s>>>(S.slot_ptr, S.slot_sub_ptr, ns,
-                                                            S.sub_slot, S.sub_begin, S.sub_end));
-    }
+    build_subsegments(S, kSubLen, s);
 
   } else {
     S.ns = S.nsub = S.nz = 0;

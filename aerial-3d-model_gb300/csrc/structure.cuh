@@ -31,6 +31,10 @@ void build_cam_index(const Prob& P, StructBufs& S, cudaStream_t s);
 // pair_bytes_cap: < 0 always build the Schur pair list and the reduced
 // matrix layout; 0 never (matrix-free); > 0 only if they fit in that many
 // bytes.
+// Warp sub-segments of the Schur sums: each destination block's pair range
+// cut into runs of at most sub_len pairs (a warp each); replaces any earlier
+// sub-segments of S.
+void build_subsegments(StructBufs& S, uint32_t sub_len, cudaStream_t s);
 void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, StructBufs& S,
                      uint32_t* err, cudaStream_t s, int64_t pair_bytes_cap = -1);
 

@@ -71,6 +71,8 @@ class SolveInfo:
     pcg_ctas: int = 0             # CTAs of the PCG launch
     pcg_tuned_us: float = 0.0     # autotuned time per PCG iteration (0: not tuned)
     coarse_dim: int = 0           # coarse unknowns of the two-level preconditioner
+    schur_sub_len: int = 0        # Schur pairs per warp sub-segment
+    schur_tuned_us: float = 0.0   # autotuned Schur kernel time (0: not tuned)
 
     def stats(self) -> BaStats:
         return BaStats(self.iterations, self.initial_rms, self.final_rms)
@@ -144,6 +146,8 @@ def _info(s: native.BaStatsC) -> SolveInfo:
     info.pcg_ctas = s.pcg_ctas
     info.pcg_tuned_us = s.pcg_tuned_us
     info.coarse_dim = s.pcg_coarse_dim
+    info.schur_sub_len = s.schur_sub_len
+    info.schur_tuned_us = s.schur_tuned_us
     return info
 
 

@@ -69,7 +69,8 @@ class BaStatsC(C.Structure):
                 ("n_schur_pairs", C.c_int64), ("n_lens_entries", C.c_int64),
                 ("pcg_kernel", C.c_int32), ("pcg_cluster", C.c_int32), ("graph", C.c_int32),
                 ("pcg_ctas", C.c_int32), ("pcg_tuned_us", C.c_double),
-                ("pcg_coarse_dim", C.c_int32)]
+                ("pcg_coarse_dim", C.c_int32), ("schur_sub_len", C.c_int32),
+                ("schur_tuned_us", C.c_double)]
 
 PHASES = ["point", "camera", "schur", "assemble", "pcg", "update", "cost", "control", "setup"]
 

@@ -385,6 +385,8 @@ def gpu_arm(args, ws, rank):
             forms[form]["pcg_kernel"] = prof.pcg_kernel
             forms[form]["pcg_ctas"] = int(prof.pcg_ctas)
             forms[form]["pcg_autotuned_us_per_iter"] = prof.pcg_tuned_us
+            forms[form]["schur_sub_len"] = int(prof.schur_sub_len)
+            forms[form]["schur_autotuned_us"] = prof.schur_tuned_us
             forms[form]["device_bytes"] = int(prof.device_bytes)
             forms[form]["pcg_max_iter"] = opts.pcg_max_iter
             forms[form]["coarse_dim"] = int(prof.coarse_dim)
@@ -464,7 +466,8 @@ def gpu_arm(args, ws, rank):
     zs = prof.sizes
     sz = dict(n_obs=tot["n_obs"], n_points=tot["n_points"], n_cams=tot["n_cams"], nb=zs["blocks"],
               nz_blocks=zs["nonzero_blocks"], pairs=zs["schur_pairs"],
-              subsegments=zs["schur_pairs"] // 512 + (zs["nonzero_blocks"] + zs["blocks"]) // 2)
+              subsegments=zs["schur_pairs"] // max(int(prof.schur_sub_len), 1)
+              + (zs["nonzero_blocks"] + zs["blocks"]) // 2)
     s = 8 if chosen == "fp64" else 4
     per_launch_ms = dom_ms / max(dom_n, 1)
     if dom == "pcg":

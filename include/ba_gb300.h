@@ -117,9 +117,10 @@ typedef struct ba_options {
   int32_t no_graph;     /* 1: launch each kernel directly instead of replaying
                            a CUDA graph of the LM iteration                */
   int32_t autotune;     /* 1: before the first solve of a form on a context,
-                           time the PCG configurations (grid rows per CTA,
-                           cluster sizes) on its first system and keep the
-                           fastest for this and later solves               */
+                           time the Schur sub-segment lengths (pairs per
+                           warp) and the PCG configurations (grid rows per
+                           CTA, cluster sizes) on its first system and keep
+                           the fastest for this and later solves          */
   int32_t stop_patience; /* LM stops after this many consecutive accepted
                            steps with relative decrease < 1e-6; 0 or 1:
                            the reference's rule (ba.rs:372-374)          */
@@ -183,6 +184,9 @@ typedef struct ba_stats {
   double pcg_tuned_us;    /* autotuner's time per PCG iteration (0: none)  */
   int32_t pcg_coarse_dim; /* coarse unknowns of the two-level preconditioner
                              (largest model), 0: block-Jacobi alone       */
+  int32_t schur_sub_len;  /* Schur pair contributions per warp sub-segment
+                             (chosen by the autotuner, else 512)          */
+  double schur_tuned_us;  /* autotuner's Schur kernel time (0: not tuned) */
 } ba_stats;
 
 /* Defaults: max_iter 60, sigma_px 1, Cauchy, FP64, PCG 400 / 1e-20. */

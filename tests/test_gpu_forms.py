@@ -95,6 +95,10 @@ def test_autotuner_picks_a_configuration_and_keeps_the_result(precision):
         again = ctx.solve(60, 1.0, Options(precision=precision))[0]  # reuses the tuning
     assert tuned.pcg_tuned_us > 0.0
     assert again.pcg_kernel == tuned.pcg_kernel and again.pcg_ctas == tuned.pcg_ctas
+    # the Schur sub-segment length is tuned too, and kept
+    assert base.schur_sub_len == 512 and tuned.schur_tuned_us > 0.0
+    assert tuned.schur_sub_len in (256, 512, 1024, 2048)
+    assert again.schur_sub_len == tuned.schur_sub_len
     assert again.final_cost == tuned.final_cost
     # a different PCG layout only reorders sums: FP64 sums in the FP64 form;
     # FP32 sums in the mixed form, whose end game then takes other small
