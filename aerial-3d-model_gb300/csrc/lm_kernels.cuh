@@ -1419,9 +1419,40 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1)
 
 // ---- assemble S and g (ba.rs:293-331) ----------------------------------------
 
+// Destination blocks with more than kFoldMin sub-segments (the lens block of
+// a model gets a pair from every point) are summed first by a CTA each: warp
+// w takes entries w, w + 8, ...; lane l adds sub-segments l, l + 32, ... in
+// order, then a fixed butterfly; the total replaces the block's first
+// partial, and assemble_kernel reads that one alone (sub_end[s] = first + 1).
+constexpr uint32_t kFoldMin = 64;
+constexpr int kFoldThreads = 256;
+
+static __global__ void __launch_bounds__(kFoldThreads)
+    schur_fold_kernel(Prob P, StructView S, double* part, const uint32_t* fold_slots,
+                      const int32_t* active) {
+  const uint32_t s = fold_slots[blockIdx.x];
+  if (!active[P.blk_model[S.slot_row[s]]]) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t u0 = S.slot_sub_ptr[s], u1 = S.slot_sub_ptr[s + 1];
+  double tot[5];
+  int n = 0;
+  for (int el = warp; el < 36; el += kFoldThreads / 32, ++n) {
+    double v = 0.0;
+    for (uint32_t u = u0 + lane; u < u1; u += 32) v += part[(size_t)u * 36 + el];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    tot[n] = v;
+  }
+  __syncthreads();  // every partial read before the first is replaced
+  n = 0;
+  for (int el = warp; el < 36; el += kFoldThreads / 32, ++n)
+    if (lane == 0) part[(size_t)u0 * 36 + el] = tot[n];
+}
+
 template <typename R>
 __global__ void assemble_kernel(Prob P, StateView st, StructView S, IterBufs<R> B,
-                                const int32_t* active, const double* lambda, double* S64) {
+                                const int32_t* active, const double* lambda, double* S64,
+                                const uint32_t* sub_end) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.ns * 36) return;
   const int64_t s = t / 36;
@@ -1429,11 +1460,10 @@ __global__ void assemble_kernel(Prob P, StateView st, StructView S, IterBufs<R> 
   const uint32_t a = S.slot_row[s], bcol = S.slot_col[s];
   const uint32_t m = P.blk_model[a];
   if (!active[m]) return;
-  // Sub-segment sums in FP64 in both forms, in sub-segment order.  A block
-  // with many sub-segments (the lens block of a model: one per 512 points)
-  // is one long dependent chain: its loads are issued eight at a time.
+  // Sub-segment sums in FP64 in both forms, in sub-segment order (a folded
+  // block: its one folded total).
   double sum = 0.0;
-  const uint32_t u1 = S.slot_sub_ptr[s + 1];
+  const uint32_t u1 = sub_end ? sub_end[s] : S.slot_sub_ptr[s + 1];
   const double* pp = B.part + el;
   uint32_t u = S.slot_sub_ptr[s];
   for (; u + 8 <= u1; u += 8) {

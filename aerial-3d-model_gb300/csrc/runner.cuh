@@ -455,6 +455,8 @@ struct LmEngine {
   DevBuf<int32_t> lens_row, lens_pos;
   uint32_t smem_rows = 0, smem_blocks = 0;
   uint32_t sub_len = kSubLen;  // Schur pairs per warp sub-segment
+  DevBuf<uint32_t> fold_slots, sub_end;  // blocks folded before assembly
+  uint32_t n_fold = 0;
   size_t smem_bytes = 0;
   int pcg_rows_target = 0, grid_rows_target = 0, max_ctas = 0;
   std::vector<int32_t> h_lens;
@@ -513,6 +515,7 @@ struct LmEngine {
     ctx.last_matrix_free = implicit;
     sub_len = kSubLen;
     ctx.last_sub_len = implicit ? 0 : (int32_t)sub_len;
+    plan_fold();
     SV = SB.view();
     ctx.last_nz = SB.nz, ctx.last_pairs = SB.npairs - nb, ctx.last_nl = SB.nl;
     lin.alloc(at_least_1(no) * kLinW, s), gsub.alloc(at_least_1(no) * 9, s);
@@ -635,6 +638,29 @@ struct LmEngine {
     B.part = part;
     sub_len = L;
     ctx.last_sub_len = (int32_t)L;
+    plan_fold();
+  }
+
+  // Blocks with more than kFoldMin sub-segments, folded by schur_fold_kernel
+  // before assembly, and every block's effective end of sub-segments.
+  void plan_fold() {
+    n_fold = 0;
+    if (implicit || SB.ns == 0) return;
+    std::vector<uint32_t> ptr((size_t)SB.ns + 1);
+    check(cudaMemcpyAsync(ptr.data(), SB.slot_sub_ptr.p, 4 * ptr.size(), cudaMemcpyDeviceToHost, s),
+          "d2h");
+    check(cudaStreamSynchronize(s), "sync");
+    std::vector<uint32_t> fs, end((size_t)SB.ns);
+    for (int64_t k = 0; k < SB.ns; ++k) {
+      const bool fold = ptr[k + 1] - ptr[k] > kFoldMin;
+      if (fold) fs.push_back((uint32_t)k);
+      end[k] = fold ? ptr[k] + 1 : ptr[k + 1];
+    }
+    n_fold = (uint32_t)fs.size();
+    if (fs.empty()) fs.push_back(0);
+    detail::h2d(fold_slots, fs, s);
+    detail::h2d(sub_end, end, s);
+    check(cudaStreamSynchronize(s), "sync");
   }
 
   // Matrix-free PCG: one cooperative launch over every SM, one group.
@@ -985,10 +1011,13 @@ struct LmEngine {
     }
     if (SB.nsub > 0)
       BA_LAUNCH(schur_kernel<R><<<grid_for(SB.nsub * 32, 256), 256, 0, s>>>(P, SV, B, active));
+    if (n_fold > 0)
+      BA_LAUNCH(schur_fold_kernel<<<n_fold, kFoldThreads, 0, s>>>(P, SV, part, fold_slots,
+                                                                 active));
     T.mark(BA_PHASE_SCHUR);
     if (SB.ns > 0)
       BA_LAUNCH(assemble_kernel<R><<<grid_for(SB.ns * 36, 256), 256, 0, s>>>(
-          P, cur, SV, B, active, lambda, c_S64.p));
+          P, cur, SV, B, active, lambda, c_S64.p, sub_end.p));
     BA_LAUNCH(rhs_kernel<R><<<grid_for(ctx.nb * 6, 256), 256, 0, s>>>(P, cur, B, active));
     BA_LAUNCH(precond_kernel<R><<<grid_for(ctx.nb, 128), 128, 0, s>>>(P, SV, B, active));
     T.mark(BA_PHASE_ASSEMBLE);
