@@ -42,11 +42,14 @@ namespace cgx = cooperative_groups;
 constexpr int kCgThreads = 512;
 constexpr int kCgWarps = kCgThreads / 32;
 constexpr int kCgMaxCluster = 16;
-// Row state in floats: x r z p0 p1 q (8 each, 6 used) | M (36) | the row's
-// first and end block, its lens block, its coarse group slot and its
-// subscriber range (int bits) | pad.
-constexpr int kCgX = 0, kCgR = 8, kCgZ = 16, kCgP = 24, kCgQ = 40, kCgM = 48, kCgIdx = 84;
-constexpr int kCgRow = 92;
+// Row state in floats: x r z p0 p1 q (6 each) | M (36) | the row's first and
+// end block, its lens block, its coarse group slot and its subscriber range
+// (int bits) | pad.  Accessed one component per lane.
+constexpr int kCgX = 0, kCgR = 6, kCgZ = 12, kCgP = 18, kCgQ = 30, kCgM = 36, kCgIdx = 72;
+constexpr int kCgRow = 80;
+// A block's column is one of the CTA's own rows when its slot carries this
+// bit (the low bits are the local row), else a slot of the neighbour cache.
+constexpr uint32_t kCgOwnRow = 0x80000000u;
 // Neighbour cache slot in floats: z (8, 6 used) | p buffer 0 (8) | p buffer 1.
 constexpr int kCgCache = 24;
 
@@ -99,12 +102,11 @@ inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks, uint32_t cap
          (size_t)cap_cache * kCgCache * 4;
 }
 
-// Extra shared memory of the two-level form, in floats: per row W (42),
-// W^T r (8) and W^T q (8); per own group its rows of E^-1 (7 x D) and c (7);
-// the model's group sums of W^T r (two buffers by iteration parity: owners
-// push the next one while the current one is read) and of W^T q (D each),
-// pushed by every group's owner.
-constexpr int kCgCoarseRowF = 42 + 8 + 8;
+// Extra shared memory of the two-level form, in floats: per row W (42); per
+// own group its rows of E^-1 (7 x D) and c (7); the model's group sums of
+// W^T r (two buffers by iteration parity: owners push the next one while the
+// current one is read) and of W^T q (D each), pushed by every group's owner.
+constexpr int kCgCoarseRowF = 42;
 __host__ __device__ constexpr size_t cg_coarse_fixed_floats(uint32_t cap_groups,
                                                             uint32_t cap_dim) {
   return (size_t)cap_groups * (kCoarseModes * cap_dim + kCoarseModes) + 3 * (size_t)cap_dim;
@@ -255,30 +257,27 @@ __device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const
   return add;
 }
 
-// One row's W^T x (7 values) into t[0..6]: lane i < 6 holds x_i; lane j < 7
-// forms mode j from the six broadcast components.
-__device__ __forceinline__ void cg_row_wtr(const float* w, float xi, float* t) {
-  const int lane = threadIdx.x & 31;
-  const int j = lane < kCoarseModes ? lane : 0;
-  float v = 0.0f;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) v += w[kCoarseModes * i + j] * __shfl_sync(kFull, xi, i);
-  if (lane < kCoarseModes) t[j] = v;
-}
-
-// Per own group: the sum over its rows of W^T x, in row order (thread per
-// group and mode; rows hold their W^T x in sT), pushed into the model-wide
-// array `dst` (D floats, at this CTA's groups' offset) of every CTA.
+// Per own group: sum over its rows (in row order) of W^T x, x the row-state
+// vector at float offset `xoff` (thread per group and mode; each row's six
+// products in component order), pushed into the model-wide array `dst` (D
+// floats, at this CTA's groups' offset) of every CTA.
 __device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int32_t ngr,
                                                    const int32_t* grp_row0,
                                                    const int32_t* grp_row1, int32_t g0,
-                                                   int32_t goff, uint32_t row0, const float* sT,
-                                                   float* dst) {
+                                                   int32_t goff, uint32_t row0, const float* sW,
+                                                   const float* rs, int xoff, float* dst) {
   const int csize = (int)cl.num_blocks();
   for (int o = threadIdx.x; o < ngr * kCoarseModes; o += kCgThreads) {
     const int l = o / kCoarseModes, j = o % kCoarseModes;
     float v = 0.0f;
-    for (int32_t r = grp_row0[g0 + l]; r < grp_row1[g0 + l]; ++r) v += sT[(size_t)(r - row0) * 8 + j];
+    for (int32_t r = grp_row0[g0 + l]; r < grp_row1[g0 + l]; ++r) {
+      const float* w = sW + (size_t)(r - row0) * 42 + j;
+      const float* x = rs + (size_t)(r - row0) * kCgRow + xoff;
+      float t = 0.0f;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) t += w[kCoarseModes * i] * x[i];
+      v += t;
+    }
     for (int k = 0; k < csize; ++k) cl.map_shared_rank(dst, (unsigned)k)[goff + o] = v;
   }
 }
@@ -325,9 +324,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   float* cache = sS + (size_t)A.cap_blocks * 36;
   uint32_t* sL = reinterpret_cast<uint32_t*>(cache + (size_t)A.cap_cache * kCgCache);
   float* sW = reinterpret_cast<float*>(sL + A.cap_blocks);
-  float* sT = sW + (size_t)A.cap_rows * 42;
-  float* sTq = sT + (size_t)A.cap_rows * 8;
-  float* sEi = sTq + (size_t)A.cap_rows * 8;
+  float* sEi = sW + (size_t)A.cap_rows * 42;
   const size_t gsz = (size_t)A.cap_groups * kCoarseModes;
   float* scf = sEi + gsz * A.cap_dim;
   float* wall_r = scf + gsz;                  // [2][D]
@@ -396,11 +393,10 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       st[kCgX + ci] = 0.0f;
       st[kCgR + ci] = ri;
       st[kCgZ + ci] = zi;
-      st[kCgP + 8 + ci] = 0.0f;  // p buffer 1 = p(prev) of iteration 0
+      st[kCgP + 6 + ci] = 0.0f;  // p buffer 1 = p(prev) of iteration 0
       drz += ri * zi;
       dbb += ri * ri;
     }
-    if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, ri, sT + (size_t)lr * 8);
   }
   const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
   // The first barrier also makes every CTA's shared memory live for DSMEM:
@@ -413,7 +409,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   });
   if constexpr (kCoarse) {
     // z = B^-1 b + W E^-1 W^T b, and r . z with it.
-    cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sT, wall_r);
+    cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgR, wall_r);
     cl.sync();
     cg_coarse_solve(A, J.model, ngr, sEi, wall_r, nullptr, 0.0f, scf);
     float drz0 = 0.0f;
@@ -453,13 +449,20 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       for (uint32_t k = b0 + lane; k < b1; k += 32) {
         const uint32_t kk = k - B0;
         const uint32_t slot = kk < ncached ? sL[kk] : __ldg(A.blk_slot + k);
-        const float* crow = cache + (size_t)slot * kCgCache;
-        const float4 z0 = *reinterpret_cast<const float4*>(crow);
-        const float4 z1 = *reinterpret_cast<const float4*>(crow + 4);
-        const float4 q0 = *reinterpret_cast<const float4*>(crow + 8 + 8 * prv);
-        const float4 q1 = *reinterpret_cast<const float4*>(crow + 8 + 8 * prv + 4);
-        const float pp[6] = {z0.x + q0.x * bf, z0.y + q0.y * bf, z0.z + q0.z * bf,
-                             z0.w + q0.w * bf, z1.x + q1.x * bf, z1.y + q1.y * bf};
+        float pp[6];
+        if (slot & kCgOwnRow) {  // one of this CTA's rows: its row state
+          const float* o = CGROW(slot & ~kCgOwnRow);
+#pragma unroll
+          for (int j = 0; j < 6; ++j) pp[j] = o[kCgZ + j] + o[kCgP + 6 * prv + j] * bf;
+        } else {
+          const float* crow = cache + (size_t)slot * kCgCache;
+          const float4 z0 = *reinterpret_cast<const float4*>(crow);
+          const float4 z1 = *reinterpret_cast<const float4*>(crow + 4);
+          const float4 q0 = *reinterpret_cast<const float4*>(crow + 8 + 8 * prv);
+          const float4 q1 = *reinterpret_cast<const float4*>(crow + 8 + 8 * prv + 4);
+          pp[0] = z0.x + q0.x * bf, pp[1] = z0.y + q0.y * bf, pp[2] = z0.z + q0.z * bf;
+          pp[3] = z0.w + q0.w * bf, pp[4] = z1.x + q1.x * bf, pp[5] = z1.y + q1.y * bf;
+        }
         float m[36];
         load_block(kk < ncached ? sS + (size_t)kk * 36 : A.S + (size_t)k * 36, m);
 #pragma unroll
@@ -472,11 +475,11 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       }
       warp_sum8(acc);  // lane 4i holds q_i
       const float qi = __shfl_sync(kFull, acc[0], 4 * ci);
-      const float pi = st[kCgZ + ci] + st[kCgP + 8 * prv + ci] * bf;
+      const float pi = st[kCgZ + ci] + st[kCgP + 6 * prv + ci] * bf;
       __syncwarp();
       if (vl) {
         st[kCgQ + ci] = qi;
-        st[kCgP + 8 * cur + ci] = pi;
+        st[kCgP + 6 * cur + ci] = pi;
       }
       if (vl) dpq += pi * qi;
       cg_push_row(cl, cache, A.sub_ent, (uint32_t)__float_as_int(st[kCgIdx + 4]),
@@ -492,7 +495,6 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       }
       // W^T q of the row for the next coarse vector (the lens row, in no
       // group, has W = 0; its transposed terms arrive after the reduction).
-      if constexpr (kCoarse) cg_row_wtr(sW + (size_t)lr * 42, qi, sTq + (size_t)lr * 8);
       const int32_t lp = __float_as_int(st[kCgIdx + 2]);
       if (lp >= 0) {  // S_cg^T p_c for the lens column
         const int t = lane / 3, j = lane - 3 * (lane / 3);
@@ -513,7 +515,8 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
                          __shfl_sync(kFull, dlens, 2)};
     if constexpr (kCoarse) {
       __syncthreads();
-      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sTq, wall_q);
+      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgQ,
+                         wall_q);
     }
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
     cg_reduce<4>(cl, w4, wsm, inbox[0], tot, [&] {
@@ -545,7 +548,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
       float* st = CGROW(lr);
       float ri = 0.0f;
       if (vl) {
-        st[kCgX + ci] += st[kCgP + 8 * cur + ci] * af;
+        st[kCgX + ci] += st[kCgP + 6 * cur + ci] * af;
         ri = st[kCgR + ci] - st[kCgQ + ci] * af;
         st[kCgR + ci] = ri;
       }
@@ -553,9 +556,8 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
 #pragma unroll
       for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
       if constexpr (kCoarse) {
-        // z = B^-1 r + W c, and W^T r of the row for the next iteration
+        // z = B^-1 r + W c
         zi += cg_row_wc(sW + (size_t)lr * 42, __float_as_int(st[kCgIdx + 3]), scf, ci);
-        cg_row_wtr(sW + (size_t)lr * 42, ri, sT + (size_t)lr * 8);
       }
       if (vl) {
         st[kCgZ + ci] = zi;
@@ -567,7 +569,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     }
     if constexpr (kCoarse) {
       __syncthreads();
-      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sT,
+      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgR,
                          wall_r + (size_t)prv * A.cap_dim);
     }
     const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};

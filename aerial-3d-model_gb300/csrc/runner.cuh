@@ -166,9 +166,10 @@ inline bool plan_cluster(const Context& ctx, const std::vector<uint32_t>& row_pt
 }
 
 // Neighbour caches of the cluster PCG: for each CTA the distinct columns its
-// rows' blocks multiply (the lens row: its diagonal block only), in order of
-// first use; blk_slot[k] = the cache slot of block k's column in its row's
-// CTA; per row the (CTA rank << 16 | slot) entries of the caches that hold
+// rows' blocks multiply (the lens row: its diagonal block only) that other
+// CTAs own, in order of first use; blk_slot[k] = the cache slot of block k's
+// column in its row's CTA, or kCgOwnRow | local row when the CTA owns the
+// column; per row the (CTA rank << 16 | slot) entries of the caches that hold
 // it, which its owner pushes the row's z and p into.
 struct CachePlan {
   std::vector<uint32_t> blk_slot, sub_ptr, sub_ent;
@@ -178,6 +179,7 @@ struct CachePlan {
 inline bool plan_cache(const ClusterPlan& cp, int csize, const std::vector<uint32_t>& row_ptr,
                        const std::vector<uint32_t>& col_idx, const std::vector<uint32_t>& diag_pos,
                        const std::vector<int32_t>& lens_row, int64_t nb, CachePlan& pl) {
+  const std::vector<uint32_t>& row_loc = cp.row_loc;
   pl = CachePlan{};
   pl.blk_slot.assign(std::max<size_t>(col_idx.size(), 1), 0);
   std::vector<std::vector<uint32_t>> subs((size_t)nb);
@@ -193,6 +195,10 @@ inline bool plan_cache(const ClusterPlan& cp, int csize, const std::vector<uint3
       if ((int32_t)r == lens) b0 = diag_pos[r], b1 = b0 + 1;
       for (uint32_t k = b0; k < b1; ++k) {
         const uint32_t c = col_idx[k];
+        if ((row_loc[c] >> 16) == rank) {  // own row: read from the row state
+          pl.blk_slot[k] = kCgOwnRow | (row_loc[c] & 0xffffu);
+          continue;
+        }
         if (stamp[c] != (int64_t)g) {
           stamp[c] = (int64_t)g;
           slot_of[c] = n++;
