@@ -257,28 +257,30 @@ __device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const
   return add;
 }
 
-// Per own group: sum over its rows (in row order) of W^T x, x the row-state
-// vector at float offset `xoff` (thread per group and mode; each row's six
-// products in component order), pushed into the model-wide array `dst` (D
-// floats, at this CTA's groups' offset) of every CTA.
+// Per own group: the sum over its rows of W^T x, x the row-state vector at
+// float offset `xoff`, pushed into the model-wide array `dst` (D floats, at
+// this CTA's groups' offset) of every CTA.  A warp per (group, mode): lane l
+// takes rows l, l + 32, ... (each row's six products in component order),
+// then a fixed butterfly.
 __device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int32_t ngr,
                                                    const int32_t* grp_row0,
                                                    const int32_t* grp_row1, int32_t g0,
                                                    int32_t goff, uint32_t row0, const float* sW,
                                                    const float* rs, int xoff, float* dst) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int csize = (int)cl.num_blocks();
-  for (int o = threadIdx.x; o < ngr * kCoarseModes; o += kCgThreads) {
+  for (int o = warp; o < ngr * kCoarseModes; o += kCgWarps) {
     const int l = o / kCoarseModes, j = o % kCoarseModes;
     float v = 0.0f;
-    for (int32_t r = grp_row0[g0 + l]; r < grp_row1[g0 + l]; ++r) {
+    for (int32_t r = grp_row0[g0 + l] + lane; r < grp_row1[g0 + l]; r += 32) {
       const float* w = sW + (size_t)(r - row0) * 42 + j;
       const float* x = rs + (size_t)(r - row0) * kCgRow + xoff;
-      float t = 0.0f;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) t += w[kCoarseModes * i] * x[i];
-      v += t;
+      for (int i = 0; i < 6; ++i) v += w[kCoarseModes * i] * x[i];
     }
-    for (int k = 0; k < csize; ++k) cl.map_shared_rank(dst, (unsigned)k)[goff + o] = v;
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
+    if (lane < csize) cl.map_shared_rank(dst, (unsigned)lane)[goff + o] = v;
   }
 }
 

@@ -166,11 +166,12 @@ inline bool plan_cluster(const Context& ctx, const std::vector<uint32_t>& row_pt
 }
 
 // Neighbour caches of the cluster PCG: for each CTA the distinct columns its
-// rows' blocks multiply (the lens row: its diagonal block only) that other
-// CTAs own, in order of first use; blk_slot[k] = the cache slot of block k's
-// column in its row's CTA, or kCgOwnRow | local row when the CTA owns the
-// column; per row the (CTA rank << 16 | slot) entries of the caches that hold
-// it, which its owner pushes the row's z and p into.
+// rows' blocks multiply (the lens row: its diagonal block only), in order of
+// first use; blk_slot[k] = the cache slot of block k's column in its row's
+// CTA; per row the (CTA rank << 16 | slot) entries of the caches that hold
+// it, which its owner pushes the row's z and p into.  With own_rows false the
+// CTA's own columns are not cached (blk_slot = kCgOwnRow | local row: read
+// from the row state), for models whose row state leaves little room.
 struct CachePlan {
   std::vector<uint32_t> blk_slot, sub_ptr, sub_ent;
   uint32_t cap = 0;
@@ -178,7 +179,8 @@ struct CachePlan {
 
 inline bool plan_cache(const ClusterPlan& cp, int csize, const std::vector<uint32_t>& row_ptr,
                        const std::vector<uint32_t>& col_idx, const std::vector<uint32_t>& diag_pos,
-                       const std::vector<int32_t>& lens_row, int64_t nb, CachePlan& pl) {
+                       const std::vector<int32_t>& lens_row, int64_t nb, bool own_rows,
+                       CachePlan& pl) {
   const std::vector<uint32_t>& row_loc = cp.row_loc;
   pl = CachePlan{};
   pl.blk_slot.assign(std::max<size_t>(col_idx.size(), 1), 0);
@@ -195,7 +197,7 @@ inline bool plan_cache(const ClusterPlan& cp, int csize, const std::vector<uint3
       if ((int32_t)r == lens) b0 = diag_pos[r], b1 = b0 + 1;
       for (uint32_t k = b0; k < b1; ++k) {
         const uint32_t c = col_idx[k];
-        if ((row_loc[c] >> 16) == rank) {  // own row: read from the row state
+        if (!own_rows && (row_loc[c] >> 16) == rank) {  // own row: from the row state
           pl.blk_slot[k] = kCgOwnRow | (row_loc[c] & 0xffffu);
           continue;
         }
@@ -757,12 +759,25 @@ struct LmEngine {
                             cudaMemcpyDeviceToHost, s), "d2h");
       check(cudaStreamSynchronize(s), "sync");
     }
+    // Own rows in the cache too (vector loads, uniform reads) when it fits,
+    // else from the row state.
     detail::CachePlan kp;
-    if (!detail::plan_cache(cp, csize, SB.h_row_ptr, h_col_idx, h_diag_pos, h_lens, ctx.nb, kp))
-      return unusable("a CTA's neighbour cache exceeds 65,535 rows");
     const size_t row_bytes = (size_t)cp.max_rows * kCgRow * 4;
+    bool fits = false;
+    for (bool own : {true, false}) {
+      if (!detail::plan_cache(cp, csize, SB.h_row_ptr, h_col_idx, h_diag_pos, h_lens, ctx.nb, own,
+                              kp))
+        return unusable("a CTA's neighbour cache exceeds 65,535 rows");
+      // leave room for a quarter of the S blocks, or all of them
+      const size_t need = row_bytes + coarse_bytes + (size_t)kp.cap * kCgCache * 4 +
+                          std::min<size_t>(cp.max_blocks / 4 + 1, cp.max_blocks) * (36 * 4 + 4);
+      if (need < avail) {
+        fits = true;
+        break;
+      }
+    }
     const size_t cache_bytes = (size_t)kp.cap * kCgCache * 4;
-    if (row_bytes + coarse_bytes + cache_bytes >= avail)
+    if (!fits || row_bytes + coarse_bytes + cache_bytes >= avail)
       return unusable("row state and neighbour cache do not fit");
     const uint32_t cap_blocks = (uint32_t)std::min<size_t>(
         cp.max_blocks, (avail - row_bytes - coarse_bytes - cache_bytes) / (36 * 4 + 4));

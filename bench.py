@@ -668,10 +668,13 @@ def main():
     ap.add_argument("--stage", default="ba",
                     choices=["ba", "triangulate", "ransac", "pair_fits", "summary"])
     ap.add_argument("--matrix-free", action="store_true",
-                    help="mixed form: matrix-free PCG (S p from per-observation factors)")
+                    help="mixed form: S-free PCG (S p from per-observation factors)")
+    ap.add_argument("--mixed-patience", type=int, default=MIXED_STOP_PATIENCE,
+                    help="mixed forms: consecutive small decreases before stopping")
     args = ap.parse_args()
-    global MIXED_MATRIX_FREE
+    global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE
     MIXED_MATRIX_FREE = args.matrix_free
+    MIXED_STOP_PATIENCE = args.mixed_patience
     ws, rank = dist_env()
     if args.stage != "ba":
         out = stage_arm(args, ws, rank)
