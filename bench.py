@@ -669,12 +669,13 @@ def main():
                     choices=["ba", "triangulate", "ransac", "pair_fits", "summary"])
     ap.add_argument("--matrix-free", action="store_true",
                     help="mixed form: S-free PCG (S p from per-observation factors)")
-    ap.add_argument("--mixed-patience", type=int, default=MIXED_STOP_PATIENCE,
-                    help="mixed forms: consecutive small decreases before stopping")
+    ap.add_argument("--mixed-patience", type=int, default=0,
+                    help="mixed forms: consecutive small decreases before stopping (0: default)")
     args = ap.parse_args()
     global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE
     MIXED_MATRIX_FREE = args.matrix_free
-    MIXED_STOP_PATIENCE = args.mixed_patience
+    if args.mixed_patience > 0:
+        MIXED_STOP_PATIENCE = args.mixed_patience
     ws, rank = dist_env()
     if args.stage != "ba":
         out = stage_arm(args, ws, rank)
