@@ -761,23 +761,21 @@ struct LmEngine {
     }
     // Own rows in the cache too (vector loads, uniform reads) when it fits,
     // else from the row state.
+    // Own rows in the cache too (vector loads) when that leaves room for a
+    // quarter of the S blocks; else only other CTAs' rows (S blocks that do
+    // not fit are read from L2).
     detail::CachePlan kp;
     const size_t row_bytes = (size_t)cp.max_rows * kCgRow * 4;
-    bool fits = false;
-    for (bool own : {true, false}) {
-      if (!detail::plan_cache(cp, csize, SB.h_row_ptr, h_col_idx, h_diag_pos, h_lens, ctx.nb, own,
-                              kp))
-        return unusable("a CTA's neighbour cache exceeds 65,535 rows");
-      // leave room for a quarter of the S blocks, or all of them
-      const size_t need = row_bytes + coarse_bytes + (size_t)kp.cap * kCgCache * 4 +
-                          std::min<size_t>(cp.max_blocks / 4 + 1, cp.max_blocks) * (36 * 4 + 4);
-      if (need < avail) {
-        fits = true;
-        break;
-      }
-    }
+    if (!detail::plan_cache(cp, csize, SB.h_row_ptr, h_col_idx, h_diag_pos, h_lens, ctx.nb, true,
+                            kp))
+      return unusable("a CTA's neighbour cache exceeds 65,535 rows");
+    if (row_bytes + coarse_bytes + (size_t)kp.cap * kCgCache * 4 +
+            (size_t)(cp.max_blocks / 4 + 1) * (36 * 4 + 4) >= avail &&
+        !detail::plan_cache(cp, csize, SB.h_row_ptr, h_col_idx, h_diag_pos, h_lens, ctx.nb, false,
+                            kp))
+      return unusable("a CTA's neighbour cache exceeds 65,535 rows");
     const size_t cache_bytes = (size_t)kp.cap * kCgCache * 4;
-    if (!fits || row_bytes + coarse_bytes + cache_bytes >= avail)
+    if (row_bytes + coarse_bytes + cache_bytes >= avail)
       return unusable("row state and neighbour cache do not fit");
     const uint32_t cap_blocks = (uint32_t)std::min<size_t>(
         cp.max_blocks, (avail - row_bytes - coarse_bytes - cache_bytes) / (36 * 4 + 4));
