@@ -17,14 +17,12 @@
 //
 // E is assembled per group of rows in a fixed order, Jacobi-scaled (its
 // condition then is about 1e4 on the surveys measured, from about 1e8) and
-// inverted in FP32 by Gauss-Jordan in one CTA's shared memory; the inverse
-// is symmetrised and applied in FP32 inside the cluster PCG kernel.
+// inverted in FP32 by Gauss-Jordan in the registers of one CTA per model; the
+// inverse is symmetrised and applied in FP32 inside the cluster PCG kernel.
 #pragma once
 
 #include "ba_common.cuh"
 #include "lm_kernels.cuh"
-
-#include <cooperative_groups.h>
 
 namespace ba {
 
@@ -199,181 +197,247 @@ static __global__ void coarse_sum_kernel(CoarseArgs A, const int64_t* row_pair0,
   }
 }
 
-// E^-1 per model, one thread-block cluster of kInvCl CTAs per model: Jacobi
-// scaling, then in-place block Gauss-Jordan without pivoting (E is symmetric
-// positive definite), four pivots per step.  The matrix, padded with identity
-// to Dq = a multiple of 32 (<= 192), is split into kInvCl column slabs of
-// W = Dq / kInvCl columns, one per CTA, held in registers (a thread holds 3
-// rows x 3 columns).  Per step the CTA owning the four pivot columns
-// publishes them and the inverse of the 4 x 4 pivot block (a scalar pivot
-// below 1e-6 of the scaled unit diagonal is raised to 1e-6) in double-
-// buffered shared memory; after one cluster barrier every CTA copies them
-// through distributed shared memory and updates its slab:
+// E^-1 per model, one CTA of kInvThreads threads per model: Jacobi scaling,
+// then in-place block Gauss-Jordan without pivoting (E is symmetric positive
+// definite), four pivots per step.  E is staged in shared memory and there
+// symmetrised, scaled and padded with identity to Dq = a multiple of 32
+// (<= 192); the matrix then lives in registers: thread t holds the 12 x 12
+// tile at rows 12 (t / 16), columns 12 (t % 16), rows 2 p and 2 p + 1 of a
+// column in one 64-bit register pair, so that the update runs on packed FP32
+// FMAs (fma.rn.f32x2: two round-to-nearest FP32 FMAs, the results of two
+// fmaf).  Per step the threads holding the four pivot columns, then the four
+// pivot rows, copy them to shared memory and zero them in the tile; a thread
+// per column then inverts the 4 x 4 pivot block (a scalar pivot below 1e-6 of
+// the scaled unit diagonal is raised to 1e-6) and forms that column of the new
+// pivot rows rn; every thread then updates its tile, a <- a + cn . rn, with
+// cn = -(pivot columns) but e_y on pivot row y:
 //   pivot rows        <- Pinv * (pivot rows)   (Pinv itself in the pivot columns)
 //   pivot columns     <- -(pivot columns) * Pinv
 //   everything else  -= (pivot columns) * Pinv * (pivot rows).
-// The result is unscaled and symmetrised.
-constexpr int kInvCl = 8;
-constexpr int kInvClThreads = 512;
+// The shared pivot rows and columns alternate between two buffers, so a step
+// takes two barriers.  The result is unscaled and symmetrised.
+constexpr int kInvThreads = 256;
+constexpr int kInvTile = 12;  // rows and columns of a thread's tile
+constexpr int kInvPairs = kInvTile / 2;
 constexpr int kInvMaxPad = 192;  // kCoarseMaxDim rounded up to a multiple of 32
-static_assert(kInvMaxPad >= kCoarseMaxDim && kInvMaxPad % 32 == 0, "slab layout");
-static_assert(kInvMaxPad / kInvCl <= 24 && kInvClThreads == 64 * 8, "3 x 3 elements a thread");
+static_assert(kInvMaxPad >= kCoarseMaxDim && kInvMaxPad % 32 == 0, "padding");
+static_assert((kInvThreads / 16) * kInvTile == kInvMaxPad && 16 * kInvTile == kInvMaxPad,
+              "12 x 12 tiles cover the padded matrix");
+static_assert(kInvTile % 4 == 0, "pivot groups of four lie inside one tile");
+static_assert(kInvThreads >= kInvMaxPad, "a thread per column of the pivot rows");
+// E staged whole in dynamic shared memory; the even pitch keeps a row pair of
+// one column 8-byte aligned.
+constexpr int kInvPitch = kInvMaxPad + 2;
+constexpr size_t kInvSmemBytes = (size_t)kInvMaxPad * kInvPitch * sizeof(float);
+// Column j of the new pivot rows sits at j + j / 12: the 16 threads of a tile
+// row read columns 12 k + c, which then fall in 16 different bank quads
+// (13 k + c mod 8 differs for any 8 consecutive k).
+__device__ __forceinline__ int inv_rn_slot(int j) { return j + j / kInvTile; }
+constexpr int kInvRnSlots = kInvMaxPad + kInvMaxPad / kInvTile;
 
-static __global__ void __cluster_dims__(kInvCl, 1, 1) __launch_bounds__(kInvClThreads, 1)
-    coarse_invert_kernel(CoarseArgs A) {
-  namespace cgi = cooperative_groups;
-  cgi::cluster_group cl = cgi::this_cluster();
-  __shared__ float dsc[kInvMaxPad];
-  __shared__ __align__(16) float colP[2][kInvMaxPad][4];  // published pivot columns
-  __shared__ float pinvP[2][4][4];                        // published pivot-block inverse
-  __shared__ __align__(16) float colL[kInvMaxPad][4];     // this step's copies
-  __shared__ float pinvL[4][4];
-  __shared__ float rowL[4][kInvMaxPad / kInvCl];          // this slab's part of the pivot rows
-  const int q = (int)cl.block_rank();
-  const int m = blockIdx.x / kInvCl;  // uniform over the cluster
-  if (!A.active[m]) return;
-  const int D = kCoarseModes * (A.model_g0[m + 1] - A.model_g0[m]);
-  if (D == 0) return;
-  const int Dq = ((D + 31) / 32) * 32, W = Dq / kInvCl;
-  const int t = threadIdx.x, r0 = (t >> 3) * 3, c0 = (t & 7) * 3;
-  float* Em = A.E + A.model_eoff[m];
-  for (int i = t; i < kInvMaxPad; i += kInvClThreads) {
-    const float d = i < D ? Em[(size_t)i * D + i] : 0.0f;
-    dsc[i] = d > 0.0f ? rsqrtf(d) : 0.0f;
-  }
-  __syncthreads();
-  float a[3][3];
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+// acc <- x * y + acc, elementwise on two FP32 lanes, each rounded once.
+__device__ __forceinline__ void f2_fma(uint64_t& acc, uint64_t x, uint64_t y) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(x), "l"(y));
+}
+
+// Inverse of the 4 x 4 pivot block pb (scalar Gauss-Jordan, in place).
+__device__ __forceinline__ void inv4_pivot(float (&pb)[4][4]) {
 #pragma unroll
-  for (int r = 0; r < 3; ++r)
+  for (int kk = 0; kk < 4; ++kk) {
+    const float rp = 1.0f / fmaxf(pb[kk][kk], 1e-6f);
+    float rk[4], ck[4];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int i = r0 + r, jl = c0 + c, j = q * W + jl;
-      float v = 0.0f;
-      if (i < Dq && jl < W) {
-        if (i >= D || j >= D || dsc[i] == 0.0f || dsc[j] == 0.0f)
-          v = i == j ? 1.0f : 0.0f;
-        else  // symmetrise the assembled E while scaling
-          v = 0.5f * (Em[(size_t)i * D + j] + Em[(size_t)j * D + i]) * dsc[i] * dsc[j];
-      }
-      a[r][c] = v;
-    }
-  for (int k0 = 0, step = 0; k0 < Dq; k0 += 4, ++step) {
-    const int buf = step & 1;
-    const int owner = k0 / W, kl = k0 - owner * W;  // W is a multiple of 4
-    __syncthreads();  // the previous step's reads of rowL, colL and pinvL are done
+    for (int y = 0; y < 4; ++y) rk[y] = y == kk ? rp : pb[kk][y] * rp;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const int y = r0 + r - k0;
-      if (y >= 0 && y < 4)
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          if (c0 + c < W) rowL[y][c0 + c] = a[r][c];
-    }
-    if (q == owner) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int x = c0 + c - kl;
-        if (x >= 0 && x < 4)
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-            if (r0 + r < Dq) colP[buf][r0 + r][x] = a[r][c];
-      }
-      __syncthreads();
-      if (t == 0) {  // inverse of the 4 x 4 pivot block (scalar Gauss-Jordan)
-        float pb[4][4];
-#pragma unroll
-        for (int x = 0; x < 4; ++x)
-#pragma unroll
-          for (int y = 0; y < 4; ++y) pb[x][y] = colP[buf][k0 + x][y];
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const float rp = 1.0f / fmaxf(pb[kk][kk], 1e-6f);
-          float rk[4], ck[4];
-#pragma unroll
-          for (int y = 0; y < 4; ++y) rk[y] = y == kk ? rp : pb[kk][y] * rp;
-#pragma unroll
-          for (int x = 0; x < 4; ++x) ck[x] = pb[x][kk];
-#pragma unroll
-          for (int x = 0; x < 4; ++x)
-#pragma unroll
-            for (int y = 0; y < 4; ++y)
-              pb[x][y] = x == kk ? rk[y] : (y == kk ? -ck[x] * rp : pb[x][y] - ck[x] * rk[y]);
-        }
-#pragma unroll
-        for (int x = 0; x < 4; ++x)
-#pragma unroll
-          for (int y = 0; y < 4; ++y) pinvP[buf][x][y] = pb[x][y];
-      }
-    }
-    cl.sync();  // the owner's pivot columns and Pinv, and every slab's pivot rows
-    {
-      const float* srcC = cl.map_shared_rank(&colP[buf][0][0], (unsigned)owner);
-      const float* srcP = cl.map_shared_rank(&pinvP[buf][0][0], (unsigned)owner);
-      for (int u = t; u < Dq * 4; u += kInvClThreads) (&colL[0][0])[u] = srcC[u];
-      if (t < 16) (&pinvL[0][0])[t] = srcP[t];
-    }
-    __syncthreads();
-    float rn[4][3];  // Pinv * (pivot rows) for this thread's columns
+    for (int x = 0; x < 4; ++x) ck[x] = pb[x][kk];
 #pragma unroll
     for (int x = 0; x < 4; ++x)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int jl = c0 + c < W ? c0 + c : 0;
-        float v = 0.0f;
-#pragma unroll
-        for (int y = 0; y < 4; ++y) v += pinvL[x][y] * rowL[y][jl];
-        rn[x][c] = v;
-      }
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const int i = r0 + r, y = i - k0;
-      const float4 cv = *reinterpret_cast<const float4*>(&colL[i < Dq ? i : 0][0]);
-      const bool prow = y >= 0 && y < 4;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int x = c0 + c - kl;
-        const bool pcol = q == owner && x >= 0 && x < 4;
-        if (prow) {
-          a[r][c] = pcol ? pinvL[y][x] : rn[y][c];
-        } else if (pcol) {
-          float w = 0.0f;
-          w += cv.x * pinvL[0][x];
-          w += cv.y * pinvL[1][x];
-          w += cv.z * pinvL[2][x];
-          w += cv.w * pinvL[3][x];
-          a[r][c] = -w;
-        } else {
-          float v = a[r][c];
-          v -= cv.x * rn[0][c];
-          v -= cv.y * rn[1][c];
-          v -= cv.z * rn[2][c];
-          v -= cv.w * rn[3][c];
-          a[r][c] = v;
-        }
-      }
-    }
+      for (int y = 0; y < 4; ++y)
+        pb[x][y] = x == kk ? rk[y] : (y == kk ? -ck[x] * rp : pb[x][y] - ck[x] * rk[y]);
   }
-  // Unscale into E (no longer needed), then symmetrise into E^-1 once every
-  // slab is written.
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int i = r0 + r, jl = c0 + c, j = q * W + jl;
-      if (i < D && jl < W && j < D) Em[(size_t)i * D + j] = a[r][c] * dsc[i] * dsc[j];
-    }
-  __threadfence();
-  cl.sync();
-  float* Im = A.Einv + A.model_eoff[m];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int i = r0 + r, jl = c0 + c, j = q * W + jl;
-      if (i < D && jl < W && j < D)
-        Im[(size_t)i * D + j] = 0.5f * (Em[(size_t)i * D + j] + Em[(size_t)j * D + i]);
-    }
 }
 
+static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(CoarseArgs A) {
+  __shared__ float dsc[kInvMaxPad];
+  __shared__ float4 colS[2][kInvMaxPad];                  // pivot columns, a row each
+  __shared__ __align__(16) float rowS[2][4][kInvMaxPad];  // pivot rows
+  __shared__ ulonglong2 rnA[2][kInvRnSlots];  // new pivot rows per column: (x, x), (y, y)
+  __shared__ ulonglong2 rnB[2][kInvRnSlots];  //                            (z, z), (w, w)
+  __shared__ __align__(16) float cnS[2][4][kInvMaxPad];   // cn, by component
+  extern __shared__ __align__(16) float smE[];            // [kInvMaxPad][kInvPitch]
+  const int m = blockIdx.x;
+  if (!A.active[m]) return;
+  const int D = kCoarseModes * (A.model_g0[m + 1] - A.model_g0[m]);
+  if (D == 0) return;
+  const int Dq = ((D + 31) / 32) * 32;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int r0 = (t >> 4) * kInvTile, c0 = (t & 15) * kInvTile;
+  const float* Em = A.E + A.model_eoff[m];
+  // Asynchronous 4-byte copies: every load in flight at once, none through
+  // registers (E was just written and is read once).
+  for (int i = wid; i < D; i += kInvThreads / 32)
+    for (int j = lane; j < D; j += 32) {
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(smE + i * kInvPitch + j);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst),
+                   "l"(Em + (size_t)i * D + j)
+                   : "memory");
+    }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+  for (int i = t; i < kInvMaxPad; i += kInvThreads) {
+    const float d = i < D ? smE[i * kInvPitch + i] : 0.0f;
+    dsc[i] = d > 0.0f ? rsqrtf(d) : 0.0f;
+  }
+  __syncthreads();
+  // Symmetrise, scale and pad in place, a thread per pair {(i, j), (j, i)}.
+  for (int i = wid; i < kInvMaxPad; i += kInvThreads / 32)
+    for (int j = lane; j <= i; j += 32) {
+      float vij = (i == j && i < Dq) ? 1.0f : 0.0f, vji = vij;
+      if (i < D && dsc[i] != 0.0f && dsc[j] != 0.0f) {
+        const float h = 0.5f * (smE[i * kInvPitch + j] + smE[j * kInvPitch + i]);
+        vij = h * dsc[i] * dsc[j];
+        vji = h * dsc[j] * dsc[i];
+      }
+      smE[i * kInvPitch + j] = vij;
+      smE[j * kInvPitch + i] = vji;
+    }
+  __syncthreads();
+  // The tile, read down the columns of the symmetric matrix: rows (2 p, 2 p + 1)
+  // of column c are entries (2 p, 2 p + 1) of row c.
+  uint64_t a2[kInvPairs][kInvTile];
+#pragma unroll
+  for (int p = 0; p < kInvPairs; ++p)
+#pragma unroll
+    for (int c = 0; c < kInvTile; ++c)
+      a2[p][c] = *reinterpret_cast<const uint64_t*>(&smE[(c0 + c) * kInvPitch + r0 + 2 * p]);
+  const bool live = r0 < Dq && c0 < Dq;  // tiles beyond the padded size hold nothing
+  // Buffer b of step k is rewritten at step k + 2, after its barriers, which
+  // every thread reaches only once done with step k + 1, hence with step k.
+  for (int k0 = 0, b = 0; k0 < Dq; k0 += 4, b ^= 1) {
+    if (live) {
+      // Pivot columns: the tile's columns 4 g .. 4 g + 3 when c0 + 4 g = k0.
+#pragma unroll
+      for (int g = 0; g < kInvTile / 4; ++g)
+        if (c0 + 4 * g == k0) {
+#pragma unroll
+          for (int p = 0; p < kInvPairs; ++p) {
+            float l[4], h[4];
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+              f2_unpack(a2[p][4 * g + x], l[x], h[x]);
+              a2[p][4 * g + x] = 0ull;
+            }
+            colS[b][r0 + 2 * p] = make_float4(l[0], l[1], l[2], l[3]);
+            colS[b][r0 + 2 * p + 1] = make_float4(h[0], h[1], h[2], h[3]);
+          }
+        }
+      // Pivot rows: the tile's rows 4 g .. 4 g + 3 (pairs 2 g, 2 g + 1) when
+      // r0 + 4 g = k0.  Their entries in the pivot columns are not read.
+#pragma unroll
+      for (int g = 0; g < kInvTile / 4; ++g)
+        if (r0 + 4 * g == k0) {
+#pragma unroll
+          for (int q = 0; q < 2; ++q)
+#pragma unroll
+            for (int c = 0; c < kInvTile; c += 4) {
+              float l[4], h[4];
+#pragma unroll
+              for (int x = 0; x < 4; ++x) {
+                f2_unpack(a2[2 * g + q][c + x], l[x], h[x]);
+                a2[2 * g + q][c + x] = 0ull;
+              }
+              *reinterpret_cast<float4*>(&rowS[b][2 * q][c0 + c]) = make_float4(l[0], l[1], l[2], l[3]);
+              *reinterpret_cast<float4*>(&rowS[b][2 * q + 1][c0 + c]) = make_float4(h[0], h[1], h[2], h[3]);
+            }
+        }
+    }
+    __syncthreads();
+    // Column t of the new pivot rows: Pinv * (pivot rows) at t, or the pivot
+    // block's own column of Pinv; and row t of cn.  Every such thread inverts
+    // the 4 x 4 pivot block itself (cheaper than another barrier).
+    if (t < Dq) {
+      float pb[4][4];
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y) pb[x][y] = reinterpret_cast<const float*>(&colS[b][k0 + x])[y];
+      inv4_pivot(pb);
+      const int x = t - k0;
+      float4 rv, cn;
+      if (x >= 0 && x < 4) {
+        rv.x = x == 0 ? pb[0][0] : x == 1 ? pb[0][1] : x == 2 ? pb[0][2] : pb[0][3];
+        rv.y = x == 0 ? pb[1][0] : x == 1 ? pb[1][1] : x == 2 ? pb[1][2] : pb[1][3];
+        rv.z = x == 0 ? pb[2][0] : x == 1 ? pb[2][1] : x == 2 ? pb[2][2] : pb[2][3];
+        rv.w = x == 0 ? pb[3][0] : x == 1 ? pb[3][1] : x == 2 ? pb[3][2] : pb[3][3];
+        cn = make_float4(x == 0 ? 1.0f : 0.0f, x == 1 ? 1.0f : 0.0f, x == 2 ? 1.0f : 0.0f,
+                         x == 3 ? 1.0f : 0.0f);
+      } else {
+        const float q0 = rowS[b][0][t], q1 = rowS[b][1][t], q2 = rowS[b][2][t], q3 = rowS[b][3][t];
+        rv.x = pb[0][0] * q0 + pb[0][1] * q1 + pb[0][2] * q2 + pb[0][3] * q3;
+        rv.y = pb[1][0] * q0 + pb[1][1] * q1 + pb[1][2] * q2 + pb[1][3] * q3;
+        rv.z = pb[2][0] * q0 + pb[2][1] * q1 + pb[2][2] * q2 + pb[2][3] * q3;
+        rv.w = pb[3][0] * q0 + pb[3][1] * q1 + pb[3][2] * q2 + pb[3][3] * q3;
+        const float4 cv = colS[b][t];
+        cn = make_float4(-cv.x, -cv.y, -cv.z, -cv.w);
+      }
+      const int sl = inv_rn_slot(t);
+      rnA[b][sl] = make_ulonglong2(f2_pack(rv.x, rv.x), f2_pack(rv.y, rv.y));
+      rnB[b][sl] = make_ulonglong2(f2_pack(rv.z, rv.z), f2_pack(rv.w, rv.w));
+      cnS[b][0][t] = cn.x, cnS[b][1][t] = cn.y, cnS[b][2][t] = cn.z, cnS[b][3][t] = cn.w;
+    } else if (t < kInvMaxPad) {  // columns past Dq inside the last tiles
+      const int sl = inv_rn_slot(t);
+      rnA[b][sl] = make_ulonglong2(0ull, 0ull);
+      rnB[b][sl] = make_ulonglong2(0ull, 0ull);
+      cnS[b][0][t] = 0.0f, cnS[b][1][t] = 0.0f, cnS[b][2][t] = 0.0f, cnS[b][3][t] = 0.0f;
+    }
+    __syncthreads();
+    if (!live) continue;
+    // a <- a + cn . rn: the tile's cn row pairs stay in registers across its
+    // columns; four passes over the row pairs keep consecutive FMAs apart.
+    uint64_t cnp[kInvPairs][4];
+#pragma unroll
+    for (int p = 0; p < kInvPairs; ++p)
+#pragma unroll
+      for (int y = 0; y < 4; ++y) cnp[p][y] = *reinterpret_cast<const uint64_t*>(&cnS[b][y][r0 + 2 * p]);
+#pragma unroll
+    for (int c = 0; c < kInvTile; ++c) {
+      const int sl = inv_rn_slot(c0 + c);
+      const ulonglong2 ra = rnA[b][sl], rb = rnB[b][sl];
+#pragma unroll
+      for (int p = 0; p < kInvPairs; ++p) f2_fma(a2[p][c], cnp[p][0], ra.x);
+#pragma unroll
+      for (int p = 0; p < kInvPairs; ++p) f2_fma(a2[p][c], cnp[p][1], ra.y);
+#pragma unroll
+      for (int p = 0; p < kInvPairs; ++p) f2_fma(a2[p][c], cnp[p][2], rb.x);
+#pragma unroll
+      for (int p = 0; p < kInvPairs; ++p) f2_fma(a2[p][c], cnp[p][3], rb.y);
+    }
+  }
+  // The tile back to shared memory, transposed as it was read (the prologue's
+  // reads of it ended at the first step's barriers); then unscale and
+  // symmetrise into E^-1: smE[j][i] holds entry (i, j).
+#pragma unroll
+  for (int p = 0; p < kInvPairs; ++p)
+#pragma unroll
+    for (int c = 0; c < kInvTile; ++c)
+      *reinterpret_cast<uint64_t*>(&smE[(c0 + c) * kInvPitch + r0 + 2 * p]) = a2[p][c];
+  __syncthreads();
+  float* Im = A.Einv + A.model_eoff[m];
+  for (int i = wid; i < D; i += kInvThreads / 32)
+    for (int j = lane; j < D; j += 32) {
+      const float xij = smE[j * kInvPitch + i] * dsc[i] * dsc[j];
+      const float xji = smE[i * kInvPitch + j] * dsc[j] * dsc[i];
+      Im[(size_t)i * D + j] = 0.5f * (xij + xji);
+    }
+}
 
 }  // namespace ba

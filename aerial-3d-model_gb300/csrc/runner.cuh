@@ -1059,7 +1059,10 @@ struct LmEngine {
               SV, c_S64.p, cargs, c_npairs, c_pair_row, c_pair_grp, c_P));
         BA_LAUNCH(coarse_sum_kernel<<<dim3((unsigned)c_ngroups, 6), 224, 0, s>>>(cargs, c_row_pair0,
                                                                             c_P));
-        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)(ctx.nm * kInvCl), kInvClThreads, 0, s>>>(
+        check(cudaFuncSetAttribute(coarse_invert_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInvSmemBytes),
+              "coarse inverse shared memory");
+        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, kInvSmemBytes, s>>>(
             cargs));
       }
       cudaLaunchConfig_t cfg{};
