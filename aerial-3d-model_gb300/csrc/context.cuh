@@ -111,6 +111,8 @@ struct Opts {
   int32_t graph = 1;       // capture each LM iteration as a CUDA graph
   int32_t autotune = 0;    // tune the PCG configuration before solving
   int32_t stop_patience = 0;  // 0 or 1: the reference's stop rule
+  int32_t pcg_end_max_iter = 0;  // PCG cap once a step's relative decrease < pcg_end_rel (0: off)
+  double pcg_end_rel = 1e-5;
   int32_t coarse = 0;         // mixed cluster PCG: two-level preconditioner
   int32_t hold_cta = 0;       // fault injection: grid PCG CTA hold_cta-1 skips its exchanges
   long long wait_limit = kSpinCycles;  // spin limit of device-side waits (cycles)

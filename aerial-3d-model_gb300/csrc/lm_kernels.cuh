@@ -1281,6 +1281,9 @@ static __global__ void control_kernel(int64_t nm, Control C) {
     } else {
       C.small[m] = 0;
     }
+    // Inexact-Newton forcing (Eisenstat and Walker, SIAM J. Sci. Comput. 17,
+    // 1996): the inner solves tighten as the outer iteration converges.
+    if (C.end_cap > 0 && rel < C.end_rel) C.pcg_cap[m] = C.end_cap;
   } else {
     C.lambda[m] = lam * 5.0;
     if (C.lambda[m] > 1e6) act = 0;

@@ -69,6 +69,7 @@ struct PcgArgs {
   unsigned* err;
   long long spin;    // spin limit of a group wait, in SM clock cycles
   int32_t hold_cta;  // fault injection: CTA hold_cta - 1 leaves before its first exchange (0: off)
+  const int32_t* cap = nullptr;  // [nm] or null: per-model iteration cap (below max_iter)
 };
 
 // Partial-sum slots.  Grid kernel: 0,1 init (rz, bb) | 2..5 (pq, lens q
@@ -346,7 +347,8 @@ __device__ bool pcg_job(const PcgArgs<R>& A, const PcgJob& J, double* wsm, doubl
       }))
     return false;
   int32_t spmv = 0;
-  for (int32_t it = 0; it < A.max_iter; ++it) {
+  const int32_t max_it = A.cap ? min(A.max_iter, A.cap[J.model]) : A.max_iter;
+  for (int32_t it = 0; it < max_it; ++it) {
     R* pcur = A.p2 + (size_t)(it & 1) * 6 * A.nb;
     const R* pprev = A.p2 + (size_t)((it + 1) & 1) * 6 * A.nb;
     const R beta = sc.beta_r;

@@ -95,6 +95,7 @@ struct CgArgs {
   const uint32_t* sub_ptr;   // [nb + 1]
   const uint32_t* sub_ent;
   uint32_t cap_cache;        // cache slots per CTA
+  const int32_t* cap = nullptr;  // [nm] or null: per-model iteration cap (below max_iter)
 };
 
 inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks, uint32_t cap_cache) {
@@ -439,7 +440,8 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     cl.sync();  // z of iteration 0 in every cache
   }
   int32_t spmv = 0;
-  for (int32_t it = 0; it < A.max_iter; ++it) {
+  const int32_t max_it = A.cap ? min(A.max_iter, A.cap[J.model]) : A.max_iter;
+  for (int32_t it = 0; it < max_it; ++it) {
     const int cur = it & 1, prv = cur ^ 1;
     const float bf = sc.bf;
     float dpq = 0.0f, dlens = 0.0f;

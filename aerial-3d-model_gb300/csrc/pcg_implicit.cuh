@@ -54,6 +54,7 @@ struct ImpArgs {
   int32_t max_iter;
   double tol;
   long long spin;  // spin limit of a group wait, in SM clock cycles
+  const int32_t* cap = nullptr;  // [1] or null: iteration cap of the model (below max_iter)
 };
 
 // Implicit-product scalars, computed once per CTA by thread 0.
@@ -108,7 +109,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
       }))
     return;
   int32_t spmv = 0;
-  for (int32_t it = 0; it < A.max_iter; ++it) {
+  const int32_t max_it = A.cap ? min(A.max_iter, A.cap[0]) : A.max_iter;
+  for (int32_t it = 0; it < max_it; ++it) {
     R* pcur = A.p2 + (size_t)(it & 1) * 6 * A.nb;
     const R* pprev = A.p2 + (size_t)((it + 1) & 1) * 6 * A.nb;
     const R br = sc.beta_r;

@@ -450,10 +450,11 @@ struct LmEngine {
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
   DevBuf<int64_t> n_front, pcg_total;
-  DevBuf<int32_t> active, accepted, iters, pcg_iters, any, small;
+  DevBuf<int32_t> active, accepted, iters, pcg_iters, any, small, pcg_cap;
   DevBuf<double> log_cost, log_lam;
   DevBuf<int32_t> log_pcg, log_acc;
   int32_t log_cap = 0;
+  int32_t pcg_limit = 0;  // PCG launch limit: the larger of the two caps
   Control C{};
   detail::PcgPlan plan;
   DevBuf<PcgJob> jobs;
@@ -576,10 +577,20 @@ struct LmEngine {
     }
     small.alloc(nm, s);
     small.zero();
+    // PCG iteration cap per model: pcg_max_iter, raised to pcg_end_max_iter by
+    // the control kernel in the end game; the kernels take the smaller of it
+    // and their launch limit (which the autotuner lowers for its trials).
+    pcg_limit = std::max(o.pcg_max_iter, o.pcg_end_max_iter);
+    pcg_cap.alloc(nm, s);
+    {
+      std::vector<int32_t> cap(nm, o.pcg_max_iter);
+      check(cudaMemcpyAsync(pcg_cap.p, cap.data(), 4 * nm, cudaMemcpyHostToDevice, s), "h2d");
+      check(cudaStreamSynchronize(s), "sync");
+    }
     const int32_t patience = o.stop_patience > 0 ? o.stop_patience : 1;
     C = Control{lambda, cost, new_cost, rms, sq, n_front, active, accepted, iters, pcg_iters,
-                pcg_total, any, sigma, small, patience, o.max_iter, log_cap, log_cost, log_lam,
-                log_pcg, log_acc};
+                pcg_total, any, sigma, small, patience, o.max_iter, pcg_cap,
+                o.pcg_end_max_iter, o.pcg_end_rel, log_cap, log_cost, log_lam, log_pcg, log_acc};
     // PCG: shared memory per grid-kernel CTA (a fixed budget) holds row state
     // for up to smem_rows rows, then as many S blocks as fit.  A large batch
     // needs more rows per CTA: all CTAs of the cooperative launch must be
@@ -686,7 +697,8 @@ struct LmEngine {
     pcg_part.alloc(kParts * (size_t)imp_ncta, s);
     ia = ImpArgs<R>{bar, bar_base, pcg_part, imp_ncta, ctx.err, P, SV, Z, Zl, kept, own, camX,
                     pre, g, x, rbuf, z, p, qbuf, tbuf, h_lens[0], (int32_t)ctx.nb, pcg_iters,
-                    o.pcg_max_iter, o.pcg_tol, o.wait_limit};
+                    pcg_limit, o.pcg_tol, o.wait_limit};
+    ia.cap = pcg_cap;
     ctx.last_pcg_kernel = 3, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = imp_ncta;
   }
 
@@ -704,8 +716,9 @@ struct LmEngine {
     check(cudaStreamSynchronize(s), "sync");  // host plan vectors
     pa = PcgArgs<R>{jobs, cta_job0, bar, bar_base, pcg_part, plan.ncta, SB.row_ptr, SB.col_idx,
                     S, pre, g, x, z, p, ctx.nb, lens_row, lens_pos, SB.diag_pos, smem_rows,
-                    smem_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol, ctx.err,
+                    smem_blocks, active, pcg_iters, pcg_limit, o.pcg_tol, ctx.err,
                     o.wait_limit, o.hold_cta};
+    pa.cap = pcg_cap;
     grid_rows_target = rows_target;
     ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = plan.ncta;
   }
@@ -816,7 +829,8 @@ struct LmEngine {
     detail::h2d(cg_sube, kp.sub_ent, s);
     ca = CgArgs{cg_jobs, cg_loc, SB.row_ptr, SB.col_idx, (const float*)S.p, (const float*)pre.p,
                 (const float*)g.p, (float*)x.p, lens_row, lens_pos, SB.diag_pos, cp.max_rows,
-                cap_blocks, active, pcg_iters, o.pcg_max_iter, o.pcg_tol};
+                cap_blocks, active, pcg_iters, pcg_limit, o.pcg_tol};
+    ca.cap = pcg_cap;
     ca.blk_slot = cg_slot, ca.sub_ptr = cg_subp, ca.sub_ent = cg_sube, ca.cap_cache = kp.cap;
     use_coarse = coarse;
     ctx.last_coarse_dim = 0;

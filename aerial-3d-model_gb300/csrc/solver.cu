@@ -239,6 +239,8 @@ Opts resolve_options(const ba_options* o) {
     r.hold_cta = o->fault_hold_pcg_cta;
     if (o->wait_limit_cycles > 0) r.wait_limit = o->wait_limit_cycles;
     r.workspace_limit = o->workspace_limit_bytes > 0 ? o->workspace_limit_bytes : 0;
+    r.pcg_end_max_iter = o->pcg_end_max_iter;
+    if (o->pcg_end_rel > 0.0) r.pcg_end_rel = o->pcg_end_rel;
   }
   if (r.max_iter < 0) throw BadInput("max_iter must be >= 0");
   if (!(r.sigma > 0.0) || !std::isfinite(r.sigma)) throw BadInput("sigma_px must be finite and > 0");
@@ -249,6 +251,8 @@ Opts resolve_options(const ba_options* o) {
   if (r.stop_patience < 0) throw BadInput("stop_patience must be >= 0");
   if (r.coarse != 0 && r.coarse != 1) throw BadInput("coarse must be 0 or 1");
   if (r.hold_cta < 0) throw BadInput("fault_hold_pcg_cta must be >= 0");
+  if (r.pcg_end_max_iter < 0) throw BadInput("pcg_end_max_iter must be >= 0");
+  if (!std::isfinite(r.pcg_end_rel)) throw BadInput("pcg_end_rel must be finite");
   return r;
 }
 

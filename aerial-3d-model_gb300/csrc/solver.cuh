@@ -99,6 +99,11 @@ struct Control {
   int32_t* small;     // consecutive accepted steps below the 1e-6 decrease
   int32_t patience;   // stop after this many (1: the reference's rule)
   int32_t max_iter;
+  // End-game PCG cap: once an accepted step decreases a model's cost by less
+  // than end_rel (relative), pcg_cap[m] becomes end_cap (end_cap 0: off).
+  int32_t* pcg_cap;
+  int32_t end_cap;
+  double end_rel;
   // per-iteration log of model 0 (device arrays, log_cap entries)
   int32_t log_cap;
   double* log_new_cost;

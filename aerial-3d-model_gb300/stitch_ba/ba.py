@@ -40,6 +40,8 @@ class Options:
     coarse: bool = False          # mixed form, cluster PCG: two-level preconditioner
     wait_limit_cycles: int = 0    # spin limit of device-side waits (0: ~2 s)
     workspace_limit_bytes: int = 0  # device memory the call may hold (0: no limit) -> BA_OOM
+    pcg_end_max_iter: int = 0     # PCG cap once a step's relative decrease < pcg_end_rel (0: off)
+    pcg_end_rel: float = 0.0      # <= 0: 1e-5
     fault_hold_pcg_cta: int = 0   # tests of the timeout path: grid PCG CTA k-1 skips its exchanges
 
 
@@ -102,6 +104,8 @@ def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> n
     c.coarse = 1 if o.coarse else 0
     c.wait_limit_cycles = int(o.wait_limit_cycles)
     c.workspace_limit_bytes = int(o.workspace_limit_bytes)
+    c.pcg_end_max_iter = int(o.pcg_end_max_iter)
+    c.pcg_end_rel = float(o.pcg_end_rel)
     c.fault_hold_pcg_cta = int(o.fault_hold_pcg_cta)
     c.log = C.cast(C.pointer(log), C.c_void_p) if log is not None else None
     return c

@@ -54,7 +54,8 @@ class BaOptions(C.Structure):
                 ("pcg_kernel", C.c_int32), ("no_graph", C.c_int32), ("autotune", C.c_int32),
                 ("stop_patience", C.c_int32), ("coarse", C.c_int32),
                 ("fault_hold_pcg_cta", C.c_int32), ("wait_limit_cycles", C.c_int64),
-                ("workspace_limit_bytes", C.c_int64)]
+                ("workspace_limit_bytes", C.c_int64), ("pcg_end_max_iter", C.c_int32),
+                ("pcg_end_rel", C.c_double)]
 
 
 class BaStatsC(C.Structure):

@@ -91,6 +91,16 @@ MIXED_LARGE_CAMS = 1000
 # 64-model batch 7 models ended up to 1.1e-5 above their FP64 cost with one
 # step, none (at most +8.4e-7) with two, at 7% more time.
 MIXED_STOP_PATIENCE = 2
+# End game of the mixed form: once an accepted step decreases a model's cost by
+# less than 1e-5 (relative), its PCG cap rises to 100 for the rest of the solve
+# (an inexact-Newton forcing rule: tighter inner solves as the outer iteration
+# converges).  Measured (median of two solves, GB300): without it the 77-camera
+# survey stops 5.5e-6 above its FP64 cost (11.7 ms) and one of the 64 batched
+# models 1.07e-6 above; with it every model of the 77- and 500-camera surveys,
+# the 2000-camera survey and the batch ends at or below its FP64 cost, at
+# 21.4 / 35.2 / 196 / 305 ms against 11.7 / 32.8 / 188 / 273 ms without.
+MIXED_END_PCG_ITERS = 100
+MIXED_END_REL = 1e-5
 # Ablation: the mixed form's FP32 records, Schur sums and PCG vectors with the
 # reference's block-Jacobi preconditioner alone, capped at 200 PCG iterations.
 ABLATION_PCG_ITERS = 200
@@ -206,6 +216,9 @@ def form_options(form: str, **kw):
         mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
         kw.setdefault("coarse", not MIXED_MATRIX_FREE)
         kw.setdefault("stop_patience", MIXED_STOP_PATIENCE)
+        if MIXED_END_PCG_ITERS > 0:
+            kw.setdefault("pcg_end_max_iter", max(MIXED_END_PCG_ITERS, MIXED_PCG_CAP))
+            kw.setdefault("pcg_end_rel", MIXED_END_REL)
         return Options(precision="mixed", pcg_max_iter=MIXED_PCG_CAP, matrix_free=mf, **kw)
     if form == "mixed_bj":
         kw.setdefault("stop_patience", MIXED_STOP_PATIENCE)
@@ -389,6 +402,7 @@ def gpu_arm(args, ws, rank):
             forms[form]["schur_autotuned_us"] = prof.schur_tuned_us
             forms[form]["device_bytes"] = int(prof.device_bytes)
             forms[form]["pcg_max_iter"] = opts.pcg_max_iter
+            forms[form]["pcg_end_max_iter"] = opts.pcg_end_max_iter
             forms[form]["coarse_dim"] = int(prof.coarse_dim)
             forms[form]["graph"] = bool(info.graph)
     if "fp64" in forms:
@@ -671,11 +685,15 @@ def main():
                     help="mixed form: S-free PCG (S p from per-observation factors)")
     ap.add_argument("--mixed-patience", type=int, default=0,
                     help="mixed forms: consecutive small decreases before stopping (0: default)")
+    ap.add_argument("--mixed-end-iters", type=int, default=-1,
+                    help="mixed form: end-game PCG cap (-1: default 100, 0: off)")
     args = ap.parse_args()
-    global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE
+    global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE, MIXED_END_PCG_ITERS
     MIXED_MATRIX_FREE = args.matrix_free
     if args.mixed_patience > 0:
         MIXED_STOP_PATIENCE = args.mixed_patience
+    if args.mixed_end_iters >= 0:
+        MIXED_END_PCG_ITERS = args.mixed_end_iters
     ws, rank = dist_env()
     if args.stage != "ba":
         out = stage_arm(args, ws, rank)

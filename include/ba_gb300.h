@@ -141,6 +141,13 @@ typedef struct ba_options {
                            (problem copies and workspace); an allocation
                            beyond it fails with BA_OOM before it is made;
                            <= 0: no limit                                 */
+  int32_t pcg_end_max_iter; /* end-game PCG cap: once an accepted LM step
+                           decreases a model's cost by less than
+                           pcg_end_rel (relative), that model's PCG runs up
+                           to this many iterations per solve for the rest of
+                           the call (tighter inner solves as the outer
+                           iteration converges); 0: off                   */
+  double pcg_end_rel;   /* <= 0: 1e-5                                      */
 } ba_options;
 
 /* Kernel phases timed when ba_options.profile is set (ba_stats.ms_phase). */

@@ -182,6 +182,36 @@ def test_coarse_preconditioner_reaches_fp64_cost_in_fewer_pcg_iterations():
     assert err(ctxs[1]) < 0.5 * err(ctxs[0]), (err(ctxs[1]), err(ctxs[0]))
 
 
+def test_end_game_pcg_cap_rises_after_a_small_decrease():
+    """Inexact-Newton forcing: once an accepted step decreases the cost by
+    less than pcg_end_rel (relative), the model's PCG cap rises from
+    pcg_max_iter to pcg_end_max_iter for the rest of the solve.
+
+    The final cost of a mixed solve of this 77-camera survey depends on the
+    PCG layout through its end game (rejected steps raise the damping, and
+    two small decreases then stop the solve): with these settings it ended
+    4.2e-6 above the FP64 cost with a 3-CTA cluster and 2.5e-6 below with the
+    autotuned 12-CTA one; without the end-game cap, 1.7e-6 below and 5.5e-6
+    above (measured).  The bound is the mixed form's end-game spread."""
+    p, _ = survey.generate("lawnmower77", seed=1)
+    _, _, f64 = solve(p, Options(), sigma=1.0)
+    _, _, end = solve(p, Options(precision="mixed", coarse=True, pcg_max_iter=40, stop_patience=2,
+                                 pcg_end_max_iter=100, pcg_end_rel=1e-5), sigma=1.0)
+    assert abs(end.final_cost / f64.final_cost - 1.0) <= 1e-5, (end.final_cost, f64.final_cost)
+    n = end.iterations
+    pcg, acc, new = end.pcg_iters[:n], end.accepted[:n], end.new_cost[:n]
+    cost, first = end.initial_cost, None
+    for i in range(n):
+        if acc[i]:
+            if first is None and (cost - new[i]) / cost < 1e-5:
+                first = i
+            cost = new[i]
+    assert first is not None and first + 1 < n
+    assert max(pcg[:first + 1]) <= 40
+    assert 40 < max(pcg[first + 1:]) <= 100
+    assert min(pcg[first + 1:]) > 40  # 100 unless the PCG tolerance ends it first
+
+
 def test_coarse_option_is_inert_for_fp64_and_graph_replay_matches():
     p, _ = ref_survey()
     _, _, a = solve(p, Options(coarse=True))
