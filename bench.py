@@ -604,10 +604,18 @@ def cpu_solves(ps, max_iter: int, budget_s: float = CPU_SAMPLE_S):
     k = len(results)
     what = ("one complete solve of the survey" if len(ps) == 1 else
             f"complete solves of {k} of {len(ps)} models (models 0..{k - 1}), scaled by observations")
+    # Per-phase wall time of the CPU solves (seconds, summed over the models
+    # solved): linearise / point systems / assembly / Schur / PCG /
+    # back-substitution / cost, as the oracle times them.
+    phases = {}
+    for r in results:
+        for k, v in (r.phases or {}).items():
+            phases[k] = phases.get(k, 0.0) + float(v)
     return {"baseline": {"value": len(ps) / est, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{what} ({t_all:.1f} s, {max(r.iterations for r in results)} "
                                    f"LM iterations max)",
-                         "iterations": [int(r.iterations) for r in results]},
+                         "iterations": [int(r.iterations) for r in results],
+                         "phases_s": {k: round(v, 3) for k, v in phases.items()}},
             "results": results, "solutions": sols}
 
 
@@ -662,7 +670,10 @@ def reference_arm(args, ws, rank):
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "solution": {"iterations": int(r0.iterations), "final_cost": r0.final_cost,
                      "final_rms": r0.final_rms, "accepted": [int(a) for a in r0.accepted],
-                     "step_seconds": [round(t, 3) for t in times]},
+                     "step_seconds": [round(t, 3) for t in times],
+                     # the last step's per-phase wall time, summed over its models
+                     "phases_s": {k: round(sum(float((r.phases or {}).get(k, 0.0)) for r in last), 3)
+                                  for k in (r0.phases or {})}},
     }
 
 
