@@ -25,9 +25,12 @@ struct PcgTuning {
   int kernel = 1;       // 1 grid, 2 cluster
   int rows_target = 4;  // grid kernel: block rows per CTA
   int cluster = 0;      // cluster kernel: CTAs per cluster
+  int cg_threads = 512; // cluster kernel: threads per CTA (512 or 1024)
   double us_per_iter = 0.0;
   int sub_len = 0;      // Schur pairs per warp sub-segment (0: the default)
   double schur_us = 0.0;
+  int point_kernel = 0;  // mixed form's per-observation passes (0: the default)
+  double point_us = 0.0;
 };
 
 struct Context {
@@ -61,6 +64,7 @@ struct Context {
   int64_t phase_n[kPhases] = {0};
   int64_t last_nz = 0, last_pairs = 0, last_nl = 0;
   int32_t last_pcg_kernel = 0, last_pcg_cluster = 0, last_pcg_ctas = 0, last_coarse_dim = 0;
+  int32_t last_pcg_threads = 0, last_point_kernel = 0;
   int32_t last_sub_len = 0;
   PcgTuning tuning[2];  // [0] FP64 form, [1] mixed form
   bool last_graph = false;
@@ -117,6 +121,7 @@ struct Opts {
   int32_t hold_cta = 0;       // fault injection: grid PCG CTA hold_cta-1 skips its exchanges
   long long wait_limit = kSpinCycles;  // spin limit of device-side waits (cycles)
   int64_t workspace_limit = 0;         // device bytes the call may hold (0: no limit)
+  int32_t point_kernel = 0;  // mixed form's per-observation passes (ba_options numbering)
 };
 
 // One solve of the uploaded batch from its initial states, in precision R.

@@ -39,7 +39,16 @@ struct IterBufs {
   R* x;           // [nb][6] (dx)
   double* cost_part;  // [ncost][3]
   float* ptf;         // [np][9] mixed form: L (6) | t = V^-1 v (3) in FP32 for the Z pass
+  // Mixed form with a pair list: observation k's Schur factor is stored at
+  // Z[zpos[k]], its position in the camera ordering, so that the factors a
+  // destination block (a, b) gathers lie in the segments of cameras a and b
+  // in increasing order; null: at Z[k].
+  const uint32_t* zpos = nullptr;
 };
+
+__device__ __forceinline__ size_t z_index(const uint32_t* zpos, int64_t k) {
+  return zpos ? (size_t)zpos[k] : (size_t)k;
+}
 
 __device__ __forceinline__ double robust_weight(double e2, double sigma, int loss) {
   if (loss == LOSS_HUBER) {
@@ -511,7 +520,7 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
   B.kept[p] = ok ? 2 : 0;
   if (!ok) {
     for (uint32_t k = s; k < e; ++k) {
-      for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = 0.0f;
+      for (int i = 0; i < 18; ++i) B.Z[z_index(B.zpos, k) * 18 + i] = 0.0f;
       for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = 0.0f;
     }
     for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j)
@@ -528,7 +537,7 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
   B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
   const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
   for (uint32_t k = s; k < e; ++k) {
-    float* Z = B.Z + (size_t)k * 18;
+    float* Z = B.Z + z_index(B.zpos, k) * 18;
     float* gs = B.gsub + (size_t)k * 9;
     double o[kLinW];
     if (!linearise<double>(P, st, k, sg, refine, o)) {
@@ -694,6 +703,114 @@ __device__ __forceinline__ void chol3_rsqrt(const double* A, double* L) {
   L[0] = l00, L[1] = l10, L[2] = l11, L[3] = l20, L[4] = l21, L[5] = l22;
 }
 
+// The end of a point's mixed-form system once its sums are done (both point
+// kernels): FP64 V and v from the double-float sums, damping, the
+// conditioning test (an ill-conditioned point takes the FP64 path), V^-1 and
+// its Cholesky factor, the point's outputs and its lens entries (ba.rs:238-268).
+// rec(k): observation k's record (shared or global memory); pf_local: null, or
+// where the point's FP32 factor and step (9 floats) go besides B.ptf.
+template <typename Rec>
+__device__ __forceinline__ void point_mixed_finish(
+    const Prob& P, const StateView& st, const StructView& S, const IterBufs<float>& B, int64_t p,
+    uint32_t m, uint32_t s, uint32_t e, uint32_t l0, uint32_t l1, bool sum, const float (&Vh)[6],
+    const float (&Vl)[6], const float (&vh)[3], const float (&vl)[3], float (&Y)[9],
+    const double* lambda, const double* sigma, Rec&& rec, float* pf_local) {
+  const bool refine = P.model_refine[m] != 0;
+  if (!sum) {  // fewer than two observations (ba.rs:238)
+    B.kept[p] = 0;
+    for (uint32_t j = l0; j < l1; ++j)
+      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
+    return;
+  }
+  double V[6], v[3];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) V[t] = f2d_exact(Vh[t]) + f2d_exact(Vl[t]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) v[i] = f2d_exact(vh[i]) + f2d_exact(vl[i]);
+  const double lam = lambda[m];
+  double A[9];
+  sym3_full(V, A);
+  A[0] = A[0] * (1.0 + lam) + 1e-9;  // ba.rs:262-264
+  A[4] = A[4] * (1.0 + lam) + 1e-9;
+  A[8] = A[8] * (1.0 + lam) + 1e-9;
+  // Cofactors of the first row: the determinant serves the conditioning
+  // test and the inverse (ba.rs:265; exactly-singular V is skipped).
+  const double c00 = A[4] * A[8] - A[5] * A[7];
+  const double c01 = A[5] * A[6] - A[3] * A[8];
+  const double c02 = A[3] * A[7] - A[4] * A[6];
+  const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+  const double tr = A[0] + A[4] + A[8];
+  if (!(det > 0.0) || tr * tr * tr > 4.0 * kMixedCondLimit * det) {
+    point_system_mixed_ill(P, st, S, B, p, refine, sigma[m], lam);
+    return;
+  }
+  double Ai[9];
+  {
+    const double id = 1.0 / det;
+    Ai[0] = c00 * id;
+    Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+    Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+    Ai[3] = c01 * id;
+    Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+    Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+    Ai[6] = c02 * id;
+    Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+    Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+  }
+  double L[6];
+  chol3_rsqrt(Ai, L);
+  B.kept[p] = 1;
+  const double zv0 = L[0] * v[0] + L[1] * v[1] + L[3] * v[2];
+  const double zv1 = L[2] * v[1] + L[4] * v[2];
+  const double zv2 = L[5] * v[2];
+  double* pl = B.ptL + 6 * (size_t)p;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) pl[i] = L[i];
+  B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
+  float pfv[9];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) pfv[i] = (float)L[i];
+  pfv[6] = (float)(L[0] * zv0);
+  pfv[7] = (float)(L[1] * zv0 + L[2] * zv1);
+  pfv[8] = (float)(L[3] * zv0 + L[4] * zv1 + L[5] * zv2);
+  float* pf = B.ptf + 9 * (size_t)p;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) pf[i] = pfv[i];
+  if (pf_local)
+#pragma unroll
+    for (int i = 0; i < 9; ++i) pf_local[i] = pfv[i];
+  const float l00 = (float)L[0], l10 = (float)L[1], l11 = (float)L[2], l20 = (float)L[3],
+              l21 = (float)L[4], l22 = (float)L[5];
+  for (uint32_t j = l0; j < l1; ++j) {  // lens entries (ba.rs:251-259)
+    if (j > l0) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) Y[i] = 0.0f;
+    }
+    for (uint32_t k = s; k < e && j > l0; ++k) {
+      if (S.obs_lens[k] != j) continue;
+      const float* o = rec(k);
+      if (o[27] == 0.0f) continue;
+      const float w = o[26];
+      const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float ga = o[18 + a], gb = o[21 + a];
+        Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
+        Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
+        Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
+      }
+    }
+    float* Zl = B.Zl + (size_t)j * 9;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
+      Zl[3 * a + 0] = y0 * l00 + y1 * l10 + y2 * l20;
+      Zl[3 * a + 1] = y1 * l11 + y2 * l21;
+      Zl[3 * a + 2] = y2 * l22;
+    }
+  }
+}
+
 // Pass 2, a thread per point: V and v summed in FP64 from the stored FP32
 // records (products of FP32 numbers are exact in FP64, so V^-1 v is the
 // exact least-squares step of the stored Jacobians and residuals), the
@@ -783,94 +900,8 @@ static __global__ void __launch_bounds__(kPtSolveThreads, 6)
     __syncthreads();
   }
   if (!act) return;
-  const bool refine = P.model_refine[m] != 0;
-  if (!sum) {  // fewer than two observations (ba.rs:238)
-    B.kept[p] = 0;
-    for (uint32_t j = l0; j < l1; ++j)
-      for (int i = 0; i < 9; ++i) B.Zl[(size_t)j * 9 + i] = 0.0f;
-    return;
-  }
-  double V[6], v[3];
-#pragma unroll
-  for (int t = 0; t < 6; ++t) V[t] = f2d_exact(Vh[t]) + f2d_exact(Vl[t]);
-#pragma unroll
-  for (int i = 0; i < 3; ++i) v[i] = f2d_exact(vh[i]) + f2d_exact(vl[i]);
-  const double lam = lambda[m];
-  double A[9];
-  sym3_full(V, A);
-  A[0] = A[0] * (1.0 + lam) + 1e-9;  // ba.rs:262-264
-  A[4] = A[4] * (1.0 + lam) + 1e-9;
-  A[8] = A[8] * (1.0 + lam) + 1e-9;
-  // Cofactors of the first row: the determinant serves the conditioning
-  // test and the inverse (ba.rs:265; exactly-singular V is skipped).
-  const double c00 = A[4] * A[8] - A[5] * A[7];
-  const double c01 = A[5] * A[6] - A[3] * A[8];
-  const double c02 = A[3] * A[7] - A[4] * A[6];
-  const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
-  const double tr = A[0] + A[4] + A[8];
-  if (!(det > 0.0) || tr * tr * tr > 4.0 * kMixedCondLimit * det) {
-    point_system_mixed_ill(P, st, S, B, p, refine, sigma[m], lam);
-    return;
-  }
-  double Ai[9];
-  {
-    const double id = 1.0 / det;
-    Ai[0] = c00 * id;
-    Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
-    Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
-    Ai[3] = c01 * id;
-    Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
-    Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
-    Ai[6] = c02 * id;
-    Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
-    Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
-  }
-  double L[6];
-  chol3_rsqrt(Ai, L);
-  B.kept[p] = 1;
-  const double zv0 = L[0] * v[0] + L[1] * v[1] + L[3] * v[2];
-  const double zv1 = L[2] * v[1] + L[4] * v[2];
-  const double zv2 = L[5] * v[2];
-  double* pl = B.ptL + 6 * (size_t)p;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) pl[i] = L[i];
-  B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
-  float* pf = B.ptf + 9 * (size_t)p;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) pf[i] = (float)L[i];
-  pf[6] = (float)(L[0] * zv0);
-  pf[7] = (float)(L[1] * zv0 + L[2] * zv1);
-  pf[8] = (float)(L[3] * zv0 + L[4] * zv1 + L[5] * zv2);
-  const float l00 = (float)L[0], l10 = (float)L[1], l11 = (float)L[2], l20 = (float)L[3],
-              l21 = (float)L[4], l22 = (float)L[5];
-  for (uint32_t j = l0; j < l1; ++j) {  // lens entries (ba.rs:251-259)
-    if (j > l0) {
-#pragma unroll
-      for (int i = 0; i < 9; ++i) Y[i] = 0.0f;
-    }
-    for (uint32_t k = s; k < e && j > l0; ++k) {
-      if (S.obs_lens[k] != j) continue;
-      const float* o = B.lin + (size_t)k * kLinW;
-      if (o[27] == 0.0f) continue;
-      const float w = o[26];
-      const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float ga = o[18 + a], gb = o[21 + a];
-        Y[3 * a + 0] += (ga * j0 + gb * j3) * w;
-        Y[3 * a + 1] += (ga * j1 + gb * j4) * w;
-        Y[3 * a + 2] += (ga * j2 + gb * j5) * w;
-      }
-    }
-    float* Zl = B.Zl + (size_t)j * 9;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float y0 = Y[3 * a], y1 = Y[3 * a + 1], y2 = Y[3 * a + 2];
-      Zl[3 * a + 0] = y0 * l00 + y1 * l10 + y2 * l20;
-      Zl[3 * a + 1] = y1 * l11 + y2 * l21;
-      Zl[3 * a + 2] = y2 * l22;
-    }
-  }
+  point_mixed_finish(P, st, S, B, p, m, s, e, l0, l1, sum, Vh, Vl, vh, vl, Y, lambda, sigma,
+                     [&](uint32_t k) { return B.lin + (size_t)k * kLinW; }, nullptr);
 }
 
 // Pass 3, a thread per observation: Z = Y L (Y = w Jc^T Jp) and the
@@ -932,8 +963,243 @@ static __global__ void __launch_bounds__(kObsThreads)
   const uint32_t mask = __ballot_sync(0xffffffffu, mine);
   __syncwarp();
   const int n = P.no - k0 < 32 ? (int)(P.no - k0) : 32;
-  warp_store_records<18>(smz[warp], kZPitch, B.Z + k0 * 18, n, mask, lane);
+  if (B.zpos) {
+    // camera-major factors: each lane stores its own 72-byte record (8-byte
+    // aligned) at its camera-order position
+    if (mine) {
+      float2* dst = reinterpret_cast<float2*>(B.Z + (size_t)B.zpos[k] * 18);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) dst[i] = make_float2(Z[2 * i], Z[2 * i + 1]);
+    }
+  } else {
+    warp_store_records<18>(smz[warp], kZPitch, B.Z + k0 * 18, n, mask, lane);
+  }
   warp_store_records<9>(smg[warp], kGPitch, B.gsub + k0 * 9, n, mask, lane);
+}
+
+// ---- mixed form: the three passes fused per chunk of observations ---------
+//
+// One CTA per chunk of kChunk consecutive observations.  Its points are those
+// whose first observation lies in the chunk (fu_p0[b] .. fu_p0[b + 1], built
+// by chunk_points_kernel), so its observations are one contiguous run of
+// records: the chunk plus the rest of its last point's track.  The CTA
+//   1. forms each record (a thread per observation) in shared memory and
+//      copies the run to global memory, for the camera sums, with coalesced
+//      stores;
+//   2. sums each point's system from the shared records (a thread per point,
+//      its observations in order) and keeps the point's FP32 factor and step
+//      in shared memory;
+//   3. forms each observation's Schur factor and gradient share (a thread per
+//      observation) from its shared record and its point's shared factor,
+//      staged for coalesced stores in the record slots the warp has read.
+// The records cross HBM once (written) instead of three times (written, then
+// read by the point and factor passes).  Every value comes from the same
+// arithmetic in the same order as obs_record_kernel, point_solve_mixed_kernel
+// and obs_factor_kernel, so the results are bit-identical to theirs.  Records
+// beyond kCap of a run (a track longer than half a chunk at its end) are
+// read back from global memory.
+template <int kChunk>
+struct FusedPoint {
+  static constexpr int kThreads = kChunk;  // a thread per observation of the chunk
+  static constexpr int kCap = kChunk * 3 / 2;
+  static constexpr int kPtF = 10;  // per point slot: ptf (9) | kept
+  static constexpr size_t kSmem =
+      (size_t)kCap * kLinPitch * 4 + (size_t)kChunk * kPtF * 4 + (size_t)kCap * 4;
+  static constexpr int kMinBlocks = 768 / kChunk;
+};
+
+// fu_p0[b] = the first point whose first observation is at or after b kChunk
+// (b = 0 .. nchunks); the last entry is np.
+static __global__ void chunk_points_kernel(int64_t np, const uint32_t* pt_ptr, uint32_t chunk,
+                                           int64_t nchunks, uint32_t* fu_p0) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0) fu_p0[0] = 0, fu_p0[nchunks] = (uint32_t)np;
+  if (p >= np) return;
+  const uint32_t lo = pt_ptr[p], hi = pt_ptr[p + 1];
+  // chunk starts b kChunk in (lo, hi]: point p + 1 is the first at or after them
+  for (int64_t b = lo / chunk + 1; b <= (int64_t)(hi / chunk) && b < nchunks; ++b)
+    fu_p0[b] = (uint32_t)(p + 1);
+}
+
+template <int kChunk>
+static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
+                                         FusedPoint<kChunk>::kMinBlocks)
+    point_fused_mixed_kernel(Prob P, StateView st, StructView S, IterBufs<float> B,
+                             const float* camf, const uint32_t* fu_p0, const int32_t* active,
+                             const double* lambda, const double* sigma) {
+  using F = FusedPoint<kChunk>;
+  constexpr int kCap = F::kCap, kThreads = F::kThreads;
+  extern __shared__ __align__(16) float fu_sm[];
+  float* srec = fu_sm;                                // [kCap][kLinPitch]
+  float* spt = srec + (size_t)kCap * kLinPitch;       // [kChunk][kPtF]
+  // per staged record: 1 if its model is active | its point's slot << 1
+  uint32_t* sslot = reinterpret_cast<uint32_t*>(spt + (size_t)kChunk * F::kPtF);
+  const uint32_t p0 = fu_p0[blockIdx.x], p1 = fu_p0[blockIdx.x + 1];
+  if (p0 >= p1) return;  // uniform over the CTA
+  const uint32_t o_lo = S.pt_ptr[p0], n = S.pt_ptr[p1] - o_lo;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  auto rec = [&](uint32_t k) -> float* {
+    const uint32_t j = k - o_lo;
+    return j < (uint32_t)kCap ? srec + (size_t)j * kLinPitch : B.lin + (size_t)k * kLinW;
+  };
+  // 1. Records (as obs_record_kernel).
+  for (uint32_t j = threadIdx.x; j < n; j += kThreads) {
+    const uint32_t k = o_lo + j;
+    const uint32_t m = P.pt_model[P.obs_pt[k]];
+    const bool act = active[m] != 0;
+    if (j < (uint32_t)kCap) sslot[j] = act ? 1u : 0u;
+    if (!act) continue;
+    float* out = rec(k);
+    const double sg = sigma[m];
+    const float sg_f = (float)sg, inv_s2 = 1.0f / (sg_f * sg_f);
+    float jpf[6], wf;
+    double ev[2];
+    if (!linearise_mixed(P, st, camf, k, sg, sg_f, inv_s2, P.model_refine[m] != 0, out, jpf, ev,
+                         wf)) {
+#pragma unroll
+      for (int i = 0; i < kLinW; ++i) out[i] = 0.0f;
+    }
+  }
+  __syncthreads();
+  {  // staged records of active models out to global memory, contiguous
+    const uint32_t ns = n < (uint32_t)kCap ? n : (uint32_t)kCap;
+    float* dst = B.lin + (size_t)o_lo * kLinW;
+    for (uint32_t i = threadIdx.x; i < ns * kLinW; i += kThreads) {
+      const uint32_t j = i / kLinW;
+      if (sslot[j] & 1u) dst[i] = srec[(size_t)j * kLinPitch + (i - j * kLinW)];
+    }
+  }
+  // 2. Point systems (as point_solve_mixed_kernel).
+  for (uint32_t p = p0 + threadIdx.x; p < p1; p += kThreads) {
+    const uint32_t m = P.pt_model[p];
+    const bool act = active[m] != 0;
+    if (!act) continue;
+    const uint32_t s = S.pt_ptr[p], e = S.pt_ptr[p + 1];
+    const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
+    const uint32_t slot = s - o_lo;  // < kChunk for a point with observations
+    for (uint32_t k = s; k < e; ++k)
+      if (k - o_lo < (uint32_t)kCap) sslot[k - o_lo] |= slot << 1;
+    const bool sum = e - s >= 2;  // ba.rs:238
+    float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};
+    float vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0};
+    float Y[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t k = sum ? s : e; k < e; ++k) {
+      const float* o = rec(k) + 12;  // o[i] = lin[12 + i]
+      if (o[15] == 0.0f) continue;   // valid
+      const float w = o[14];
+      const float jp[6] = {o[0], o[1], o[2], o[3], o[4], o[5]};
+      if (l1 > l0 && S.obs_lens[k] == l0) {
+        const float jg[6] = {o[6], o[7], o[8], o[9], o[10], o[11]};
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          const float ga = jg[t], gb = jg[3 + t];
+          Y[3 * t + 0] += (ga * jp[0] + gb * jp[3]) * w;
+          Y[3 * t + 1] += (ga * jp[1] + gb * jp[4]) * w;
+          Y[3 * t + 2] += (ga * jp[2] + gb * jp[5]) * w;
+        }
+      }
+      float ph[6], pq[6];  // w jp = ph + pq exactly
+#pragma unroll
+      for (int i = 0; i < 6; ++i) ph[i] = w * jp[i], pq[i] = fmaf(w, jp[i], -ph[i]);
+      constexpr int VI[6] = {0, 0, 0, 1, 1, 2}, VJ[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        df_add_prod(Vh[t], Vl[t], ph[VI[t]], pq[VI[t]], jp[VJ[t]]);
+        df_add_prod(Vh[t], Vl[t], ph[3 + VI[t]], pq[3 + VI[t]], jp[3 + VJ[t]]);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        df_add_prod(vh[i], vl[i], ph[i], pq[i], o[12]);
+        df_add_prod(vh[i], vl[i], ph[3 + i], pq[3 + i], o[13]);
+      }
+    }
+    float* pt_sm = e > s ? spt + (size_t)slot * F::kPtF : nullptr;
+    point_mixed_finish(P, st, S, B, p, m, s, e, l0, l1, sum, Vh, Vl, vh, vl, Y, lambda, sigma,
+                       rec, pt_sm);
+    if (pt_sm) pt_sm[9] = __uint_as_float((uint32_t)B.kept[p]);
+  }
+  __syncthreads();
+  // 3. Schur factors and gradient shares (as obs_factor_kernel).
+  for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
+    const uint32_t j = j0 + lane, k = o_lo + j;
+    bool mine = false;
+    float Z[18], gs[9];
+    if (j < n) {
+      const uint32_t p = P.obs_pt[k];
+      bool act;
+      uint32_t slot;
+      if (j < (uint32_t)kCap) {
+        const uint32_t sl = sslot[j];
+        act = (sl & 1u) != 0, slot = sl >> 1;
+      } else {
+        act = active[P.pt_model[p]] != 0, slot = S.pt_ptr[p] - o_lo;
+      }
+      const float* pf = spt + (size_t)slot * F::kPtF;
+      const uint32_t kp = act ? __float_as_uint(pf[9]) : 0u;
+      if (act && kp != 2) {
+        mine = true;
+        const float* o = rec(k);
+        if (kp == 0 || o[27] == 0.0f) {
+#pragma unroll
+          for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
+#pragma unroll
+          for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
+        } else {
+          const float l00 = pf[0], l10 = pf[1], l11 = pf[2], l20 = pf[3], l21 = pf[4],
+                      l22 = pf[5];
+          const float t0 = pf[6], t1 = pf[7], t2 = pf[8];
+          const float w = o[26];
+          const float j0v = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+          const float r0 = (o[24] - (j0v * t0 + j1 * t1 + j2 * t2)) * w;
+          const float r1 = (o[25] - (j3 * t0 + j4 * t1 + j5 * t2)) * w;
+#pragma unroll
+          for (int r = 0; r < 6; ++r) {
+            const float ca = o[r], cb = o[6 + r];
+            const float y0 = (ca * j0v + cb * j3) * w;
+            const float y1 = (ca * j1 + cb * j4) * w;
+            const float y2 = (ca * j2 + cb * j5) * w;
+            Z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
+            Z[3 * r + 1] = y1 * l11 + y2 * l21;
+            Z[3 * r + 2] = y2 * l22;
+            gs[r] = ca * r0 + cb * r1;
+          }
+#pragma unroll
+          for (int a = 0; a < 3; ++a) gs[6 + a] = o[18 + a] * r0 + o[21 + a] * r1;
+        }
+      }
+    }
+    const uint32_t mask = __ballot_sync(0xffffffffu, mine);
+    const int nw = n - j0 < 32u ? (int)(n - j0) : 32;
+    if (B.zpos) {  // camera-major factors: each lane stores its own record
+      if (mine) {
+        float2* dst = reinterpret_cast<float2*>(B.Z + (size_t)B.zpos[k] * 18);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) dst[i] = make_float2(Z[2 * i], Z[2 * i + 1]);
+      }
+    }
+    if (j0 + 32 <= (uint32_t)kCap) {
+      // the warp's 32 record slots (read above) stage its stores
+      __syncwarp();
+      float* stg = srec + (size_t)j0 * kLinPitch;  // 32 x 29 floats
+      float* stz = stg;                            // [32][kZPitch]
+      float* stgs = stg + 32 * kZPitch;            // [32][kGPitch]
+      if (mine) {
+#pragma unroll
+        for (int i = 0; i < 18; ++i) stz[lane * kZPitch + i] = Z[i];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) stgs[lane * kGPitch + i] = gs[i];
+      }
+      __syncwarp();
+      if (!B.zpos) warp_store_records<18>(stz, kZPitch, B.Z + (size_t)(o_lo + j0) * 18, nw, mask, lane);
+      warp_store_records<9>(stgs, kGPitch, B.gsub + (size_t)(o_lo + j0) * 9, nw, mask, lane);
+    } else if (mine) {
+      if (!B.zpos)
+#pragma unroll
+        for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = Z[i];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = gs[i];
+    }
+  }
 }
 
 // ---- per camera: U, g, lens terms (ba.rs:273-292) ----------------------------
@@ -1599,7 +1865,7 @@ static __global__ void __launch_bounds__(256)
   const uint32_t p = P.obs_pt[k];
   if (!active[P.pt_model[p]] || B.kept[p] != 1) return;
   float z[18];
-  load_Z18(B.Z + (size_t)k * 18, z);
+  load_Z18(B.Z + z_index(B.zpos, k) * 18, z);
   const float* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
   float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f;
 #pragma unroll

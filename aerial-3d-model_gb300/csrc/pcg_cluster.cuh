@@ -39,8 +39,12 @@ namespace ba {
 
 namespace cgx = cooperative_groups;
 
+// Threads per CTA: 512, or 1024 for a warp per block row where a CTA holds
+// about 32 rows (the autotuner picks per problem shape).  The row loops take
+// rows warp, warp + warps, ...; the reductions sum the warps' partials in a
+// fixed order for either size.
 constexpr int kCgThreads = 512;
-constexpr int kCgWarps = kCgThreads / 32;
+constexpr int kCgThreadsWide = 1024;
 constexpr int kCgMaxCluster = 16;
 // Row state in floats: x r z p0 p1 q (6 each) | M (36) | the row's first and
 // end block, its lens block, its coarse group slot and its subscriber range
@@ -166,7 +170,7 @@ __device__ __forceinline__ DFloat df_shfl_xor(DFloat v, int o) {
 // release.  Consecutive reductions use different inboxes: a CTA can only
 // write inbox n + 2 after the barrier of reduction n + 1, which every reader
 // of inbox n has passed.
-template <int N, typename Post>
+template <int kWarps, int N, typename Post>
 __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&wv)[N],
                                           float* wsm, DFloat (*inbox)[4], DFloat* tot,
                                           Post&& post) {
@@ -177,9 +181,12 @@ __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&
   __syncthreads();
   const int csize = (int)cl.num_blocks();
   if (warp == 0) {
-    // lane = 4 w + i: warps w and w + 8 (value i), then over w in a fixed tree
-    static_assert(kCgWarps * 4 == 64, "two warp partials per lane");
+    // lane = 4 w + i: warps w, w + 8, ... (value i) in order, then over w in
+    // a fixed tree
+    static_assert(kWarps % 8 == 0 && kWarps >= 16 && kWarps <= 32, "2-4 warp partials per lane");
     DFloat c = df_sum(DFloat{wsm[lane], 0.0f}, DFloat{wsm[32 + lane], 0.0f});
+#pragma unroll
+    for (int h = 2; h < kWarps / 8; ++h) c = df_sum(c, DFloat{wsm[32 * h + lane], 0.0f});
     c = df_sum(c, df_shfl_xor(c, 4));
     c = df_sum(c, df_shfl_xor(c, 8));
     c = df_sum(c, df_shfl_xor(c, 16));
@@ -226,12 +233,13 @@ struct CgScalars {
 // pushed: c = E^-1 w for this CTA's groups (into sc, 7 per group), with the
 // model's w = W^T r − α W^T q (α = 0 and no W^T q at the start: w = W^T b).
 // Ends with a CTA barrier.
+template <int kWarps>
 __device__ __forceinline__ void cg_coarse_solve(const CgArgs& A, int m, int32_t ngr,
                                                 const float* sEi, const float* wr,
                                                 const float* wq, float alpha, float* sc) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int D = kCoarseModes * (A.model_g0[m + 1] - A.model_g0[m]);
-  for (int o = warp; o < ngr * kCoarseModes; o += kCgWarps) {
+  for (int o = warp; o < ngr * kCoarseModes; o += kWarps) {
     const float* er = sEi + (size_t)o * A.cap_dim;
     float v = 0.0f;
     if (wq)
@@ -263,6 +271,7 @@ __device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const
 // this CTA's groups' offset) of every CTA.  A warp per (group, mode): lane l
 // takes rows l, l + 32, ... (each row's six products in component order),
 // then a fixed butterfly.
+template <int kWarps>
 __device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int32_t ngr,
                                                    const int32_t* grp_row0,
                                                    const int32_t* grp_row1, int32_t g0,
@@ -270,7 +279,7 @@ __device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int32
                                                    const float* rs, int xoff, float* dst) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int csize = (int)cl.num_blocks();
-  for (int o = warp; o < ngr * kCoarseModes; o += kCgWarps) {
+  for (int o = warp; o < ngr * kCoarseModes; o += kWarps) {
     const int l = o / kCoarseModes, j = o % kCoarseModes;
     float v = 0.0f;
     for (int32_t r = grp_row0[g0 + l] + lane; r < grp_row1[g0 + l]; r += 32) {
@@ -302,8 +311,9 @@ __device__ __forceinline__ void cg_push_row(cgx::cluster_group& cl, float* cache
   }
 }
 
-template <bool kCoarse>
-static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A) {
+template <bool kCoarse, int kThreads>
+static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) {
+  constexpr int kCgWarps = kThreads / 32;
   __shared__ float wsm[kCgWarps * 4];
   __shared__ DFloat inbox[3][kCgMaxCluster][4];  // reduction inboxes (push)
   __shared__ DFloat tot[4];
@@ -404,7 +414,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
   // The first barrier also makes every CTA's shared memory live for DSMEM:
   // nothing is pushed before it.
-  cg_reduce<2>(cl, w2, wsm, inbox[1], tot, [&] {
+  cg_reduce<kCgWarps, 2>(cl, w2, wsm, inbox[1], tot, [&] {
     sc.rz = tot[0];
     sc.b2 = tot[1].hi;
     sc.bf = 0.0f;
@@ -412,9 +422,10 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
   });
   if constexpr (kCoarse) {
     // z = B^-1 b + W E^-1 W^T b, and r . z with it.
-    cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgR, wall_r);
+    cg_group_sums_push<kCgWarps>(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs,
+                                 kCgR, wall_r);
     cl.sync();
-    cg_coarse_solve(A, J.model, ngr, sEi, wall_r, nullptr, 0.0f, scf);
+    cg_coarse_solve<kCgWarps>(A, J.model, ngr, sEi, wall_r, nullptr, 0.0f, scf);
     float drz0 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
@@ -430,7 +441,7 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
                   (uint32_t)__float_as_int(st[kCgIdx + 5]), zi, 0);
     }
     const float w1[1] = {cg_sum8f(drz0)};
-    cg_reduce<1>(cl, w1, wsm, inbox[2], tot, [&] { sc.rz = tot[0]; });
+    cg_reduce<kCgWarps, 1>(cl, w1, wsm, inbox[2], tot, [&] { sc.rz = tot[0]; });
   } else {
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       const float* st = CGROW(lr);
@@ -519,11 +530,11 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
                          __shfl_sync(kFull, dlens, 2)};
     if constexpr (kCoarse) {
       __syncthreads();
-      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgQ,
-                         wall_q);
+      cg_group_sums_push<kCgWarps>(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs,
+                                   kCgQ, wall_q);
     }
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
-    cg_reduce<4>(cl, w4, wsm, inbox[0], tot, [&] {
+    cg_reduce<kCgWarps, 4>(cl, w4, wsm, inbox[0], tot, [&] {
       DFloat pq = tot[0];
       if (lens >= 0) {
         // The lens row's q gets the transposed camera terms; its share of
@@ -546,7 +557,8 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     // Two-level form: c = E^-1 w for this CTA's groups, with the next
     // residual's coarse vector w = W^T r − α W^T q from every group's owner.
     if constexpr (kCoarse)
-      cg_coarse_solve(A, J.model, ngr, sEi, wall_r + (size_t)cur * A.cap_dim, wall_q, af, scf);
+      cg_coarse_solve<kCgWarps>(A, J.model, ngr, sEi, wall_r + (size_t)cur * A.cap_dim, wall_q,
+                                af, scf);
     float drr = 0.0f, drz2 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
@@ -573,11 +585,11 @@ static __global__ void __launch_bounds__(kCgThreads) pcg_cluster_kernel(CgArgs A
     }
     if constexpr (kCoarse) {
       __syncthreads();
-      cg_group_sums_push(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgR,
-                         wall_r + (size_t)prv * A.cap_dim);
+      cg_group_sums_push<kCgWarps>(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs,
+                                   kCgR, wall_r + (size_t)prv * A.cap_dim);
     }
     const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};
-    cg_reduce<2>(cl, w2b, wsm, inbox[1], tot, [&] {
+    cg_reduce<kCgWarps, 2>(cl, w2b, wsm, inbox[1], tot, [&] {
       sc.stop = tot[0].hi < (float)A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
       sc.bf = tot[1].hi / sc.rz.hi;                        // ba.rs:189-190
       sc.rz = tot[1];

@@ -307,6 +307,15 @@ void h2d(DevBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
 
 inline int64_t at_least_1(int64_t n) { return n > 0 ? n : 1; }
 
+// The cluster PCG kernel for the coarse flag and the threads per CTA.
+using CgKernel = void (*)(CgArgs);
+inline CgKernel cg_kernel(bool coarse, int threads) {
+  if (threads == kCgThreadsWide)
+    return coarse ? pcg_cluster_kernel<true, kCgThreadsWide>
+                  : pcg_cluster_kernel<false, kCgThreadsWide>;
+  return coarse ? pcg_cluster_kernel<true, kCgThreads> : pcg_cluster_kernel<false, kCgThreads>;
+}
+
 }  // namespace detail
 
 // CUDA-event timing of kernel phases (only when profiling is asked for).
@@ -446,6 +455,12 @@ struct LmEngine {
   DevBuf<double> ptL, ptzv, part;
   DevBuf<uint8_t> kept;
   DevBuf<float> ptf, camf, obs_u;  // mixed form only
+  // Mixed form's per-observation passes (ba_options.point_kernel numbering:
+  // 1 three kernels, 2 / 3 fused over 128- / 256-observation chunks) and the
+  // first point of every chunk of the fused kernel.
+  int point_variant = 0;
+  DevBuf<uint32_t> fu_p0;
+  int64_t fu_chunks = 0;
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
@@ -479,6 +494,7 @@ struct LmEngine {
   // Cluster-resident PCG (mixed form).
   bool use_cluster = false;
   int cl_size = 0;
+  int cl_threads = kCgThreads;  // threads per CTA of the cluster kernel
   DevBuf<CgJob> cg_jobs;
   DevBuf<uint32_t> cg_loc, cg_slot, cg_subp, cg_sube;
   std::vector<uint32_t> h_col_idx, h_diag_pos;  // host copies for the cache plan
@@ -519,7 +535,9 @@ struct LmEngine {
     const int64_t cap = o.matrix_free == 2 ? 0
                         : (o.matrix_free == 0 && mf_ok && o.memory_cap > 0) ? o.memory_cap
                                                                             : -1;
-    build_structure(P, ctx.h_obs0, SB, ctx.err, s, cap);
+    // Mixed form: Schur factors stored camera-major (the Schur kernel's
+    // gathers of a destination block then walk two camera segments).
+    build_structure(P, ctx.h_obs0, SB, ctx.err, s, cap, sizeof(R) == 4);
     implicit = SB.implicit;
     ctx.last_matrix_free = implicit;
     sub_len = kSubLen;
@@ -559,6 +577,7 @@ struct LmEngine {
     if (sizeof(R) == 4 && o.coarse && !implicit) c_S64.alloc(at_least_1(SB.nz) * 36, s);
     B = IterBufs<R>{lin, gsub, Z, Zl, ptL, ptzv, kept, camU, camgj, camgs, camX, caml,
                     grpU, grpg, part, S, pre, g, x, cost_part, ptf.p};
+    B.zpos = sizeof(R) == 4 && SB.z_by_camera ? SB.cam_pos.p : nullptr;
     lambda.alloc(nm, s), cost.alloc(nm, s), new_cost.alloc(nm, s), rms.alloc(nm, s);
     sq.alloc(nm, s), sigma.alloc(nm, s), n_front.alloc(nm, s), pcg_total.alloc(nm, s);
     active.alloc(nm, s), accepted.alloc(nm, s), iters.alloc(nm, s), pcg_iters.alloc(nm, s);
@@ -618,13 +637,14 @@ struct LmEngine {
     bar.alloc(nm, s);
     bar_base.alloc(nm, s);
     if (implicit) {
+      choose_point_variant();
       setup_implicit();
       return;
     }
     if (nb > 0)
       BA_LAUNCH(lens_pos_kernel<<<grid_for(nb, 256), 256, 0, s>>>(nb, SB.row_ptr, SB.col_idx,
                                                                  P.blk_model, lens_row, lens_pos));
-    if (sizeof(R) == 8 && o.pcg_kernel == 2)
+    if (sizeof(R) == 8 && (o.pcg_kernel == 2 || o.pcg_kernel == 3))
       throw CudaError(cudaErrorNotSupported, "cluster PCG: the FP64 form uses the grid kernel");
     // Configuration: an earlier tuning of this context for this form, or the
     // defaults (FP64 instructions serialise per SM sub-partition: one row per
@@ -636,15 +656,78 @@ struct LmEngine {
       if (it != tune_cache().end()) tu = it->second;
     }
     if (tu.valid && tu.sub_len > 0) set_sub_len((uint32_t)tu.sub_len);
+    choose_point_variant();
     if (tu.valid && o.pcg_kernel == 0) {
-      if (tu.kernel != 2 || !try_cluster(tu.cluster, false, true)) plan_grid(tu.rows_target);
-    } else if (o.pcg_kernel == 2) {
-      try_cluster(0, true);
+      if (tu.kernel != 2 || !try_cluster(tu.cluster, false, true, tu.cg_threads))
+        plan_grid(tu.rows_target);
+    } else if (o.pcg_kernel == 2 || o.pcg_kernel == 3) {
+      try_cluster(0, true, false, o.pcg_kernel == 3 ? kCgThreadsWide : kCgThreads);
     } else if (sizeof(R) == 4 && o.pcg_kernel == 0 && try_cluster(0, false)) {
       // mixed form: the cluster kernel when every model fits
     } else {
       plan_grid(pcg_rows_target > 0 ? pcg_rows_target : (sizeof(R) == 8 ? 4 : 8));
     }
+  }
+
+  // The mixed form's per-observation passes: the option, else this form's
+  // tuning (of this context or of the problem shape in this process), else
+  // the three kernels (measured fastest on the 500-camera survey: the fused
+  // kernel's point pass runs a thread per point on the few points of a
+  // chunk, and this GPU's FP64 warp instructions cost the same however few
+  // lanes are active).
+  void choose_point_variant() {
+    if constexpr (sizeof(R) == 8) return;
+    int v = o.point_kernel;
+    if (v == 0) {
+      PcgTuning tu = ctx.tuning[1];
+      if (!tu.valid && o.autotune) {
+        std::lock_guard<std::mutex> lk(tune_mutex());
+        auto it = tune_cache().find(tune_key());
+        if (it != tune_cache().end()) tu = it->second;
+      }
+      v = tu.valid && tu.point_kernel > 0 ? tu.point_kernel : 1;
+    }
+    set_point_variant(v);
+  }
+
+  void set_point_variant(int v) {
+    if constexpr (sizeof(R) == 8) return;
+    point_variant = v;
+    ctx.last_point_kernel = v;
+    if (v == 1) return;
+    const int64_t chunk = v == 2 ? 128 : 256;
+    fu_chunks = std::max<int64_t>(1, (ctx.no + chunk - 1) / chunk);
+    fu_p0.alloc(fu_chunks + 1, s);
+    BA_LAUNCH(chunk_points_kernel<<<grid_for(std::max<int64_t>(ctx.np, 1), 256), 256, 0, s>>>(
+        ctx.np, SB.pt_ptr, (uint32_t)chunk, fu_chunks, fu_p0));
+  }
+
+  // The mixed form's per-observation passes at the current state.
+  void point_passes(const StateView& cur) {
+    if (point_variant == 1) {
+      if (ctx.no > 0)
+        BA_LAUNCH(obs_record_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
+            P, cur, B, camf, active, sigma));
+      BA_LAUNCH(point_solve_mixed_kernel<<<grid_for(ctx.np, kPtSolveThreads), kPtSolveThreads, 0,
+                                           s>>>(P, cur, SV, B, active, lambda, sigma));
+      if (ctx.no > 0)
+        BA_LAUNCH(obs_factor_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
+            P, B, active));
+    } else if (point_variant == 2) {
+      launch_fused<128>(cur);
+    } else {
+      launch_fused<256>(cur);
+    }
+  }
+
+  template <int kChunk>
+  void launch_fused(const StateView& cur) {
+    using F = FusedPoint<kChunk>;
+    check(cudaFuncSetAttribute(point_fused_mixed_kernel<kChunk>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F::kSmem),
+          "fused point shared memory");
+    BA_LAUNCH(point_fused_mixed_kernel<kChunk><<<(unsigned)fu_chunks, F::kThreads, F::kSmem, s>>>(
+        P, cur, SV, B, camf, fu_p0, active, lambda, sigma));
   }
 
   // Schur sub-segments of at most L pairs (a warp each): rebuilt from the
@@ -700,6 +783,7 @@ struct LmEngine {
                     pcg_limit, o.pcg_tol, o.wait_limit};
     ia.cap = pcg_cap;
     ctx.last_pcg_kernel = 3, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = imp_ncta;
+    ctx.last_pcg_threads = kPcgThreads;
   }
 
   // Grid kernel plan: about rows_target block rows per CTA.
@@ -721,12 +805,14 @@ struct LmEngine {
     pa.cap = pcg_cap;
     grid_rows_target = rows_target;
     ctx.last_pcg_kernel = 1, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = plan.ncta;
+    ctx.last_pcg_threads = kPcgThreads;
   }
 
   // Mixed form: one cluster of `csize` CTAs (0: by size, up to 16) per model
   // with the whole PCG in distributed shared memory.  Returns false (or throws
   // BA_NOT_SUPPORTED when `required`) if a model does not fit.
-  bool try_cluster(int csize_req, bool required, bool prefer_cluster = false) {
+  bool try_cluster(int csize_req, bool required, bool prefer_cluster = false,
+                   int threads = kCgThreads) {
     if constexpr (sizeof(R) == 8) return false;
     auto unusable = [&](const std::string& why) {
       if (required) throw CudaError(cudaErrorNotSupported, "cluster PCG: " + why);
@@ -742,7 +828,8 @@ struct LmEngine {
     check(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx.device),
           "attr");
     const bool coarse = o.coarse != 0;
-    const auto kfn = coarse ? pcg_cluster_kernel<true> : pcg_cluster_kernel<false>;
+    if (threads != kCgThreadsWide) threads = kCgThreads;
+    const detail::CgKernel kfn = detail::cg_kernel(coarse, threads);
     cudaFuncAttributes fa{};
     check(cudaFuncGetAttributes(&fa, kfn), "func attr");
     const size_t avail = (size_t)smem_optin - fa.sharedSizeBytes;
@@ -805,7 +892,7 @@ struct LmEngine {
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3((unsigned)cp.jobs.size());
-    cfg.blockDim = dim3(kCgThreads);
+    cfg.blockDim = dim3((unsigned)threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cfg.attrs = attr;
@@ -859,8 +946,9 @@ struct LmEngine {
     check(cudaStreamSynchronize(s), "sync");
     cg_smem = smem;
     cl_size = csize;
+    cl_threads = threads;
     use_cluster = true;
-    ctx.last_pcg_kernel = 2, ctx.last_pcg_cluster = csize;
+    ctx.last_pcg_kernel = 2, ctx.last_pcg_cluster = csize, ctx.last_pcg_threads = threads;
     ctx.last_pcg_ctas = (int32_t)cp.jobs.size();
     return true;
   }
@@ -879,6 +967,38 @@ struct LmEngine {
       ~Restore() { t.on = v; }
     } restore{T, timing};
     build_system();
+    // Per-observation passes of the mixed form: three kernels, or fused over
+    // 128- or 256-observation chunks (all give the same values).
+    double point_us = 0.0;
+    if constexpr (sizeof(R) == 4) {
+      if (o.point_kernel == 0 && ctx.no > 0) {
+        cudaEvent_t a, b;
+        check(cudaEventCreate(&a), "event");
+        check(cudaEventCreate(&b), "event");
+        const StateView cur = ctx.cur();
+        // an untimed run of each first, then the variants in turn (clock
+        // ramps and cache state spread over all of them), best of four
+        float best[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+        for (int rep = -1; rep < 4; ++rep)
+          for (int v : {1, 2, 3}) {
+            set_point_variant(v);
+            check(cudaEventRecord(a, s), "event");
+            point_passes(cur);
+            check(cudaEventRecord(b, s), "event");
+            check(cudaEventSynchronize(b), "tune");
+            float ms = 0;
+            check(cudaEventElapsedTime(&ms, a, b), "event");
+            if (rep >= 0) best[v] = std::min(best[v], ms);
+          }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        int best_v = 1;
+        for (int v : {2, 3})
+          if (best[v] < best[best_v]) best_v = v;
+        set_point_variant(best_v);
+        point_us = best[best_v] * 1000.0;
+      }
+    }
     // Schur sub-segment length: pairs per warp (more warps in flight to hide
     // the factor gathers, against more partial sums to add).
     double schur_us = 0.0;
@@ -906,15 +1026,19 @@ struct LmEngine {
       schur_us = best_ms * 1000.0;
       build_system();  // the system with the kept sub-segments
     }
-    std::vector<std::pair<int, int>> cand;  // (kernel, rows_target or cluster size)
+    struct Cand {
+      int kernel, param, threads;  // grid: rows_target; cluster: CTAs per cluster
+    };
+    std::vector<Cand> cand;
     // With the two-level preconditioner (cluster kernel only) the PCG needs a
     // fraction of the iterations, so only cluster layouts compete; the grid
     // layouts remain the fallback when no cluster fits.
     const bool coarse_only = sizeof(R) == 4 && o.coarse != 0;
     if (!coarse_only)
-      for (int rt : {2, 3, 4, 6, 8, 12, 16}) cand.push_back({1, rt});
+      for (int rt : {2, 3, 4, 6, 8, 12, 16}) cand.push_back({1, rt, kPcgThreads});
     if constexpr (sizeof(R) == 4)
-      for (int cs : {4, 8, 12, 16}) cand.push_back({2, cs});
+      for (int th : {kCgThreads, kCgThreadsWide})
+        for (int cs : {4, 8, 12, 16}) cand.push_back({2, cs, th});
     cudaEvent_t e0, e1;
     check(cudaEventCreate(&e0), "event");
     check(cudaEventCreate(&e1), "event");
@@ -923,13 +1047,13 @@ struct LmEngine {
       ~Ev() { cudaEventDestroy(a), cudaEventDestroy(b); }
     } ev{e0, e1};
     double best = 1e300;
-    std::pair<int, int> best_c{1, 4};
+    Cand best_c{1, 4, kPcgThreads};
     bool any = false;
     std::vector<int32_t> hit(ctx.nm);
     for (const auto& c : cand) {
-      if (c.first == 1) {
-        plan_grid(c.second);
-      } else if (!try_cluster(c.second, false, true)) {
+      if (c.kernel == 1) {
+        plan_grid(c.param);
+      } else if (!try_cluster(c.param, false, true, c.threads)) {
         continue;
       }
       const int32_t mi = pa.max_iter;
@@ -965,22 +1089,25 @@ struct LmEngine {
         float ms = 0;
         check(cudaEventElapsedTime(&ms, e0, e1), "event");
         const double per = (double)ms / kTuneIters;
-        if (per < best) best = per, best_c = {1, rt};
+        if (per < best) best = per, best_c = {1, rt, kPcgThreads};
       }
     }
     PcgTuning& tu = ctx.tuning[sizeof(R) == 8 ? 0 : 1];
     tu.valid = true;
-    tu.kernel = best_c.first;
-    tu.rows_target = best_c.first == 1 ? best_c.second : 4;
-    tu.cluster = best_c.first == 2 ? best_c.second : 0;
+    tu.kernel = best_c.kernel;
+    tu.rows_target = best_c.kernel == 1 ? best_c.param : 4;
+    tu.cluster = best_c.kernel == 2 ? best_c.param : 0;
+    tu.cg_threads = best_c.kernel == 2 ? best_c.threads : kCgThreads;
     tu.us_per_iter = best * 1000.0;
     tu.sub_len = (int)sub_len;
     tu.schur_us = schur_us;
+    tu.point_kernel = sizeof(R) == 4 && o.point_kernel == 0 ? point_variant : 0;
+    tu.point_us = point_us;
     {
       std::lock_guard<std::mutex> lk(tune_mutex());
       tune_cache()[tune_key()] = tu;
     }
-    if (best_c.first == 2 && try_cluster(best_c.second, false, true)) return;
+    if (best_c.kernel == 2 && try_cluster(best_c.param, false, true, best_c.threads)) return;
     plan_grid(tu.rows_target);
   }
 
@@ -1009,14 +1136,7 @@ struct LmEngine {
     if constexpr (sizeof(R) == 4) {
       if (ctx.nc > 0)
         BA_LAUNCH(cam_f32_kernel<<<grid_for(ctx.nc, 128), 128, 0, s>>>(P, cur, camf, active));
-      if (ctx.no > 0)
-        BA_LAUNCH(obs_record_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
-            P, cur, B, camf, active, sigma));
-      BA_LAUNCH(point_solve_mixed_kernel<<<grid_for(ctx.np, kPtSolveThreads), kPtSolveThreads, 0, s>>>(
-          P, cur, SV, B, active, lambda, sigma));
-      if (ctx.no > 0)
-        BA_LAUNCH(obs_factor_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
-            P, B, active));
+      point_passes(cur);
     } else {
       BA_LAUNCH(point_kernel<R><<<grid_for(ctx.np, 128), 128, 0, s>>>(P, cur, SV, B, active,
                                                                      lambda, sigma));
@@ -1086,15 +1206,13 @@ struct LmEngine {
       attr[0].val.clusterDim.y = 1;
       attr[0].val.clusterDim.z = 1;
       cfg.gridDim = dim3((unsigned)(ctx.nm * cl_size));
-      cfg.blockDim = dim3(kCgThreads);
+      cfg.blockDim = dim3((unsigned)cl_threads);
       cfg.dynamicSmemBytes = cg_smem;
       cfg.stream = s;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      if (use_coarse)
-        check(cudaLaunchKernelEx(&cfg, pcg_cluster_kernel<true>, ca), "pcg cluster launch");
-      else
-        check(cudaLaunchKernelEx(&cfg, pcg_cluster_kernel<false>, ca), "pcg cluster launch");
+      check(cudaLaunchKernelEx(&cfg, detail::cg_kernel(use_coarse, cl_threads), ca),
+            "pcg cluster launch");
     } else {
       void* args[] = {&pa};
       check(cudaLaunchCooperativeKernel((void*)pcg_kernel<R>, dim3(plan.ncta), dim3(kPcgThreads),

@@ -241,17 +241,19 @@ Opts resolve_options(const ba_options* o) {
     r.workspace_limit = o->workspace_limit_bytes > 0 ? o->workspace_limit_bytes : 0;
     r.pcg_end_max_iter = o->pcg_end_max_iter;
     if (o->pcg_end_rel > 0.0) r.pcg_end_rel = o->pcg_end_rel;
+    r.point_kernel = o->point_kernel;
   }
   if (r.max_iter < 0) throw BadInput("max_iter must be >= 0");
   if (!(r.sigma > 0.0) || !std::isfinite(r.sigma)) throw BadInput("sigma_px must be finite and > 0");
   if (r.loss != 0 && r.loss != 1) throw BadInput("unknown loss");
   if (r.precision != 0 && r.precision != 1) throw BadInput("unknown precision");
   if (r.matrix_free < 0 || r.matrix_free > 2) throw BadInput("unknown matrix_free mode");
-  if (r.pcg_kernel < 0 || r.pcg_kernel > 2) throw BadInput("unknown pcg_kernel");
+  if (r.pcg_kernel < 0 || r.pcg_kernel > 3) throw BadInput("unknown pcg_kernel");
   if (r.stop_patience < 0) throw BadInput("stop_patience must be >= 0");
   if (r.coarse != 0 && r.coarse != 1) throw BadInput("coarse must be 0 or 1");
   if (r.hold_cta < 0) throw BadInput("fault_hold_pcg_cta must be >= 0");
   if (r.pcg_end_max_iter < 0) throw BadInput("pcg_end_max_iter must be >= 0");
+  if (r.point_kernel < 0 || r.point_kernel > 3) throw BadInput("unknown point_kernel");
   if (!std::isfinite(r.pcg_end_rel)) throw BadInput("pcg_end_rel must be finite");
   return r;
 }
@@ -361,6 +363,11 @@ void solve(Context& c, const ba_options* opt, ba_stats* stats) {
       st.pcg_cluster = c.last_pcg_cluster;
       st.graph = c.last_graph ? 1 : 0;
       st.pcg_ctas = c.last_pcg_ctas;
+      st.pcg_threads = c.last_pcg_threads;
+      st.point_kernel = c.last_point_kernel;
+      st.point_tuned_us = c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].valid
+                              ? c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].point_us
+                              : 0.0;
       st.pcg_coarse_dim = c.last_coarse_dim;
       st.schur_sub_len = c.last_sub_len;
       st.schur_tuned_us = c.tuning[o.precision == BA_PRECISION_MIXED ? 1 : 0].valid

@@ -174,9 +174,12 @@ __global__ void pair_count_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t
   cnt[p] = n;
 }
 
+// zpos: null, or the storage position of each observation's Schur factor
+// (entries of observations are stored as that position; lens entries,
+// numbered from no, are kept).
 __global__ void pair_fill_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t* lens_ptr,
                                  const uint32_t* lens_grp, const uint32_t* off,
-                                 uint64_t* keys, uint64_t* vals) {
+                                 const uint32_t* zpos, uint64_t* keys, uint64_t* vals) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P.np) return;
   const Entries E = entries_of(pt_ptr, lens_ptr, p);
@@ -187,9 +190,11 @@ __global__ void pair_fill_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t*
   for (uint32_t i = 0; i < ne; ++i) {
     uint32_t ei, bi;
     E.get(P, lens_grp, i, ei, bi);
+    if (zpos && (int64_t)ei < P.no) ei = zpos[ei];
     for (uint32_t j = 0; j < ne; ++j) {
       uint32_t ej, bj;
       E.get(P, lens_grp, j, ej, bj);
+      if (zpos && (int64_t)ej < P.no) ej = zpos[ej];
       if (bi <= bj) {
         keys[o] = (uint64_t)bi * nb + bj;
         vals[o] = (uint64_t)ei | ((uint64_t)ej << 32);
@@ -197,6 +202,11 @@ __global__ void pair_fill_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t*
       }
     }
   }
+}
+
+__global__ void inverse_perm_kernel(const uint32_t* perm, int64_t n, uint32_t* inv) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) inv[perm[i]] = (uint32_t)i;
 }
 
 __global__ void diag_marker_kernel(uint64_t* keys, uint64_t* vals, int64_t base, int64_t nb) {
@@ -411,7 +421,7 @@ void build_subsegments(StructBufs& S, uint32_t sub_len, cudaStream_t s) {
 }
 
 void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, StructBufs& S,
-                     uint32_t* err, cudaStream_t s, int64_t pair_bytes_cap) {
+                     uint32_t* err, cudaStream_t s, int64_t pair_bytes_cap, bool z_by_camera) {
   const int64_t nc = P.nc, np = P.np, no = P.no, ng = P.ng, nb = P.nb, nm = P.nm;
 
   // Point ranges (obs are sorted by point).
@@ -458,6 +468,11 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
   // Schur partial sums) above the memory cap: no pair list, no S.
   if (pair_bytes_cap == 0 || (pair_bytes_cap > 0 && (int64_t)total * 40 > pair_bytes_cap))
     S.implicit = true;
+  S.z_by_camera = !S.implicit && z_by_camera && no > 0;
+  if (S.z_by_camera) {
+    S.cam_pos.alloc(no, s);
+    BA_LAUNCH(inverse_perm_kernel<<<grid_for(no, T), T, 0, s>>>(S.cam_obs, no, S.cam_pos));
+  }
   if (!S.implicit) {
     if (total >= 0xffffffffULL)
       throw std::runtime_error("too many Schur pair contributions for one call");
@@ -465,8 +480,9 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
     keys.alloc(npairs, s);
     S.pairs.alloc(npairs, s);
     if (np > 0)
-      BA_LAUNCH(pair_fill_kernel<<<grid_for(np, T), T, 0, s>>>(P, S.pt_ptr, S.lens_ptr,
-                                                             S.lens_grp, off, keys, S.pairs));
+      BA_LAUNCH(pair_fill_kernel<<<grid_for(np, T), T, 0, s>>>(
+          P, S.pt_ptr, S.lens_ptr, S.lens_grp, off, S.z_by_camera ? S.cam_pos.p : nullptr, keys,
+          S.pairs));
     BA_LAUNCH(diag_marker_kernel<<<grid_for(nb, T), T, 0, s>>>(keys, S.pairs, (int64_t)npt, nb));
     DevBuf<uint64_t> kt(npairs, s), vt(npairs, s);
     radix_sort_u64_u64(keys, S.pairs, kt, vt, npairs, bits_for((uint64_t)nb * nb - 1), s);

@@ -19,6 +19,10 @@ from . import native
 from .problem import BaStats, Problem
 
 
+# ba_options.point_kernel / ba_stats.point_kernel numbering
+POINT_KERNELS = ["auto", "three_pass", "fused128", "fused256"]
+
+
 @dataclass
 class Options:
     """Solver options beyond the reference's (max_iter, sigma_px).
@@ -33,7 +37,8 @@ class Options:
     memory_cap_bytes: int = 0
     stream: int | None = None     # cudaStream_t as an integer handle
     profile: bool = False         # per-phase CUDA-event timing (SolveInfo.phases)
-    pcg_kernel: str = "auto"      # "auto" | "grid" | "cluster" (mixed form)
+    pcg_kernel: str = "auto"      # "auto" | "grid" | "cluster" | "cluster_wide" (mixed form;
+                                  # cluster_wide: 1024 threads per CTA)
     graph: bool = True            # replay a CUDA graph per LM iteration
     autotune: bool = False        # time PCG configurations on the first solve of a form
     stop_patience: int = 0        # consecutive small accepted steps before stopping (0/1: ba.rs rule)
@@ -43,6 +48,8 @@ class Options:
     pcg_end_max_iter: int = 0     # PCG cap once a step's relative decrease < pcg_end_rel (0: off)
     pcg_end_rel: float = 0.0      # <= 0: 1e-5
     fault_hold_pcg_cta: int = 0   # tests of the timeout path: grid PCG CTA k-1 skips its exchanges
+    point_kernel: str = "auto"    # mixed form's per-observation passes: "auto" | "three_pass" |
+                                  # "fused128" | "fused256" (bit-identical results)
 
 
 @dataclass
@@ -75,6 +82,9 @@ class SolveInfo:
     coarse_dim: int = 0           # coarse unknowns of the two-level preconditioner
     schur_sub_len: int = 0        # Schur pairs per warp sub-segment
     schur_tuned_us: float = 0.0   # autotuned Schur kernel time (0: not tuned)
+    pcg_threads: int = 0          # threads per CTA of the PCG launch
+    point_kernel: str = "none"    # mixed form's per-observation passes that ran
+    point_tuned_us: float = 0.0   # autotuned time of those passes (0: not tuned)
 
     def stats(self) -> BaStats:
         return BaStats(self.iterations, self.initial_rms, self.final_rms)
@@ -97,7 +107,7 @@ def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> n
     c.memory_cap_bytes = int(o.memory_cap_bytes)
     c.stream = o.stream
     c.profile = 1 if o.profile else 0
-    c.pcg_kernel = {"auto": 0, "grid": 1, "cluster": 2}[o.pcg_kernel]
+    c.pcg_kernel = {"auto": 0, "grid": 1, "cluster": 2, "cluster_wide": 3}[o.pcg_kernel]
     c.no_graph = 0 if o.graph else 1
     c.autotune = 1 if o.autotune else 0
     c.stop_patience = int(o.stop_patience)
@@ -107,6 +117,7 @@ def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> n
     c.pcg_end_max_iter = int(o.pcg_end_max_iter)
     c.pcg_end_rel = float(o.pcg_end_rel)
     c.fault_hold_pcg_cta = int(o.fault_hold_pcg_cta)
+    c.point_kernel = POINT_KERNELS.index(o.point_kernel)
     c.log = C.cast(C.pointer(log), C.c_void_p) if log is not None else None
     return c
 
@@ -152,6 +163,9 @@ def _info(s: native.BaStatsC) -> SolveInfo:
     info.coarse_dim = s.pcg_coarse_dim
     info.schur_sub_len = s.schur_sub_len
     info.schur_tuned_us = s.schur_tuned_us
+    info.pcg_threads = s.pcg_threads
+    info.point_kernel = POINT_KERNELS[s.point_kernel] if s.point_kernel > 0 else "none"
+    info.point_tuned_us = s.point_tuned_us
     return info
 
 

@@ -55,7 +55,7 @@ class BaOptions(C.Structure):
                 ("stop_patience", C.c_int32), ("coarse", C.c_int32),
                 ("fault_hold_pcg_cta", C.c_int32), ("wait_limit_cycles", C.c_int64),
                 ("workspace_limit_bytes", C.c_int64), ("pcg_end_max_iter", C.c_int32),
-                ("pcg_end_rel", C.c_double)]
+                ("pcg_end_rel", C.c_double), ("point_kernel", C.c_int32)]
 
 
 class BaStatsC(C.Structure):
@@ -71,7 +71,8 @@ class BaStatsC(C.Structure):
                 ("pcg_kernel", C.c_int32), ("pcg_cluster", C.c_int32), ("graph", C.c_int32),
                 ("pcg_ctas", C.c_int32), ("pcg_tuned_us", C.c_double),
                 ("pcg_coarse_dim", C.c_int32), ("schur_sub_len", C.c_int32),
-                ("schur_tuned_us", C.c_double)]
+                ("schur_tuned_us", C.c_double), ("pcg_threads", C.c_int32),
+                ("point_kernel", C.c_int32), ("point_tuned_us", C.c_double)]
 
 PHASES = ["point", "camera", "schur", "assemble", "pcg", "update", "cost", "control", "setup"]
 

@@ -397,6 +397,7 @@ def gpu_arm(args, ws, rank):
             infos_by_form[form] = infos
             forms[form]["pcg_kernel"] = prof.pcg_kernel
             forms[form]["pcg_ctas"] = int(prof.pcg_ctas)
+            forms[form]["pcg_threads_per_cta"] = int(prof.pcg_threads)
             forms[form]["pcg_autotuned_us_per_iter"] = prof.pcg_tuned_us
             forms[form]["schur_sub_len"] = int(prof.schur_sub_len)
             forms[form]["schur_autotuned_us"] = prof.schur_tuned_us

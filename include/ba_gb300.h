@@ -113,7 +113,9 @@ typedef struct ba_options {
   int32_t pcg_kernel;   /* 0: auto (mixed form: cluster kernel when every
                            model fits, else grid), 1: grid-wide kernel,
                            2: one thread-block cluster per model (mixed
-                           form; BA_NOT_SUPPORTED when a model does not fit) */
+                           form; BA_NOT_SUPPORTED when a model does not fit),
+                           512 threads per CTA; 3: the same with 1024
+                           threads per CTA (a warp per block row)        */
   int32_t no_graph;     /* 1: launch each kernel directly instead of replaying
                            a CUDA graph of the LM iteration                */
   int32_t autotune;     /* 1: before the first solve of a form on a context,
@@ -148,6 +150,13 @@ typedef struct ba_options {
                            the call (tighter inner solves as the outer
                            iteration converges); 0: off                   */
   double pcg_end_rel;   /* <= 0: 1e-5                                      */
+  int32_t point_kernel; /* mixed form, per-observation passes (ba.rs:222-268):
+                           0: auto (the autotuner's choice, else the three
+                           kernels), 1: three kernels (records,
+                           point systems, Schur factors), 2: the three fused
+                           in one kernel over 128-observation chunks, 3: the
+                           same over 256-observation chunks (bit-identical
+                           results; the fused kernels keep the records on chip) */
 } ba_options;
 
 /* Kernel phases timed when ba_options.profile is set (ba_stats.ms_phase). */
@@ -194,6 +203,11 @@ typedef struct ba_stats {
   int32_t schur_sub_len;  /* Schur pair contributions per warp sub-segment
                              (chosen by the autotuner, else 512)          */
   double schur_tuned_us;  /* autotuner's Schur kernel time (0: not tuned) */
+  int32_t pcg_threads;    /* threads per CTA of the PCG launch (the cluster
+                             kernel: 512 or 1024, chosen by the autotuner) */
+  int32_t point_kernel;   /* mixed form's per-observation passes that ran
+                             (ba_options.point_kernel numbering), else 0 */
+  double point_tuned_us;  /* autotuner's time of those passes (0: not tuned) */
 } ba_stats;
 
 /* Defaults: max_iter 60, sigma_px 1, Cauchy, FP64, PCG 400 / 1e-20. */

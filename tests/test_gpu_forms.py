@@ -40,11 +40,13 @@ def test_graph_replay_is_bit_identical_to_direct_launches():
     assert a.final_cost == b.final_cost
 
 
-@pytest.mark.parametrize("kernel", ["grid", "cluster"])
+@pytest.mark.parametrize("kernel", ["grid", "cluster", "cluster_wide"])
 def test_mixed_form_passes_reference_known_answer(kernel):
     p, f_true = ref_survey()
     q, st, info = solve(p, Options(precision="mixed", pcg_kernel=kernel))
-    assert info.pcg_kernel == kernel
+    assert info.pcg_kernel == kernel.replace("_wide", "")
+    if kernel.startswith("cluster"):
+        assert info.pcg_threads == (1024 if kernel == "cluster_wide" else 512)
     # ba.rs:483-492 thresholds
     assert st.initial_rms > 20.0
     assert st.final_rms < 0.8
@@ -69,14 +71,17 @@ def test_cluster_and_grid_kernels_agree_on_one_system():
         a = ctx.debug_step(1e-4, 1.0, Options(precision="mixed", pcg_kernel="grid"), dense=False)
         b = ctx.debug_step(1e-4, 1.0, Options(precision="mixed", pcg_kernel="cluster"),
                            dense=False)
-    # both stop on the same |r|^2 < 1e-20 |b|^2 test; after a few hundred
-    # iterations the FP32 residual sits at its rounding floor, where the two
+        c = ctx.debug_step(1e-4, 1.0, Options(precision="mixed", pcg_kernel="cluster_wide"),
+                           dense=False)
+    # all stop on the same |r|^2 < 1e-20 |b|^2 test; after a few hundred
+    # iterations the FP32 residual sits at its rounding floor, where the
     # kernels' different summation orders move the stopping iteration by a
     # few (up to 2 % of the count)
-    ia, ib = a["pcg_iters"], b["pcg_iters"]
-    assert abs(ia - ib) <= max(3, 0.02 * max(ia, ib)), (ia, ib)
-    rel = np.linalg.norm(a["dx"] - b["dx"]) / np.linalg.norm(a["dx"])
-    assert rel < 1e-3, rel
+    for other in (b, c):
+        ia, ib = a["pcg_iters"], other["pcg_iters"]
+        assert abs(ia - ib) <= max(3, 0.02 * max(ia, ib)), (ia, ib)
+        rel = np.linalg.norm(a["dx"] - other["dx"]) / np.linalg.norm(a["dx"])
+        assert rel < 1e-3, rel
 
 
 def test_cluster_kernel_is_refused_for_fp64():
@@ -252,3 +257,38 @@ def test_mixed_batch_matches_individual_mixed_solves():
         assert abs(info.final_cost - si.final_cost) <= 1e-12 * si.final_cost
         assert np.abs(q.center - r.center).max() <= 1e-9
         assert np.abs(q.points - r.points).max() <= 1e-9
+
+
+def _long_tracks(p, points, copies):
+    """p with each observation of the given points repeated `copies` times
+    (still sorted by point): tracks longer than a fused chunk's staging."""
+    rep = np.where(np.isin(p.obs_pt, points), copies, 1)
+    idx = np.repeat(np.arange(len(p.obs_pt)), rep)
+    q = p.copy()
+    q.obs_cam, q.obs_pt = p.obs_cam[idx].copy(), p.obs_pt[idx].copy()
+    q.obs_uv = np.ascontiguousarray(p.obs_uv[idx])
+    return q
+
+
+@pytest.mark.parametrize("variant", ["fused128", "fused256"])
+def test_fused_point_passes_are_bit_identical(variant):
+    """The fused per-observation kernel forms every record, point system and
+    Schur factor with the same arithmetic in the same order as the three
+    kernels it replaces, so a whole mixed solve gives bit-identical results
+    — also when a point's track is longer than the records a chunk stages
+    in shared memory (the rest is read back from global memory)."""
+    p, _ = survey.generate("lawnmower77", seed=3, n_cams=24, n_points=8000)
+    for prob in (p, _long_tracks(p, [5, 4000], 60)):
+        qa, _, a = solve(prob, Options(precision="mixed", point_kernel="three_pass"), sigma=1.0)
+        qb, _, b = solve(prob, Options(precision="mixed", point_kernel=variant), sigma=1.0)
+        assert a.point_kernel == "three_pass" and b.point_kernel == variant
+        assert a.iterations == b.iterations and a.final_cost == b.final_cost
+        for x, y in ((qa.points, qb.points), (qa.center, qb.center), (qa.rot, qb.rot),
+                     (qa.intr, qb.intr)):
+            assert np.array_equal(x, y)
+
+
+def test_autotuner_picks_a_point_pass_variant():
+    p, _ = survey.generate("lawnmower77", seed=4, n_cams=24, n_points=8000)
+    _, _, t = solve(p, Options(precision="mixed", autotune=True), sigma=1.0)
+    assert t.point_kernel in ("three_pass", "fused128", "fused256") and t.point_tuned_us > 0.0
