@@ -291,7 +291,7 @@ constexpr int kCamF = 12;
 
 static __global__ void cam_f32_kernel(Prob P, StateView st, float* camf, const int32_t* active) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= P.nc || !active[P.cam_model[c]]) return;
+  if (c >= P.nc || (active && !active[P.cam_model[c]])) return;
   const double* R = st.rot + 9 * (size_t)c;
   const double* K = st.intr + 5 * (size_t)P.cam_group[c];
   float* o = camf + kCamF * (size_t)c;
@@ -386,27 +386,14 @@ static __device__ __noinline__ void linearise_mixed_extreme(const Prob& P, const
 // nearly singular V, and any rounding between V, v and the records would be
 // amplified by V^-1.  On return `ev` is the FP64 residual matching the
 // record (whitened for an extreme record).
-__device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& st,
-                                                const float* camf, int64_t k, double sigma,
-                                                float sigma_f, float inv_s2, bool refine,
-                                                float* out, float (&jp)[6], double (&ev)[2],
-                                                float& w) {
+// The FP32 part of a mixed record, from the point in camera coordinates xc
+// (FP64, in front of the camera) and the FP64 residual ev of observation k.
+__device__ __forceinline__ void mixed_record_from(const Prob& P, const StateView& st,
+                                                  const float* camf, int64_t k, double sigma,
+                                                  float sigma_f, float inv_s2, bool refine,
+                                                  const double (&xc)[3], double (&ev)[2],
+                                                  float* out, float (&jp)[6], float& w) {
   const uint32_t cam = P.obs_cam[k];
-  const double* Rm = st.rot + 9 * (size_t)cam;
-  const double* C = st.center + 3 * (size_t)cam;
-  const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
-  const double* X = st.points + 3 * (size_t)P.obs_pt[k];
-  double xc[3];
-  bacam::to_cam(Rm, C, X, xc);
-  if (xc[2] <= 1e-6) return false;
-  {
-    const double iz = rcp_newton(xc[2]);
-    const double px = xc[0] * iz, py = xc[1] * iz;
-    const double r2 = px * px + py * py;
-    const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
-    ev[0] = P.obs_uv[2 * k] - (K[0] * (px * d) + K[1]);
-    ev[1] = P.obs_uv[2 * k + 1] - (K[0] * (py * d) + K[2]);
-  }
   const float* cf = camf + kCamF * (size_t)cam;
   const float x0 = (float)xc[0], x1 = (float)xc[1], x2 = (float)xc[2];
   const float f = cf[9], k1 = cf[10], k2 = cf[11];
@@ -437,7 +424,7 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
 #pragma unroll
     for (int i = 0; i < 6; ++i) jp[i] = out[12 + i];
     w = 1.0f;
-    return true;
+    return;
   }
   if (P.loss == LOSS_HUBER) {
     const float a = sqrtf(e2);
@@ -474,6 +461,30 @@ __device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& 
   out[25] = e1;
   out[26] = w;
   out[27] = 1.0f;
+}
+
+__device__ __forceinline__ bool linearise_mixed(const Prob& P, const StateView& st,
+                                                const float* camf, int64_t k, double sigma,
+                                                float sigma_f, float inv_s2, bool refine,
+                                                float* out, float (&jp)[6], double (&ev)[2],
+                                                float& w) {
+  const uint32_t cam = P.obs_cam[k];
+  const double* Rm = st.rot + 9 * (size_t)cam;
+  const double* C = st.center + 3 * (size_t)cam;
+  const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
+  const double* X = st.points + 3 * (size_t)P.obs_pt[k];
+  double xc[3];
+  bacam::to_cam(Rm, C, X, xc);
+  if (xc[2] <= 1e-6) return false;
+  {
+    const double iz = rcp_newton(xc[2]);
+    const double px = xc[0] * iz, py = xc[1] * iz;
+    const double r2 = px * px + py * py;
+    const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
+    ev[0] = P.obs_uv[2 * k] - (K[0] * (px * d) + K[1]);
+    ev[1] = P.obs_uv[2 * k + 1] - (K[0] * (py * d) + K[2]);
+  }
+  mixed_record_from(P, st, camf, k, sigma, sigma_f, inv_s2, refine, xc, ev, out, jp, w);
   return true;
 }
 
@@ -636,9 +647,11 @@ __device__ __forceinline__ void warp_store_records(const float* sm, int pitch, f
 
 // Pass 1, a thread per observation: the FP32 record (linearise_mixed: FP64
 // residual, FP32 Jacobians and weight).
+// stale: null, or per model whether its records must be formed here (else
+// the trial cost of its accepted step left them, at this state).
 static __global__ void __launch_bounds__(kObsThreads, 4)
     obs_record_kernel(Prob P, StateView st, IterBufs<float> B, const float* camf,
-                      const int32_t* active, const double* sigma) {
+                      const int32_t* active, const double* sigma, const int32_t* stale) {
   __shared__ float sm[kObsWarps][32 * kLinPitch];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t k0 = (int64_t)blockIdx.x * kObsThreads + warp * 32;
@@ -648,7 +661,7 @@ static __global__ void __launch_bounds__(kObsThreads, 4)
   bool mine = false;
   if (k < P.no) {
     const uint32_t m = P.pt_model[P.obs_pt[k]];
-    if (active[m]) {
+    if (active[m] && (!stale || stale[m])) {
       mine = true;
       const double sg = sigma[m];
       const float sg_f = (float)sg, inv_s2 = 1.0f / (sg_f * sg_f);
@@ -1026,13 +1039,14 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
                                          FusedPoint<kChunk>::kMinBlocks)
     point_fused_mixed_kernel(Prob P, StateView st, StructView S, IterBufs<float> B,
                              const float* camf, const uint32_t* fu_p0, const int32_t* active,
-                             const double* lambda, const double* sigma) {
+                             const double* lambda, const double* sigma, const int32_t* stale) {
   using F = FusedPoint<kChunk>;
   constexpr int kCap = F::kCap, kThreads = F::kThreads;
   extern __shared__ __align__(16) float fu_sm[];
   float* srec = fu_sm;                                // [kCap][kLinPitch]
   float* spt = srec + (size_t)kCap * kLinPitch;       // [kChunk][kPtF]
-  // per staged record: 1 if its model is active | its point's slot << 1
+  // per staged record: 1 if its model is active | 2 if formed here (else
+  // loaded: the trial cost of an accepted step left it) | point slot << 2
   uint32_t* sslot = reinterpret_cast<uint32_t*>(spt + (size_t)kChunk * F::kPtF);
   const uint32_t p0 = fu_p0[blockIdx.x], p1 = fu_p0[blockIdx.x + 1];
   if (p0 >= p1) return;  // uniform over the CTA
@@ -1047,9 +1061,18 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
     const uint32_t k = o_lo + j;
     const uint32_t m = P.pt_model[P.obs_pt[k]];
     const bool act = active[m] != 0;
-    if (j < (uint32_t)kCap) sslot[j] = act ? 1u : 0u;
+    const bool form = act && (!stale || stale[m]);
+    if (j < (uint32_t)kCap) sslot[j] = (act ? 1u : 0u) | (form ? 2u : 0u);
     if (!act) continue;
     float* out = rec(k);
+    if (!form) {  // stage the stored record
+      if (j < (uint32_t)kCap) {
+        const float* src = B.lin + (size_t)k * kLinW;
+#pragma unroll
+        for (int i = 0; i < kLinW; ++i) out[i] = src[i];
+      }
+      continue;
+    }
     const double sg = sigma[m];
     const float sg_f = (float)sg, inv_s2 = 1.0f / (sg_f * sg_f);
     float jpf[6], wf;
@@ -1066,7 +1089,7 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
     float* dst = B.lin + (size_t)o_lo * kLinW;
     for (uint32_t i = threadIdx.x; i < ns * kLinW; i += kThreads) {
       const uint32_t j = i / kLinW;
-      if (sslot[j] & 1u) dst[i] = srec[(size_t)j * kLinPitch + (i - j * kLinW)];
+      if (sslot[j] & 2u) dst[i] = srec[(size_t)j * kLinPitch + (i - j * kLinW)];
     }
   }
   // 2. Point systems (as point_solve_mixed_kernel).
@@ -1078,7 +1101,7 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
     const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
     const uint32_t slot = s - o_lo;  // < kChunk for a point with observations
     for (uint32_t k = s; k < e; ++k)
-      if (k - o_lo < (uint32_t)kCap) sslot[k - o_lo] |= slot << 1;
+      if (k - o_lo < (uint32_t)kCap) sslot[k - o_lo] |= slot << 2;
     const bool sum = e - s >= 2;  // ba.rs:238
     float Vh[6] = {0, 0, 0, 0, 0, 0}, Vl[6] = {0, 0, 0, 0, 0, 0};
     float vh[3] = {0, 0, 0}, vl[3] = {0, 0, 0};
@@ -1130,7 +1153,7 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
       uint32_t slot;
       if (j < (uint32_t)kCap) {
         const uint32_t sl = sslot[j];
-        act = (sl & 1u) != 0, slot = sl >> 1;
+        act = (sl & 1u) != 0, slot = sl >> 2;
       } else {
         act = active[P.pt_model[p]] != 0, slot = S.pt_ptr[p] - o_lo;
       }
@@ -1487,6 +1510,93 @@ static __global__ void __launch_bounds__(kCostThreads)
   }
 }
 
+// Mixed form: the robust cost of a state (as cost_chunk_kernel, bit for bit)
+// and, for the models in `active`, every observation's FP32 record at that
+// state, formed from the same FP64 point in camera coordinates and the same
+// FP64 residual the cost uses (the residual's FP64 projection is the costly
+// part of a record on this GPU).  Called on the trial state of every LM
+// iteration: when the step is accepted those records are the next
+// iteration's, and the record pass skips the model (rec_stale); when it is
+// rejected the record pass forms them again at the restored state.
+static __global__ void __launch_bounds__(kCostThreads)
+    cost_record_kernel(Prob P, StateView st, StructView S, IterBufs<float> B, const float* camf,
+                       double* part, const int32_t* active, const double* sigma) {
+  __shared__ double scratch[3 * 32];
+  __shared__ float sm[kCostThreads / 32][32 * kLinPitch];
+  const int64_t ch = blockIdx.x;
+  if (ch >= S.ncost) return;
+  const uint32_t m = S.cost_chunk_model[ch];
+  if (active && !active[m]) return;
+  const double sg = sigma[m];
+  const double s2 = sg * sg, inv_s2 = 1.0 / s2;
+  const double behind = s2 * 10.0;  // ba.rs:116
+  const bool cauchy = P.loss == LOSS_CAUCHY;
+  const float sg_f = (float)sg, inv_s2f = 1.0f / (sg_f * sg_f);
+  const bool refine = P.model_refine[m] != 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double prod = 1.0;  // as cost_chunk_kernel
+  int64_t expo = 0;
+  double acc[3] = {0.0, 0.0, 0.0};
+  const uint32_t c1 = S.cost_chunk_end[ch];
+  // thread t takes observations begin + t, begin + t + blockDim, ... (the
+  // order of cost_chunk_kernel); a warp's 32 records are staged and stored
+  // as contiguous runs
+  for (uint32_t kb = S.cost_chunk_begin[ch] + warp * 32; kb < c1; kb += blockDim.x) {
+    const uint32_t k = kb + lane;
+    float* rec = &sm[warp][lane * kLinPitch];
+    if (k < c1) {
+      const uint32_t cam = P.obs_cam[k];
+      const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
+      double xc[3];
+      bacam::to_cam(st.rot + 9 * (size_t)cam, st.center + 3 * (size_t)cam,
+                    st.points + 3 * (size_t)P.obs_pt[k], xc);
+      if (xc[2] > 1e-6) {  // Pose::project (geometry.rs:28-32, 66-72)
+        const double iz = 1.0 / xc[2];
+        const double px = xc[0] * iz, py = xc[1] * iz;
+        const double r2 = px * px + py * py;
+        const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
+        double ev[2];
+        ev[0] = P.obs_uv[2 * (size_t)k] - (K[0] * d * px + K[1]);
+        ev[1] = P.obs_uv[2 * (size_t)k + 1] - (K[0] * d * py + K[2]);
+        const double e2 = ev[0] * ev[0] + ev[1] * ev[1];
+        if (cauchy) {
+          const double q = 1.0 + e2 * inv_s2;  // ba.rs:114
+          if (q < 1.0e300) {
+            prod *= q;
+            const int hi = __double2hiint(prod);
+            expo += (hi >> 20) - 1023;
+            prod = __hiloint2double((hi & 0x800FFFFF) | (1023 << 20), __double2loint(prod));
+          } else {
+            acc[0] += s2 * log(q);
+          }
+        } else {
+          acc[0] += robust_rho(e2, sg, P.loss);
+        }
+        acc[1] += e2;
+        acc[2] += 1.0;
+        float jpf[6], wf;
+        mixed_record_from(P, st, camf, k, sg, sg_f, inv_s2f, refine, xc, ev, rec, jpf, wf);
+      } else {
+        acc[0] += behind;
+#pragma unroll
+        for (int i = 0; i < kLinW; ++i) rec[i] = 0.0f;
+      }
+    }
+    __syncwarp();
+    const int n = c1 - kb < 32u ? (int)(c1 - kb) : 32;
+    warp_store_records<kLinW>(sm[warp], kLinPitch, B.lin + (size_t)kb * kLinW, n, 0xffffffffu,
+                              lane);
+    __syncwarp();
+  }
+  if (cauchy) acc[0] += s2 * (log(prod) + (double)expo * 0.69314718055994530942);
+  block_sum<3>(acc, scratch);
+  if (threadIdx.x == 0) {
+    part[3 * ch] = acc[0];
+    part[3 * ch + 1] = acc[1];
+    part[3 * ch + 2] = acc[2];
+  }
+}
+
 // CTA per model: the chunk partials and the GPS prior term over the model's
 // cameras (ba.rs:103-128), summed in a fixed order (strided per thread, then
 // the block's fixed tree).
@@ -1557,6 +1667,9 @@ static __global__ void control_kernel(int64_t nm, Control C) {
   if (it + 1 >= C.max_iter) act = 0;
   C.accepted[m] = acc;
   C.active[m] = act;
+  // mixed form: the trial cost left the records of the trial state; they are
+  // the current state's only if the step was accepted
+  if (C.rec_stale) C.rec_stale[m] = acc ? 0 : 1;
   if (act) atomicOr(C.any_active, 1);
   if (m == 0 && it < C.log_cap) {
     C.log_new_cost[it] = nc;
@@ -1637,8 +1750,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1)
 #pragma unroll
   for (int i = 0; i < 36; ++i) acc[i] = (R)0;
   const uint32_t b = S.sub_begin[sub], e = S.sub_end[sub];
+  // The next pair's entry is loaded while this pair's factors are gathered
+  // and multiplied (one dependent load less per pair on the critical path).
+  uint64_t nxt = b + lane < e ? S.pairs[b + lane] : kSentinel;
   for (uint32_t i = b + lane; i < e; i += 32) {
-    const uint64_t pr = S.pairs[i];
+    const uint64_t pr = nxt;
+    nxt = i + 32 < e ? S.pairs[i + 32] : kSentinel;
     if (pr == kSentinel) continue;
     if ((int64_t)(pr & 0xffffffffu) >= P.no + S.nl || (int64_t)(pr >> 32) >= P.no + S.nl) continue;
     R za[18], zb[18];

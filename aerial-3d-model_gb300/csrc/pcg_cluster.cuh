@@ -160,7 +160,10 @@ __device__ __forceinline__ DFloat df_shfl_xor(DFloat v, int o) {
 // and then over the cluster's CTAs, in a fixed order, by warp 0.  wv: N
 // (<= 4) values held by lane 0 of every warp; all threads receive the totals
 // in tot (shared memory).  Every CTA sums the same partials in the same
-// order, so every CTA sees bit-identical totals.
+// order, so every CTA sees bit-identical totals.  While warp 0 sums and
+// pushes the CTA's partials, warps 1.. run side(w) with w = warp - 1 (the
+// coarse group sums, which read the same row state after the same CTA
+// barrier).
 //
 // Exchange by push: before the cluster barrier, lane r of warp 0 stores the
 // CTA's partials into CTA r's inbox (inbox[source rank][value]); after it,
@@ -170,10 +173,10 @@ __device__ __forceinline__ DFloat df_shfl_xor(DFloat v, int o) {
 // release.  Consecutive reductions use different inboxes: a CTA can only
 // write inbox n + 2 after the barrier of reduction n + 1, which every reader
 // of inbox n has passed.
-template <int kWarps, int N, typename Post>
+template <int kWarps, int N, typename Side, typename Post>
 __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&wv)[N],
                                           float* wsm, DFloat (*inbox)[4], DFloat* tot,
-                                          Post&& post) {
+                                          Side&& side, Post&& post) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
@@ -199,6 +202,8 @@ __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&
 #pragma unroll
       for (int i = 0; i < N; ++i) dst[i] = v[i];
     }
+  } else {
+    side(warp - 1);
   }
   cl.sync();
   if (warp == 0) {
@@ -268,18 +273,19 @@ __device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const
 
 // Per own group: the sum over its rows of W^T x, x the row-state vector at
 // float offset `xoff`, pushed into the model-wide array `dst` (D floats, at
-// this CTA's groups' offset) of every CTA.  A warp per (group, mode): lane l
-// takes rows l, l + 32, ... (each row's six products in component order),
-// then a fixed butterfly.
-template <int kWarps>
-__device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int32_t ngr,
+// this CTA's groups' offset) of every CTA.  A warp per (group, mode), warp
+// `w` of kWorkers taking (group, mode) w, w + kWorkers, ...: lane l takes
+// rows l, l + 32, ... (each row's six products in component order), then a
+// fixed butterfly.
+template <int kWorkers>
+__device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int w, int32_t ngr,
                                                    const int32_t* grp_row0,
                                                    const int32_t* grp_row1, int32_t g0,
                                                    int32_t goff, uint32_t row0, const float* sW,
                                                    const float* rs, int xoff, float* dst) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int csize = (int)cl.num_blocks();
-  for (int o = warp; o < ngr * kCoarseModes; o += kWarps) {
+  for (int o = w; o < ngr * kCoarseModes; o += kWorkers) {
     const int l = o / kCoarseModes, j = o % kCoarseModes;
     float v = 0.0f;
     for (int32_t r = grp_row0[g0 + l] + lane; r < grp_row1[g0 + l]; r += 32) {
@@ -388,7 +394,9 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
       }
     }
   }
-  __syncthreads();
+  // Every CTA of the cluster has started (its shared memory is live for the
+  // pushes below) and its staging is done.
+  cl.sync();
   const bool vl = lane < 6;
   const int ci = vl ? lane : 0;
 #define CGROW(lr) (rs + (size_t)(lr) * kCgRow)
@@ -412,19 +420,23 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
     }
   }
   const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
-  // The first barrier also makes every CTA's shared memory live for DSMEM:
-  // nothing is pushed before it.
-  cg_reduce<kCgWarps, 2>(cl, w2, wsm, inbox[1], tot, [&] {
-    sc.rz = tot[0];
-    sc.b2 = tot[1].hi;
-    sc.bf = 0.0f;
-    sc.stop = 0;
-  });
+  // r.z and b.b; the two-level form pushes the group sums of W^T b beside it
+  // (z = B^-1 b + W E^-1 W^T b below)
+  cg_reduce<kCgWarps, 2>(
+      cl, w2, wsm, inbox[1], tot,
+      [&](int w) {
+        if constexpr (kCoarse)
+          cg_group_sums_push<kCgWarps - 1>(cl, w, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0,
+                                           sW, rs, kCgR, wall_r);
+      },
+      [&] {
+        sc.rz = tot[0];
+        sc.b2 = tot[1].hi;
+        sc.bf = 0.0f;
+        sc.stop = 0;
+      });
   if constexpr (kCoarse) {
     // z = B^-1 b + W E^-1 W^T b, and r . z with it.
-    cg_group_sums_push<kCgWarps>(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs,
-                                 kCgR, wall_r);
-    cl.sync();
     cg_coarse_solve<kCgWarps>(A, J.model, ngr, sEi, wall_r, nullptr, 0.0f, scf);
     float drz0 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
@@ -441,7 +453,7 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
                   (uint32_t)__float_as_int(st[kCgIdx + 5]), zi, 0);
     }
     const float w1[1] = {cg_sum8f(drz0)};
-    cg_reduce<kCgWarps, 1>(cl, w1, wsm, inbox[2], tot, [&] { sc.rz = tot[0]; });
+    cg_reduce<kCgWarps, 1>(cl, w1, wsm, inbox[2], tot, [](int) {}, [&] { sc.rz = tot[0]; });
   } else {
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       const float* st = CGROW(lr);
@@ -528,13 +540,13 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
     }
     const float w4[4] = {cg_sum8f(dpq), __shfl_sync(kFull, dlens, 0), __shfl_sync(kFull, dlens, 1),
                          __shfl_sync(kFull, dlens, 2)};
-    if constexpr (kCoarse) {
-      __syncthreads();
-      cg_group_sums_push<kCgWarps>(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs,
-                                   kCgQ, wall_q);
-    }
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
-    cg_reduce<kCgWarps, 4>(cl, w4, wsm, inbox[0], tot, [&] {
+    // p.q; the two-level form pushes the group sums of W^T q beside it
+    cg_reduce<kCgWarps, 4>(cl, w4, wsm, inbox[0], tot, [&](int w) {
+      if constexpr (kCoarse)
+        cg_group_sums_push<kCgWarps - 1>(cl, w, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0,
+                                         sW, rs, kCgQ, wall_q);
+    }, [&] {
       DFloat pq = tot[0];
       if (lens >= 0) {
         // The lens row's q gets the transposed camera terms; its share of
@@ -583,13 +595,14 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
       cg_push_row(cl, cache, A.sub_ent, (uint32_t)__float_as_int(st[kCgIdx + 4]),
                   (uint32_t)__float_as_int(st[kCgIdx + 5]), zi, 0);
     }
-    if constexpr (kCoarse) {
-      __syncthreads();
-      cg_group_sums_push<kCgWarps>(cl, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs,
-                                   kCgR, wall_r + (size_t)prv * A.cap_dim);
-    }
     const float w2b[2] = {cg_sum8f(drr), cg_sum8f(drz2)};
-    cg_reduce<kCgWarps, 2>(cl, w2b, wsm, inbox[1], tot, [&] {
+    // r.r and r.z; the two-level form pushes the group sums of the next
+    // W^T r beside them
+    cg_reduce<kCgWarps, 2>(cl, w2b, wsm, inbox[1], tot, [&](int w) {
+      if constexpr (kCoarse)
+        cg_group_sums_push<kCgWarps - 1>(cl, w, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0,
+                                         sW, rs, kCgR, wall_r + (size_t)prv * A.cap_dim);
+    }, [&] {
       sc.stop = tot[0].hi < (float)A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
       sc.bf = tot[1].hi / sc.rz.hi;                        // ba.rs:189-190
       sc.rz = tot[1];

@@ -461,6 +461,9 @@ struct LmEngine {
   int point_variant = 0;
   DevBuf<uint32_t> fu_p0;
   int64_t fu_chunks = 0;
+  // Per model: 1 if the stored records are not at the current state (the
+  // trial cost forms the trial state's records; see cost_record_kernel).
+  DevBuf<int32_t> rec_stale;
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
@@ -610,6 +613,11 @@ struct LmEngine {
     C = Control{lambda, cost, new_cost, rms, sq, n_front, active, accepted, iters, pcg_iters,
                 pcg_total, any, sigma, small, patience, o.max_iter, pcg_cap,
                 o.pcg_end_max_iter, o.pcg_end_rel, log_cap, log_cost, log_lam, log_pcg, log_acc};
+    if constexpr (sizeof(R) == 4) {
+      rec_stale.alloc(nm, s);
+      mark_records_stale();
+      C.rec_stale = rec_stale.p;
+    }
     // PCG: shared memory per grid-kernel CTA (a fixed budget) holds row state
     // for up to smem_rows rows, then as many S blocks as fit.  A large batch
     // needs more rows per CTA: all CTAs of the cooperative launch must be
@@ -702,12 +710,18 @@ struct LmEngine {
         ctx.np, SB.pt_ptr, (uint32_t)chunk, fu_chunks, fu_p0));
   }
 
+  void mark_records_stale() {
+    std::vector<int32_t> one(ctx.nm, 1);
+    check(cudaMemcpyAsync(rec_stale.p, one.data(), 4 * ctx.nm, cudaMemcpyHostToDevice, s), "h2d");
+    check(cudaStreamSynchronize(s), "sync");
+  }
+
   // The mixed form's per-observation passes at the current state.
   void point_passes(const StateView& cur) {
     if (point_variant == 1) {
       if (ctx.no > 0)
         BA_LAUNCH(obs_record_kernel<<<grid_for(ctx.no, kObsThreads), kObsThreads, 0, s>>>(
-            P, cur, B, camf, active, sigma));
+            P, cur, B, camf, active, sigma, rec_stale.p));
       BA_LAUNCH(point_solve_mixed_kernel<<<grid_for(ctx.np, kPtSolveThreads), kPtSolveThreads, 0,
                                            s>>>(P, cur, SV, B, active, lambda, sigma));
       if (ctx.no > 0)
@@ -727,7 +741,7 @@ struct LmEngine {
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F::kSmem),
           "fused point shared memory");
     BA_LAUNCH(point_fused_mixed_kernel<kChunk><<<(unsigned)fu_chunks, F::kThreads, F::kSmem, s>>>(
-        P, cur, SV, B, camf, fu_p0, active, lambda, sigma));
+        P, cur, SV, B, camf, fu_p0, active, lambda, sigma, rec_stale.p));
   }
 
   // Schur sub-segments of at most L pairs (a warp each): rebuilt from the
@@ -1121,10 +1135,22 @@ struct LmEngine {
     check(cudaStreamSynchronize(s), "sync");
   }
 
+  // records (mixed form): also form every active model's records at `st`.
   void eval_cost(const StateView& st, const int32_t* act, double* out_cost, double* out_sq,
-                 int64_t* out_n) {
-    BA_LAUNCH(cost_chunk_kernel<<<(unsigned)detail::at_least_1(SB.ncost), kCostThreads, 0, s>>>(
-        P, st, SV, cost_part, act, sigma));
+                 int64_t* out_n, bool records = false) {
+    bool done = false;
+    if constexpr (sizeof(R) == 4) {
+      if (records) {
+        if (ctx.nc > 0)
+          BA_LAUNCH(cam_f32_kernel<<<grid_for(ctx.nc, 128), 128, 0, s>>>(P, st, camf, act));
+        BA_LAUNCH(cost_record_kernel<<<(unsigned)detail::at_least_1(SB.ncost), kCostThreads, 0,
+                                       s>>>(P, st, SV, B, camf, cost_part, act, sigma));
+        done = true;
+      }
+    }
+    if (!done)
+      BA_LAUNCH(cost_chunk_kernel<<<(unsigned)detail::at_least_1(SB.ncost), kCostThreads, 0, s>>>(
+          P, st, SV, cost_part, act, sigma));
     BA_LAUNCH(cost_final_kernel<<<(unsigned)ctx.nm, kCostFinalThreads, 0, s>>>(
         P, st, SV, cost_part, act, out_cost, out_sq, out_n));
   }
@@ -1250,7 +1276,7 @@ struct LmEngine {
     build_system();
     solve_pcg();
     update();
-    eval_cost(ctx.trial(), active, new_cost, rms, n_front);
+    eval_cost(ctx.trial(), active, new_cost, rms, n_front, true);
     T.mark(BA_PHASE_COST);
     control_and_commit();
   }
@@ -1261,7 +1287,9 @@ struct LmEngine {
     setup();
     T.mark(BA_PHASE_SETUP);
     if (o.autotune && !ctx.tuning[sizeof(R) == 8 ? 0 : 1].valid) autotune();
-    eval_cost(ctx.cur(), nullptr, cost, sq, n_front);  // ba.rs:216
+    eval_cost(ctx.cur(), nullptr, cost, sq, n_front, true);  // ba.rs:216
+    if constexpr (sizeof(R) == 4)  // the records of the initial state are in place
+      check(cudaMemsetAsync(rec_stale.p, 0, 4 * nm, s), "memset");
     std::vector<double> h_cost0(nm), h_sq0(nm);
     std::vector<int64_t> h_n0(nm);
     check(cudaMemcpyAsync(h_cost0.data(), cost.p, 8 * nm, cudaMemcpyDeviceToHost, s), "d2h");

@@ -110,6 +110,9 @@ struct Control {
   double* log_lambda;
   int32_t* log_pcg;
   int32_t* log_accept;
+  // mixed form: per model, 1 if the stored records are not at the current
+  // state (set after every trial cost; null in the FP64 form)
+  int32_t* rec_stale = nullptr;
 };
 
 }  // namespace ba

@@ -278,12 +278,19 @@ def dist_env():
 BATCH_MODELS = 64
 
 
+# Points of a single survey (0: the workload's own count).  A smaller count
+# keeps the camera network, hence the reduced system and the PCG kernels, of
+# the full workload: the small case for full ncu captures of those kernels.
+N_POINTS = 0
+
+
 def make_workload(name: str, seed: int):
     """A list of problems: one for a single survey, BATCH_MODELS for batch64."""
     from stitch_ba import survey
     if name == "batch64":
         return [m[0] for m in survey.batched_models(BATCH_MODELS, seed=seed)]
-    p, truth = survey.generate(name, seed=seed)
+    kw = {"n_points": N_POINTS} if N_POINTS > 0 else {}
+    p, truth = survey.generate(name, seed=seed, **kw)
     return [p]
 
 
@@ -699,8 +706,12 @@ def main():
                     help="mixed forms: consecutive small decreases before stopping (0: default)")
     ap.add_argument("--mixed-end-iters", type=int, default=-1,
                     help="mixed form: end-game PCG cap (-1: default 100, 0: off)")
+    ap.add_argument("--n-points", type=int, default=0,
+                    help="points of a single survey (0: the workload's own); a smaller case "
+                         "with the same camera network, for profiling")
     args = ap.parse_args()
-    global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE, MIXED_END_PCG_ITERS
+    global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE, MIXED_END_PCG_ITERS, N_POINTS
+    N_POINTS = args.n_points
     MIXED_MATRIX_FREE = args.matrix_free
     if args.mixed_patience > 0:
         MIXED_STOP_PATIENCE = args.mixed_patience
