@@ -515,12 +515,66 @@ struct LmEngine {
   int64_t c_npairs = 0;
   CoarseArgs cargs{};
   int32_t c_ngroups = 0;
+  // The coarse setup (basis, W^T S W, its inverse) runs on a second stream
+  // beside the right-hand side and block-Jacobi kernels, forked after the
+  // assembly and joined before the PCG; coarse_pending: forked, not joined.
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool coarse_pending = false;
   PhaseTimer T;
 
   LmEngine(Context& c, const Opts& opts) : ctx(c), o(opts), s(c.stream) {
     T.on = o.profile != 0;
     T.s = s;
     for (int k = 0; k < kPhases; ++k) ctx.phase_ms[k] = 0, ctx.phase_n[k] = 0;
+  }
+  ~LmEngine() {
+    if (coarse_pending && s2) cudaStreamSynchronize(s2);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (s2) cudaStreamDestroy(s2);
+  }
+  LmEngine(const LmEngine&) = delete;
+  LmEngine& operator=(const LmEngine&) = delete;
+
+  // The stream s waits for the forked coarse setup (before the PCG reads it,
+  // and before anything it uses is planned or freed again).
+  void join_coarse() {
+    if (!coarse_pending) return;
+    check(cudaStreamWaitEvent(s, ev_join, 0), "join");
+    coarse_pending = false;
+  }
+
+  // Coarse setup of the two-level PCG on stream st.
+  void launch_coarse_chain(cudaStream_t st) {
+    BA_LAUNCH(coarse_basis_kernel<<<grid_for((int64_t)c_ngroups * 32, 128), 128, 0, st>>>(
+        P, ctx.cur(), cargs));
+    if (c_npairs > 0)
+      BA_LAUNCH(coarse_rowgroup_kernel<<<grid_for(c_npairs * 32, kCoarseMatThreads),
+                                         kCoarseMatThreads, 0, st>>>(SV, c_S64.p, cargs, c_npairs,
+                                                                     c_pair_row, c_pair_grp, c_P));
+    BA_LAUNCH(coarse_sum_kernel<<<dim3((unsigned)c_ngroups, 6), 224, 0, st>>>(cargs, c_row_pair0,
+                                                                         c_P));
+    check(cudaFuncSetAttribute(coarse_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)kInvSmemBytes),
+          "coarse inverse shared memory");
+    BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, kInvSmemBytes, st>>>(cargs));
+  }
+
+  // After the assembly: fork the coarse setup onto the second stream.
+  void fork_coarse() {
+    if (!(use_cluster && use_coarse && c_ngroups > 0)) return;
+    join_coarse();
+    if (!s2) {
+      check(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking), "side stream");
+      check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "event");
+      check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "event");
+    }
+    check(cudaEventRecord(ev_fork, s), "fork");
+    check(cudaStreamWaitEvent(s2, ev_fork, 0), "fork");
+    launch_coarse_chain(s2);
+    check(cudaEventRecord(ev_join, s2), "join");
+    coarse_pending = true;
   }
 
   void setup() {
@@ -781,6 +835,7 @@ struct LmEngine {
 
   // Matrix-free PCG: one cooperative launch over every SM, one group.
   void setup_implicit() {
+    join_coarse();
     use_cluster = false;
     use_coarse = false;
     ctx.last_coarse_dim = 0;
@@ -802,6 +857,7 @@ struct LmEngine {
 
   // Grid kernel plan: about rows_target block rows per CTA.
   void plan_grid(int rows_target) {
+    join_coarse();
     use_cluster = false;
     use_coarse = false;
     ctx.last_coarse_dim = 0;
@@ -827,6 +883,7 @@ struct LmEngine {
   // BA_NOT_SUPPORTED when `required`) if a model does not fit.
   bool try_cluster(int csize_req, bool required, bool prefer_cluster = false,
                    int threads = kCgThreads) {
+    join_coarse();
     if constexpr (sizeof(R) == 8) return false;
     auto unusable = [&](const std::string& why) {
       if (required) throw CudaError(cudaErrorNotSupported, "cluster PCG: " + why);
@@ -982,10 +1039,13 @@ struct LmEngine {
     } restore{T, timing};
     build_system();
     // Per-observation passes of the mixed form: three kernels, or fused over
-    // 128- or 256-observation chunks (all give the same values).
+    // 128- or 256-observation chunks (all give the same values), timed as in
+    // an LM iteration after an accepted step: the records are in place (the
+    // build above formed them), so the record pass is skipped.
     double point_us = 0.0;
     if constexpr (sizeof(R) == 4) {
       if (o.point_kernel == 0 && ctx.no > 0) {
+        check(cudaMemsetAsync(rec_stale.p, 0, 4 * ctx.nm, s), "memset");
         cudaEvent_t a, b;
         check(cudaEventCreate(&a), "event");
         check(cudaEventCreate(&b), "event");
@@ -1197,6 +1257,7 @@ struct LmEngine {
     if (SB.ns > 0)
       BA_LAUNCH(assemble_kernel<R><<<grid_for(SB.ns * 36, 256), 256, 0, s>>>(
           P, cur, SV, B, active, lambda, c_S64.p, sub_end.p));
+    fork_coarse();
     BA_LAUNCH(rhs_kernel<R><<<grid_for(ctx.nb * 6, 256), 256, 0, s>>>(P, cur, B, active));
     BA_LAUNCH(precond_kernel<R><<<grid_for(ctx.nb, 128), 128, 0, s>>>(P, SV, B, active));
     T.mark(BA_PHASE_ASSEMBLE);
@@ -1211,19 +1272,12 @@ struct LmEngine {
             "pcg launch");
     } else if (use_cluster) {
       if (use_coarse && c_ngroups > 0) {
-        BA_LAUNCH(coarse_basis_kernel<<<grid_for((int64_t)c_ngroups * 32, 128), 128, 0, s>>>(
-            P, ctx.cur(), cargs));
-        if (c_npairs > 0)
-          BA_LAUNCH(coarse_rowgroup_kernel<<<grid_for(c_npairs * 32, kCoarseMatThreads),
-                                             kCoarseMatThreads, 0, s>>>(
-              SV, c_S64.p, cargs, c_npairs, c_pair_row, c_pair_grp, c_P));
-        BA_LAUNCH(coarse_sum_kernel<<<dim3((unsigned)c_ngroups, 6), 224, 0, s>>>(cargs, c_row_pair0,
-                                                                            c_P));
-        check(cudaFuncSetAttribute(coarse_invert_kernel,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInvSmemBytes),
-              "coarse inverse shared memory");
-        BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, kInvSmemBytes, s>>>(
-            cargs));
+        // forked after the assembly of this system, or (a new PCG plan since)
+        // run here
+        if (coarse_pending)
+          join_coarse();
+        else
+          launch_coarse_chain(s);
       }
       cudaLaunchConfig_t cfg{};
       cudaLaunchAttribute attr[1];

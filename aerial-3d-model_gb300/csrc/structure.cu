@@ -153,25 +153,56 @@ __device__ __forceinline__ Entries entries_of(const uint32_t* pt_ptr, const uint
   return E;
 }
 
+// Pair enumeration, a warp per point: lane t holds entry t's id and block
+// (entries 32.. are loaded as needed), and entry i is broadcast from its lane
+// while the lanes test and emit the pairs (i, j), j = lane, lane + 32, ...;
+// a ballot ranks the emitted pairs, so they keep the order of a sequential
+// loop over i, then j.
+struct WarpEntries {
+  Entries E;
+  uint32_t ne, my_e, my_b;
+  __device__ __forceinline__ void load(const Prob& P, const uint32_t* lens_grp, int lane) {
+    ne = E.count();
+    my_e = 0, my_b = 0;
+    if ((uint32_t)lane < ne) E.get(P, lens_grp, (uint32_t)lane, my_e, my_b);
+  }
+  __device__ __forceinline__ void at(const Prob& P, const uint32_t* lens_grp, uint32_t t,
+                                     uint32_t& e, uint32_t& b) const {
+    if (t < 32) {  // uniform over the warp
+      e = __shfl_sync(kFull, my_e, (int)t);
+      b = __shfl_sync(kFull, my_b, (int)t);
+    } else {
+      E.get(P, lens_grp, t, e, b);
+    }
+  }
+};
+
 __global__ void pair_count_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t* lens_ptr,
                                   const uint32_t* lens_grp, uint32_t* cnt) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (p >= P.np) return;
-  const Entries E = entries_of(pt_ptr, lens_ptr, p);
+  WarpEntries W;
+  W.E = entries_of(pt_ptr, lens_ptr, p);
   uint32_t n = 0;
-  if (E.m >= 2) {
-    const uint32_t ne = E.count();
-    for (uint32_t i = 0; i < ne; ++i) {
+  if (W.E.m >= 2) {
+    W.load(P, lens_grp, lane);
+    for (uint32_t i = 0; i < W.ne; ++i) {
       uint32_t ei, bi;
-      E.get(P, lens_grp, i, ei, bi);
-      for (uint32_t j = 0; j < ne; ++j) {
-        uint32_t ej, bj;
-        E.get(P, lens_grp, j, ej, bj);
-        n += (bi <= bj) ? 1u : 0u;
+      W.at(P, lens_grp, i, ei, bi);
+      for (uint32_t j0 = 0; j0 < W.ne; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        uint32_t ej = 0, bj = 0;
+        if (j0 == 0) {
+          ej = W.my_e, bj = W.my_b;
+        } else if (j < W.ne) {
+          W.E.get(P, lens_grp, j, ej, bj);
+        }
+        n += __popc(__ballot_sync(kFull, j < W.ne && bi <= bj));
       }
     }
   }
-  cnt[p] = n;
+  if (lane == 0) cnt[p] = n;
 }
 
 // zpos: null, or the storage position of each observation's Schur factor
@@ -180,26 +211,37 @@ __global__ void pair_count_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t
 __global__ void pair_fill_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t* lens_ptr,
                                  const uint32_t* lens_grp, const uint32_t* off,
                                  const uint32_t* zpos, uint64_t* keys, uint64_t* vals) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (p >= P.np) return;
-  const Entries E = entries_of(pt_ptr, lens_ptr, p);
-  if (E.m < 2) return;
+  WarpEntries W;
+  W.E = entries_of(pt_ptr, lens_ptr, p);
+  if (W.E.m < 2) return;  // uniform over the warp
+  W.load(P, lens_grp, lane);
   uint64_t o = off[p];
-  const uint32_t ne = E.count();
   const uint64_t nb = (uint64_t)P.nb;
-  for (uint32_t i = 0; i < ne; ++i) {
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint32_t i = 0; i < W.ne; ++i) {
     uint32_t ei, bi;
-    E.get(P, lens_grp, i, ei, bi);
+    W.at(P, lens_grp, i, ei, bi);
     if (zpos && (int64_t)ei < P.no) ei = zpos[ei];
-    for (uint32_t j = 0; j < ne; ++j) {
-      uint32_t ej, bj;
-      E.get(P, lens_grp, j, ej, bj);
-      if (zpos && (int64_t)ej < P.no) ej = zpos[ej];
-      if (bi <= bj) {
-        keys[o] = (uint64_t)bi * nb + bj;
-        vals[o] = (uint64_t)ei | ((uint64_t)ej << 32);
-        ++o;
+    for (uint32_t j0 = 0; j0 < W.ne; j0 += 32) {
+      const uint32_t j = j0 + lane;
+      uint32_t ej = 0, bj = 0;
+      if (j0 == 0) {
+        ej = W.my_e, bj = W.my_b;
+      } else if (j < W.ne) {
+        W.E.get(P, lens_grp, j, ej, bj);
       }
+      const bool take = j < W.ne && bi <= bj;
+      const uint32_t mask = __ballot_sync(kFull, take);
+      if (take) {
+        if (zpos && (int64_t)ej < P.no) ej = zpos[ej];
+        const uint64_t q = o + __popc(mask & lt);
+        keys[q] = (uint64_t)bi * nb + bj;
+        vals[q] = (uint64_t)ei | ((uint64_t)ej << 32);
+      }
+      o += __popc(mask);
     }
   }
 }
@@ -460,8 +502,8 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
   DevBuf<uint32_t> cnt(np + 1, s), off(np + 1, s);
   cnt.zero();
   if (np > 0)
-    BA_LAUNCH(pair_count_kernel<<<grid_for(np, T), T, 0, s>>>(P, S.pt_ptr, S.lens_ptr,
-                                                            S.lens_grp, cnt));
+    BA_LAUNCH(pair_count_kernel<<<grid_for(np * 32, T), T, 0, s>>>(P, S.pt_ptr, S.lens_ptr,
+                                                                 S.lens_grp, cnt));
   const uint64_t npt = exclusive_scan_u32(cnt, off, np + 1, s);
   const uint64_t total = npt + (uint64_t)nb;
   // Matrix-free calls (cap 0), or a pair list (with its sort buffers and the
@@ -480,7 +522,7 @@ void build_structure(const Prob& P, const std::vector<uint32_t>& h_model_obs0, S
     keys.alloc(npairs, s);
     S.pairs.alloc(npairs, s);
     if (np > 0)
-      BA_LAUNCH(pair_fill_kernel<<<grid_for(np, T), T, 0, s>>>(
+      BA_LAUNCH(pair_fill_kernel<<<grid_for(np * 32, T), T, 0, s>>>(
           P, S.pt_ptr, S.lens_ptr, S.lens_grp, off, S.z_by_camera ? S.cam_pos.p : nullptr, keys,
           S.pairs));
     BA_LAUNCH(diag_marker_kernel<<<grid_for(nb, T), T, 0, s>>>(keys, S.pairs, (int64_t)npt, nb));

@@ -212,6 +212,8 @@ def form_options(form: str, **kw):
     mixed form with block-Jacobi PCG alone: the ablation)."""
     from stitch_ba import Options
     kw.setdefault("autotune", True)
+    if form != "fp64":
+        kw.setdefault("point_kernel", POINT_KERNEL)
     if form == "mixed":
         mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
         kw.setdefault("coarse", not MIXED_MATRIX_FREE)
@@ -282,6 +284,11 @@ BATCH_MODELS = 64
 # keeps the camera network, hence the reduced system and the PCG kernels, of
 # the full workload: the small case for full ncu captures of those kernels.
 N_POINTS = 0
+# Mixed forms' per-observation passes ("auto": the autotuner's choice).  Under
+# ncu the autotuner's timings are distorted (every launch is serialised and
+# instrumented, which penalises the three-kernel variant), so the launch-list
+# command fixes the variant the plain run chose.
+POINT_KERNEL = "auto"
 
 
 def make_workload(name: str, seed: int):
@@ -706,12 +713,16 @@ def main():
                     help="mixed forms: consecutive small decreases before stopping (0: default)")
     ap.add_argument("--mixed-end-iters", type=int, default=-1,
                     help="mixed form: end-game PCG cap (-1: default 100, 0: off)")
+    ap.add_argument("--point-kernel", default="auto",
+                    choices=["auto", "three_pass", "fused128", "fused256"],
+                    help="mixed forms: per-observation passes (auto: the autotuner's choice)")
     ap.add_argument("--n-points", type=int, default=0,
                     help="points of a single survey (0: the workload's own); a smaller case "
                          "with the same camera network, for profiling")
     args = ap.parse_args()
-    global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE, MIXED_END_PCG_ITERS, N_POINTS
+    global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE, MIXED_END_PCG_ITERS, N_POINTS, POINT_KERNEL
     N_POINTS = args.n_points
+    POINT_KERNEL = args.point_kernel
     MIXED_MATRIX_FREE = args.matrix_free
     if args.mixed_patience > 0:
         MIXED_STOP_PATIENCE = args.mixed_patience
