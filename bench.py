@@ -214,6 +214,7 @@ def form_options(form: str, **kw):
     kw.setdefault("autotune", True)
     if form != "fp64":
         kw.setdefault("point_kernel", POINT_KERNEL)
+        kw.setdefault("pcg_kernel", PCG_KERNEL)
     if form == "mixed":
         mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
         kw.setdefault("coarse", not MIXED_MATRIX_FREE)
@@ -289,6 +290,8 @@ N_POINTS = 0
 # instrumented, which penalises the three-kernel variant), so the launch-list
 # command fixes the variant the plain run chose.
 POINT_KERNEL = "auto"
+# Mixed forms' PCG layout ("auto": the autotuner's choice; same caveat).
+PCG_KERNEL = "auto"
 
 
 def make_workload(name: str, seed: int):
@@ -713,6 +716,9 @@ def main():
                     help="mixed forms: consecutive small decreases before stopping (0: default)")
     ap.add_argument("--mixed-end-iters", type=int, default=-1,
                     help="mixed form: end-game PCG cap (-1: default 100, 0: off)")
+    ap.add_argument("--pcg-kernel", default="auto", choices=["auto", "cluster", "cluster_wide"],
+                    help="mixed forms: PCG layout (auto: the autotuner's choice; cluster / "
+                         "cluster_wide: one cluster per model of 512- / 1024-thread CTAs)")
     ap.add_argument("--point-kernel", default="auto",
                     choices=["auto", "three_pass", "fused128", "fused256"],
                     help="mixed forms: per-observation passes (auto: the autotuner's choice)")
@@ -721,8 +727,10 @@ def main():
                          "with the same camera network, for profiling")
     args = ap.parse_args()
     global MIXED_MATRIX_FREE, MIXED_STOP_PATIENCE, MIXED_END_PCG_ITERS, N_POINTS, POINT_KERNEL
+    global PCG_KERNEL
     N_POINTS = args.n_points
     POINT_KERNEL = args.point_kernel
+    PCG_KERNEL = args.pcg_kernel
     MIXED_MATRIX_FREE = args.matrix_free
     if args.mixed_patience > 0:
         MIXED_STOP_PATIENCE = args.mixed_patience
