@@ -44,7 +44,23 @@ struct IterBufs {
   // destination block (a, b) gathers lie in the segments of cameras a and b
   // in increasing order; null: at Z[k].
   const uint32_t* zpos = nullptr;
+  // Values per Schur factor record: 18, or 24 with zpos (96 bytes, three
+  // whole 32-byte sectors: the scattered stores of the camera-major layout
+  // then write whole sectors, and a gather is three 32-byte-aligned loads).
+  int32_t zpitch = 18;
 };
+
+// Store an 18-value FP32 Schur factor as a 24-value record (96-byte aligned;
+// the last six values are zero).
+__device__ __forceinline__ void store_Z24(float* dst, const float (&z)[18]) {
+  float4* d = reinterpret_cast<float4*>(dst);
+  d[0] = make_float4(z[0], z[1], z[2], z[3]);
+  d[1] = make_float4(z[4], z[5], z[6], z[7]);
+  d[2] = make_float4(z[8], z[9], z[10], z[11]);
+  d[3] = make_float4(z[12], z[13], z[14], z[15]);
+  d[4] = make_float4(z[16], z[17], 0.0f, 0.0f);
+  d[5] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
 
 __device__ __forceinline__ size_t z_index(const uint32_t* zpos, int64_t k) {
   return zpos ? (size_t)zpos[k] : (size_t)k;
@@ -531,7 +547,7 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
   B.kept[p] = ok ? 2 : 0;
   if (!ok) {
     for (uint32_t k = s; k < e; ++k) {
-      for (int i = 0; i < 18; ++i) B.Z[z_index(B.zpos, k) * 18 + i] = 0.0f;
+      for (int i = 0; i < 18; ++i) B.Z[z_index(B.zpos, k) * B.zpitch + i] = 0.0f;
       for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = 0.0f;
     }
     for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j)
@@ -548,7 +564,7 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
   B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
   const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
   for (uint32_t k = s; k < e; ++k) {
-    float* Z = B.Z + z_index(B.zpos, k) * 18;
+    float* Z = B.Z + z_index(B.zpos, k) * B.zpitch;
     float* gs = B.gsub + (size_t)k * 9;
     double o[kLinW];
     if (!linearise<double>(P, st, k, sg, refine, o)) {
@@ -977,12 +993,13 @@ static __global__ void __launch_bounds__(kObsThreads)
   __syncwarp();
   const int n = P.no - k0 < 32 ? (int)(P.no - k0) : 32;
   if (B.zpos) {
-    // camera-major factors: each lane stores its own 72-byte record (8-byte
-    // aligned) at its camera-order position
+    // camera-major factors: each lane stores its own 96-byte record at its
+    // camera-order position
     if (mine) {
-      float2* dst = reinterpret_cast<float2*>(B.Z + (size_t)B.zpos[k] * 18);
+      float z[18];
 #pragma unroll
-      for (int i = 0; i < 9; ++i) dst[i] = make_float2(Z[2 * i], Z[2 * i + 1]);
+      for (int i = 0; i < 18; ++i) z[i] = Z[i];
+      store_Z24(B.Z + (size_t)B.zpos[k] * B.zpitch, z);
     }
   } else {
     warp_store_records<18>(smz[warp], kZPitch, B.Z + k0 * 18, n, mask, lane);
@@ -1194,11 +1211,7 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
     const uint32_t mask = __ballot_sync(0xffffffffu, mine);
     const int nw = n - j0 < 32u ? (int)(n - j0) : 32;
     if (B.zpos) {  // camera-major factors: each lane stores its own record
-      if (mine) {
-        float2* dst = reinterpret_cast<float2*>(B.Z + (size_t)B.zpos[k] * 18);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) dst[i] = make_float2(Z[2 * i], Z[2 * i + 1]);
-      }
+      if (mine) store_Z24(B.Z + (size_t)B.zpos[k] * B.zpitch, Z);
     }
     if (j0 + 32 <= (uint32_t)kCap) {
       // the warp's 32 record slots (read above) stage its stores
@@ -1723,10 +1736,30 @@ __device__ __forceinline__ void load_Z18(const float* s, float* z) {
   for (int i = 0; i < 18; ++i) z[i] = off ? f[i + 2] : f[i];
 }
 
+// A 96-byte-aligned FP32 record of the camera-major layout: two 32-byte
+// loads and one 8-byte load (three sectors, three L1 requests per lane where
+// five 16-byte loads of a 72-byte record make five).
+__device__ __forceinline__ void load_Z24(const float* s, float* z) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(z[0]), "=f"(z[1]), "=f"(z[2]), "=f"(z[3]), "=f"(z[4]), "=f"(z[5]), "=f"(z[6]),
+        "=f"(z[7])
+      : "l"(s));
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(z[8]), "=f"(z[9]), "=f"(z[10]), "=f"(z[11]), "=f"(z[12]), "=f"(z[13]), "=f"(z[14]),
+        "=f"(z[15])
+      : "l"(s + 8));
+  const float2 t = __ldg(reinterpret_cast<const float2*>(s + 16));
+  z[16] = t.x, z[17] = t.y;
+}
+__device__ __forceinline__ void load_Z24(const double*, double*) {}  // FP32 layout only
+
 template <typename R>
 __device__ __forceinline__ void load_Z(const IterBufs<R>& B, int64_t no, uint32_t eid, R* z) {
   if ((int64_t)eid < no) {
-    load_Z18(B.Z + (size_t)eid * 18, z);
+    if (sizeof(R) == 4 && B.zpitch == 24)
+      load_Z24(B.Z + (size_t)eid * 24, z);
+    else
+      load_Z18(B.Z + (size_t)eid * B.zpitch, z);
   } else {
     const R* s = B.Zl + (size_t)(eid - no) * 9;
 #pragma unroll
@@ -1982,7 +2015,10 @@ static __global__ void __launch_bounds__(256)
   const uint32_t p = P.obs_pt[k];
   if (!active[P.pt_model[p]] || B.kept[p] != 1) return;
   float z[18];
-  load_Z18(B.Z + z_index(B.zpos, k) * 18, z);
+  if (B.zpitch == 24)
+    load_Z24(B.Z + z_index(B.zpos, k) * 24, z);
+  else
+    load_Z18(B.Z + z_index(B.zpos, k) * B.zpitch, z);
   const float* d = B.x + 6 * (size_t)P.cam_blk[P.obs_cam[k]];
   float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f;
 #pragma unroll

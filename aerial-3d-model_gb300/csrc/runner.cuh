@@ -605,7 +605,11 @@ struct LmEngine {
     lin.alloc(at_least_1(no) * kLinW, s), gsub.alloc(at_least_1(no) * 9, s);
     // 16 bytes of padding: FP32 records are read as 16-byte vectors from the
     // 16-byte boundary at or below each 72-byte record.
-    Z.alloc(at_least_1(no) * 18 + 4, s), Zl.alloc(at_least_1(SB.nl) * 9, s);
+    // Schur factors: 24 values per record when stored camera-major (the
+    // mixed form with a pair list), else 18; 4 values of padding after the
+    // last record for the 16-byte loads of 18-value FP32 records.
+    const bool z24 = sizeof(R) == 4 && SB.z_by_camera;
+    Z.alloc(at_least_1(no) * (z24 ? 24 : 18) + 4, s), Zl.alloc(at_least_1(SB.nl) * 9, s);
     ptL.alloc(at_least_1(np) * 6, s), ptzv.alloc(at_least_1(np) * 3, s);
     kept.alloc(at_least_1(np), s);
     camU.alloc(at_least_1(nc) * 21, s), camgj.alloc(at_least_1(nc) * 6, s);
@@ -635,6 +639,7 @@ struct LmEngine {
     B = IterBufs<R>{lin, gsub, Z, Zl, ptL, ptzv, kept, camU, camgj, camgs, camX, caml,
                     grpU, grpg, part, S, pre, g, x, cost_part, ptf.p};
     B.zpos = sizeof(R) == 4 && SB.z_by_camera ? SB.cam_pos.p : nullptr;
+    B.zpitch = B.zpos ? 24 : 18;
     lambda.alloc(nm, s), cost.alloc(nm, s), new_cost.alloc(nm, s), rms.alloc(nm, s);
     sq.alloc(nm, s), sigma.alloc(nm, s), n_front.alloc(nm, s), pcg_total.alloc(nm, s);
     active.alloc(nm, s), accepted.alloc(nm, s), iters.alloc(nm, s), pcg_iters.alloc(nm, s);
