@@ -201,29 +201,31 @@ static __global__ void coarse_sum_kernel(CoarseArgs A, const int64_t* row_pair0,
 // then in-place block Gauss-Jordan without pivoting (E is symmetric positive
 // definite), four pivots per step.  E is staged in shared memory and there
 // symmetrised, scaled and padded with identity to Dq = a multiple of 32
-// (<= 192); the matrix then lives in registers: thread t holds the 12 x 12
-// tile at rows 12 (t / 16), columns 12 (t % 16), rows 2 p and 2 p + 1 of a
-// column in one 64-bit register pair, so that the update runs on packed FP32
-// FMAs (fma.rn.f32x2: two round-to-nearest FP32 FMAs, the results of two
-// fmaf).  Per step the threads holding the four pivot columns, then the four
-// pivot rows, copy them to shared memory and zero them in the tile; a thread
-// per column then inverts the 4 x 4 pivot block (a scalar pivot below 1e-6 of
-// the scaled unit diagonal is raised to 1e-6) and forms that column of the new
-// pivot rows rn; every thread then updates its tile, a <- a + cn . rn, with
-// cn = -(pivot columns) but e_y on pivot row y:
+// (<= 192); the matrix then lives in registers: thread t of 384 holds the
+// 8 x 12 tile at rows 8 (t / 16), columns 12 (t % 16) (three warps per SM
+// sub-partition to hide the FMA and shared-memory latencies), rows 2 p and
+// 2 p + 1 of a column in one 64-bit register pair, so that the update runs
+// on packed FP32 FMAs (fma.rn.f32x2: two round-to-nearest FP32 FMAs, the
+// results of two fmaf).  Per step the threads holding the four pivot
+// columns, then the four pivot rows, copy them to shared memory and zero them
+// in the tile; a thread per column then inverts the 4 x 4 pivot block (a
+// scalar pivot below 1e-6 of the scaled unit diagonal is raised to 1e-6) and
+// forms that column of the new pivot rows rn; every thread then updates its
+// tile, a <- a + cn . rn, with cn = -(pivot columns) but e_y on pivot row y:
 //   pivot rows        <- Pinv * (pivot rows)   (Pinv itself in the pivot columns)
 //   pivot columns     <- -(pivot columns) * Pinv
 //   everything else  -= (pivot columns) * Pinv * (pivot rows).
 // The shared pivot rows and columns alternate between two buffers, so a step
 // takes two barriers.  The result is unscaled and symmetrised.
-constexpr int kInvThreads = 256;
-constexpr int kInvTile = 12;  // rows and columns of a thread's tile
-constexpr int kInvPairs = kInvTile / 2;
+constexpr int kInvThreads = 384;
+constexpr int kInvTileR = 8;   // rows of a thread's tile
+constexpr int kInvTileC = 12;  // columns of a thread's tile
+constexpr int kInvPairs = kInvTileR / 2;
 constexpr int kInvMaxPad = 192;  // kCoarseMaxDim rounded up to a multiple of 32
 static_assert(kInvMaxPad >= kCoarseMaxDim && kInvMaxPad % 32 == 0, "padding");
-static_assert((kInvThreads / 16) * kInvTile == kInvMaxPad && 16 * kInvTile == kInvMaxPad,
-              "12 x 12 tiles cover the padded matrix");
-static_assert(kInvTile % 4 == 0, "pivot groups of four lie inside one tile");
+static_assert((kInvThreads / 16) * kInvTileR == kInvMaxPad && 16 * kInvTileC == kInvMaxPad,
+              "8 x 12 tiles cover the padded matrix");
+static_assert(kInvTileR % 4 == 0 && kInvTileC % 4 == 0, "pivot groups of four lie inside one tile");
 static_assert(kInvThreads >= kInvMaxPad, "a thread per column of the pivot rows");
 // E staged whole in dynamic shared memory; the even pitch keeps a row pair of
 // one column 8-byte aligned.
@@ -232,8 +234,8 @@ constexpr size_t kInvSmemBytes = (size_t)kInvMaxPad * kInvPitch * sizeof(float);
 // Column j of the new pivot rows sits at j + j / 12: the 16 threads of a tile
 // row read columns 12 k + c, which then fall in 16 different bank quads
 // (13 k + c mod 8 differs for any 8 consecutive k).
-__device__ __forceinline__ int inv_rn_slot(int j) { return j + j / kInvTile; }
-constexpr int kInvRnSlots = kInvMaxPad + kInvMaxPad / kInvTile;
+__device__ __forceinline__ int inv_rn_slot(int j) { return j + j / kInvTileC; }
+constexpr int kInvRnSlots = kInvMaxPad + kInvMaxPad / kInvTileC;
 
 __device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
   uint64_t r;
@@ -280,7 +282,7 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
   if (D == 0) return;
   const int Dq = ((D + 31) / 32) * 32;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  const int r0 = (t >> 4) * kInvTile, c0 = (t & 15) * kInvTile;
+  const int r0 = (t >> 4) * kInvTileR, c0 = (t & 15) * kInvTileC;
   const float* Em = A.E + A.model_eoff[m];
   // Asynchronous 4-byte copies: every load in flight at once, none through
   // registers (E was just written and is read once).
@@ -313,11 +315,11 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
   __syncthreads();
   // The tile, read down the columns of the symmetric matrix: rows (2 p, 2 p + 1)
   // of column c are entries (2 p, 2 p + 1) of row c.
-  uint64_t a2[kInvPairs][kInvTile];
+  uint64_t a2[kInvPairs][kInvTileC];
 #pragma unroll
   for (int p = 0; p < kInvPairs; ++p)
 #pragma unroll
-    for (int c = 0; c < kInvTile; ++c)
+    for (int c = 0; c < kInvTileC; ++c)
       a2[p][c] = *reinterpret_cast<const uint64_t*>(&smE[(c0 + c) * kInvPitch + r0 + 2 * p]);
   const bool live = r0 < Dq && c0 < Dq;  // tiles beyond the padded size hold nothing
   // Buffer b of step k is rewritten at step k + 2, after its barriers, which
@@ -326,7 +328,7 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
     if (live) {
       // Pivot columns: the tile's columns 4 g .. 4 g + 3 when c0 + 4 g = k0.
 #pragma unroll
-      for (int g = 0; g < kInvTile / 4; ++g)
+      for (int g = 0; g < kInvTileC / 4; ++g)
         if (c0 + 4 * g == k0) {
 #pragma unroll
           for (int p = 0; p < kInvPairs; ++p) {
@@ -343,12 +345,12 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
       // Pivot rows: the tile's rows 4 g .. 4 g + 3 (pairs 2 g, 2 g + 1) when
       // r0 + 4 g = k0.  Their entries in the pivot columns are not read.
 #pragma unroll
-      for (int g = 0; g < kInvTile / 4; ++g)
+      for (int g = 0; g < kInvTileR / 4; ++g)
         if (r0 + 4 * g == k0) {
 #pragma unroll
           for (int q = 0; q < 2; ++q)
 #pragma unroll
-            for (int c = 0; c < kInvTile; c += 4) {
+            for (int c = 0; c < kInvTileC; c += 4) {
               float l[4], h[4];
 #pragma unroll
               for (int x = 0; x < 4; ++x) {
@@ -409,7 +411,7 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
 #pragma unroll
       for (int y = 0; y < 4; ++y) cnp[p][y] = *reinterpret_cast<const uint64_t*>(&cnS[b][y][r0 + 2 * p]);
 #pragma unroll
-    for (int c = 0; c < kInvTile; ++c) {
+    for (int c = 0; c < kInvTileC; ++c) {
       const int sl = inv_rn_slot(c0 + c);
       const ulonglong2 ra = rnA[b][sl], rb = rnB[b][sl];
 #pragma unroll
@@ -428,7 +430,7 @@ static __global__ void __launch_bounds__(kInvThreads, 1) coarse_invert_kernel(Co
 #pragma unroll
   for (int p = 0; p < kInvPairs; ++p)
 #pragma unroll
-    for (int c = 0; c < kInvTile; ++c)
+    for (int c = 0; c < kInvTileC; ++c)
       *reinterpret_cast<uint64_t*>(&smE[(c0 + c) * kInvPitch + r0 + 2 * p]) = a2[p][c];
   __syncthreads();
   float* Im = A.Einv + A.model_eoff[m];
