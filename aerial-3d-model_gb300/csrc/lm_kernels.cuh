@@ -808,8 +808,7 @@ __device__ __forceinline__ void point_mixed_finish(
   if (pf_local)
 #pragma unroll
     for (int i = 0; i < 9; ++i) pf_local[i] = pfv[i];
-  const float l00 = (float)L[0], l10 = (float)L[1], l11 = (float)L[2], l20 = (float)L[3],
-              l21 = (float)L[4], l22 = (float)L[5];
+  const float l00 = pfv[0], l10 = pfv[1], l11 = pfv[2], l20 = pfv[3], l21 = pfv[4], l22 = pfv[5];
   for (uint32_t j = l0; j < l1; ++j) {  // lens entries (ba.rs:251-259)
     if (j > l0) {
 #pragma unroll
