@@ -514,7 +514,9 @@ constexpr double kMixedCondLimit = 1e4;
 // exact point step of the Jacobians the Schur factors are formed from (FP32
 // rounding of the records would be amplified by V^-1).  Z and the gradient
 // shares are rounded to FP32 once.  About 0.4 % of the points of a converging
-// survey take this path.
+// survey take this path.  kZ false: the Schur factors are not stored (the
+// matrix-free PCG recomputes them where it uses them).
+template <bool kZ>
 static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const StateView& st,
                                                            const StructView& S,
                                                            const IterBufs<float>& B, int64_t p,
@@ -547,7 +549,8 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
   B.kept[p] = ok ? 2 : 0;
   if (!ok) {
     for (uint32_t k = s; k < e; ++k) {
-      for (int i = 0; i < 18; ++i) B.Z[z_index(B.zpos, k) * B.zpitch + i] = 0.0f;
+      if constexpr (kZ)
+        for (int i = 0; i < 18; ++i) B.Z[z_index(B.zpos, k) * B.zpitch + i] = 0.0f;
       for (int i = 0; i < 9; ++i) B.gsub[(size_t)k * 9 + i] = 0.0f;
     }
     for (uint32_t j = S.lens_ptr[p]; j < S.lens_ptr[p + 1]; ++j)
@@ -564,12 +567,13 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
   B.ptzv[3 * p] = zv0, B.ptzv[3 * p + 1] = zv1, B.ptzv[3 * p + 2] = zv2;
   const uint32_t l0 = S.lens_ptr[p], l1 = S.lens_ptr[p + 1];
   for (uint32_t k = s; k < e; ++k) {
-    float* Z = B.Z + z_index(B.zpos, k) * B.zpitch;
+    float* Z = kZ ? B.Z + z_index(B.zpos, k) * B.zpitch : nullptr;
     float* gs = B.gsub + (size_t)k * 9;
     double o[kLinW];
     if (!linearise<double>(P, st, k, sg, refine, o)) {
+      if constexpr (kZ)
 #pragma unroll
-      for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
+        for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
 #pragma unroll
       for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
       continue;
@@ -584,9 +588,11 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
       const double y0 = (ca * j0 + cb * j3) * w;
       const double y1 = (ca * j1 + cb * j4) * w;
       const double y2 = (ca * j2 + cb * j5) * w;
-      Z[3 * r + 0] = (float)(y0 * L[0] + y1 * L[1] + y2 * L[3]);
-      Z[3 * r + 1] = (float)(y1 * L[2] + y2 * L[4]);
-      Z[3 * r + 2] = (float)(y2 * L[5]);
+      if constexpr (kZ) {
+        Z[3 * r + 0] = (float)(y0 * L[0] + y1 * L[1] + y2 * L[3]);
+        Z[3 * r + 1] = (float)(y1 * L[2] + y2 * L[4]);
+        Z[3 * r + 2] = (float)(y2 * L[5]);
+      }
       gs[r] = (float)(ca * r0 + cb * r1);
     }
 #pragma unroll
@@ -770,7 +776,10 @@ __device__ __forceinline__ void point_mixed_finish(
   const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
   const double tr = A[0] + A[4] + A[8];
   if (!(det > 0.0) || tr * tr * tr > 4.0 * kMixedCondLimit * det) {
-    point_system_mixed_ill(P, st, S, B, p, refine, sigma[m], lam);
+    if (B.Z)
+      point_system_mixed_ill<true>(P, st, S, B, p, refine, sigma[m], lam);
+    else
+      point_system_mixed_ill<false>(P, st, S, B, p, refine, sigma[m], lam);
     return;
   }
   double Ai[9];
@@ -1000,7 +1009,7 @@ static __global__ void __launch_bounds__(kObsThreads)
       for (int i = 0; i < 18; ++i) z[i] = Z[i];
       store_Z24(B.Z + (size_t)B.zpos[k] * B.zpitch, z);
     }
-  } else {
+  } else if (B.Z) {
     warp_store_records<18>(smz[warp], kZPitch, B.Z + k0 * 18, n, mask, lane);
   }
   warp_store_records<9>(smg[warp], kGPitch, B.gsub + k0 * 9, n, mask, lane);
@@ -1225,10 +1234,11 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
         for (int i = 0; i < 9; ++i) stgs[lane * kGPitch + i] = gs[i];
       }
       __syncwarp();
-      if (!B.zpos) warp_store_records<18>(stz, kZPitch, B.Z + (size_t)(o_lo + j0) * 18, nw, mask, lane);
+      if (!B.zpos && B.Z)
+        warp_store_records<18>(stz, kZPitch, B.Z + (size_t)(o_lo + j0) * 18, nw, mask, lane);
       warp_store_records<9>(stgs, kGPitch, B.gsub + (size_t)(o_lo + j0) * 9, nw, mask, lane);
     } else if (mine) {
-      if (!B.zpos)
+      if (!B.zpos && B.Z)
 #pragma unroll
         for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = Z[i];
 #pragma unroll
@@ -2004,17 +2014,100 @@ __global__ void update_cameras_kernel(Prob P, StateView cur, StateView trial, It
   }
 }
 
+// Mixed form, J^T J recomputed where it is used (the matrix-free PCG with
+// nothing of size (observations x factor) stored, the Schur factors' other
+// readers): observation k's factor Z_k = Y_k L_p, Y_k = w Jc^T Jp, from its
+// stored FP32 record and its point's FP32 L (kept points), or from an FP64
+// re-linearisation at the current state and the point's FP64 L (points with
+// kept == 2).  The arithmetic of obs_factor_kernel and point_system_mixed_ill,
+// so the values are those the factor passes store.
+static __device__ __noinline__ void z_of_obs_ill(const Prob& P, const StateView& st,
+                                                 const double* ptL, const double* sigma,
+                                                 int64_t k, uint32_t p, float* z) {
+  const uint32_t m = P.pt_model[p];
+  double o[kLinW];
+  if (!linearise<double>(P, st, k, sigma[m], P.model_refine[m] != 0, o)) {
+#pragma unroll
+    for (int i = 0; i < 18; ++i) z[i] = 0.0f;
+    return;
+  }
+  const double* L = ptL + 6 * (size_t)p;
+  const double w = o[26];
+  const double j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    const double ca = o[r], cb = o[6 + r];
+    const double y0 = (ca * j0 + cb * j3) * w;
+    const double y1 = (ca * j1 + cb * j4) * w;
+    const double y2 = (ca * j2 + cb * j5) * w;
+    z[3 * r + 0] = (float)(y0 * L[0] + y1 * L[1] + y2 * L[3]);
+    z[3 * r + 1] = (float)(y1 * L[2] + y2 * L[4]);
+    z[3 * r + 2] = (float)(y2 * L[5]);
+  }
+}
+
+struct ZSource {
+  Prob P;
+  StateView st;         // the current state (ill-conditioned points)
+  const float* lin;     // [no][kLinW] records
+  const float* ptf;     // [np][9] FP32 L | t
+  const double* ptL;    // [np][6] FP64 L
+  const uint8_t* kept;  // [np]
+  const double* sigma;  // [nm]
+};
+
+__device__ __forceinline__ void z_of_obs(const ZSource& Q, int64_t k, uint32_t p, float* z) {
+  const uint32_t kp = Q.kept[p];
+  if (kp == 2) {
+    z_of_obs_ill(Q.P, Q.st, Q.ptL, Q.sigma, k, p, z);
+    return;
+  }
+  const float* o = Q.lin + (size_t)k * kLinW;
+  const float2 wv = *reinterpret_cast<const float2*>(o + 26);  // w, valid
+  if (kp == 0 || wv.y == 0.0f) {
+#pragma unroll
+    for (int i = 0; i < 18; ++i) z[i] = 0.0f;
+    return;
+  }
+  float j[20];
+  const float4* o4 = reinterpret_cast<const float4*>(o);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const float4 q = o4[i];
+    j[4 * i] = q.x, j[4 * i + 1] = q.y, j[4 * i + 2] = q.z, j[4 * i + 3] = q.w;
+  }
+  const float* pf = Q.ptf + 9 * (size_t)p;
+  const float l00 = pf[0], l10 = pf[1], l11 = pf[2], l20 = pf[3], l21 = pf[4], l22 = pf[5];
+  const float w = wv.x;
+  const float j0 = j[12], j1 = j[13], j2 = j[14], j3 = j[15], j4 = j[16], j5 = j[17];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    const float ca = j[r], cb = j[6 + r];
+    const float y0 = (ca * j0 + cb * j3) * w;
+    const float y1 = (ca * j1 + cb * j4) * w;
+    const float y2 = (ca * j2 + cb * j5) * w;
+    z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
+    z[3 * r + 1] = y1 * l11 + y2 * l21;
+    z[3 * r + 2] = y2 * l22;
+  }
+}
+
 // Mixed form, first pass of the back-substitution: a thread per observation
 // of a kept, well-conditioned point forms u_k = Z_k^T dx of its camera (FP32,
 // coalesced; the per-point pass then sums the point's u_k in order).
+// kRecompute: the factors are not stored (B.Z null) but recomputed from zsrc.
+template <bool kRecompute>
 static __global__ void __launch_bounds__(256)
-    obs_backsub_kernel(Prob P, IterBufs<float> B, float* obs_u, const int32_t* active) {
+    obs_backsub_kernel(Prob P, IterBufs<float> B, float* obs_u, const int32_t* active,
+                       ZSource zsrc) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= P.no) return;
   const uint32_t p = P.obs_pt[k];
   if (!active[P.pt_model[p]] || B.kept[p] != 1) return;
   float z[18];
-  if (B.zpitch == 24)
+  if (kRecompute)
+    z_of_obs(zsrc, k, p, z);
+  else if (B.zpitch == 24)
     load_Z24(B.Z + z_index(B.zpos, k) * 24, z);
   else
     load_Z18(B.Z + z_index(B.zpos, k) * B.zpitch, z);

@@ -1,11 +1,15 @@
 // Matrix-free block-Jacobi PCG (ba.rs:155-196) for one model whose reduced
 // matrix is not formed.  The product with the reduced camera system
 //     S p = A p - sum over points of E_p^T (E_p p)
-// is applied from the per-observation Schur factors Z_k = Y_k L_p stored by
-// the point kernel (E_p stacks the point's Z_k^T and its lens entries'
-// factors), the cameras' own blocks A_c (damped U_c with priors) and their
-// camera-lens blocks X_c, and the lens block A_g.  Nothing of size
-// (camera pairs) is stored: no pair list, no Schur sums, no S.
+// is applied from the per-observation Schur factors Z_k = Y_k L_p (E_p stacks
+// the point's Z_k^T and its lens entries' factors), the cameras' own blocks
+// A_c (damped U_c with priors) and their camera-lens blocks X_c, and the lens
+// block A_g.  Nothing of size (camera pairs) is stored: no pair list, no
+// Schur sums, no S.  The factors are either stored by the point kernels
+// (Z non-null) or, in the mixed form's J^T J-recompute mode (Z null),
+// recomputed in every product from the stored FP32 Jacobians and the
+// points' factors (z_of_obs), so nothing of size (observations x factor) is
+// stored either.
 //
 // One persistent cooperative launch per LM iteration; the CTAs form one
 // group.  An iteration has four phases separated by group exchanges:
@@ -35,7 +39,7 @@ struct ImpArgs {
   // problem and per-iteration buffers
   Prob P;
   StructView SV;
-  const R* Z;        // [no][18]
+  const R* Z;        // [no][18], or null: recomputed (mixed form, from zsrc)
   const R* Zl;       // [nl][9]
   const uint8_t* kept;
   const R* own;      // [nb][36]: A_c (cameras) / A_g (lens row)
@@ -55,7 +59,18 @@ struct ImpArgs {
   double tol;
   long long spin;  // spin limit of a group wait, in SM clock cycles
   const int32_t* cap = nullptr;  // [1] or null: iteration cap of the model (below max_iter)
+  ZSource zsrc{};                 // the factors' source when Z is null
 };
+
+// Observation k's Schur factor: stored, or recomputed (kRecompute: the
+// mixed form with Z null).
+template <bool kRecompute, typename R>
+__device__ __forceinline__ void imp_factor(const ImpArgs<R>& A, int64_t k, uint32_t p, R* zk) {
+  if constexpr (kRecompute && sizeof(R) == 4)
+    z_of_obs(A.zsrc, k, p, zk);
+  else
+    load_Z18(A.Z + 18 * (size_t)k, zk);
+}
 
 // Implicit-product scalars, computed once per CTA by thread 0.
 template <typename R>
@@ -65,7 +80,7 @@ struct ImpScalars {
   int stop;
 };
 
-template <typename R>
+template <typename R, bool kRecompute>
 __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A) {
   __shared__ double wsm[kPcgWarps * 4];
   __shared__ double tot[4];
@@ -136,7 +151,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
         for (uint32_t k = A.SV.pt_ptr[pt]; k < A.SV.pt_ptr[pt + 1]; ++k) {
           const uint32_t cb = A.P.cam_blk[A.P.obs_cam[k]];
           R zk[18], pv[6];
-          load_Z18(A.Z + 18 * (size_t)k, zk);
+          imp_factor<kRecompute>(A, k, (uint32_t)pt, zk);
 #pragma unroll
           for (int i = 0; i < 6; ++i) pv[i] = __ldcg(pcur + 6 * (size_t)cb + i);
 #pragma unroll
@@ -183,9 +198,10 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_implicit_kernel(ImpArgs<R> A)
       R acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       for (uint32_t i = A.SV.cam_ptr[c] + threadIdx.x; i < A.SV.cam_ptr[c + 1]; i += blockDim.x) {
         const uint32_t k = A.SV.cam_obs[i];
+        const uint32_t pk = A.P.obs_pt[k];
         R zk[18];
-        load_Z18(A.Z + 18 * (size_t)k, zk);
-        const R* tp = A.t + 3 * (size_t)A.P.obs_pt[k];
+        imp_factor<kRecompute>(A, k, pk, zk);
+        const R* tp = A.t + 3 * (size_t)pk;
         const R u0 = __ldcg(tp), u1 = __ldcg(tp + 1), u2 = __ldcg(tp + 2);
 #pragma unroll
         for (int r = 0; r < 6; ++r) acc[r] -= zk[3 * r] * u0 + zk[3 * r + 1] * u1 + zk[3 * r + 2] * u2;
@@ -314,10 +330,12 @@ __global__ void lens_diag_kernel(StructView S, IterBufs<R> B, double* lens_part)
     for (int i = 0; i < 9; ++i) lens_part[9 * ch + i] = s[i];
 }
 
+// Z null: the factors recomputed from zsrc (mixed form).
 template <typename R>
 __global__ void implicit_blocks_kernel(Prob P, StateView st, StructView S, IterBufs<R> B,
                                        const R* Z, R* own, const int32_t* active,
-                                       const double* lambda, const double* lens_part) {
+                                       const double* lambda, const double* lens_part,
+                                       ZSource zsrc) {
   __shared__ double red[36 * 32];
   const int64_t b = blockIdx.x;
   if (b >= P.nb) return;
@@ -331,7 +349,11 @@ __global__ void implicit_blocks_kernel(Prob P, StateView st, StructView S, IterB
   for (int i = 0; i < 36; ++i) s[i] = 0.0;
   if (!lens_b) {
     for (uint32_t i = S.cam_ptr[id] + threadIdx.x; i < S.cam_ptr[id + 1]; i += blockDim.x) {
-      const R* Zk = Z + 18 * (size_t)S.cam_obs[i];
+      const uint32_t k = S.cam_obs[i];
+      R zr[18];
+      const R* Zk = Z ? Z + 18 * (size_t)k : zr;
+      if constexpr (sizeof(R) == 4)
+        if (!Z) z_of_obs(zsrc, k, P.obs_pt[k], zr);
 #pragma unroll
       for (int r = 0; r < 6; ++r)
 #pragma unroll

@@ -464,6 +464,10 @@ struct LmEngine {
   // Per model: 1 if the stored records are not at the current state (the
   // trial cost forms the trial state's records; see cost_record_kernel).
   DevBuf<int32_t> rec_stale;
+  // Mixed form, J^T J recomputed in the matrix-free PCG (no Schur factors
+  // stored): where the factors are recomputed from.
+  bool z_recompute = false;
+  ZSource zsrc{};
   DevBuf<double> camU, camgj, camgs, camX, caml, grpU, grpg, cost_part;
   IterBufs<R> B{};
   DevBuf<double> lambda, cost, new_cost, rms, sq, sigma;
@@ -586,10 +590,14 @@ struct LmEngine {
     // auto mode when the explicit layout would exceed the memory cap.  One
     // model with at most one lens group.
     const bool mf_ok = nm == 1 && ng <= 1;
-    if (o.matrix_free == 2 && !mf_ok)
+    const bool mf_forced = o.matrix_free == 2 || o.matrix_free == 3;
+    if (mf_forced && !mf_ok)
       throw CudaError(cudaErrorNotSupported,
                       "matrix-free PCG: one model with at most one lens group per call");
-    const int64_t cap = o.matrix_free == 2 ? 0
+    if (o.matrix_free == 3 && sizeof(R) == 8)
+      throw CudaError(cudaErrorNotSupported,
+                      "J^T J recompute in the PCG: the mixed form (FP32 Jacobians) only");
+    const int64_t cap = mf_forced ? 0
                         : (o.matrix_free == 0 && mf_ok && o.memory_cap > 0) ? o.memory_cap
                                                                             : -1;
     // Mixed form: Schur factors stored camera-major (the Schur kernel's
@@ -603,13 +611,17 @@ struct LmEngine {
     SV = SB.view();
     ctx.last_nz = SB.nz, ctx.last_pairs = SB.npairs - nb, ctx.last_nl = SB.nl;
     lin.alloc(at_least_1(no) * kLinW, s), gsub.alloc(at_least_1(no) * 9, s);
-    // 16 bytes of padding: FP32 records are read as 16-byte vectors from the
-    // 16-byte boundary at or below each 72-byte record.
     // Schur factors: 24 values per record when stored camera-major (the
     // mixed form with a pair list), else 18; 4 values of padding after the
-    // last record for the 16-byte loads of 18-value FP32 records.
+    // last record for the 16-byte loads of 18-value FP32 records.  The mixed
+    // form's J^T J-recompute mode stores none (they are recomputed where used).
     const bool z24 = sizeof(R) == 4 && SB.z_by_camera;
-    Z.alloc(at_least_1(no) * (z24 ? 24 : 18) + 4, s), Zl.alloc(at_least_1(SB.nl) * 9, s);
+    z_recompute = sizeof(R) == 4 && implicit && o.matrix_free == 3;
+    if (z_recompute)
+      Z.release();
+    else
+      Z.alloc(at_least_1(no) * (z24 ? 24 : 18) + 4, s);
+    Zl.alloc(at_least_1(SB.nl) * 9, s);
     ptL.alloc(at_least_1(np) * 6, s), ptzv.alloc(at_least_1(np) * 3, s);
     kept.alloc(at_least_1(np), s);
     camU.alloc(at_least_1(nc) * 21, s), camgj.alloc(at_least_1(nc) * 6, s);
@@ -640,8 +652,11 @@ struct LmEngine {
                     grpU, grpg, part, S, pre, g, x, cost_part, ptf.p};
     B.zpos = sizeof(R) == 4 && SB.z_by_camera ? SB.cam_pos.p : nullptr;
     B.zpitch = B.zpos ? 24 : 18;
+    B.Z = z_recompute ? nullptr : Z.p;
     lambda.alloc(nm, s), cost.alloc(nm, s), new_cost.alloc(nm, s), rms.alloc(nm, s);
     sq.alloc(nm, s), sigma.alloc(nm, s), n_front.alloc(nm, s), pcg_total.alloc(nm, s);
+    if constexpr (sizeof(R) == 4)
+      zsrc = ZSource{P, ctx.cur(), lin.p, ptf.p, ptL.p, kept.p, sigma.p};
     active.alloc(nm, s), accepted.alloc(nm, s), iters.alloc(nm, s), pcg_iters.alloc(nm, s);
     any.alloc(1, s);
     log_cap = o.log ? std::max(0, o.log->cap) : 0;
@@ -838,6 +853,11 @@ struct LmEngine {
     check(cudaStreamSynchronize(s), "sync");
   }
 
+  // The matrix-free PCG kernel: Schur factors stored or recomputed.
+  void (*implicit_kernel())(ImpArgs<R>) {
+    return z_recompute ? pcg_implicit_kernel<R, true> : pcg_implicit_kernel<R, false>;
+  }
+
   // Matrix-free PCG: one cooperative launch over every SM, one group.
   void setup_implicit() {
     join_coarse();
@@ -845,17 +865,17 @@ struct LmEngine {
     use_coarse = false;
     ctx.last_coarse_dim = 0;
     int occ = 0;
-    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg_implicit_kernel<R>, kPcgThreads,
-                                                        0),
+    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, implicit_kernel(), kPcgThreads, 0),
           "occupancy");
     imp_ncta = std::min(std::max(1, occ) * ctx.n_sm, kMaxGroupCtas);
     bar.zero();
     bar_base.zero();
     pcg_part.alloc(kParts * (size_t)imp_ncta, s);
-    ia = ImpArgs<R>{bar, bar_base, pcg_part, imp_ncta, ctx.err, P, SV, Z, Zl, kept, own, camX,
+    ia = ImpArgs<R>{bar, bar_base, pcg_part, imp_ncta, ctx.err, P, SV, B.Z, Zl, kept, own, camX,
                     pre, g, x, rbuf, z, p, qbuf, tbuf, h_lens[0], (int32_t)ctx.nb, pcg_iters,
                     pcg_limit, o.pcg_tol, o.wait_limit};
     ia.cap = pcg_cap;
+    ia.zsrc = zsrc;
     ctx.last_pcg_kernel = 3, ctx.last_pcg_cluster = 0, ctx.last_pcg_ctas = imp_ncta;
     ctx.last_pcg_threads = kPcgThreads;
   }
@@ -1246,9 +1266,8 @@ struct LmEngine {
     if (implicit) {
       T.mark(BA_PHASE_SCHUR);
       BA_LAUNCH(lens_diag_kernel<R><<<kLensChunks, 256, 0, s>>>(SV, B, lens_part));
-      BA_LAUNCH(implicit_blocks_kernel<R><<<(unsigned)ctx.nb, 256, 0, s>>>(P, cur, SV, B, Z, own,
-                                                                          active, lambda,
-                                                                          lens_part));
+      BA_LAUNCH(implicit_blocks_kernel<R><<<(unsigned)ctx.nb, 256, 0, s>>>(
+          P, cur, SV, B, B.Z, own, active, lambda, lens_part, zsrc));
       BA_LAUNCH(rhs_kernel<R><<<grid_for(ctx.nb * 6, 256), 256, 0, s>>>(P, cur, B, active));
       T.mark(BA_PHASE_ASSEMBLE);
       return;
@@ -1272,7 +1291,7 @@ struct LmEngine {
   void solve_pcg() {
     if (implicit) {
       void* args[] = {&ia};
-      check(cudaLaunchCooperativeKernel((void*)pcg_implicit_kernel<R>, dim3(imp_ncta),
+      check(cudaLaunchCooperativeKernel((void*)implicit_kernel(), dim3(imp_ncta),
                                         dim3(kPcgThreads), args, 0, s),
             "pcg launch");
     } else if (use_cluster) {
@@ -1315,7 +1334,14 @@ struct LmEngine {
         P, cur, tri, B, active));
     if constexpr (sizeof(R) == 4) {
       if (ctx.no > 0)
-        BA_LAUNCH(obs_backsub_kernel<<<grid_for(ctx.no, 256), 256, 0, s>>>(P, B, obs_u.p, active));
+      {
+        if (z_recompute)
+          BA_LAUNCH(obs_backsub_kernel<true><<<grid_for(ctx.no, 256), 256, 0, s>>>(
+              P, B, obs_u.p, active, zsrc));
+        else
+          BA_LAUNCH(obs_backsub_kernel<false><<<grid_for(ctx.no, 256), 256, 0, s>>>(
+              P, B, obs_u.p, active, zsrc));
+      }
     }
     BA_LAUNCH(backsub_kernel<R><<<grid_for(ctx.np, 256), 256, 0, s>>>(P, SV, cur, tri, B, sigma,
                                                                      active, obs_u.p));

@@ -247,7 +247,7 @@ Opts resolve_options(const ba_options* o) {
   if (!(r.sigma > 0.0) || !std::isfinite(r.sigma)) throw BadInput("sigma_px must be finite and > 0");
   if (r.loss != 0 && r.loss != 1) throw BadInput("unknown loss");
   if (r.precision != 0 && r.precision != 1) throw BadInput("unknown precision");
-  if (r.matrix_free < 0 || r.matrix_free > 2) throw BadInput("unknown matrix_free mode");
+  if (r.matrix_free < 0 || r.matrix_free > 3) throw BadInput("unknown matrix_free mode");
   if (r.pcg_kernel < 0 || r.pcg_kernel > 3) throw BadInput("unknown pcg_kernel");
   if (r.stop_patience < 0) throw BadInput("stop_patience must be >= 0");
   if (r.coarse != 0 && r.coarse != 1) throw BadInput("coarse must be 0 or 1");

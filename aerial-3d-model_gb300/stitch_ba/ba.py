@@ -33,7 +33,8 @@ class Options:
     precision: str = "fp64"       # "fp64" | "mixed"
     pcg_max_iter: int = 400
     pcg_tol: float = 1e-20
-    matrix_free: str = "auto"     # "auto" | "stored" | "matrix_free"
+    matrix_free: str = "auto"     # "auto" | "stored" | "matrix_free" | "recompute" (mixed form:
+                                  # matrix-free with J^T J recomputed in the PCG)
     memory_cap_bytes: int = 0
     stream: int | None = None     # cudaStream_t as an integer handle
     profile: bool = False         # per-phase CUDA-event timing (SolveInfo.phases)
@@ -90,7 +91,7 @@ class SolveInfo:
         return BaStats(self.iterations, self.initial_rms, self.final_rms)
 
 
-_MF = {"auto": 0, "stored": 1, "matrix_free": 2}
+_MF = {"auto": 0, "stored": 1, "matrix_free": 2, "recompute": 3}
 
 
 def _c_options(max_iter: int, sigma_px: float, o: Options | None, log=None) -> native.BaOptions:

@@ -195,7 +195,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-MIXED_MATRIX_FREE = False  # --matrix-free: the mixed form applies S without forming it
+# --matrix-free: the mixed form applies S without forming it ("recompute" with
+# --jtj-recompute: J^T J recomputed in the PCG, no Schur factors stored)
+MIXED_MATRIX_FREE = False
 MIXED_PCG_CAP = MIXED_PCG_ITERS  # set per workload by set_mixed_cap
 
 
@@ -216,7 +218,8 @@ def form_options(form: str, **kw):
         kw.setdefault("point_kernel", POINT_KERNEL)
         kw.setdefault("pcg_kernel", PCG_KERNEL)
     if form == "mixed":
-        mf = "matrix_free" if MIXED_MATRIX_FREE else "auto"
+        mf = ("recompute" if MIXED_MATRIX_FREE == "recompute"
+              else "matrix_free" if MIXED_MATRIX_FREE else "auto")
         kw.setdefault("coarse", not MIXED_MATRIX_FREE)
         kw.setdefault("stop_patience", MIXED_STOP_PATIENCE)
         if MIXED_END_PCG_ITERS > 0:
@@ -711,7 +714,10 @@ def main():
     ap.add_argument("--stage", default="ba",
                     choices=["ba", "triangulate", "ransac", "pair_fits", "summary"])
     ap.add_argument("--matrix-free", action="store_true",
-                    help="mixed form: S-free PCG (S p from per-observation factors)")
+                    help="mixed form: S p applied from the stored Schur factors, S not formed")
+    ap.add_argument("--jtj-recompute", action="store_true",
+                    help="mixed form: matrix-free with J^T J recomputed in every PCG product "
+                         "from the stored FP32 Jacobians (no Schur factors stored)")
     ap.add_argument("--mixed-patience", type=int, default=0,
                     help="mixed forms: consecutive small decreases before stopping (0: default)")
     ap.add_argument("--mixed-end-iters", type=int, default=-1,
@@ -731,7 +737,7 @@ def main():
     N_POINTS = args.n_points
     POINT_KERNEL = args.point_kernel
     PCG_KERNEL = args.pcg_kernel
-    MIXED_MATRIX_FREE = args.matrix_free
+    MIXED_MATRIX_FREE = "recompute" if args.jtj_recompute else args.matrix_free
     if args.mixed_patience > 0:
         MIXED_STOP_PATIENCE = args.mixed_patience
     if args.mixed_end_iters >= 0:

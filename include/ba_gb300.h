@@ -104,7 +104,10 @@ typedef struct ba_options {
   double pcg_tol;       /* <=0: 1e-20, on |r|^2 / |b|^2 (ba.rs:182)        */
   int32_t matrix_free;  /* 0: auto (by memory cap), 1: stored S, 2: matrix-free
                            (S p applied from the per-observation Schur factors;
-                           one model with at most one lens group)          */
+                           one model with at most one lens group), 3: the same
+                           with J^T J recomputed in every product from the
+                           stored FP32 Jacobians (mixed form; no Schur factors
+                           stored; the results of mode 2)                  */
   int64_t memory_cap_bytes; /* auto mode: go matrix-free when the Schur pair list
                            and reduced matrix would exceed this (<=0: no cap) */
   void* stream;         /* cudaStream_t to run on, NULL: the library's own */

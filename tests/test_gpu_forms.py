@@ -292,3 +292,25 @@ def test_autotuner_picks_a_point_pass_variant():
     p, _ = survey.generate("lawnmower77", seed=4, n_cams=24, n_points=8000)
     _, _, t = solve(p, Options(precision="mixed", autotune=True), sigma=1.0)
     assert t.point_kernel in ("three_pass", "fused128", "fused256") and t.point_tuned_us > 0.0
+
+
+def test_jtj_recompute_matches_stored_factors_bit_for_bit():
+    """Matrix-free PCG with J^T J recomputed in every product (mixed form):
+    each observation's Schur factor is formed from its stored FP32 Jacobians
+    and its point's factor with the arithmetic of the factor pass, so a whole
+    solve gives the results of the stored-factor mode bit for bit while
+    holding no per-observation factors."""
+    p, _ = survey.generate("lawnmower77", seed=4, n_cams=30, n_points=6000)
+    qa, _, a = solve(p, Options(precision="mixed", matrix_free="matrix_free", pcg_max_iter=60),
+                     sigma=1.0)
+    qb, _, b = solve(p, Options(precision="mixed", matrix_free="recompute", pcg_max_iter=60),
+                     sigma=1.0)
+    assert a.pcg_kernel == b.pcg_kernel == "matrix_free"
+    assert a.iterations == b.iterations and a.final_cost == b.final_cost
+    for x, y in ((qa.points, qb.points), (qa.center, qb.center), (qa.rot, qb.rot),
+                 (qa.intr, qb.intr)):
+        assert np.array_equal(x, y)
+    # the factors (72 bytes per observation) are not held
+    assert b.device_bytes <= a.device_bytes - 60 * p.n_obs
+    with pytest.raises(RuntimeError, match="mixed form"):
+        solve(p, Options(precision="fp64", matrix_free="recompute"), sigma=1.0)
