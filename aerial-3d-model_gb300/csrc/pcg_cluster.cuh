@@ -21,8 +21,10 @@
 // vector of the next residual, w = W^T r_{k+1}, is formed as W^T r_k −
 // α W^T q_k from group sums every CTA publishes before the iteration's first
 // barrier (α is known right after it), so an iteration still needs only two
-// cluster reductions: p·q (then α, the coarse gather and c = E^-1 w), and
-// r·r with r·z (then β).
+// cluster reductions: p·q (then α), and r·r with r·z (then β).  The coarse
+// step c = E^-1 w is split as E^-1 W^T r_k − α E^-1 W^T q_k: its two halves
+// run on the warps beside warp 0's reduction of p·q (before and after the
+// barrier), so it adds no CTA barrier to the iteration.
 //
 // Every CTA of a cluster executes the same sequence of cluster barriers:
 // loop exits depend only on reduced scalars, which every CTA computes from
@@ -108,13 +110,14 @@ inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks, uint32_t cap
 }
 
 // Extra shared memory of the two-level form, in floats: per row W (42); per
-// own group its rows of E^-1 (7 x D) and c (7); the model's group sums of
-// W^T r (two buffers by iteration parity: owners push the next one while the
-// current one is read) and of W^T q (D each), pushed by every group's owner.
+// own group its rows of E^-1 (7 x D) and the two halves of c (7 each:
+// E^-1 W^T r and E^-1 W^T q); the model's group sums of W^T r (two buffers by
+// iteration parity: owners push the next one while the current one is read)
+// and of W^T q (D each), pushed by every group's owner.
 constexpr int kCgCoarseRowF = 42;
 __host__ __device__ constexpr size_t cg_coarse_fixed_floats(uint32_t cap_groups,
                                                             uint32_t cap_dim) {
-  return (size_t)cap_groups * (kCoarseModes * cap_dim + kCoarseModes) + 3 * (size_t)cap_dim;
+  return (size_t)cap_groups * (kCoarseModes * cap_dim + 2 * kCoarseModes) + 3 * (size_t)cap_dim;
 }
 inline size_t cg_coarse_smem_bytes(uint32_t cap_rows, uint32_t cap_groups, uint32_t cap_dim) {
   return ((size_t)cap_rows * kCgCoarseRowF + cg_coarse_fixed_floats(cap_groups, cap_dim)) * 4;
@@ -163,7 +166,8 @@ __device__ __forceinline__ DFloat df_shfl_xor(DFloat v, int o) {
 // order, so every CTA sees bit-identical totals.  While warp 0 sums and
 // pushes the CTA's partials, warps 1.. run side(w) with w = warp - 1 (the
 // coarse group sums, which read the same row state after the same CTA
-// barrier).
+// barrier); while warp 0 sums the inbox after the cluster barrier, they run
+// after(w) (coarse work that reads what the barrier published).
 //
 // Exchange by push: before the cluster barrier, lane r of warp 0 stores the
 // CTA's partials into CTA r's inbox (inbox[source rank][value]); after it,
@@ -173,10 +177,10 @@ __device__ __forceinline__ DFloat df_shfl_xor(DFloat v, int o) {
 // release.  Consecutive reductions use different inboxes: a CTA can only
 // write inbox n + 2 after the barrier of reduction n + 1, which every reader
 // of inbox n has passed.
-template <int kWarps, int N, typename Side, typename Post>
+template <int kWarps, int N, typename Side, typename Post, typename After>
 __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&wv)[N],
                                           float* wsm, DFloat (*inbox)[4], DFloat* tot,
-                                          Side&& side, Post&& post) {
+                                          Side&& side, Post&& post, After&& after) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
@@ -221,6 +225,8 @@ __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&
       for (int i = 0; i < N; ++i) tot[i] = v[i];
       post();  // the iteration's scalars, once per CTA
     }
+  } else {
+    after(warp - 1);
   }
   __syncthreads();
 }
@@ -234,40 +240,37 @@ struct CgScalars {
   int stop;
 };
 
-// The coarse step of the two-level form, once every group's sums have been
-// pushed: c = E^-1 w for this CTA's groups (into sc, 7 per group), with the
-// model's w = W^T r − α W^T q (α = 0 and no W^T q at the start: w = W^T b).
-// Ends with a CTA barrier.
-template <int kWarps>
-__device__ __forceinline__ void cg_coarse_solve(const CgArgs& A, int m, int32_t ngr,
-                                                const float* sEi, const float* wr,
-                                                const float* wq, float alpha, float* sc) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int D = kCoarseModes * (A.model_g0[m + 1] - A.model_g0[m]);
-  for (int o = warp; o < ngr * kCoarseModes; o += kWarps) {
-    const float* er = sEi + (size_t)o * A.cap_dim;
-    float v = 0.0f;
-    if (wq)
-      for (int t = lane; t < D; t += 32) v += er[t] * (wr[t] - alpha * wq[t]);
-    else
-      for (int t = lane; t < D; t += 32) v += er[t] * wr[t];
+// One output of the coarse step's halves: out[o] = (E^-1 w)_o for this
+// CTA's (group, mode) output o, w one of the model's group-sum vectors (D
+// floats); a warp, then a fixed butterfly.
+__device__ __forceinline__ void cg_coarse_dot(const float* sEi, uint32_t cap_dim, int D, int o,
+                                              const float* w, float* out) {
+  const int lane = threadIdx.x & 31;
+  const float* er = sEi + (size_t)o * cap_dim;
+  float v = 0.0f;
+  for (int t = lane; t < D; t += 32) v += er[t] * w[t];
 #pragma unroll
-    for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
-    if (lane == 0) sc[o] = v;
-  }
-  __syncthreads();
+  for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
+  if (lane == 0) out[o] = v;
 }
 
-// A row's coarse share of z, (W c)_i for lane i < 6 (rows outside every
-// group, such as the lens row, add nothing).
-__device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const float* sc,
-                                           int ci) {
+// A row's coarse share of z, (W c)_i for lane i < 6, c = cr − α cq (the two
+// halves of the coarse step; cq null at the start: c = cr).  Rows outside
+// every group, such as the lens row, add nothing.
+__device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const float* cr,
+                                           const float* cq, float alpha, int ci) {
   if (lg < 0) return 0.0f;
   const float* w = sWrow + kCoarseModes * ci;
-  const float* c = sc + kCoarseModes * lg;
+  const float* a = cr + kCoarseModes * lg;
   float add = 0.0f;
+  if (cq) {
+    const float* b = cq + kCoarseModes * lg;
 #pragma unroll
-  for (int j = 0; j < kCoarseModes; ++j) add += w[j] * c[j];
+    for (int j = 0; j < kCoarseModes; ++j) add += w[j] * (a[j] - alpha * b[j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < kCoarseModes; ++j) add += w[j] * a[j];
+  }
   return add;
 }
 
@@ -277,27 +280,33 @@ __device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const
 // `w` of kWorkers taking (group, mode) w, w + kWorkers, ...: lane l takes
 // rows l, l + 32, ... (each row's six products in component order), then a
 // fixed butterfly.
+__device__ __forceinline__ void cg_group_sum_push(cgx::cluster_group& cl, int o,
+                                                  const int32_t* grp_row0,
+                                                  const int32_t* grp_row1, int32_t g0,
+                                                  int32_t goff, uint32_t row0, const float* sW,
+                                                  const float* rs, int xoff, float* dst) {
+  const int lane = threadIdx.x & 31;
+  const int csize = (int)cl.num_blocks();
+  const int l = o / kCoarseModes, j = o % kCoarseModes;
+  float v = 0.0f;
+  for (int32_t r = grp_row0[g0 + l] + lane; r < grp_row1[g0 + l]; r += 32) {
+    const float* w = sW + (size_t)(r - row0) * 42 + j;
+    const float* x = rs + (size_t)(r - row0) * kCgRow + xoff;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) v += w[kCoarseModes * i] * x[i];
+  }
+#pragma unroll
+  for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
+  if (lane < csize) cl.map_shared_rank(dst, (unsigned)lane)[goff + o] = v;
+}
 template <int kWorkers>
 __device__ __forceinline__ void cg_group_sums_push(cgx::cluster_group& cl, int w, int32_t ngr,
                                                    const int32_t* grp_row0,
                                                    const int32_t* grp_row1, int32_t g0,
                                                    int32_t goff, uint32_t row0, const float* sW,
                                                    const float* rs, int xoff, float* dst) {
-  const int lane = threadIdx.x & 31;
-  const int csize = (int)cl.num_blocks();
-  for (int o = w; o < ngr * kCoarseModes; o += kWorkers) {
-    const int l = o / kCoarseModes, j = o % kCoarseModes;
-    float v = 0.0f;
-    for (int32_t r = grp_row0[g0 + l] + lane; r < grp_row1[g0 + l]; r += 32) {
-      const float* w = sW + (size_t)(r - row0) * 42 + j;
-      const float* x = rs + (size_t)(r - row0) * kCgRow + xoff;
-#pragma unroll
-      for (int i = 0; i < 6; ++i) v += w[kCoarseModes * i] * x[i];
-    }
-#pragma unroll
-    for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
-    if (lane < csize) cl.map_shared_rank(dst, (unsigned)lane)[goff + o] = v;
-  }
+  for (int o = w; o < ngr * kCoarseModes; o += kWorkers)
+    cg_group_sum_push(cl, o, grp_row0, grp_row1, g0, goff, row0, sW, rs, xoff, dst);
 }
 
 // Push a row's six values (lane i < 6 holds x_i) into the neighbour cache of
@@ -335,8 +344,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
   const uint32_t nblk = A.row_ptr[J.row1] - B0;
   const uint32_t ncached = nblk < A.cap_blocks ? nblk : A.cap_blocks;
   // Shared memory: row state | cached S blocks | neighbour cache | cached
-  // blocks' cache slots | two-level form: W, W^T r and W^T q per row, E^-1
-  // rows and c per own group, the model's group sums of W^T r (two buffers)
+  // blocks' cache slots | two-level form: W per row, E^-1 rows and the two
+  // halves of c per own group, the model's group sums of W^T r (two buffers)
   // and W^T q.
   float* rs = reinterpret_cast<float*>(cg_smem);
   float* sS = rs + (size_t)A.cap_rows * kCgRow;
@@ -345,13 +354,17 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
   float* sW = reinterpret_cast<float*>(sL + A.cap_blocks);
   float* sEi = sW + (size_t)A.cap_rows * 42;
   const size_t gsz = (size_t)A.cap_groups * kCoarseModes;
-  float* scf = sEi + gsz * A.cap_dim;
-  float* wall_r = scf + gsz;                  // [2][D]
+  float* scr = sEi + gsz * A.cap_dim;        // E^-1 W^T r, own outputs
+  float* scq = scr + gsz;                     // E^-1 W^T q
+  float* wall_r = scq + gsz;                  // [2][D]
   float* wall_q = wall_r + 2 * (size_t)A.cap_dim;  // [D]
   const int32_t cg0 = kCoarse ? A.job_g0[blockIdx.x] : 0;
   const int32_t ngr = kCoarse ? A.job_g1[blockIdx.x] - cg0 : 0;
   const int32_t goff = kCoarse ? kCoarseModes * (cg0 - A.model_g0[J.model]) : 0;
   const int32_t lens = A.lens_row[J.model];
+  // the model's coarse dimension and this CTA's coarse outputs (two-level form)
+  const int cD = kCoarse ? kCoarseModes * (A.model_g0[J.model + 1] - A.model_g0[J.model]) : 0;
+  const int nco = kCoarseModes * ngr;
   {
     const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
     float4* dst = reinterpret_cast<float4*>(sS);
@@ -421,7 +434,7 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
   }
   const float w2[2] = {cg_sum8f(drz), cg_sum8f(dbb)};
   // r.z and b.b; the two-level form pushes the group sums of W^T b beside it
-  // (z = B^-1 b + W E^-1 W^T b below)
+  // and forms c = E^-1 W^T b after the barrier (z = B^-1 b + W c below)
   cg_reduce<kCgWarps, 2>(
       cl, w2, wsm, inbox[1], tot,
       [&](int w) {
@@ -434,15 +447,19 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
         sc.b2 = tot[1].hi;
         sc.bf = 0.0f;
         sc.stop = 0;
+      },
+      [&](int w) {
+        if constexpr (kCoarse) {
+          for (int o = w; o < nco; o += kCgWarps - 1) cg_coarse_dot(sEi, A.cap_dim, cD, o, wall_r, scr);
+        }
       });
   if constexpr (kCoarse) {
     // z = B^-1 b + W E^-1 W^T b, and r . z with it.
-    cg_coarse_solve<kCgWarps>(A, J.model, ngr, sEi, wall_r, nullptr, 0.0f, scf);
     float drz0 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
       const int32_t lg = __float_as_int(st[kCgIdx + 3]);
-      const float add = cg_row_wc(sW + (size_t)lr * 42, lg, scf, ci);
+      const float add = cg_row_wc(sW + (size_t)lr * 42, lg, scr, nullptr, 0.0f, ci);
       float zi = 0.0f;
       if (vl) {
         zi = st[kCgZ + ci] + add;
@@ -453,7 +470,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
                   (uint32_t)__float_as_int(st[kCgIdx + 5]), zi, 0);
     }
     const float w1[1] = {cg_sum8f(drz0)};
-    cg_reduce<kCgWarps, 1>(cl, w1, wsm, inbox[2], tot, [](int) {}, [&] { sc.rz = tot[0]; });
+    cg_reduce<kCgWarps, 1>(cl, w1, wsm, inbox[2], tot, [](int) {}, [&] { sc.rz = tot[0]; },
+                           [](int) {});
   } else {
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       const float* st = CGROW(lr);
@@ -541,11 +559,20 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
     const float w4[4] = {cg_sum8f(dpq), __shfl_sync(kFull, dlens, 0), __shfl_sync(kFull, dlens, 1),
                          __shfl_sync(kFull, dlens, 2)};
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
-    // p.q; the two-level form pushes the group sums of W^T q beside it
+    // p.q; the two-level form pushes the group sums of W^T q and forms
+    // E^-1 W^T r beside it, and E^-1 W^T q after the barrier
+    const float* wr_cur = wall_r + (size_t)cur * A.cap_dim;
     cg_reduce<kCgWarps, 4>(cl, w4, wsm, inbox[0], tot, [&](int w) {
-      if constexpr (kCoarse)
-        cg_group_sums_push<kCgWarps - 1>(cl, w, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0,
-                                         sW, rs, kCgQ, wall_q);
+      if constexpr (kCoarse) {
+        for (int t = w; t < 2 * nco; t += kCgWarps - 1) {
+          if (t < nco) {
+            cg_group_sum_push(cl, t, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgQ,
+                              wall_q);
+          } else {
+            cg_coarse_dot(sEi, A.cap_dim, cD, t - nco, wr_cur, scr);
+          }
+        }
+      }
     }, [&] {
       DFloat pq = tot[0];
       if (lens >= 0) {
@@ -562,15 +589,14 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
       // ba.rs:174 breaks on a vanishing p.q; an FP32 quotient needs it normal
       sc.stop = fabsf(pq.hi) < 1.17549435e-38f ? 1 : 0;
       sc.af = sc.stop ? 0.0f : sc.rz.hi / pq.hi;
+    }, [&](int w) {
+      if constexpr (kCoarse) {
+        for (int o = w; o < nco; o += kCgWarps - 1) cg_coarse_dot(sEi, A.cap_dim, cD, o, wall_q, scq);
+      }
     });
     ++spmv;
     if (sc.stop) break;
     const float af = sc.af;
-    // Two-level form: c = E^-1 w for this CTA's groups, with the next
-    // residual's coarse vector w = W^T r − α W^T q from every group's owner.
-    if constexpr (kCoarse)
-      cg_coarse_solve<kCgWarps>(A, J.model, ngr, sEi, wall_r + (size_t)cur * A.cap_dim, wall_q,
-                                af, scf);
     float drr = 0.0f, drz2 = 0.0f;
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
@@ -584,8 +610,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
 #pragma unroll
       for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
       if constexpr (kCoarse) {
-        // z = B^-1 r + W c
-        zi += cg_row_wc(sW + (size_t)lr * 42, __float_as_int(st[kCgIdx + 3]), scf, ci);
+        // z = B^-1 r + W c, c = E^-1 (W^T r − α W^T q) of the next residual
+        zi += cg_row_wc(sW + (size_t)lr * 42, __float_as_int(st[kCgIdx + 3]), scr, scq, af, ci);
       }
       if (vl) {
         st[kCgZ + ci] = zi;
@@ -606,7 +632,7 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
       sc.stop = tot[0].hi < (float)A.tol * sc.b2 ? 1 : 0;  // ba.rs:182
       sc.bf = tot[1].hi / sc.rz.hi;                        // ba.rs:189-190
       sc.rz = tot[1];
-    });
+    }, [](int) {});
     if (sc.stop) break;
   }
   for (uint32_t lr = warp; lr < nrows; lr += kCgWarps)

@@ -80,22 +80,32 @@ void scan_rec(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s) {
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;  // 2048
-constexpr int kRadix = 256;
+// 9-bit digits: the keys sorted here carry up to 18 bits (a destination block
+// a * B + b of a few hundred block rows, a camera or point index), two passes.
+constexpr int kRadixBits = 9;
+constexpr int kRadix = 1 << kRadixBits;  // 512
+constexpr int kPerThread = kRadix / kSortThreads;  // buckets per thread
+static_assert(kRadix % kSortThreads == 0, "whole buckets per thread");
 
 __global__ void __launch_bounds__(kSortThreads)
     radix_hist_kernel(const uint64_t* keys, size_t n, int shift,
                       uint32_t* hist, size_t ntiles) {
   __shared__ uint32_t cnt[kRadix];
-  cnt[threadIdx.x] = 0;
+#pragma unroll
+  for (int j = 0; j < kPerThread; ++j) cnt[threadIdx.x + j * kSortThreads] = 0;
   __syncthreads();
   const size_t base = (size_t)blockIdx.x * kSortTile;
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const size_t i = base + (size_t)r * kSortThreads + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xff], 1u);
+    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & (kRadix - 1)], 1u);
   }
   __syncthreads();
-  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
+#pragma unroll
+  for (int j = 0; j < kPerThread; ++j) {
+    const int d = threadIdx.x + j * kSortThreads;
+    hist[(size_t)d * ntiles + blockIdx.x] = cnt[d];
+  }
 }
 
 // Stable scatter: items of one tile are ranked in index order, 256 at a time.
@@ -107,8 +117,12 @@ __global__ void __launch_bounds__(kSortThreads)
   __shared__ uint32_t base_s[kRadix];
   __shared__ uint32_t wcnt[kSortThreads / 32][kRadix];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  base_s[threadIdx.x] = offs[(size_t)threadIdx.x * ntiles + blockIdx.x];
-  for (int w = 0; w < kSortThreads / 32; ++w) wcnt[w][threadIdx.x] = 0;
+#pragma unroll
+  for (int j = 0; j < kPerThread; ++j) {
+    const int d = threadIdx.x + j * kSortThreads;
+    base_s[d] = offs[(size_t)d * ntiles + blockIdx.x];
+    for (int w = 0; w < kSortThreads / 32; ++w) wcnt[w][d] = 0;
+  }
   __syncthreads();
   const size_t tbase = (size_t)blockIdx.x * kSortTile;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -121,7 +135,7 @@ __global__ void __launch_bounds__(kSortThreads)
     if (valid) {
       k = keys[i];
       v = vals[i];
-      d = (unsigned)((k >> shift) & 0xff);
+      d = (unsigned)((k >> shift) & (kRadix - 1));
     }
     const unsigned peers = __match_any_sync(kFull, d);
     const unsigned rank = __popc(peers & lt_mask);
@@ -137,12 +151,16 @@ __global__ void __launch_bounds__(kSortThreads)
       }
     }
     __syncthreads();
-    uint32_t tot = 0;
-    for (int w = 0; w < kSortThreads / 32; ++w) {
-      tot += wcnt[w][threadIdx.x];
-      wcnt[w][threadIdx.x] = 0;
+#pragma unroll
+    for (int j = 0; j < kPerThread; ++j) {
+      const int b = threadIdx.x + j * kSortThreads;
+      uint32_t tot = 0;
+      for (int w = 0; w < kSortThreads / 32; ++w) {
+        tot += wcnt[w][b];
+        wcnt[w][b] = 0;
+      }
+      base_s[b] += tot;
     }
-    base_s[threadIdx.x] += tot;
     __syncthreads();
   }
 }
@@ -156,7 +174,7 @@ void radix_sort(uint64_t* keys, V* vals, uint64_t* keys_tmp, V* vals_tmp,
   uint64_t *ki = keys, *ko = keys_tmp;
   V *vi = vals, *vo = vals_tmp;
   int passes = 0;
-  for (int shift = 0; shift < bits; shift += 8, ++passes) {
+  for (int shift = 0; shift < bits; shift += kRadixBits, ++passes) {
     BA_LAUNCH(radix_hist_kernel<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ki, n, shift, hist,
                                                                       ntiles));
     scan_rec(hist, hist, ntiles * kRadix, s);
