@@ -83,6 +83,11 @@ __device__ __forceinline__ double robust_rho(double e2, double sigma, int loss) 
   return s2 * log(1.0 + e2 / s2);  // ba.rs:114
 }
 
+// Bits of 1e300 as a signed 64-bit integer: for the Cauchy factors q >= 1 (or
+// NaN) of the cost kernels, q < 1e300 exactly when their bit patterns
+// compare so (an integer compare instead of an FP64 one).
+constexpr long long kQMaxBits = 0x7e37e43c8800759cLL;
+
 // linearise (ba.rs:56-101) of observation k into out[kLinW]; false if the
 // point is not in front of the camera (z <= 1e-6).
 template <typename R>
@@ -97,7 +102,7 @@ __device__ __forceinline__ bool linearise(const Prob& P, const StateView& st, in
   bacam::to_cam(Rm, C, X, xc);
   if (xc[2] <= 1e-6) return false;
   const double f = K[0], k1 = K[3], k2 = K[4];
-  const double iz = 1.0 / xc[2];
+  const double iz = __drcp_rn(xc[2]);  // IEEE 1 / z, as a reciprocal
   const double px = xc[0] * iz, py = xc[1] * iz;
   const double r2 = px * px + py * py;
   const double d = 1.0 + k1 * r2 + k2 * r2 * r2;
@@ -339,7 +344,7 @@ static __device__ __noinline__ void linearise_mixed_extreme(const Prob& P, const
   const double* Rm = st.rot + 9 * (size_t)cam;
   const double* K = st.intr + 5 * (size_t)P.cam_group[cam];
   const double f = K[0], k1 = K[3], k2 = K[4];
-  const double iz = 1.0 / xc[2];
+  const double iz = __drcp_rn(xc[2]);  // IEEE 1 / z, as a reciprocal
   const double px = xc[0] * iz, py = xc[1] * iz;
   const double r2 = px * px + py * py;
   const double d = 1.0 + k1 * r2 + k2 * r2 * r2;
@@ -1489,6 +1494,7 @@ static __global__ void __launch_bounds__(kCostThreads)
   double prod = 1.0;
   int64_t expo = 0;
   double acc[3] = {0.0, 0.0, 0.0};
+  uint32_t nfront = 0;  // in-front count (acc[2], exact in FP64 at the end)
   for (uint32_t k = S.cost_chunk_begin[ch] + threadIdx.x; k < S.cost_chunk_end[ch];
        k += blockDim.x) {
     const uint32_t cam = P.obs_cam[k];
@@ -1497,7 +1503,7 @@ static __global__ void __launch_bounds__(kCostThreads)
     bacam::to_cam(st.rot + 9 * (size_t)cam, st.center + 3 * (size_t)cam,
                   st.points + 3 * (size_t)P.obs_pt[k], xc);
     if (xc[2] > 1e-6) {  // Pose::project (geometry.rs:28-32, 66-72)
-      const double iz = 1.0 / xc[2];
+      const double iz = __drcp_rn(xc[2]);  // IEEE 1 / z, as a reciprocal
       const double px = xc[0] * iz, py = xc[1] * iz;
       const double r2 = px * px + py * py;
       const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
@@ -1506,7 +1512,7 @@ static __global__ void __launch_bounds__(kCostThreads)
       const double e2 = ex * ex + ey * ey;
       if (cauchy) {
         const double q = 1.0 + e2 * inv_s2;  // ba.rs:114
-        if (q < 1.0e300) {
+        if (__double_as_longlong(q) < kQMaxBits) {  // q < 1e300 (q >= 1 or NaN)
           prod *= q;
           const int hi = __double2hiint(prod);
           expo += (hi >> 20) - 1023;
@@ -1518,12 +1524,13 @@ static __global__ void __launch_bounds__(kCostThreads)
         acc[0] += robust_rho(e2, sg, P.loss);
       }
       acc[1] += e2;
-      acc[2] += 1.0;
+      ++nfront;
     } else {
       acc[0] += behind;
     }
   }
   if (cauchy) acc[0] += s2 * (log(prod) + (double)expo * 0.69314718055994530942);
+  acc[2] = (double)nfront;
   block_sum<3>(acc, scratch);
   if (threadIdx.x == 0) {
     part[3 * ch] = acc[0];
@@ -1559,6 +1566,7 @@ static __global__ void __launch_bounds__(kCostThreads)
   double prod = 1.0;  // as cost_chunk_kernel
   int64_t expo = 0;
   double acc[3] = {0.0, 0.0, 0.0};
+  uint32_t nfront = 0;  // in-front count (acc[2], exact in FP64 at the end)
   const uint32_t c1 = S.cost_chunk_end[ch];
   // thread t takes observations begin + t, begin + t + blockDim, ... (the
   // order of cost_chunk_kernel); a warp's 32 records are staged and stored
@@ -1573,7 +1581,7 @@ static __global__ void __launch_bounds__(kCostThreads)
       bacam::to_cam(st.rot + 9 * (size_t)cam, st.center + 3 * (size_t)cam,
                     st.points + 3 * (size_t)P.obs_pt[k], xc);
       if (xc[2] > 1e-6) {  // Pose::project (geometry.rs:28-32, 66-72)
-        const double iz = 1.0 / xc[2];
+        const double iz = __drcp_rn(xc[2]);  // IEEE 1 / z, as a reciprocal
         const double px = xc[0] * iz, py = xc[1] * iz;
         const double r2 = px * px + py * py;
         const double d = 1.0 + K[3] * r2 + K[4] * r2 * r2;
@@ -1583,7 +1591,7 @@ static __global__ void __launch_bounds__(kCostThreads)
         const double e2 = ev[0] * ev[0] + ev[1] * ev[1];
         if (cauchy) {
           const double q = 1.0 + e2 * inv_s2;  // ba.rs:114
-          if (q < 1.0e300) {
+          if (__double_as_longlong(q) < kQMaxBits) {  // q < 1e300 (q >= 1 or NaN)
             prod *= q;
             const int hi = __double2hiint(prod);
             expo += (hi >> 20) - 1023;
@@ -1595,7 +1603,7 @@ static __global__ void __launch_bounds__(kCostThreads)
           acc[0] += robust_rho(e2, sg, P.loss);
         }
         acc[1] += e2;
-        acc[2] += 1.0;
+        ++nfront;
         float jpf[6], wf;
         mixed_record_from(P, st, camf, k, sg, sg_f, inv_s2f, refine, xc, ev, rec, jpf, wf);
       } else {
@@ -1611,6 +1619,7 @@ static __global__ void __launch_bounds__(kCostThreads)
     __syncwarp();
   }
   if (cauchy) acc[0] += s2 * (log(prod) + (double)expo * 0.69314718055994530942);
+  acc[2] = (double)nfront;
   block_sum<3>(acc, scratch);
   if (threadIdx.x == 0) {
     part[3 * ch] = acc[0];
