@@ -74,7 +74,7 @@ __device__ __forceinline__ bool inv3(const double* A, double* Ai) {
   const double c02 = A[3] * A[7] - A[4] * A[6];
   const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
   if (det == 0.0) return false;
-  const double id = 1.0 / det;
+  const double id = __drcp_rn(det);  // IEEE 1 / det
   Ai[0] = c00 * id;
   Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
   Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;

@@ -71,7 +71,7 @@ __device__ __forceinline__ double robust_weight(double e2, double sigma, int los
     const double a = sqrt(e2);
     return a <= sigma ? 1.0 : sigma / a;
   }
-  return 1.0 / (1.0 + e2 / (sigma * sigma));  // ba.rs:99
+  return __drcp_rn(1.0 + e2 / (sigma * sigma));  // ba.rs:99 (IEEE 1 / x)
 }
 
 __device__ __forceinline__ double robust_rho(double e2, double sigma, int loss) {
@@ -789,7 +789,7 @@ __device__ __forceinline__ void point_mixed_finish(
   }
   double Ai[9];
   {
-    const double id = 1.0 / det;
+    const double id = __drcp_rn(det);  // IEEE 1 / det
     Ai[0] = c00 * id;
     Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
     Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
