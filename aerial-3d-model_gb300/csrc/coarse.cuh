@@ -132,6 +132,13 @@ static __global__ void __launch_bounds__(kCoarseMatThreads)
     }
     hi = a0;
   }
+  if (lo == hi) {
+    // No block of row r in group g (most pairs: a camera's blocks lie in a
+    // few groups): P is zero, +0.0 as the products below would give it,
+    // without their FP64 instructions.
+    for (int o = lane; o < kCoarseModes * kCoarseModes; o += 32) P[o] = 0.0;
+    return;
+  }
   // T = sum_k S_k W_col(k) (6 x 7): lane = 7 q + j handles column j of the
   // blocks lo + q, lo + q + 4, ... (q < 4); the four partials are summed in
   // order q = 0..3.

@@ -519,12 +519,15 @@ struct LmEngine {
   int64_t c_npairs = 0;
   CoarseArgs cargs{};
   int32_t c_ngroups = 0;
-  // The coarse setup (basis, W^T S W, its inverse) runs on a second stream
-  // beside the right-hand side and block-Jacobi kernels, forked after the
-  // assembly and joined before the PCG; coarse_pending: forked, not joined.
+  // The coarse setup (basis, W^T S W, its inverse) runs on a second stream:
+  // the basis, which reads only the state, beside the point passes (forked
+  // at the start of the iteration), the rest beside the right-hand side and
+  // block-Jacobi kernels (forked after the assembly), joined before the PCG;
+  // coarse_pending: forked, not joined; basis_forked: this iteration's basis
+  // is on the side stream.
   cudaStream_t s2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  bool coarse_pending = false;
+  bool coarse_pending = false, basis_forked = false;
   PhaseTimer T;
 
   LmEngine(Context& c, const Opts& opts) : ctx(c), o(opts), s(c.stream) {
@@ -549,10 +552,11 @@ struct LmEngine {
     coarse_pending = false;
   }
 
-  // Coarse setup of the two-level PCG on stream st.
-  void launch_coarse_chain(cudaStream_t st) {
-    BA_LAUNCH(coarse_basis_kernel<<<grid_for((int64_t)c_ngroups * 32, 128), 128, 0, st>>>(
-        P, ctx.cur(), cargs));
+  // Coarse setup of the two-level PCG on stream st (basis: W as well).
+  void launch_coarse_chain(cudaStream_t st, bool basis = true) {
+    if (basis)
+      BA_LAUNCH(coarse_basis_kernel<<<grid_for((int64_t)c_ngroups * 32, 128), 128, 0, st>>>(
+          P, ctx.cur(), cargs));
     if (c_npairs > 0)
       BA_LAUNCH(coarse_rowgroup_kernel<<<grid_for(c_npairs * 32, kCoarseMatThreads),
                                          kCoarseMatThreads, 0, st>>>(SV, c_S64.p, cargs, c_npairs,
@@ -565,18 +569,39 @@ struct LmEngine {
     BA_LAUNCH(coarse_invert_kernel<<<(unsigned)ctx.nm, kInvThreads, kInvSmemBytes, st>>>(cargs));
   }
 
-  // After the assembly: fork the coarse setup onto the second stream.
-  void fork_coarse() {
-    if (!(use_cluster && use_coarse && c_ngroups > 0)) return;
+  bool coarse_on() const { return use_cluster && use_coarse && c_ngroups > 0; }
+  void side_stream() {
+    if (s2) return;
+    check(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking), "side stream");
+    check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "event");
+    check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "event");
+  }
+
+  // At the start of an iteration: fork the coarse basis onto the second
+  // stream (it runs beside the point passes).
+  void fork_coarse_basis() {
+    if (!coarse_on()) return;
     join_coarse();
-    if (!s2) {
-      check(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking), "side stream");
-      check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "event");
-      check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "event");
-    }
+    side_stream();
     check(cudaEventRecord(ev_fork, s), "fork");
     check(cudaStreamWaitEvent(s2, ev_fork, 0), "fork");
-    launch_coarse_chain(s2);
+    BA_LAUNCH(coarse_basis_kernel<<<grid_for((int64_t)c_ngroups * 32, 128), 128, 0, s2>>>(
+        P, ctx.cur(), cargs));
+    check(cudaEventRecord(ev_join, s2), "join");
+    coarse_pending = true;
+    basis_forked = true;
+  }
+
+  // After the assembly: fork the rest of the coarse setup onto the second
+  // stream (the basis too unless it was forked at the start).
+  void fork_coarse() {
+    if (!coarse_on()) return;
+    join_coarse();  // the basis, finished long before
+    side_stream();
+    check(cudaEventRecord(ev_fork, s), "fork");
+    check(cudaStreamWaitEvent(s2, ev_fork, 0), "fork");
+    launch_coarse_chain(s2, !basis_forked);
+    basis_forked = false;
     check(cudaEventRecord(ev_join, s2), "join");
     coarse_pending = true;
   }
@@ -1244,6 +1269,7 @@ struct LmEngine {
   void build_system() {
     const StateView cur = ctx.cur();
     T.mark(-1);
+    fork_coarse_basis();
     if constexpr (sizeof(R) == 4) {
       if (ctx.nc > 0)
         BA_LAUNCH(cam_f32_kernel<<<grid_for(ctx.nc, 128), 128, 0, s>>>(P, cur, camf, active));
@@ -1298,10 +1324,13 @@ struct LmEngine {
       if (use_coarse && c_ngroups > 0) {
         // forked after the assembly of this system, or (a new PCG plan since)
         // run here
-        if (coarse_pending)
+        if (coarse_pending && !basis_forked) {
           join_coarse();
-        else
+        } else {
+          join_coarse();
+          basis_forked = false;
           launch_coarse_chain(s);
+        }
       }
       cudaLaunchConfig_t cfg{};
       cudaLaunchAttribute attr[1];
