@@ -978,6 +978,9 @@ static __global__ void __launch_bounds__(kObsThreads)
         for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
 #pragma unroll
         for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
+        // a skipped point's observations leave the camera sums (ba.rs:274-277):
+        // marked invalid in the record, which the camera pass then reads alone
+        if (kp == 0 && o[27] != 0.0f) B.lin[(size_t)k * kLinW + 27] = 0.0f;
       } else {
         const float* pf = B.ptf + 9 * (size_t)p;
         const float l00 = pf[0], l10 = pf[1], l11 = pf[2], l20 = pf[3], l21 = pf[4], l22 = pf[5];
@@ -1197,6 +1200,9 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
           for (int i = 0; i < 18; ++i) Z[i] = 0.0f;
 #pragma unroll
           for (int i = 0; i < 9; ++i) gs[i] = 0.0f;
+          // as obs_factor_kernel: a skipped point's observation is marked
+          // invalid in the stored record for the camera pass
+          if (kp == 0 && o[27] != 0.0f) B.lin[(size_t)k * kLinW + 27] = 0.0f;
         } else {
           const float l00 = pf[0], l10 = pf[1], l11 = pf[2], l20 = pf[3], l21 = pf[4],
                       l22 = pf[5];
@@ -1374,13 +1380,14 @@ static __global__ void __launch_bounds__(kCamMixThreads)
       const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
       const float4 q6 = o4[6];  // e 24..25, w 26, valid 27
       const float4 q0 = o4[0], q1 = o4[1], q2 = o4[2];
-      const uint32_t pt = P.obs_pt[k];
       const float* gs = B.gsub + (size_t)k * 9;
       float gv[6];
 #pragma unroll
       for (int a = 0; a < 6; ++a) gv[a] = gs[a];
       i = in, k = kn;
-      if (q6.w == 0.0f || !B.kept[pt]) continue;  // ba.rs:274-277
+      // ba.rs:274-277: the factor pass marked the observations of skipped
+      // points (kept 0) invalid, so the record's flag is the whole test
+      if (q6.w == 0.0f) continue;
       const float jc[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
       const float w = q6.z;
       int u = 0;
