@@ -50,16 +50,30 @@ struct IterBufs {
   int32_t zpitch = 18;
 };
 
-// Store an 18-value FP32 Schur factor as a 24-value record (96-byte aligned;
-// the last six values are zero).
-__device__ __forceinline__ void store_Z24(float* dst, const float (&z)[18]) {
+// Store an 18-value FP32 Schur factor as a 24-value record (96-byte aligned).
+// Values 18..20 carry what the camera pass needs of the observation, read
+// in camera order from the same record: its weighted point-step residual
+// r' = (r0, r1) (its gradient shares are Jc^T r' and Jg^T r', formed there
+// by gshare as the factor pass would), or mode 1: the shares are in gsub
+// (points on the FP64 ill-conditioned path).  Values 21..23 are zero.
+__device__ __forceinline__ void store_Z24(float* dst, const float (&z)[18], float r0 = 0.0f,
+                                          float r1 = 0.0f, float mode = 0.0f) {
   float4* d = reinterpret_cast<float4*>(dst);
   d[0] = make_float4(z[0], z[1], z[2], z[3]);
   d[1] = make_float4(z[4], z[5], z[6], z[7]);
   d[2] = make_float4(z[8], z[9], z[10], z[11]);
   d[3] = make_float4(z[12], z[13], z[14], z[15]);
-  d[4] = make_float4(z[16], z[17], 0.0f, 0.0f);
-  d[5] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  d[4] = make_float4(z[16], z[17], r0, r1);
+  d[5] = make_float4(mode, 0.0f, 0.0f, 0.0f);
+}
+// Value offsets of r' and the mode in a 24-value factor record.
+constexpr int kZ24R = 18, kZ24Mode = 20;
+
+// An observation's share of the reduced gradient, a Jc^T r' or Jg^T r'
+// component: the same expression in the factor pass and the camera pass, so
+// that the two give the same FP32 value.
+__device__ __forceinline__ float gshare(float a, float b, float r0, float r1) {
+  return a * r0 + b * r1;
 }
 
 __device__ __forceinline__ size_t z_index(const uint32_t* zpos, int64_t k) {
@@ -574,6 +588,12 @@ static __device__ __noinline__ void point_system_mixed_ill(const Prob& P, const 
   for (uint32_t k = s; k < e; ++k) {
     float* Z = kZ ? B.Z + z_index(B.zpos, k) * B.zpitch : nullptr;
     float* gs = B.gsub + (size_t)k * 9;
+    if constexpr (kZ) {
+      if (B.zpitch == 24) {  // the camera pass takes this observation's shares from gsub
+#pragma unroll
+        for (int i = kZ24R; i < 24; ++i) Z[i] = i == kZ24Mode ? 1.0f : 0.0f;
+      }
+    }
     double o[kLinW];
     if (!linearise<double>(P, st, k, sg, refine, o)) {
       if constexpr (kZ)
@@ -961,6 +981,7 @@ static __global__ void __launch_bounds__(kObsThreads)
   float* Z = &smz[warp][lane * kZPitch];
   float* gs = &smg[warp][lane * kGPitch];
   bool mine = false;
+  float fr0 = 0.0f, fr1 = 0.0f;  // r' for the camera-major record's tail
   if (k < P.no) {
     const uint32_t p = P.obs_pt[k];
     const uint8_t kp = B.kept[p];
@@ -989,6 +1010,7 @@ static __global__ void __launch_bounds__(kObsThreads)
         const float j0 = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
         const float r0 = (o[24] - (j0 * t0 + j1 * t1 + j2 * t2)) * w;
         const float r1 = (o[25] - (j3 * t0 + j4 * t1 + j5 * t2)) * w;
+        fr0 = r0, fr1 = r1;
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
           const float ca = o[r], cb = o[6 + r];
@@ -998,10 +1020,10 @@ static __global__ void __launch_bounds__(kObsThreads)
           Z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
           Z[3 * r + 1] = y1 * l11 + y2 * l21;
           Z[3 * r + 2] = y2 * l22;
-          gs[r] = ca * r0 + cb * r1;
+          gs[r] = gshare(ca, cb, r0, r1);
         }
 #pragma unroll
-        for (int a = 0; a < 3; ++a) gs[6 + a] = o[18 + a] * r0 + o[21 + a] * r1;
+        for (int a = 0; a < 3; ++a) gs[6 + a] = gshare(o[18 + a], o[21 + a], r0, r1);
       }
     }
   }
@@ -1010,17 +1032,18 @@ static __global__ void __launch_bounds__(kObsThreads)
   const int n = P.no - k0 < 32 ? (int)(P.no - k0) : 32;
   if (B.zpos) {
     // camera-major factors: each lane stores its own 96-byte record at its
-    // camera-order position
+    // camera-order position, with r' for the camera pass (which then needs
+    // no gradient shares from here)
     if (mine) {
       float z[18];
 #pragma unroll
       for (int i = 0; i < 18; ++i) z[i] = Z[i];
-      store_Z24(B.Z + (size_t)B.zpos[k] * B.zpitch, z);
+      store_Z24(B.Z + (size_t)B.zpos[k] * B.zpitch, z, fr0, fr1, 0.0f);
     }
-  } else if (B.Z) {
-    warp_store_records<18>(smz[warp], kZPitch, B.Z + k0 * 18, n, mask, lane);
+  } else {
+    if (B.Z) warp_store_records<18>(smz[warp], kZPitch, B.Z + k0 * 18, n, mask, lane);
+    warp_store_records<9>(smg[warp], kGPitch, B.gsub + k0 * 9, n, mask, lane);
   }
-  warp_store_records<9>(smg[warp], kGPitch, B.gsub + k0 * 9, n, mask, lane);
 }
 
 // ---- mixed form: the three passes fused per chunk of observations ---------
@@ -1180,6 +1203,7 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
     const uint32_t j = j0 + lane, k = o_lo + j;
     bool mine = false;
     float Z[18], gs[9];
+    float fr0 = 0.0f, fr1 = 0.0f;  // r' for the camera-major record's tail
     if (j < n) {
       const uint32_t p = P.obs_pt[k];
       bool act;
@@ -1211,6 +1235,7 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
           const float j0v = o[12], j1 = o[13], j2 = o[14], j3 = o[15], j4 = o[16], j5 = o[17];
           const float r0 = (o[24] - (j0v * t0 + j1 * t1 + j2 * t2)) * w;
           const float r1 = (o[25] - (j3 * t0 + j4 * t1 + j5 * t2)) * w;
+          fr0 = r0, fr1 = r1;
 #pragma unroll
           for (int r = 0; r < 6; ++r) {
             const float ca = o[r], cb = o[6 + r];
@@ -1220,17 +1245,17 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
             Z[3 * r + 0] = y0 * l00 + y1 * l10 + y2 * l20;
             Z[3 * r + 1] = y1 * l11 + y2 * l21;
             Z[3 * r + 2] = y2 * l22;
-            gs[r] = ca * r0 + cb * r1;
+            gs[r] = gshare(ca, cb, r0, r1);
           }
 #pragma unroll
-          for (int a = 0; a < 3; ++a) gs[6 + a] = o[18 + a] * r0 + o[21 + a] * r1;
+          for (int a = 0; a < 3; ++a) gs[6 + a] = gshare(o[18 + a], o[21 + a], r0, r1);
         }
       }
     }
     const uint32_t mask = __ballot_sync(0xffffffffu, mine);
     const int nw = n - j0 < 32u ? (int)(n - j0) : 32;
-    if (B.zpos) {  // camera-major factors: each lane stores its own record
-      if (mine) store_Z24(B.Z + (size_t)B.zpos[k] * B.zpitch, Z);
+    if (B.zpos) {  // camera-major factors: each lane stores its own record, with r'
+      if (mine) store_Z24(B.Z + (size_t)B.zpos[k] * B.zpitch, Z, fr0, fr1, 0.0f);
     }
     if (j0 + 32 <= (uint32_t)kCap) {
       // the warp's 32 record slots (read above) stage its stores
@@ -1245,11 +1270,13 @@ static __global__ void __launch_bounds__(FusedPoint<kChunk>::kThreads,
         for (int i = 0; i < 9; ++i) stgs[lane * kGPitch + i] = gs[i];
       }
       __syncwarp();
-      if (!B.zpos && B.Z)
-        warp_store_records<18>(stz, kZPitch, B.Z + (size_t)(o_lo + j0) * 18, nw, mask, lane);
-      warp_store_records<9>(stgs, kGPitch, B.gsub + (size_t)(o_lo + j0) * 9, nw, mask, lane);
-    } else if (mine) {
-      if (!B.zpos && B.Z)
+      if (!B.zpos) {  // camera-major records carry r' instead of the shares
+        if (B.Z)
+          warp_store_records<18>(stz, kZPitch, B.Z + (size_t)(o_lo + j0) * 18, nw, mask, lane);
+        warp_store_records<9>(stgs, kGPitch, B.gsub + (size_t)(o_lo + j0) * 9, nw, mask, lane);
+      }
+    } else if (mine && !B.zpos) {
+      if (B.Z)
 #pragma unroll
         for (int i = 0; i < 18; ++i) B.Z[(size_t)k * 18 + i] = Z[i];
 #pragma unroll
@@ -1367,6 +1394,8 @@ static __global__ void __launch_bounds__(kCamMixThreads)
 #pragma unroll
   for (int i = 0; i < 9; ++i) gh[i] = 0.0f, gl[i] = 0.0f;
   const uint32_t b = S.cam_ptr[c], e = S.cam_ptr[c + 1];
+  // camera-major factor records (zpitch 24) carry each observation's r'
+  const bool tail = B.zpos != nullptr && B.Z != nullptr && B.zpitch == 24;
   for (uint32_t base = b; base < e; base += kCamMixThreads * kCamRun) {
     // The next observation's index is loaded one step ahead, and a record is
     // read whole before its validity is tested: two dependent loads per step.
@@ -1380,16 +1409,34 @@ static __global__ void __launch_bounds__(kCamMixThreads)
       const float4* o4 = reinterpret_cast<const float4*>(B.lin + (size_t)k * kLinW);
       const float4 q6 = o4[6];  // e 24..25, w 26, valid 27
       const float4 q0 = o4[0], q1 = o4[1], q2 = o4[2];
+      // Gradient shares: with camera-major factor records, from r' in the
+      // record at this camera-order position (mode 1: from gsub); else gsub.
       const float* gs = B.gsub + (size_t)k * 9;
+      float4 tl = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // z16 z17 r0 r1
+      float md = 1.0f;
       float gv[6];
+      if (tail) {
+        const float* zr = B.Z + (size_t)i * 24;
+        tl = *reinterpret_cast<const float4*>(zr + 16);
+        md = zr[kZ24Mode];
+      } else {
 #pragma unroll
-      for (int a = 0; a < 6; ++a) gv[a] = gs[a];
+        for (int a = 0; a < 6; ++a) gv[a] = gs[a];
+      }
       i = in, k = kn;
       // ba.rs:274-277: the factor pass marked the observations of skipped
       // points (kept 0) invalid, so the record's flag is the whole test
       if (q6.w == 0.0f) continue;
       const float jc[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
       const float w = q6.z;
+      const bool from_r = tail && md == 0.0f;
+      if (from_r) {
+#pragma unroll
+        for (int a = 0; a < 6; ++a) gv[a] = gshare(jc[a], jc[6 + a], tl.z, tl.w);
+      } else if (tail) {
+#pragma unroll
+        for (int a = 0; a < 6; ++a) gv[a] = gs[a];
+      }
       int u = 0;
 #pragma unroll
       for (int a = 0; a < 6; ++a)
@@ -1412,7 +1459,8 @@ static __global__ void __launch_bounds__(kCamMixThreads)
           for (int bb = a; bb < 3; ++bb)
             acc[39 + v++] += (jg[a] * jg[bb] + jg[3 + a] * jg[3 + bb]) * w;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) df_add(gh[6 + a], gl[6 + a], gs[6 + a]);
+        for (int a = 0; a < 3; ++a)
+          df_add(gh[6 + a], gl[6 + a], from_r ? gshare(jg[a], jg[3 + a], tl.z, tl.w) : gs[6 + a]);
       }
     }
     // Warp-uniform: fold these runs' FP32 sums into the lanes' FP64 sums.
