@@ -218,13 +218,15 @@ __global__ void pair_fill_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t*
   W.E = entries_of(pt_ptr, lens_ptr, p);
   if (W.E.m < 2) return;  // uniform over the warp
   W.load(P, lens_grp, lane);
+  // the first 32 entries' storage positions, looked up once per point
+  if (zpos && (uint32_t)lane < W.ne && (int64_t)W.my_e < P.no) W.my_e = zpos[W.my_e];
   uint64_t o = off[p];
   const uint64_t nb = (uint64_t)P.nb;
   const uint32_t lt = (1u << lane) - 1u;
   for (uint32_t i = 0; i < W.ne; ++i) {
     uint32_t ei, bi;
     W.at(P, lens_grp, i, ei, bi);
-    if (zpos && (int64_t)ei < P.no) ei = zpos[ei];
+    if (i >= 32 && zpos && (int64_t)ei < P.no) ei = zpos[ei];
     for (uint32_t j0 = 0; j0 < W.ne; j0 += 32) {
       const uint32_t j = j0 + lane;
       uint32_t ej = 0, bj = 0;
@@ -232,11 +234,11 @@ __global__ void pair_fill_kernel(Prob P, const uint32_t* pt_ptr, const uint32_t*
         ej = W.my_e, bj = W.my_b;
       } else if (j < W.ne) {
         W.E.get(P, lens_grp, j, ej, bj);
+        if (zpos && (int64_t)ej < P.no) ej = zpos[ej];
       }
       const bool take = j < W.ne && bi <= bj;
       const uint32_t mask = __ballot_sync(kFull, take);
       if (take) {
-        if (zpos && (int64_t)ej < P.no) ej = zpos[ej];
         const uint64_t q = o + __popc(mask & lt);
         keys[q] = (uint64_t)bi * nb + bj;
         vals[q] = (uint64_t)ei | ((uint64_t)ej << 32);
