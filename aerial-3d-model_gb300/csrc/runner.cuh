@@ -527,6 +527,8 @@ struct LmEngine {
   // is on the side stream.
   cudaStream_t s2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // The camera sums run on the second stream beside the Schur sums.
+  cudaEvent_t ev_cam = nullptr, ev_cam_join = nullptr;
   bool coarse_pending = false, basis_forked = false;
   PhaseTimer T;
 
@@ -536,9 +538,11 @@ struct LmEngine {
     for (int k = 0; k < kPhases; ++k) ctx.phase_ms[k] = 0, ctx.phase_n[k] = 0;
   }
   ~LmEngine() {
-    if (coarse_pending && s2) cudaStreamSynchronize(s2);
+    if (s2) cudaStreamSynchronize(s2);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_cam) cudaEventDestroy(ev_cam);
+    if (ev_cam_join) cudaEventDestroy(ev_cam_join);
     if (s2) cudaStreamDestroy(s2);
   }
   LmEngine(const LmEngine&) = delete;
@@ -575,6 +579,8 @@ struct LmEngine {
     check(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking), "side stream");
     check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "event");
     check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "event");
+    check(cudaEventCreateWithFlags(&ev_cam, cudaEventDisableTiming), "event");
+    check(cudaEventCreateWithFlags(&ev_cam_join, cudaEventDisableTiming), "event");
   }
 
   // At the start of an iteration: fork the coarse basis onto the second
@@ -1279,15 +1285,28 @@ struct LmEngine {
                                                                      lambda, sigma));
     }
     T.mark(BA_PHASE_POINT);
+    // The camera sums and the Schur sums read what the point passes wrote and
+    // nothing of each other, and both wait mostly on gathers: the camera pass
+    // runs on the second stream beside the Schur kernel (one after the other
+    // when phases are timed, so that each phase has its own interval).
+    const bool split = !implicit && !T.on;
+    cudaStream_t cs = s;
+    if (split) {
+      side_stream();
+      check(cudaEventRecord(ev_cam, s), "fork");
+      check(cudaStreamWaitEvent(s2, ev_cam, 0), "fork");
+      cs = s2;
+    }
     if (ctx.nc > 0) {
       if constexpr (sizeof(R) == 4)
-        BA_LAUNCH(camera_mixed_kernel<<<(unsigned)ctx.nc, kCamMixThreads, 0, s>>>(P, SV, B,
-                                                                                 active));
+        BA_LAUNCH(camera_mixed_kernel<<<(unsigned)ctx.nc, kCamMixThreads, 0, cs>>>(P, SV, B,
+                                                                                  active));
       else
-        BA_LAUNCH(camera_kernel<R><<<(unsigned)ctx.nc, kCamThreads, 0, s>>>(P, SV, B, active));
+        BA_LAUNCH(camera_kernel<R><<<(unsigned)ctx.nc, kCamThreads, 0, cs>>>(P, SV, B, active));
     }
-    BA_LAUNCH(group_kernel<<<grid_for(ctx.ng * 32, 128), 128, 0, s>>>(P, SV, caml, grpU, grpg,
-                                                                     active));
+    BA_LAUNCH(group_kernel<<<grid_for(ctx.ng * 32, 128), 128, 0, cs>>>(P, SV, caml, grpU, grpg,
+                                                                      active));
+    if (split) check(cudaEventRecord(ev_cam_join, s2), "join");
     T.mark(BA_PHASE_CAMERA);
     if (implicit) {
       T.mark(BA_PHASE_SCHUR);
@@ -1303,6 +1322,7 @@ struct LmEngine {
     if (n_fold > 0)
       BA_LAUNCH(schur_fold_kernel<<<n_fold, kFoldThreads, 0, s>>>(P, SV, part, fold_slots,
                                                                  active));
+    if (split) check(cudaStreamWaitEvent(s, ev_cam_join, 0), "join");
     T.mark(BA_PHASE_SCHUR);
     if (SB.ns > 0)
       BA_LAUNCH(assemble_kernel<R><<<grid_for(SB.ns * 36, 256), 256, 0, s>>>(
