@@ -1379,8 +1379,21 @@ struct LmEngine {
   // Trial state = current state + step (ba.rs:338-366).
   void update() {
     const StateView cur = ctx.cur(), tri = ctx.trial();
-    BA_LAUNCH(update_cameras_kernel<R><<<grid_for(std::max(ctx.nc, ctx.ng), 256), 256, 0, s>>>(
+    // The cameras' and lens groups' update and the points' back-substitution
+    // write different parts of the trial state and read only the current one:
+    // the former runs on the second stream (one after the other when phases
+    // are timed).
+    const bool split = !T.on;
+    cudaStream_t us = s;
+    if (split) {
+      side_stream();
+      check(cudaEventRecord(ev_cam, s), "fork");
+      check(cudaStreamWaitEvent(s2, ev_cam, 0), "fork");
+      us = s2;
+    }
+    BA_LAUNCH(update_cameras_kernel<R><<<grid_for(std::max(ctx.nc, ctx.ng), 256), 256, 0, us>>>(
         P, cur, tri, B, active));
+    if (split) check(cudaEventRecord(ev_cam_join, s2), "join");
     if constexpr (sizeof(R) == 4) {
       if (ctx.no > 0)
       {
@@ -1394,6 +1407,7 @@ struct LmEngine {
     }
     BA_LAUNCH(backsub_kernel<R><<<grid_for(ctx.np, 256), 256, 0, s>>>(P, SV, cur, tri, B, sigma,
                                                                      active, obs_u.p));
+    if (split) check(cudaStreamWaitEvent(s, ev_cam_join, 0), "join");
     T.mark(BA_PHASE_UPDATE);
   }
 
