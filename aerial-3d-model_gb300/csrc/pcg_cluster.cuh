@@ -21,10 +21,11 @@
 // vector of the next residual, w = W^T r_{k+1}, is formed as W^T r_k −
 // α W^T q_k from group sums every CTA publishes before the iteration's first
 // barrier (α is known right after it), so an iteration still needs only two
-// cluster reductions: p·q (then α), and r·r with r·z (then β).  The coarse
-// step c = E^-1 w is split as E^-1 W^T r_k − α E^-1 W^T q_k: its two halves
-// run on the warps beside warp 0's reduction of p·q (before and after the
-// barrier), so it adds no CTA barrier to the iteration.
+// cluster reductions: p·q (then α, the coarse gather and c = E^-1 w), and
+// r·r with r·z (then β).  The coarse step runs on the warps beside warp 0
+// after the p·q barrier: each of them sums the inbox and forms α as warp 0
+// does (the same sums in the same order, so the same α), then its rows of
+// E^-1 w, so the step adds no CTA barrier to the iteration.
 //
 // Every CTA of a cluster executes the same sequence of cluster barriers:
 // loop exits depend only on reduced scalars, which every CTA computes from
@@ -110,14 +111,13 @@ inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks, uint32_t cap
 }
 
 // Extra shared memory of the two-level form, in floats: per row W (42); per
-// own group its rows of E^-1 (7 x D) and the two halves of c (7 each:
-// E^-1 W^T r and E^-1 W^T q); the model's group sums of W^T r (two buffers by
-// iteration parity: owners push the next one while the current one is read)
-// and of W^T q (D each), pushed by every group's owner.
+// own group its rows of E^-1 (7 x D) and c (7); the model's group sums of
+// W^T r (two buffers by iteration parity: owners push the next one while the
+// current one is read) and of W^T q (D each), pushed by every group's owner.
 constexpr int kCgCoarseRowF = 42;
 __host__ __device__ constexpr size_t cg_coarse_fixed_floats(uint32_t cap_groups,
                                                             uint32_t cap_dim) {
-  return (size_t)cap_groups * (kCoarseModes * cap_dim + 2 * kCoarseModes) + 3 * (size_t)cap_dim;
+  return (size_t)cap_groups * (kCoarseModes * cap_dim + kCoarseModes) + 3 * (size_t)cap_dim;
 }
 inline size_t cg_coarse_smem_bytes(uint32_t cap_rows, uint32_t cap_groups, uint32_t cap_dim) {
   return ((size_t)cap_rows * kCgCoarseRowF + cg_coarse_fixed_floats(cap_groups, cap_dim)) * 4;
@@ -156,6 +156,20 @@ __device__ __forceinline__ DFloat df_scale(float x, DFloat y) {
 }
 __device__ __forceinline__ DFloat df_shfl_xor(DFloat v, int o) {
   return DFloat{__shfl_xor_sync(kFull, v.hi, o), __shfl_xor_sync(kFull, v.lo, o)};
+}
+
+// The cluster's totals from an inbox: lane r < cluster size (<= 16) holds CTA
+// r's values, lanes 16..31 hold zeros, and a butterfly within each half-warp
+// leaves the totals in lanes 0..15.
+template <int N>
+__device__ __forceinline__ void cg_inbox_sum(const DFloat (*inbox)[4], int csize, int lane,
+                                             DFloat (&v)[N]) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = lane < csize ? inbox[lane][i] : DFloat{0.0f, 0.0f};
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = df_sum(v[i], df_shfl_xor(v[i], o));
 }
 
 // Inner products: a warp sums its rows' products in FP32 (a few rows of six
@@ -211,15 +225,8 @@ __device__ __forceinline__ void cg_reduce(cgx::cluster_group& cl, const float (&
   }
   cl.sync();
   if (warp == 0) {
-    // lane r < cluster size (<= 16) holds CTA r's values; lanes 16..31 hold
-    // zeros and the butterfly stays within each half-warp.
     DFloat v[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) v[i] = lane < csize ? inbox[lane][i] : DFloat{0.0f, 0.0f};
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1)
-#pragma unroll
-      for (int i = 0; i < N; ++i) v[i] = df_sum(v[i], df_shfl_xor(v[i], o));
+    cg_inbox_sum<N>(inbox, csize, lane, v);
     if (lane == 0) {
 #pragma unroll
       for (int i = 0; i < N; ++i) tot[i] = v[i];
@@ -240,37 +247,53 @@ struct CgScalars {
   int stop;
 };
 
-// One output of the coarse step's halves: out[o] = (E^-1 w)_o for this
-// CTA's (group, mode) output o, w one of the model's group-sum vectors (D
-// floats); a warp, then a fixed butterfly.
+// One output of the coarse step: sc[o] = (E^-1 w)_o for this CTA's (group,
+// mode) output o, with the model's w = W^T r − α W^T q (wq null at the
+// start: w = W^T b); a warp, then a fixed butterfly.
 __device__ __forceinline__ void cg_coarse_dot(const float* sEi, uint32_t cap_dim, int D, int o,
-                                              const float* w, float* out) {
+                                              const float* wr, const float* wq, float alpha,
+                                              float* sc) {
   const int lane = threadIdx.x & 31;
   const float* er = sEi + (size_t)o * cap_dim;
   float v = 0.0f;
-  for (int t = lane; t < D; t += 32) v += er[t] * w[t];
+  if (wq)
+    for (int t = lane; t < D; t += 32) v += er[t] * (wr[t] - alpha * wq[t]);
+  else
+    for (int t = lane; t < D; t += 32) v += er[t] * wr[t];
 #pragma unroll
   for (int q = 16; q > 0; q >>= 1) v += __shfl_xor_sync(kFull, v, q);
-  if (lane == 0) out[o] = v;
+  if (lane == 0) sc[o] = v;
 }
 
-// A row's coarse share of z, (W c)_i for lane i < 6, c = cr − α cq (the two
-// halves of the coarse step; cq null at the start: c = cr).  Rows outside
-// every group, such as the lens row, add nothing.
-__device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const float* cr,
-                                           const float* cq, float alpha, int ci) {
+// The iteration's α as the p.q reduction's post forms it (the same sums in
+// the same order, so the same value), in every lane of the calling warp:
+// p.q from inbox 0 plus the lens row's share, α = r.z / p.q (0 where p.q
+// vanishes).
+__device__ __forceinline__ float cg_alpha(const DFloat (*inbox)[4], int csize, int lane,
+                                          int32_t lens, const float* lens_p, float rz) {
+  DFloat v[4];
+  cg_inbox_sum<4>(inbox, csize, lane, v);
+  DFloat t[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    t[i] = DFloat{__shfl_sync(kFull, v[i].hi, 0), __shfl_sync(kFull, v[i].lo, 0)};
+  DFloat pq = t[0];
+  if (lens >= 0)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) pq = df_sum(pq, df_scale(lens_p[c], t[1 + c]));
+  return fabsf(pq.hi) < 1.17549435e-38f ? 0.0f : rz / pq.hi;
+}
+
+// A row's coarse share of z, (W c)_i for lane i < 6 (rows outside every
+// group, such as the lens row, add nothing).
+__device__ __forceinline__ float cg_row_wc(const float* sWrow, int32_t lg, const float* sc,
+                                           int ci) {
   if (lg < 0) return 0.0f;
   const float* w = sWrow + kCoarseModes * ci;
-  const float* a = cr + kCoarseModes * lg;
+  const float* c = sc + kCoarseModes * lg;
   float add = 0.0f;
-  if (cq) {
-    const float* b = cq + kCoarseModes * lg;
 #pragma unroll
-    for (int j = 0; j < kCoarseModes; ++j) add += w[j] * (a[j] - alpha * b[j]);
-  } else {
-#pragma unroll
-    for (int j = 0; j < kCoarseModes; ++j) add += w[j] * a[j];
-  }
+  for (int j = 0; j < kCoarseModes; ++j) add += w[j] * c[j];
   return add;
 }
 
@@ -344,9 +367,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
   const uint32_t nblk = A.row_ptr[J.row1] - B0;
   const uint32_t ncached = nblk < A.cap_blocks ? nblk : A.cap_blocks;
   // Shared memory: row state | cached S blocks | neighbour cache | cached
-  // blocks' cache slots | two-level form: W per row, E^-1 rows and the two
-  // halves of c per own group, the model's group sums of W^T r (two buffers)
-  // and W^T q.
+  // blocks' cache slots | two-level form: W per row, E^-1 rows and c per own
+  // group, the model's group sums of W^T r (two buffers) and W^T q.
   float* rs = reinterpret_cast<float*>(cg_smem);
   float* sS = rs + (size_t)A.cap_rows * kCgRow;
   float* cache = sS + (size_t)A.cap_blocks * 36;
@@ -354,9 +376,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
   float* sW = reinterpret_cast<float*>(sL + A.cap_blocks);
   float* sEi = sW + (size_t)A.cap_rows * 42;
   const size_t gsz = (size_t)A.cap_groups * kCoarseModes;
-  float* scr = sEi + gsz * A.cap_dim;        // E^-1 W^T r, own outputs
-  float* scq = scr + gsz;                     // E^-1 W^T q
-  float* wall_r = scq + gsz;                  // [2][D]
+  float* scf = sEi + gsz * A.cap_dim;        // c, own outputs
+  float* wall_r = scf + gsz;                  // [2][D]
   float* wall_q = wall_r + 2 * (size_t)A.cap_dim;  // [D]
   const int32_t cg0 = kCoarse ? A.job_g0[blockIdx.x] : 0;
   const int32_t ngr = kCoarse ? A.job_g1[blockIdx.x] - cg0 : 0;
@@ -450,7 +471,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
       },
       [&](int w) {
         if constexpr (kCoarse) {
-          for (int o = w; o < nco; o += kCgWarps - 1) cg_coarse_dot(sEi, A.cap_dim, cD, o, wall_r, scr);
+          for (int o = w; o < nco; o += kCgWarps - 1)
+            cg_coarse_dot(sEi, A.cap_dim, cD, o, wall_r, nullptr, 0.0f, scf);
         }
       });
   if constexpr (kCoarse) {
@@ -459,7 +481,7 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
     for (uint32_t lr = warp; lr < nrows; lr += kCgWarps) {
       float* st = CGROW(lr);
       const int32_t lg = __float_as_int(st[kCgIdx + 3]);
-      const float add = cg_row_wc(sW + (size_t)lr * 42, lg, scr, nullptr, 0.0f, ci);
+      const float add = cg_row_wc(sW + (size_t)lr * 42, lg, scf, ci);
       float zi = 0.0f;
       if (vl) {
         zi = st[kCgZ + ci] + add;
@@ -559,20 +581,14 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
     const float w4[4] = {cg_sum8f(dpq), __shfl_sync(kFull, dlens, 0), __shfl_sync(kFull, dlens, 1),
                          __shfl_sync(kFull, dlens, 2)};
     const bool lens_here = lens >= 0 && (uint32_t)lens >= J.row0 && (uint32_t)lens < J.row1;
-    // p.q; the two-level form pushes the group sums of W^T q and forms
-    // E^-1 W^T r beside it, and E^-1 W^T q after the barrier
+    // p.q; the two-level form pushes the group sums of W^T q beside it and,
+    // after the barrier, forms c = E^-1 (W^T r − α W^T q) of the next
+    // residual beside warp 0
     const float* wr_cur = wall_r + (size_t)cur * A.cap_dim;
     cg_reduce<kCgWarps, 4>(cl, w4, wsm, inbox[0], tot, [&](int w) {
-      if constexpr (kCoarse) {
-        for (int t = w; t < 2 * nco; t += kCgWarps - 1) {
-          if (t < nco) {
-            cg_group_sum_push(cl, t, A.grp_row0, A.grp_row1, cg0, goff, J.row0, sW, rs, kCgQ,
-                              wall_q);
-          } else {
-            cg_coarse_dot(sEi, A.cap_dim, cD, t - nco, wr_cur, scr);
-          }
-        }
-      }
+      if constexpr (kCoarse)
+        cg_group_sums_push<kCgWarps - 1>(cl, w, ngr, A.grp_row0, A.grp_row1, cg0, goff, J.row0,
+                                         sW, rs, kCgQ, wall_q);
     }, [&] {
       DFloat pq = tot[0];
       if (lens >= 0) {
@@ -591,7 +607,11 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
       sc.af = sc.stop ? 0.0f : sc.rz.hi / pq.hi;
     }, [&](int w) {
       if constexpr (kCoarse) {
-        for (int o = w; o < nco; o += kCgWarps - 1) cg_coarse_dot(sEi, A.cap_dim, cD, o, wall_q, scq);
+        if (w < nco) {
+          const float a = cg_alpha(inbox[0], (int)cl.num_blocks(), lane, lens, lens_p, sc.rz.hi);
+          for (int o = w; o < nco; o += kCgWarps - 1)
+            cg_coarse_dot(sEi, A.cap_dim, cD, o, wr_cur, wall_q, a, scf);
+        }
       }
     });
     ++spmv;
@@ -610,8 +630,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
 #pragma unroll
       for (int j = 0; j < 6; ++j) zi += st[kCgM + 6 * ci + j] * __shfl_sync(kFull, ri, j);
       if constexpr (kCoarse) {
-        // z = B^-1 r + W c, c = E^-1 (W^T r − α W^T q) of the next residual
-        zi += cg_row_wc(sW + (size_t)lr * 42, __float_as_int(st[kCgIdx + 3]), scr, scq, af, ci);
+        // z = B^-1 r + W c
+        zi += cg_row_wc(sW + (size_t)lr * 42, __float_as_int(st[kCgIdx + 3]), scf, ci);
       }
       if (vl) {
         st[kCgZ + ci] = zi;
