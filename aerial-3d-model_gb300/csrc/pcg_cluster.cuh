@@ -103,7 +103,48 @@ struct CgArgs {
   const uint32_t* sub_ent;
   uint32_t cap_cache;        // cache slots per CTA
   const int32_t* cap = nullptr;  // [nm] or null: per-model iteration cap (below max_iter)
+  unsigned* err = nullptr;   // device error bits (a staging wait that gave up)
+  long long spin = 0;        // limit of that wait, in SM clock cycles
 };
+
+// The CTA's S blocks are one contiguous run of global memory (rows are
+// consecutive, blocks row-major): one bulk asynchronous copy (the TMA engine,
+// cp.async.bulk) brings them to shared memory while the threads stage the
+// rest, completing on an mbarrier.  Both addresses are 16-byte aligned (a
+// block is 144 bytes; the run and the shared row state before it are
+// multiples of 16 bytes) and the size is a multiple of 16.
+__device__ __forceinline__ void cg_bulk_stage(uint64_t* bar, float* dst, const float* src,
+                                              uint32_t bytes) {
+  const uint32_t b = (uint32_t)__cvta_generic_to_shared(bar);
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(d), "l"(src), "r"(bytes), "r"(b)
+      : "memory");
+}
+// Wait for phase 0 of the staging mbarrier, at most `spin` cycles (<= 0: the
+// default 4e9); false if it gave up.
+__device__ __forceinline__ bool cg_bulk_wait(uint64_t* bar, long long spin) {
+  const uint32_t b = (uint32_t)__cvta_generic_to_shared(bar);
+  const long long limit = spin > 0 ? spin : 4000000000LL;
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(b)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > limit) return false;
+  }
+}
 
 inline size_t cg_smem_bytes(uint32_t cap_rows, uint32_t cap_blocks, uint32_t cap_cache) {
   return (size_t)cap_rows * kCgRow * 4 + (size_t)cap_blocks * (36 * 4 + 4) +
@@ -357,6 +398,7 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
   __shared__ DFloat tot[4];
   __shared__ float lens_p[4];  // the lens row's p, pushed by its owner
   __shared__ CgScalars sc;
+  __shared__ uint64_t stage_bar;  // completion of the S blocks' bulk copy
   extern __shared__ __align__(16) unsigned char cg_smem[];
   cgx::cluster_group cl = cgx::this_cluster();
   const CgJob J = A.jobs[blockIdx.x];
@@ -387,9 +429,8 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
   const int cD = kCoarse ? kCoarseModes * (A.model_g0[J.model + 1] - A.model_g0[J.model]) : 0;
   const int nco = kCoarseModes * ngr;
   {
-    const float4* src = reinterpret_cast<const float4*>(A.S + (size_t)B0 * 36);
-    float4* dst = reinterpret_cast<float4*>(sS);
-    for (uint32_t c = threadIdx.x; c < ncached * 9; c += blockDim.x) dst[c] = src[c];
+    if (threadIdx.x == 0 && ncached > 0)
+      cg_bulk_stage(&stage_bar, sS, A.S + (size_t)B0 * 36, ncached * 36u * 4u);
     for (uint32_t t = threadIdx.x; t < ncached; t += blockDim.x) sL[t] = A.blk_slot[B0 + t];
     // p(prev) of iteration 0 is 0 in every cached row; the z values arrive
     // by push after the first cluster barrier.
@@ -428,6 +469,12 @@ static __global__ void __launch_bounds__(kThreads) pcg_cluster_kernel(CgArgs A) 
       }
     }
   }
+  // The S blocks' copy has landed: thread 0 waits on the mbarrier (the
+  // cluster barrier below then orders the copy before every thread's reads).
+  // A wait that gives up records the error; the kernel still runs its
+  // barriers to the end, and the call fails.
+  if (threadIdx.x == 0 && ncached > 0 && !cg_bulk_wait(&stage_bar, A.spin) && A.err)
+    atomicOr(A.err, ERR_BARRIER_TIMEOUT);
   // Every CTA of the cluster has started (its shared memory is live for the
   // pushes below) and its staging is done.
   cl.sync();

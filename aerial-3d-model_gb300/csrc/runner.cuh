@@ -1046,6 +1046,7 @@ struct LmEngine {
                 cap_blocks, active, pcg_iters, pcg_limit, o.pcg_tol};
     ca.cap = pcg_cap;
     ca.blk_slot = cg_slot, ca.sub_ptr = cg_subp, ca.sub_ent = cg_sube, ca.cap_cache = kp.cap;
+    ca.err = ctx.err, ca.spin = o.wait_limit;
     use_coarse = coarse;
     ctx.last_coarse_dim = 0;
     if (coarse) {
