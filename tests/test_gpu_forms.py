@@ -314,3 +314,20 @@ def test_jtj_recompute_matches_stored_factors_bit_for_bit():
     assert b.device_bytes <= a.device_bytes - 60 * p.n_obs
     with pytest.raises(RuntimeError, match="mixed form"):
         solve(p, Options(precision="fp64", matrix_free="recompute"), sigma=1.0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_second_stream_work_is_bit_identical_to_one_stream(precision):
+    """Inside an LM iteration the coarse basis, the camera sums and the camera
+    update run on a second stream beside the point passes, the Schur sums and
+    the points' back-substitution; with phase timing on they run one after
+    the other on one stream.  The work is independent, so both give the same
+    solve bit for bit."""
+    p, _ = survey.generate("lawnmower77", seed=5, n_cams=40, n_points=12000)
+    extra = dict(coarse=True, pcg_kernel="cluster") if precision == "mixed" else {}
+    qa, _, a = solve(p, Options(precision=precision, profile=False, **extra), sigma=1.0)
+    qb, _, b = solve(p, Options(precision=precision, profile=True, **extra), sigma=1.0)
+    assert a.iterations == b.iterations and a.final_cost == b.final_cost
+    for x, y in ((qa.points, qb.points), (qa.center, qb.center), (qa.rot, qb.rot),
+                 (qa.intr, qb.intr)):
+        assert np.array_equal(x, y)
